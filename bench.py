@@ -1,0 +1,306 @@
+"""Benchmark: photons/ms of per-photon tetrahedral tracing on the 1.296M-tet
+heterogeneous cube (60^3 voxels at 1 mm, 6 tets/voxel, orientation-safe
++/-0.25 mm node jitter, r=10 mm inclusion; pencil source (30,30,0) +z; 50 gates
+of 0.1 ns; 4 detectors R=2 mm saving per-medium partial paths and scatter
+counts; 1e8 photons per job).
+
+A step simulates 1e7 photons (one tenth of the 1e8-photon job) with the mesh
+and all buffers resident on the GPU; the default 10 timed steps are the whole
+job.  L2 is flushed (256 MB write) before every timed step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_STEP = 92  # 64 B face planes + 16 B neighbour ids + 4 B label + 8 B fluence RMW per ray-tet test
+PHOTONS_PER_STEP = 10_000_000
+JOB_PHOTONS = 100_000_000
+WORKLOAD = "inclusion-cube-1.3M-tets"
+
+
+def workload_config(nphoton):
+    from mmc_gb300 import meshgen
+    from mmc_gb300.core import SimConfig
+    m = meshgen.inclusion_cube(n=60, jitter=0.25, seed=12345)
+    cfg = SimConfig(media=m.media, nphoton=nphoton, seed=1648335518, srcpos=(30.0, 30.0, 0.0),
+                    srcdir=(0.0, 0.0, 1.0), tstart=0.0, tend=5e-9, tstep=1e-10, issavedet=1,
+                    detpos=meshgen.c1_detectors(), maxdetphoton=2_000_000, basisorder=0, isnormalized=1)
+    return m, cfg
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per photon of the engine kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "engine_inclusion_cube.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_photon:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.f.name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(m, cfg, target_s=12.0):
+    """The CPU oracle (C restatement of the path) on all host cores, on a
+    bounded sample of the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    import dataclasses
+    cores = os.cpu_count() or 1
+    n = 20000
+    while True:
+        c = dataclasses.replace(cfg, nphoton=n, maxdetphoton=max(1000, n))
+        t0 = time.perf_counter()
+        oracle.run(m.node, m.elem, m.label, c, nthreads=cores, normalize=False)
+        dt = time.perf_counter() - t0
+        if dt >= target_s * 0.5 or n >= 5_000_000:
+            return {"value": n / (dt * 1e3), "unit": "photons/ms", "cores": cores, "kind": "port",
+                    "sample": f"{n} photons of the {JOB_PHOTONS:.0e}-photon job, {dt:.1f} s on {cores} threads"}
+        n = int(n * min(10.0, max(1.5, target_s / max(dt, 1e-3))))
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    m, cfg = workload_config(PHOTONS_PER_STEP)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    import dataclasses
+    cores = os.cpu_count() or 1
+    # size one step to a few seconds of CPU work
+    n = 20000
+    c = dataclasses.replace(cfg, nphoton=n, maxdetphoton=n)
+    t0 = time.perf_counter()
+    oracle.run(m.node, m.elem, m.label, c, nthreads=cores, normalize=False)
+    dt = time.perf_counter() - t0
+    n = max(20000, int(n * 4.0 / max(dt, 1e-3)))
+    c = dataclasses.replace(cfg, nphoton=n, maxdetphoton=n)
+    for _ in range(args.warmup):
+        oracle.run(m.node, m.elem, m.label, dataclasses.replace(c, nphoton=2000, maxdetphoton=2000),
+                   nthreads=cores, normalize=False)
+    times = []
+    for k in range(args.steps):
+        ck = dataclasses.replace(c, photon_offset=k * n)
+        t0 = time.perf_counter()
+        oracle.run(m.node, m.elem, m.label, ck, nthreads=cores, normalize=True)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = n * args.steps / (total * 1e3)
+    line = {"impl": "reference", "metric": "photons/ms", "value": value, "unit": "photons/ms", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "photons_per_step": n, "gates": 50, "detectors": 4,
+                       "note": "CPU restatement of the reference algorithm (reference C sources are not on the box)"},
+            "cpu_baseline": {"value": value, "unit": "photons/ms", "cores": cores, "kind": "port",
+                             "sample": f"{n} photons per step x {args.steps} steps on {cores} threads"},
+            "e2e": {"value": value, "unit": "photons/ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--photons-per-step", type=int, default=PHOTONS_PER_STEP)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local_rank)
+        dist.init_process_group(backend=backend)
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    import torch
+    from mmc_gb300.core import Mesh, Session, simulate
+    import dataclasses
+
+    torch.cuda.set_device(local_rank)
+    nps = args.photons_per_step
+    m, cfg = workload_config(nps)
+    mesh = Mesh(m.node, m.elem, m.label, device=local_rank)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local_rank}")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # ---- device-resident throughput (value) ----
+    # rank r simulates photons [r*K*nps, (r+1)*K*nps) of the job: no data-path collective
+    sess = Session(mesh, dataclasses.replace(cfg, photon_offset=rank * (args.steps + args.warmup) * nps))
+    for w in range(args.warmup):
+        sess.launch(w * nps, nps)
+        sess.sync()
+    sampler = ClockSampler(local_rank)
+    barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    kernel_ms = []
+    raytet0 = None
+    t_wall = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        sess.launch((args.warmup + k) * nps, nps)
+        kernel_ms.append(sess.sync())
+    torch.cuda.synchronize()
+    barrier()
+    wall = time.perf_counter() - t_wall
+    clocks = sampler.stop()
+    res = sess.end(collect=True)
+    total_ms = float(sum(kernel_ms))
+    if dist is not None:
+        t = torch.tensor([total_ms], dtype=torch.float64, device=f"cuda:{local_rank}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    photons_all = nps * args.steps * world
+    value = photons_all / total_ms
+    steps_per_photon = res.raytet / ((args.warmup + args.steps) * nps)
+    raytet_per_launch = steps_per_photon * nps
+    avg_ms = float(np.mean(kernel_ms))
+    achieved = raytet_per_launch * BYTES_PER_STEP / (avg_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    tpp = profiled_traffic()
+
+    # ---- end to end through the public API with host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        ecfg = dataclasses.replace(cfg, photon_offset=10 ** 12 + rank * 10 ** 10)
+        simulate(mesh, dataclasses.replace(ecfg, nphoton=100000))  # warm the allocator
+        barrier()
+        t0 = time.perf_counter()
+        esteps = max(1, min(args.steps, 3))
+        d2h = 0
+        for k in range(esteps):
+            r = simulate(mesh, dataclasses.replace(ecfg, photon_offset=ecfg.photon_offset + k * nps))
+            d2h = r.field.nbytes + (r.detp.nbytes if r.detp is not None else 0) + 64
+        barrier()
+        et = time.perf_counter() - t0
+        if dist is not None:
+            t = torch.tensor([et], dtype=torch.float64, device=f"cuda:{local_rank}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            et = float(t.item())
+        h2d = cfg.media.nbytes + cfg.detpos.nbytes + 200
+        e2e = {"value": nps * esteps * world / (et * 1e3), "unit": "photons/ms", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "steps": esteps}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(m, cfg)
+
+    if rank == 0:
+        line = {
+            "metric": "photons/ms", "value": value, "unit": "photons/ms", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 fluence accumulation)",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "ne": mesh.ne, "nn": mesh.nn, "photons_per_step": nps,
+                       "job_photons": JOB_PHOTONS, "gates": 50, "detectors": 4, "savedet": True,
+                       "l2": "flushed (256 MB write) before each timed step",
+                       "steps_per_photon": steps_per_photon, "detected": res.detected,
+                       "absorbed_fraction": res.absorbed_fraction, "wall_s": wall},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": (tpp * nps) if tpp else None,
+                         "bytes_per_test": BYTES_PER_STEP, "tests_per_launch": raytet_per_launch,
+                         "avg_launch_ms": avg_ms},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

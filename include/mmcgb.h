@@ -1,0 +1,179 @@
+/*
+ * mmcgb -- GB300-native per-photon tetrahedral tracing for Mesh-based Monte
+ * Carlo (fangq/mmc).  C ABI of libmmcgb.so.
+ *
+ * The library replaces the reference's CUDA photon path, whose single entry is
+ *     void mmc_run_cu(mcconfig* cfg, tetmesh* mesh, raytracer* tracer);
+ * (src/mmc_cu_host.h:56, implemented as mmc_run_simulation in
+ * src/mmc_cu_host.cu:204-1528).  That entry takes the whole reference config
+ * and mesh structs, accumulates into cfg->exportfield and exits the process on
+ * error.  Here the same work is split into plain-pointer calls:
+ *
+ *   mmcgb_mesh_create   mesh upload + ray-tracer precompute, kept resident on
+ *                       the GPU (replaces the per-call uploads of
+ *                       src/mmc_cu_host.cu:447-487 and tracer_build/tracer_prep,
+ *                       src/mmc_mesh.c:1241-1602)
+ *   mmcgb_simulate      one simulation on a resident mesh: launch, readback,
+ *                       elem->node scatter and normalization
+ *                       (src/mmc_cu_host.cu:642-995, src/mmc_mesh.c:2154-2279)
+ *   mmcgb_simulate_batch  many simulations in one persistent launch
+ *   mmcgb_run           one-shot create + simulate + destroy, the direct
+ *                       counterpart of mmc_run_cu
+ *
+ * Every call returns an mmcgb_status; none exits the process.  The message of
+ * the last failure on the calling thread is available from mmcgb_last_error().
+ * All arrays are host memory owned by the caller unless stated otherwise.
+ * Indices in node/elem/facenb follow the reference: 1-based, 0 = no neighbour.
+ */
+#ifndef MMCGB_H
+#define MMCGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MMCGB_ABI_VERSION 1
+
+typedef enum mmcgb_status {
+    MMCGB_OK = 0,
+    MMCGB_E_ARG = 1,      /* invalid argument or configuration */
+    MMCGB_E_CUDA = 2,     /* CUDA runtime error */
+    MMCGB_E_MESH = 3,     /* malformed mesh (bad node id, too many elements) */
+    MMCGB_E_SOURCE = 4,   /* no element encloses the source */
+    MMCGB_E_BUDGET = 5,   /* photons stopped by the per-photon step budget */
+    MMCGB_E_NOMEM = 6     /* not enough device memory for the requested outputs */
+} mmcgb_status;
+
+/* output quantity, same numbering as the reference's -O option */
+typedef enum mmcgb_output {
+    MMCGB_OUT_FLUX = 0, MMCGB_OUT_FLUENCE = 1, MMCGB_OUT_ENERGY = 2,
+    MMCGB_OUT_JACOBIAN = 3, MMCGB_OUT_WL = 4, MMCGB_OUT_WP = 5
+} mmcgb_output;
+
+typedef struct mmcgb_mesh mmcgb_mesh; /* opaque, device-resident mesh */
+
+/* Mesh input (tetmesh subset, src/mmc_mesh.h:87-122). */
+typedef struct mmcgb_mesh_desc {
+    int32_t nn;              /* nodes */
+    int32_t ne;              /* tetrahedra */
+    const float* node;       /* nn*3 coordinates (mm) */
+    const int32_t* elem;     /* ne*4 node ids, 1-based */
+    const int32_t* label;    /* ne medium labels, 0 = background/void */
+    const int32_t* facenb;   /* ne*4 face neighbours, or NULL to compute */
+} mmcgb_mesh_desc;
+
+/* Simulation settings (the mcconfig fields the photon path reads,
+ * src/mmc_utils.h:210-345). */
+typedef struct mmcgb_config {
+    uint64_t nphoton;        /* photons to launch (replay: replayed photons) */
+    uint64_t photon_offset;  /* index of the first photon (sharded runs) */
+    uint64_t seed;           /* RNG seed */
+    float srcpos[3];         /* pencil source position (mm) */
+    float srcdir[3];         /* unit launch direction */
+    int32_t srctype;         /* 0 = pencil (the only source type implemented) */
+    int32_t e0;              /* initial element, 1-based; 0 = locate it */
+    float tstart, tend, tstep;  /* time gates (s) */
+    int32_t isreflect;       /* 0 no mismatch, 1 Fresnel, 2 absorbing exterior, 3 mirror */
+    int32_t isspecular;
+    int32_t voidtime;
+    int32_t issavedet;       /* save detected photons */
+    int32_t issaveseed;      /* save 16-byte RNG seeds of detected photons */
+    int32_t issaveexit;      /* save exit position/direction */
+    int32_t ismomentum;      /* save momentum transfer */
+    float minenergy;         /* roulette threshold */
+    float roulettesize;
+    float nout;              /* refractive index outside the mesh */
+    float unitinmm;
+    int32_t outputtype;      /* mmcgb_output */
+    int32_t basisorder;      /* 0 element output, 1 node output */
+    int32_t isnormalized;    /* 0 raw, 1 normalized (2 = skip surface nvol fix) */
+    uint32_t maxdetphoton;
+    int32_t nmedia;          /* rows in media, including background row 0 */
+    const float* media;      /* nmedia*4: mua mus g n (1/mm) */
+    int32_t detnum;
+    const float* detpos;     /* detnum*4: x y z radius (mm) */
+    const uint64_t* replayseed;   /* replay: nphoton*2 words (16-byte seeds), else NULL */
+    const float* replayweight;    /* replay: nphoton */
+    const float* replaytime;      /* replay: nphoton (s) */
+    int32_t accum_f64;       /* 1: double atomics (default), 0: float + overflow buffer */
+    uint64_t step_budget;    /* max ray-tet tests per photon, 0 = 100,000,000 */
+    int32_t threads;         /* threads per block, 0 = auto */
+    int32_t blocks;          /* persistent blocks, 0 = auto */
+} mmcgb_config;
+
+/* Outputs.  Pointers may be NULL to skip an output; counts are always set. */
+typedef struct mmcgb_result {
+    double* field;           /* maxgate*datalen, datalen = ne (basisorder 0) or nn */
+    float* detp;             /* maxdetphoton*reclen detected-photon records */
+    uint8_t* seeds;          /* maxdetphoton*16 */
+    float* photon_weight;    /* nphoton final weights (parity tracing), or NULL */
+    uint32_t* photon_steps;  /* nphoton ray-tet tests per photon, or NULL */
+    int32_t* photon_det;     /* nphoton detector ids (0 = none), or NULL */
+    uint32_t detected;       /* detected photons (may exceed maxdetphoton) */
+    uint32_t saved;          /* records written */
+    int32_t reclen;          /* columns per record: 1 + (2+mom)*M + 6*exit + 1 */
+    int32_t maxgate;
+    double energytot;        /* launched weight */
+    double energyesc;        /* escaped weight */
+    double normalizer;
+    uint64_t raytet;         /* ray-tetrahedron tests */
+    uint64_t aborted;        /* photons stopped by the step budget */
+    float kernel_ms;         /* device time of the photon kernel */
+} mmcgb_result;
+
+int32_t mmcgb_abi_version(void);
+const char* mmcgb_last_error(void);
+
+/* Builds the ray-tracer records for `desc` on `device` and keeps them resident.
+ * Replaces mesh_getvolume/mesh_getfacenb/tracer_build/tracer_prep
+ * (src/mmc_mesh.c:910-974, src/mmc_highorder.cpp:128-159,
+ * src/mmc_mesh.c:1496-1602, :1241-1483) and the uploads of
+ * src/mmc_cu_host.cu:447-487. */
+int32_t mmcgb_mesh_create(const mmcgb_mesh_desc* desc, int32_t device, mmcgb_mesh** out);
+int32_t mmcgb_mesh_destroy(mmcgb_mesh* mesh);
+/* Sizes of a resident mesh: nodes, elements, exterior faces. */
+int32_t mmcgb_mesh_info(const mmcgb_mesh* mesh, int32_t* nn, int32_t* ne, int32_t* nf);
+/* Host copies of the prepared mesh (any pointer may be NULL): elem after the
+ * orientation fix (ne*4), facenb with exterior faces numbered -1,-2,...
+ * (ne*4), element volumes (ne), nodal volumes before the surface fix (nn). */
+int32_t mmcgb_mesh_export(const mmcgb_mesh* mesh, int32_t* elem, int32_t* facenb,
+                          float* evol, float* nvol);
+/* First element (1-based, by index) enclosing p, 0 if none
+ * (src/mmc_mesh.c:1060-1090). */
+int32_t mmcgb_mesh_locate(const mmcgb_mesh* mesh, const float p[3]);
+
+/* One simulation on a resident mesh (src/mmc_cu_host.cu:204-1528). */
+int32_t mmcgb_simulate(mmcgb_mesh* mesh, const mmcgb_config* cfg, mmcgb_result* res);
+
+/* A simulation run as a sequence of launches that accumulate into the same
+ * device buffers (the reference's respin loop, src/mmc_cu_host.cu:656-906).
+ * begin allocates and zeroes the outputs; each launch simulates photons
+ * [photon_offset, photon_offset+nphoton) of the run asynchronously on the
+ * session's stream; sync waits and reports the last launch's device time;
+ * end reads back, normalizes into `res` (may be NULL to discard) and frees.
+ * `trace` may carry per-photon trace buffers (single-launch sessions only). */
+typedef struct mmcgb_session mmcgb_session;
+int32_t mmcgb_session_begin(mmcgb_mesh* mesh, const mmcgb_config* cfg, mmcgb_result* trace,
+                            mmcgb_session** out);
+int32_t mmcgb_session_launch(mmcgb_session* s, uint64_t photon_offset, uint64_t nphoton);
+int32_t mmcgb_session_sync(mmcgb_session* s, float* last_kernel_ms);
+int32_t mmcgb_session_end(mmcgb_session* s, mmcgb_result* res);
+
+/* `n` simulations sharing one persistent launch; meshes may differ.  Each
+ * simulation's results land in its own mmcgb_result. */
+int32_t mmcgb_simulate_batch(int32_t n, mmcgb_mesh* const* meshes, const mmcgb_config* cfgs,
+                             mmcgb_result* res);
+
+/* One-shot drop-in for mmc_run_cu (src/mmc_cu_host.h:56). */
+int32_t mmcgb_run(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, int32_t device,
+                  mmcgb_result* res);
+
+/* Fills `cfg` with the reference defaults (src/mmc_utils.c:207-363). */
+void mmcgb_config_defaults(mmcgb_config* cfg);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,118 @@
+"""Builds the native parts in-tree.
+
+* ``mmc_gb300/lib/libmmcgb.so`` -- the product: CUDA photon engine for sm_103a
+  plus the C++ host runtime, exported through the C ABI in ``include/mmcgb.h``.
+* ``oracle/liboracle.so`` -- the CPU oracle (test infrastructure), built only
+  when asked (``oracle=True``).
+
+Plain nvcc/g++ invocations run in parallel; no cmake, no torch extension
+machinery.  Float contraction is disabled everywhere in the photon path
+(``-fmad=false`` / ``-ffp-contract=off``): the float operation sequence is the
+contract that lets the oracle reproduce each GPU photon bit for bit.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "mmc_gb300")
+CSRC = os.path.join(PKG, "csrc")
+LIBDIR = os.path.join(PKG, "lib")
+BUILDDIR = os.path.join(ROOT, "_build")
+ORACLE = os.path.join(ROOT, "oracle")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _cuda_home() -> str:
+    for cand in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if cand and os.path.exists(os.path.join(cand, "bin", "nvcc")):
+            return cand
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return os.path.dirname(os.path.dirname(nvcc))
+    raise RuntimeError("nvcc not found (set CUDA_HOME)")
+
+
+def _run(cmd):
+    p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + p.stdout)
+    return p.stdout
+
+
+def _stale(target: str, sources) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(s) > t for s in sources)
+
+
+def build_library(force: bool = False, verbose: bool = False) -> str:
+    cuda = _cuda_home()
+    nvcc = os.path.join(cuda, "bin", "nvcc")
+    os.makedirs(LIBDIR, exist_ok=True)
+    os.makedirs(BUILDDIR, exist_ok=True)
+    out = os.path.join(LIBDIR, "libmmcgb.so")
+    headers = [os.path.join(CSRC, h) for h in ("engine.h", "mesh.h", "devmath.cuh")]
+    headers.append(os.path.join(ROOT, "include", "mmcgb.h"))
+    cu = ["engine.cu"]
+    cpp = ["mesh.cpp", "output.cpp", "api.cpp"]
+    srcs = [os.path.join(CSRC, f) for f in cu + cpp]
+    if not force and not _stale(out, srcs + headers):
+        return out
+    jobs = []
+    objs = []
+    for f in cu:
+        o = os.path.join(BUILDDIR, f + ".o")
+        objs.append(o)
+        jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+                     "-Xptxas", "-v", "-c", os.path.join(CSRC, f), "-o", o])
+    for f in cpp:
+        o = os.path.join(BUILDDIR, f + ".o")
+        objs.append(o)
+        jobs.append(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-std=c++17", "-Wall",
+                     "-I" + os.path.join(cuda, "include"), "-c", os.path.join(CSRC, f), "-o", o])
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        logs = list(ex.map(_run, jobs))
+    if verbose:
+        for lg in logs:
+            sys.stdout.write(lg)
+    tmp = out + ".tmp"
+    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
+    os.replace(tmp, out)
+    return out
+
+
+def build_oracle(force: bool = False) -> str:
+    out = os.path.join(ORACLE, "liboracle.so")
+    srcs = [os.path.join(ORACLE, "mmc_oracle.c"), os.path.join(ORACLE, "mmc_oracle.h")]
+    if not force and not _stale(out, srcs):
+        return out
+    tmp = out + ".tmp"
+    _run(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-Wall",
+          "-o", tmp, srcs[0], "-lm"])
+    os.replace(tmp, out)
+    return out
+
+
+def build_reference_oracle() -> str | None:
+    """Compiles the reference CPU engine into oracle/_ref when its sources exist."""
+    ref = os.environ.get("MMC_REFERENCE", "/root/reference")
+    if not os.path.isdir(os.path.join(ref, "src")):
+        return None
+    script = os.path.join(ORACLE, "build_ref.sh")
+    p = subprocess.run(["bash", script], env={**os.environ, "REF": ref},
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        return None
+    return os.path.join(ORACLE, "_ref", "mmc")
+
+
+if __name__ == "__main__":
+    print(build_library(force="--force" in sys.argv, verbose=True))
+    print(build_oracle(force="--force" in sys.argv))

@@ -1,0 +1,302 @@
+"""Python front of the photon engine: resident meshes, simulation settings and
+results as numpy arrays, over the C ABI of libmmcgb.so.
+
+    mesh = Mesh(node, elem, label)            # uploads + ray-tracer precompute
+    res = simulate(mesh, SimConfig(nphoton=1e6, media=..., srcpos=..., ...))
+    res.field   # (maxgate, datalen) float64, normalized like the reference
+
+Field layout follows the reference's exported weight array
+(src/mmc_cu_host.cu:916-976): gate-major, element (basisorder 0) or node
+(basisorder 1) fastest.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _native as N
+
+OUTPUT_TYPES = {"flux": 0, "fluence": 1, "energy": 2, "jacobian": 3, "wl": 4, "wp": 5}
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data
+
+
+class Mesh:
+    """A tetrahedral mesh resident on one GPU (mmcgb_mesh_create)."""
+
+    def __init__(self, node, elem, label, facenb=None, device: int = 0):
+        lib = N.load()
+        self._node = np.ascontiguousarray(node, dtype=np.float32).reshape(-1, 3)
+        self._elem = np.ascontiguousarray(elem, dtype=np.int32).reshape(-1, 4)
+        self._label = np.ascontiguousarray(label, dtype=np.int32).reshape(-1)
+        if self._label.shape[0] != self._elem.shape[0]:
+            raise ValueError("label must have one entry per element")
+        fnb = None if facenb is None else np.ascontiguousarray(facenb, dtype=np.int32).reshape(-1, 4)
+        desc = N.MeshDesc(self._node.shape[0], self._elem.shape[0], _ptr(self._node), _ptr(self._elem),
+                          _ptr(self._label), _ptr(fnb))
+        h = C.c_void_p()
+        N.check(lib.mmcgb_mesh_create(C.byref(desc), int(device), C.byref(h)))
+        self._h = h
+        self.device = int(device)
+        nn, ne, nf = C.c_int32(), C.c_int32(), C.c_int32()
+        N.check(lib.mmcgb_mesh_info(h, C.byref(nn), C.byref(ne), C.byref(nf)))
+        self.nn, self.ne, self.nf = nn.value, ne.value, nf.value
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise ValueError("mesh was closed")
+        return self._h
+
+    @property
+    def node(self):
+        return self._node
+
+    @property
+    def label(self):
+        return self._label
+
+    def export(self):
+        """(elem after orientation fix, facenb, evol, nvol) host copies."""
+        lib = N.load()
+        elem = np.empty((self.ne, 4), np.int32)
+        fnb = np.empty((self.ne, 4), np.int32)
+        evol = np.empty(self.ne, np.float32)
+        nvol = np.empty(self.nn, np.float32)
+        N.check(lib.mmcgb_mesh_export(self.handle, _ptr(elem), _ptr(fnb), _ptr(evol), _ptr(nvol)))
+        return elem, fnb, evol, nvol
+
+    def locate(self, p) -> int:
+        arr = (C.c_float * 3)(*[float(x) for x in p])
+        return int(N.load().mmcgb_mesh_locate(self.handle, C.byref(arr)))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            N.load().mmcgb_mesh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclasses.dataclass
+class SimConfig:
+    """Settings of one simulation (defaults: src/mmc_utils.c:207-363)."""
+    media: np.ndarray                         # (nmedia, 4) mua mus g n, row 0 = background
+    nphoton: int = 1000000
+    seed: int = 0x623F9A9E
+    srcpos: Sequence[float] = (0.0, 0.0, 0.0)
+    srcdir: Sequence[float] = (0.0, 0.0, 1.0)
+    e0: int = 0
+    tstart: float = 0.0
+    tend: float = 5e-9
+    tstep: float = 5e-9
+    isreflect: int = 1
+    isspecular: int = 0
+    voidtime: int = 1
+    issavedet: int = 0
+    issaveseed: int = 0
+    issaveexit: int = 0
+    ismomentum: int = 0
+    minenergy: float = 1e-6
+    roulettesize: float = 10.0
+    nout: float = 1.0
+    unitinmm: float = 1.0
+    outputtype: str = "flux"
+    basisorder: int = 1
+    isnormalized: int = 1
+    maxdetphoton: int = 1000000
+    detpos: Optional[np.ndarray] = None       # (ndet, 4) x y z r
+    replayseed: Optional[np.ndarray] = None   # (N, 2) uint64 initial RNG states
+    replayweight: Optional[np.ndarray] = None
+    replaytime: Optional[np.ndarray] = None
+    accum_f64: int = 1
+    photon_offset: int = 0
+    step_budget: int = 0
+    threads: int = 0
+    blocks: int = 0
+    save_field: bool = True
+
+    @property
+    def maxgate(self) -> int:
+        return int((np.float32(self.tend) - np.float32(self.tstart)) / np.float32(self.tstep) + np.float32(0.5))
+
+    def to_c(self):
+        keep = {}
+        c = N.Config()
+        c.nphoton = int(self.nphoton)
+        c.photon_offset = int(self.photon_offset)
+        c.seed = int(self.seed) & 0xFFFFFFFFFFFFFFFF
+        c.srcpos = (C.c_float * 3)(*[float(x) for x in self.srcpos])
+        c.srcdir = (C.c_float * 3)(*[float(x) for x in self.srcdir])
+        c.srctype = 0
+        c.e0 = int(self.e0)
+        c.tstart, c.tend, c.tstep = float(self.tstart), float(self.tend), float(self.tstep)
+        c.isreflect, c.isspecular, c.voidtime = int(self.isreflect), int(self.isspecular), int(self.voidtime)
+        c.issavedet, c.issaveseed = int(self.issavedet), int(self.issaveseed)
+        c.issaveexit, c.ismomentum = int(self.issaveexit), int(self.ismomentum)
+        c.minenergy, c.roulettesize = float(self.minenergy), float(self.roulettesize)
+        c.nout, c.unitinmm = float(self.nout), float(self.unitinmm)
+        ot = self.outputtype
+        c.outputtype = OUTPUT_TYPES[ot] if isinstance(ot, str) else int(ot)
+        c.basisorder, c.isnormalized = int(self.basisorder), int(self.isnormalized)
+        c.maxdetphoton = int(self.maxdetphoton)
+        med = np.ascontiguousarray(self.media, dtype=np.float32).reshape(-1, 4)
+        keep["media"] = med
+        c.nmedia, c.media = med.shape[0], _ptr(med)
+        if self.detpos is not None and len(self.detpos):
+            det = np.ascontiguousarray(self.detpos, dtype=np.float32).reshape(-1, 4)
+            keep["det"] = det
+            c.detnum, c.detpos = det.shape[0], _ptr(det)
+        if self.replayseed is not None:
+            rs = np.ascontiguousarray(self.replayseed, dtype=np.uint64).reshape(-1, 2)
+            rw = np.ascontiguousarray(self.replayweight, dtype=np.float32).reshape(-1)
+            rt = np.ascontiguousarray(self.replaytime, dtype=np.float32).reshape(-1)
+            if not (rs.shape[0] == rw.shape[0] == rt.shape[0] == c.nphoton):
+                raise ValueError("replay arrays must have nphoton entries")
+            keep.update(rs=rs, rw=rw, rt=rt)
+            c.replayseed, c.replayweight, c.replaytime = _ptr(rs), _ptr(rw), _ptr(rt)
+        c.accum_f64 = int(self.accum_f64)
+        c.step_budget = int(self.step_budget)
+        c.threads, c.blocks = int(self.threads), int(self.blocks)
+        return c, keep
+
+
+@dataclasses.dataclass
+class SimResult:
+    field: Optional[np.ndarray]      # (maxgate, datalen) float64
+    detp: Optional[np.ndarray]       # (saved, reclen) float32
+    seeds: Optional[np.ndarray]      # (saved, 16) uint8
+    detected: int
+    energytot: float
+    energyesc: float
+    normalizer: float
+    raytet: int
+    aborted: int
+    kernel_ms: float
+    maxgate: int
+    reclen: int
+    photon_weight: Optional[np.ndarray] = None
+    photon_steps: Optional[np.ndarray] = None
+    photon_det: Optional[np.ndarray] = None
+
+    @property
+    def absorbed_fraction(self) -> float:
+        return (self.energytot - self.energyesc) / self.energytot if self.energytot else 0.0
+
+
+def _alloc_result(mesh: Mesh, cfg: SimConfig, trace: bool):
+    G = cfg.maxgate
+    datalen = mesh.nn if cfg.basisorder else mesh.ne
+    nmed = np.asarray(cfg.media).reshape(-1, 4).shape[0]
+    reclen = 1 + (2 + (1 if cfg.ismomentum else 0)) * (nmed - 1) + (6 if cfg.issaveexit else 0) + 1
+    arrs = {}
+    arrs["field"] = np.zeros((G, datalen), np.float64) if cfg.save_field else None
+    if cfg.issavedet:
+        arrs["detp"] = np.zeros((int(cfg.maxdetphoton), reclen), np.float32)
+        arrs["seeds"] = np.zeros((int(cfg.maxdetphoton), 16), np.uint8) if cfg.issaveseed else None
+    else:
+        arrs["detp"] = arrs["seeds"] = None
+    if trace:
+        n = int(cfg.nphoton)
+        arrs["photon_weight"] = np.zeros(n, np.float32)
+        arrs["photon_steps"] = np.zeros(n, np.uint32)
+        arrs["photon_det"] = np.zeros(n, np.int32)
+    else:
+        arrs["photon_weight"] = arrs["photon_steps"] = arrs["photon_det"] = None
+    r = N.Result()
+    for k in ("field", "detp", "seeds", "photon_weight", "photon_steps", "photon_det"):
+        setattr(r, k, _ptr(arrs[k]))
+    return r, arrs
+
+
+def _make_result(r: N.Result, arrs) -> SimResult:
+    saved = int(r.saved)
+    detp = arrs["detp"][:saved].copy() if arrs["detp"] is not None else None
+    seeds = arrs["seeds"][:saved].copy() if arrs["seeds"] is not None else None
+    return SimResult(field=arrs["field"], detp=detp, seeds=seeds, detected=int(r.detected),
+                     energytot=r.energytot, energyesc=r.energyesc, normalizer=r.normalizer,
+                     raytet=int(r.raytet), aborted=int(r.aborted), kernel_ms=float(r.kernel_ms),
+                     maxgate=int(r.maxgate), reclen=int(r.reclen), photon_weight=arrs["photon_weight"],
+                     photon_steps=arrs["photon_steps"], photon_det=arrs["photon_det"])
+
+
+def simulate(mesh: Mesh, cfg: SimConfig, trace: bool = False) -> SimResult:
+    """Runs one simulation on a resident mesh (mmcgb_simulate)."""
+    lib = N.load()
+    c, keep = cfg.to_c()
+    r, arrs = _alloc_result(mesh, cfg, trace)
+    N.check(lib.mmcgb_simulate(mesh.handle, C.byref(c), C.byref(r)))
+    del keep
+    return _make_result(r, arrs)
+
+
+def simulate_batch(meshes: Sequence[Mesh], cfgs: Sequence[SimConfig]) -> list:
+    """Runs many simulations in one persistent launch (mmcgb_simulate_batch)."""
+    lib = N.load()
+    n = len(cfgs)
+    if len(meshes) != n or n == 0:
+        raise ValueError("need one mesh per config")
+    carr = (N.Config * n)()
+    rarr = (N.Result * n)()
+    harr = (C.c_void_p * n)()
+    keeps, allarrs = [], []
+    for i in range(n):
+        c, keep = cfgs[i].to_c()
+        carr[i] = c
+        keeps.append(keep)
+        r, arrs = _alloc_result(meshes[i], cfgs[i], False)
+        rarr[i] = r
+        allarrs.append(arrs)
+        harr[i] = meshes[i].handle
+    N.check(lib.mmcgb_simulate_batch(n, harr, carr, rarr))
+    return [_make_result(rarr[i], allarrs[i]) for i in range(n)]
+
+
+class Session:
+    """A simulation run as several launches accumulating into the same device
+    buffers (mmcgb_session_*): the reference's respin loop, and the way the
+    benchmark times device-resident work."""
+
+    def __init__(self, mesh: Mesh, cfg: SimConfig):
+        lib = N.load()
+        self.mesh, self.cfg = mesh, cfg
+        self._c, self._keep = cfg.to_c()
+        h = C.c_void_p()
+        N.check(lib.mmcgb_session_begin(mesh.handle, C.byref(self._c), None, C.byref(h)))
+        self._h = h
+
+    def launch(self, photon_offset: int, nphoton: int):
+        N.check(N.load().mmcgb_session_launch(self._h, int(photon_offset), int(nphoton)))
+
+    def sync(self) -> float:
+        ms = C.c_float()
+        N.check(N.load().mmcgb_session_sync(self._h, C.byref(ms)))
+        return float(ms.value)
+
+    def end(self, collect: bool = True) -> Optional[SimResult]:
+        lib = N.load()
+        h, self._h = self._h, None
+        if h is None:
+            return None
+        if not collect:
+            N.check(lib.mmcgb_session_end(h, None))
+            return None
+        r, arrs = _alloc_result(self.mesh, self.cfg, False)
+        N.check(lib.mmcgb_session_end(h, C.byref(r)))
+        return _make_result(r, arrs)
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None:
+            try:
+                N.load().mmcgb_session_end(self._h, None)
+            except Exception:
+                pass

@@ -1,0 +1,578 @@
+// C ABI of libmmcgb (include/mmcgb.h): resident meshes, single and batched
+// simulations.  Every failure returns a status and records a message; nothing
+// here exits the process (the reference's mcx_error path,
+// src/mmc_utils.c:1426-1443, terminates instead).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/mmcgb.h"
+#include "engine.h"
+#include "mesh.h"
+
+using namespace mmcgb;
+
+struct mmcgb_mesh {
+    HostMesh host;
+    int device = 0;
+    TetRec* rec = nullptr;
+    int4* elem = nullptr;
+    float4* node = nullptr;
+    int* label = nullptr;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(MMCGB_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                         \
+    do {                                                 \
+        cudaError_t _e = (call);                         \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+    } while (0)
+
+int gates_of(const mmcgb_config& c) { return (int)((c.tend - c.tstart) / c.tstep + 0.5f); }
+
+int validate(const HostMesh& m, const mmcgb_config& c, std::string& err) {
+    if (c.srctype != 0) { err = "only the pencil source (srctype 0) is implemented"; return MMCGB_E_ARG; }
+    if (!(c.tstep > 0.f) || !(c.tend > c.tstart)) { err = "time gates need tstep > 0 and tend > tstart"; return MMCGB_E_ARG; }
+    if (gates_of(c) < 1) { err = "time window holds no gate"; return MMCGB_E_ARG; }
+    if (c.nmedia < 2 || c.nmedia > kMaxMedia || !c.media) { err = "media table needs 2..64 rows (row 0 = background)"; return MMCGB_E_ARG; }
+    if (m.maxlabel > c.nmedia - 1) { err = "mesh label exceeds the number of media"; return MMCGB_E_ARG; }
+    if (c.detnum < 0 || (c.detnum > 0 && !c.detpos)) { err = "detnum > 0 needs detpos"; return MMCGB_E_ARG; }
+    if (c.issavedet && c.maxdetphoton == 0) { err = "issavedet needs maxdetphoton > 0"; return MMCGB_E_ARG; }
+    if (c.replayseed && (!c.replayweight || !c.replaytime)) { err = "replay needs replayseed, replayweight and replaytime"; return MMCGB_E_ARG; }
+    if (c.nphoton > 0xFFFFFFFFull && (c.replayseed)) { err = "replay photon count must fit 32 bits"; return MMCGB_E_ARG; }
+    for (int i = 0; i < c.nmedia; i++)
+        for (int k = 0; k < 4; k++)
+            if (!std::isfinite(c.media[4 * i + k])) { err = "media values must be finite"; return MMCGB_E_ARG; }
+    const float vn = c.srcdir[0] * c.srcdir[0] + c.srcdir[1] * c.srcdir[1] + c.srcdir[2] * c.srcdir[2];
+    if (!(std::fabs(vn - 1.f) < 1e-3f)) { err = "srcdir must be a unit vector"; return MMCGB_E_ARG; }
+    return MMCGB_OK;
+}
+
+// Device buffers of one simulation (stream-ordered allocations).
+struct SimBuffers {
+    float4* media = nullptr;
+    float4* det = nullptr;
+    double* f64 = nullptr;
+    float* f32 = nullptr;
+    float* detp = nullptr;
+    unsigned long long* seeds = nullptr;
+    unsigned int* detcount = nullptr;
+    double* energy = nullptr;
+    unsigned long long* counters = nullptr;
+    unsigned long long* rseed = nullptr;
+    float* rweight = nullptr;
+    float* rtime = nullptr;
+    float* pw = nullptr;
+    unsigned int* ps = nullptr;
+    int* pd = nullptr;
+    std::vector<void*> owned;
+    cudaStream_t stream = nullptr;
+
+    template <class T>
+    cudaError_t alloc(T** p, size_t count) {
+        if (count == 0) { *p = nullptr; return cudaSuccess; }
+        cudaError_t e = cudaMallocAsync((void**)p, sizeof(T) * count, stream);
+        if (e == cudaSuccess) owned.push_back(*p);
+        return e;
+    }
+    void release() {
+        for (void* p : owned) cudaFreeAsync(p, stream);
+        owned.clear();
+    }
+};
+
+struct Prepared {
+    SimDev sim;
+    SimBuffers buf;
+    int maxgate = 0;
+    int reclen = 0;   // columns per record incl. detector id
+    size_t flen = 0;
+};
+
+int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res, cudaStream_t stream, Prepared& P) {
+    const HostMesh& m = mesh->host;
+    std::string err;
+    int rc = validate(m, c, err);
+    if (rc) return fail(rc, err);
+    // initial element: keep a given one only if it encloses the source
+    // (src/mmc_mesh.c:1325-1329), otherwise locate it
+    int e0 = c.e0;
+    if (e0 > 0 && e0 <= m.ne) {
+        const float* p = c.srcpos;
+        const int* el = &m.elem[4 * (size_t)(e0 - 1)];
+        bool inside = true;
+        for (int i = 0; i < 4; i++) {
+            const float* a = &m.node[3 * (size_t)(el[kOut[i][0]] - 1)];
+            const float* b = &m.node[3 * (size_t)(el[kOut[i][1]] - 1)];
+            const float* cc = &m.node[3 * (size_t)(el[kOut[i][2]] - 1)];
+            const float ab[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+            const float ac[3] = {cc[0] - a[0], cc[1] - a[1], cc[2] - a[2]};
+            const float s[3] = {p[0] - a[0], p[1] - a[1], p[2] - a[2]};
+            const float n[3] = {ab[1] * ac[2] - ab[2] * ac[1], ab[2] * ac[0] - ab[0] * ac[2], ab[0] * ac[1] - ab[1] * ac[0]};
+            if (-(s[0] * n[0] + s[1] * n[1] + s[2] * n[2]) < 0.f) inside = false;
+        }
+        if (!inside) e0 = locate(m, c.srcpos);
+    } else {
+        e0 = locate(m, c.srcpos);
+    }
+    if (e0 <= 0) return fail(MMCGB_E_SOURCE, "initial element does not enclose the source");
+
+    P.maxgate = gates_of(c);
+    const int M = c.nmedia - 1;
+    const int reclen_dev = (2 + (c.ismomentum > 0)) * M + (c.issaveexit > 0) * 6 + 1;
+    P.reclen = reclen_dev + 1;
+    P.flen = (size_t)m.ne * P.maxgate;
+    SimBuffers& B = P.buf;
+    B.stream = stream;
+    const bool f64 = c.accum_f64 != 0;
+    const size_t maxdet = c.issavedet ? c.maxdetphoton : 0;
+    size_t need = P.flen * (f64 ? 8 : 8) + maxdet * (P.reclen * 4 + (c.issaveseed ? 16 : 0));
+    size_t freeb = 0, totalb = 0;
+    CK(cudaMemGetInfo(&freeb, &totalb));
+    if (need + (64ull << 20) > freeb) return fail(MMCGB_E_NOMEM, "not enough free device memory for fluence and detector buffers");
+    CK(B.alloc(&B.media, c.nmedia));
+    CK(B.alloc(&B.det, c.detnum));
+    if (f64) CK(B.alloc(&B.f64, P.flen)); else CK(B.alloc(&B.f32, 2 * P.flen));
+    CK(B.alloc(&B.detp, maxdet * P.reclen));
+    if (c.issaveseed) CK(B.alloc(&B.seeds, maxdet * 2));
+    CK(B.alloc(&B.detcount, 1));
+    CK(B.alloc(&B.energy, 2));
+    CK(B.alloc(&B.counters, 2));
+    if (c.replayseed) {
+        CK(B.alloc(&B.rseed, 2 * c.nphoton));
+        CK(B.alloc(&B.rweight, c.nphoton));
+        CK(B.alloc(&B.rtime, c.nphoton));
+        CK(cudaMemcpyAsync(B.rseed, c.replayseed, 16 * c.nphoton, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(B.rweight, c.replayweight, 4 * c.nphoton, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(B.rtime, c.replaytime, 4 * c.nphoton, cudaMemcpyHostToDevice, stream));
+    }
+    if (res && res->photon_weight) CK(B.alloc(&B.pw, c.nphoton));
+    if (res && res->photon_steps) CK(B.alloc(&B.ps, c.nphoton));
+    if (res && res->photon_det) CK(B.alloc(&B.pd, c.nphoton));
+    CK(cudaMemcpyAsync(B.media, c.media, sizeof(float4) * c.nmedia, cudaMemcpyHostToDevice, stream));
+    if (c.detnum) CK(cudaMemcpyAsync(B.det, c.detpos, sizeof(float4) * c.detnum, cudaMemcpyHostToDevice, stream));
+    if (f64) CK(cudaMemsetAsync(B.f64, 0, sizeof(double) * P.flen, stream));
+    else CK(cudaMemsetAsync(B.f32, 0, sizeof(float) * 2 * P.flen, stream));
+    CK(cudaMemsetAsync(B.detcount, 0, sizeof(unsigned), stream));
+    CK(cudaMemsetAsync(B.energy, 0, sizeof(double) * 2, stream));
+    CK(cudaMemsetAsync(B.counters, 0, sizeof(unsigned long long) * 2, stream));
+
+    SimDev& S = P.sim;
+    std::memset(&S, 0, sizeof(S));
+    S.rec = mesh->rec;
+    S.elem = mesh->elem;
+    S.node = mesh->node;
+    S.label = mesh->label;
+    S.ne = m.ne;
+    S.e0 = e0;
+    S.nmedia = c.nmedia;
+    S.detnum = c.detnum;
+    S.media = B.media;
+    S.det = B.det;
+    S.nphoton = c.nphoton;
+    S.photon_offset = c.photon_offset;
+    S.seed = c.seed;
+    S.step_budget = c.step_budget ? c.step_budget : 100000000ull;
+    for (int k = 0; k < 3; k++) {
+        S.srcpos[k] = c.srcpos[k];
+        S.srcdir[k] = c.srcdir[k];
+    }
+    // per-launch time window (src/mmc_cu_host.cu:642-662): all gates in one launch
+    S.tstart = c.tstart;
+    S.tend = c.tstart + c.tstep * (float)P.maxgate;
+    S.Rtstep = 1.f / c.tstep;
+    S.maxgate = P.maxgate;
+    S.roulette_on = ((S.tend - S.tstart) * S.Rtstep <= 1.f) ? 1 : 0;
+    S.minenergy = c.minenergy;
+    S.roulettesize = c.roulettesize;
+    S.nout = c.nout;
+    S.isreflect = c.isreflect;
+    S.isspecular = c.isspecular;
+    S.voidtime = c.voidtime;
+    S.issavedet = c.issavedet ? 1 : 0;
+    S.issaveexit = c.issaveexit ? 1 : 0;
+    S.ismomentum = c.ismomentum ? 1 : 0;
+    S.issaveseed = c.issaveseed ? 1 : 0;
+    S.outputtype = c.outputtype;
+    S.replay = c.replayseed ? 1 : 0;
+    S.accum_f64 = f64 ? 1 : 0;
+    S.reclen = reclen_dev;
+    S.nmed_ppath = M;
+    S.replayseed = B.rseed;
+    S.replayweight = B.rweight;
+    S.replaytime = B.rtime;
+    S.f64 = B.f64;
+    S.f32a = B.f32;
+    S.f32b = B.f32 ? B.f32 + P.flen : nullptr;
+    S.detp = B.detp;
+    S.seeds = B.seeds;
+    S.detcount = B.detcount;
+    S.maxdet = (unsigned)maxdet;
+    S.energy = B.energy;
+    S.counters = B.counters;
+    S.photon_weight = B.pw;
+    S.photon_steps = B.ps;
+    S.photon_det = B.pd;
+    return MMCGB_OK;
+}
+
+// Reads back one simulation and runs the output stage.
+int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_result* res, cudaStream_t stream,
+               unsigned long long launched) {
+    SimBuffers& B = P.buf;
+    unsigned detected = 0;
+    double energy[2] = {0, 0};
+    unsigned long long counters[2] = {0, 0};
+    CK(cudaMemcpyAsync(&detected, B.detcount, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(energy, B.energy, sizeof(energy), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(counters, B.counters, sizeof(counters), cudaMemcpyDeviceToHost, stream));
+    const size_t saved = std::min<size_t>(detected, c.issavedet ? c.maxdetphoton : 0);
+    std::vector<double> raw;
+    std::vector<float> raw32;
+    const bool f64 = c.accum_f64 != 0;
+    const bool direct = res->field && f64 && !c.basisorder;  // raw layout == element output layout
+    if (res->field) {
+        if (direct) {
+            CK(cudaMemcpyAsync(res->field, B.f64, sizeof(double) * P.flen, cudaMemcpyDeviceToHost, stream));
+        } else if (f64) {
+            raw.resize(P.flen);
+            CK(cudaMemcpyAsync(raw.data(), B.f64, sizeof(double) * P.flen, cudaMemcpyDeviceToHost, stream));
+        } else {
+            raw32.resize(2 * P.flen);
+            CK(cudaMemcpyAsync(raw32.data(), B.f32, sizeof(float) * 2 * P.flen, cudaMemcpyDeviceToHost, stream));
+        }
+    }
+    if (res->detp && saved) CK(cudaMemcpyAsync(res->detp, B.detp, sizeof(float) * P.reclen * saved, cudaMemcpyDeviceToHost, stream));
+    if (res->seeds && saved && B.seeds) CK(cudaMemcpyAsync(res->seeds, B.seeds, 16 * saved, cudaMemcpyDeviceToHost, stream));
+    if (res->photon_weight) CK(cudaMemcpyAsync(res->photon_weight, B.pw, sizeof(float) * c.nphoton, cudaMemcpyDeviceToHost, stream));
+    if (res->photon_steps) CK(cudaMemcpyAsync(res->photon_steps, B.ps, sizeof(unsigned) * c.nphoton, cudaMemcpyDeviceToHost, stream));
+    if (res->photon_det) CK(cudaMemcpyAsync(res->photon_det, B.pd, sizeof(int) * c.nphoton, cudaMemcpyDeviceToHost, stream));
+    B.release();
+    CK(cudaStreamSynchronize(stream));
+    res->detected = detected;
+    res->saved = (uint32_t)saved;
+    res->reclen = P.reclen;
+    res->maxgate = P.maxgate;
+    res->energytot = (double)launched;  // every photon launches with weight 1
+    res->energyesc = energy[1];
+    res->raytet = counters[0];
+    res->aborted = counters[1];
+    res->normalizer = 1.0;
+    if (res->field) {
+        const double* src;
+        if (direct) {
+            src = res->field;
+        } else if (f64) {
+            src = raw.data();
+        } else {
+            raw.resize(P.flen);
+            for (size_t i = 0; i < P.flen; i++) raw[i] = (double)raw32[i] + (double)raw32[i + P.flen];
+            src = raw.data();
+        }
+        res->normalizer = normalize_output(mesh->host, c, P.maxgate, src, res->energytot, res->energyesc, res->field);
+    }
+    if (res->aborted) return fail(MMCGB_E_BUDGET, "some photons exceeded the per-photon step budget");
+    return MMCGB_OK;
+}
+
+}  // namespace
+
+struct mmcgb_session {
+    mmcgb_mesh* mesh = nullptr;
+    mmcgb_config cfg;
+    Prepared P;
+    cudaStream_t stream = nullptr;
+    unsigned long long* work = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    unsigned long long launched = 0;
+    int launches = 0;
+    LaunchShape shape{0, 0};
+};
+
+namespace {
+
+void free_mesh_device(mmcgb_mesh* m) {
+    if (m->rec) cudaFree(m->rec);
+    if (m->elem) cudaFree(m->elem);
+    if (m->node) cudaFree(m->node);
+    if (m->label) cudaFree(m->label);
+    m->rec = nullptr;
+    m->elem = nullptr;
+    m->node = nullptr;
+    m->label = nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t mmcgb_abi_version(void) { return MMCGB_ABI_VERSION; }
+
+const char* mmcgb_last_error(void) { return g_err.c_str(); }
+
+void mmcgb_config_defaults(mmcgb_config* c) {
+    std::memset(c, 0, sizeof(*c));
+    c->seed = 0x623F9A9E;
+    c->srcdir[2] = 1.f;
+    c->tstart = 0.f;
+    c->tend = 5e-9f;
+    c->tstep = 5e-9f;
+    c->isreflect = 1;
+    c->isnormalized = 1;
+    c->basisorder = 1;
+    c->minenergy = 1e-6f;
+    c->roulettesize = 10.f;
+    c->nout = 1.f;
+    c->unitinmm = 1.f;
+    c->outputtype = MMCGB_OUT_FLUX;
+    c->maxdetphoton = 1000000;
+    c->accum_f64 = 1;
+}
+
+int32_t mmcgb_mesh_create(const mmcgb_mesh_desc* desc, int32_t device, mmcgb_mesh** out) {
+    if (!desc || !out) return fail(MMCGB_E_ARG, "null argument");
+    *out = nullptr;
+    std::unique_ptr<mmcgb_mesh> m(new mmcgb_mesh());
+    std::string err;
+    int rc = prepare_mesh(*desc, m->host, err);
+    if (rc) return fail(rc, err);
+    m->device = device;
+    CK(cudaSetDevice(device));
+    std::vector<TetRec> rec;
+    pack_records(m->host, rec);
+    std::vector<float4> node(m->host.nn);
+    for (int i = 0; i < m->host.nn; i++)
+        node[i] = make_float4(m->host.node[3 * (size_t)i], m->host.node[3 * (size_t)i + 1], m->host.node[3 * (size_t)i + 2], 0.f);
+    cudaError_t e;
+    if ((e = cudaMalloc((void**)&m->rec, sizeof(TetRec) * rec.size())) != cudaSuccess ||
+        (e = cudaMalloc((void**)&m->elem, sizeof(int4) * m->host.ne)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&m->node, sizeof(float4) * m->host.nn)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&m->label, sizeof(int) * m->host.ne)) != cudaSuccess ||
+        (e = cudaMemcpy(m->rec, rec.data(), sizeof(TetRec) * rec.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(m->elem, m->host.elem.data(), sizeof(int4) * m->host.ne, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(m->node, node.data(), sizeof(float4) * m->host.nn, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(m->label, m->host.label.data(), sizeof(int) * m->host.ne, cudaMemcpyHostToDevice)) != cudaSuccess) {
+        free_mesh_device(m.get());
+        return cuda_fail(e, "mesh upload");
+    }
+    *out = m.release();
+    return MMCGB_OK;
+}
+
+int32_t mmcgb_mesh_destroy(mmcgb_mesh* m) {
+    if (!m) return MMCGB_OK;
+    cudaSetDevice(m->device);
+    free_mesh_device(m);
+    delete m;
+    return MMCGB_OK;
+}
+
+int32_t mmcgb_mesh_info(const mmcgb_mesh* m, int32_t* nn, int32_t* ne, int32_t* nf) {
+    if (!m) return fail(MMCGB_E_ARG, "null mesh");
+    if (nn) *nn = m->host.nn;
+    if (ne) *ne = m->host.ne;
+    if (nf) *nf = m->host.nf;
+    return MMCGB_OK;
+}
+
+int32_t mmcgb_mesh_export(const mmcgb_mesh* m, int32_t* elem, int32_t* facenb, float* evol, float* nvol) {
+    if (!m) return fail(MMCGB_E_ARG, "null mesh");
+    const HostMesh& h = m->host;
+    if (elem) std::memcpy(elem, h.elem.data(), sizeof(int) * h.elem.size());
+    if (facenb) std::memcpy(facenb, h.facenb.data(), sizeof(int) * h.facenb.size());
+    if (evol) std::memcpy(evol, h.evol.data(), sizeof(float) * h.evol.size());
+    if (nvol) std::memcpy(nvol, h.nvol.data(), sizeof(float) * h.nvol.size());
+    return MMCGB_OK;
+}
+
+int32_t mmcgb_mesh_locate(const mmcgb_mesh* m, const float p[3]) {
+    if (!m || !p) return 0;
+    return locate(m->host, p);
+}
+
+int32_t mmcgb_session_begin(mmcgb_mesh* mesh, const mmcgb_config* cfg, mmcgb_result* trace, mmcgb_session** out) {
+    if (!mesh || !cfg || !out) return fail(MMCGB_E_ARG, "null argument");
+    *out = nullptr;
+    CK(cudaSetDevice(mesh->device));
+    std::unique_ptr<mmcgb_session> s(new mmcgb_session());
+    s->mesh = mesh;
+    s->cfg = *cfg;
+    CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    int rc = prepare_sim(mesh, *cfg, trace, s->stream, s->P);
+    if (rc == MMCGB_OK) {
+        cudaError_t e = cudaMallocAsync((void**)&s->work, sizeof(unsigned long long), s->stream);
+        if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
+        if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
+        if (e != cudaSuccess) rc = cuda_fail(e, "session setup");
+    }
+    if (rc) {
+        s->P.buf.release();
+        if (s->work) cudaFreeAsync(s->work, s->stream);
+        cudaStreamSynchronize(s->stream);
+        cudaStreamDestroy(s->stream);
+        return rc;
+    }
+    s->shape = default_shape(mesh->device, false);
+    if (cfg->threads > 0) s->shape.threads = std::max(32, std::min(cfg->threads, 128) / 32 * 32);
+    if (cfg->blocks > 0) s->shape.blocks = cfg->blocks;
+    *out = s.release();
+    return MMCGB_OK;
+}
+
+int32_t mmcgb_session_launch(mmcgb_session* s, uint64_t photon_offset, uint64_t nphoton) {
+    if (!s) return fail(MMCGB_E_ARG, "null session");
+    if (s->cfg.replayseed && (photon_offset != 0 || nphoton != s->cfg.nphoton))
+        return fail(MMCGB_E_ARG, "replay sessions run all replayed photons in one launch");
+    if ((s->P.buf.pw || s->P.buf.ps || s->P.buf.pd) && nphoton > s->cfg.nphoton)
+        return fail(MMCGB_E_ARG, "per-photon trace buffers hold cfg.nphoton photons");
+    CK(cudaSetDevice(s->mesh->device));
+    SimDev sim = s->P.sim;
+    sim.nphoton = nphoton;
+    sim.photon_offset = s->cfg.photon_offset + photon_offset;
+    CK(cudaEventRecord(s->ev0, s->stream));
+    CK(launch_plain(sim, s->work, s->shape, s->stream));
+    CK(cudaEventRecord(s->ev1, s->stream));
+    s->launched += nphoton;
+    s->launches++;
+    return MMCGB_OK;
+}
+
+int32_t mmcgb_session_sync(mmcgb_session* s, float* last_kernel_ms) {
+    if (!s) return fail(MMCGB_E_ARG, "null session");
+    CK(cudaSetDevice(s->mesh->device));
+    CK(cudaStreamSynchronize(s->stream));
+    if (last_kernel_ms) {
+        *last_kernel_ms = 0.f;
+        if (s->launches) CK(cudaEventElapsedTime(last_kernel_ms, s->ev0, s->ev1));
+    }
+    return MMCGB_OK;
+}
+
+int32_t mmcgb_session_end(mmcgb_session* s, mmcgb_result* res) {
+    if (!s) return fail(MMCGB_E_ARG, "null session");
+    cudaSetDevice(s->mesh->device);
+    int rc = MMCGB_OK;
+    if (res) {
+        rc = finish_sim(s->mesh, s->cfg, s->P, res, s->stream, s->launched);
+        float ms = 0.f;
+        if (s->launches && cudaEventElapsedTime(&ms, s->ev0, s->ev1) == cudaSuccess) res->kernel_ms = ms;
+    } else {
+        s->P.buf.release();
+    }
+    if (s->work) cudaFreeAsync(s->work, s->stream);
+    cudaStreamSynchronize(s->stream);
+    cudaEventDestroy(s->ev0);
+    cudaEventDestroy(s->ev1);
+    cudaStreamDestroy(s->stream);
+    delete s;
+    return rc;
+}
+
+int32_t mmcgb_simulate(mmcgb_mesh* mesh, const mmcgb_config* cfg, mmcgb_result* res) {
+    if (!mesh || !cfg || !res) return fail(MMCGB_E_ARG, "null argument");
+    mmcgb_session* s = nullptr;
+    int rc = mmcgb_session_begin(mesh, cfg, res, &s);
+    if (rc) return rc;
+    rc = mmcgb_session_launch(s, 0, cfg->nphoton);
+    if (rc) {
+        std::string msg = g_err;
+        mmcgb_session_end(s, nullptr);
+        return fail(rc, msg);
+    }
+    return mmcgb_session_end(s, res);
+}
+
+int32_t mmcgb_simulate_batch(int32_t n, mmcgb_mesh* const* meshes, const mmcgb_config* cfgs, mmcgb_result* res) {
+    if (n <= 0 || !meshes || !cfgs || !res) return fail(MMCGB_E_ARG, "null or empty batch");
+    const int device = meshes[0]->device;
+    for (int i = 0; i < n; i++)
+        if (!meshes[i] || meshes[i]->device != device) return fail(MMCGB_E_ARG, "batched meshes must live on one device");
+    CK(cudaSetDevice(device));
+    cudaStream_t stream;
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    std::vector<Prepared> P(n);
+    int rc = MMCGB_OK;
+    int nmed_stride = 0, reclen_max = 0, want_seed = 0;
+    std::vector<unsigned long long> cum(n);
+    unsigned long long total = 0;
+    for (int i = 0; i < n && rc == MMCGB_OK; i++) {
+        rc = prepare_sim(meshes[i], cfgs[i], &res[i], stream, P[i]);
+        if (rc) break;
+        nmed_stride = std::max(nmed_stride, cfgs[i].nmedia);
+        if (cfgs[i].issavedet) reclen_max = std::max(reclen_max, P[i].sim.reclen);
+        if (cfgs[i].issavedet && cfgs[i].issaveseed) want_seed = 1;
+        total += cfgs[i].nphoton;
+        cum[i] = total;
+    }
+    if (rc == MMCGB_OK && (size_t)n * nmed_stride * 16 > 40 * 1024) rc = fail(MMCGB_E_ARG, "batch media tables exceed shared memory; split the batch");
+    SimDev* dsims = nullptr;
+    unsigned long long* dcum = nullptr;
+    unsigned long long* work = nullptr;
+    cudaEvent_t ev0, ev1;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    if (rc == MMCGB_OK) {
+        std::vector<SimDev> sims(n);
+        for (int i = 0; i < n; i++) sims[i] = P[i].sim;
+        cudaError_t e = cudaMallocAsync((void**)&dsims, sizeof(SimDev) * n, stream);
+        if (e == cudaSuccess) e = cudaMallocAsync((void**)&dcum, sizeof(unsigned long long) * n, stream);
+        if (e == cudaSuccess) e = cudaMallocAsync((void**)&work, sizeof(unsigned long long), stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dsims, sims.data(), sizeof(SimDev) * n, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dcum, cum.data(), sizeof(unsigned long long) * n, cudaMemcpyHostToDevice, stream);
+        LaunchShape shape = default_shape(device, true);
+        if (cfgs[0].threads > 0) shape.threads = std::max(32, std::min(cfgs[0].threads, 128) / 32 * 32);
+        if (cfgs[0].blocks > 0) shape.blocks = cfgs[0].blocks;
+        if (e == cudaSuccess) e = cudaEventRecord(ev0, stream);
+        if (e == cudaSuccess) e = launch_batched(dsims, dcum, n, total, nmed_stride, reclen_max, want_seed, work, shape, stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ev1, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "batched photon engine");
+    }
+    float ms = 0.f;
+    if (rc == MMCGB_OK) cudaEventElapsedTime(&ms, ev0, ev1);
+    for (int i = 0; i < n; i++) {
+        if (rc == MMCGB_OK) {
+            int r = finish_sim(meshes[i], cfgs[i], P[i], &res[i], stream, cfgs[i].nphoton);
+            res[i].kernel_ms = ms;
+            if (r) rc = r;
+        } else {
+            P[i].buf.release();
+        }
+    }
+    if (dsims) cudaFreeAsync(dsims, stream);
+    if (dcum) cudaFreeAsync(dcum, stream);
+    if (work) cudaFreeAsync(work, stream);
+    cudaStreamSynchronize(stream);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    cudaStreamDestroy(stream);
+    return rc;
+}
+
+int32_t mmcgb_run(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, int32_t device, mmcgb_result* res) {
+    mmcgb_mesh* m = nullptr;
+    int rc = mmcgb_mesh_create(desc, device, &m);
+    if (rc) return rc;
+    rc = mmcgb_simulate(m, cfg, res);
+    mmcgb_mesh_destroy(m);
+    return rc;
+}
+
+}  // extern "C"

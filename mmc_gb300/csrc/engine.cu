@@ -1,0 +1,644 @@
+// GB300 photon engine: persistent, flat per-lane state machine over the
+// reference's per-photon algorithm (src/mmc_core.cl:1851-2161, one ray-tet step
+// per loop trip instead of the reference's nested scatter/crossing loops, so
+// every lane of a warp does one step per trip whatever phase its photon is in).
+//
+// Each trip:  (1) lanes whose photon ended draw new photon ids from a global
+//             counter (one atomic per warp), (2) every live lane performs one
+//             branchless Badouel ray-tet step (src/mmc_core.cl:721-1226) with
+//             the deposit fused in, (3) the lane applies the reference's
+//             post-step control flow (fix/cross/reflect/exit/detect/roulette/
+//             scatter) as a state transition.
+// Compile with -fmad=false: the float sequence is the contract shared with the
+// CPU oracle, and explicit fmaf() appears only in devmath.cuh.
+#include <cooperative_groups.h>
+#include <cstdio>
+#include "devmath.cuh"
+#include "engine.h"
+
+namespace cg = cooperative_groups;
+
+namespace mmcgb {
+
+namespace {
+
+constexpr float kEps = 1e-6f;                     // src/mmc_mesh.h:70 (EPS in the CUDA build)
+constexpr float kRC0 = 3.335640951981520e-12f;    // 1/c0 in s/mm
+constexpr float kMaxAccum = 1000.f;               // src/mmc_core.cl:352
+constexpr float kRMinMus = 1e9f;
+constexpr float kFixPhoton = 1e-3f;
+constexpr int kMaxTrial = 3;
+constexpr int kIdUndef = 0x7FFFFFFF;
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+enum Mode : int { M_NEED = 0, M_OUTER = 1, M_INNER = 2, M_FIXIN = 3, M_DONE = 4 };
+
+struct Lane {
+    float px, py, pz, vx, vy, vz;
+    float weight, ptime, slen, Lmove, slen0, oldw;
+    unsigned oldidx;
+    int eid, faceid, isend, hit, label, nbword;
+    int fixcount, mode;
+    unsigned steps;
+    unsigned long long t0, t1;
+    unsigned long long pid;  // photon index inside its simulation
+    int sim;
+};
+
+__device__ __forceinline__ int decode_nb(int w) { return (w << 8) >> 8; }
+__device__ __forceinline__ int decode_label(int w) { return (int)((unsigned)w >> 24); }
+
+__device__ __forceinline__ void deposit(const SimDev& S, unsigned idx, float val) {
+    if (S.accum_f64) {
+        atomicAdd(S.f64 + idx, (double)val);
+        return;
+    }
+    // Float accumulation with the reference's second buffer for running sums
+    // above MAX_ACCUM (src/mmc_core.cl:880-912).  The reference moves `old` out
+    // with a subtraction; when several lanes of a warp cross the threshold at
+    // once they all subtract and drive the first buffer far negative, where
+    // later small deposits lose their low bits.  An atomic exchange moves the
+    // whole current content instead, so the first buffer stays below ~1000.
+    const float old = atomicAdd(S.f32a + idx, val);
+    if (old > kMaxAccum) {
+        const float moved = atomicExch(S.f32a + idx, 0.f);
+        if (moved != 0.f) atomicAdd(S.f32b + idx, moved);
+    }
+}
+
+// One branchless Badouel step with fused deposit.  Requires 1 <= L.eid <= ne.
+__device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const float4* med) {
+    const TetRec* R = S.rec + (L.eid - 1);
+    const float4 nx = __ldg(&R->nx);
+    const float4 ny = __ldg(&R->ny);
+    const float4 nz = __ldg(&R->nz);
+    const float4 nd = __ldg(&R->nd);
+    const int4 nb = __ldg(&R->nb);
+    L.hit = 0;
+    L.faceid = -1;
+    L.isend = 0;
+    float S0 = ((L.vx * nx.x) + (L.vy * ny.x)) + (L.vz * nz.x);
+    float S1 = ((L.vx * nx.y) + (L.vy * ny.y)) + (L.vz * nz.y);
+    float S2 = ((L.vx * nx.z) + (L.vy * ny.z)) + (L.vz * nz.z);
+    float S3 = ((L.vx * nx.w) + (L.vy * ny.w)) + (L.vz * nz.w);
+    float T0 = nd.x - (((L.px * nx.x) + (L.py * ny.x)) + (L.pz * nz.x));
+    float T1 = nd.y - (((L.px * nx.y) + (L.py * ny.y)) + (L.pz * nz.y));
+    float T2 = nd.z - (((L.px * nx.z) + (L.py * ny.z)) + (L.pz * nz.z));
+    float T3 = nd.w - (((L.px * nx.w) + (L.py * ny.w)) + (L.pz * nz.w));
+    T0 = (S0 > 0.f) ? (T0 / S0) : 1e10f;
+    T1 = (S1 > 0.f) ? (T1 / S1) : 1e10f;
+    T2 = (S2 > 0.f) ? (T2 / S2) : 1e10f;
+    T3 = (S3 > 0.f) ? (T3 / S3) : 1e10f;
+    const float Lmin = fminf(fminf(fminf(T0, T1), T2), T3);
+    // faceorder {1,3,2,0,-1} (src/mmc_mesh.c:95)
+    int faceid = (Lmin == 1e10f) ? -1 : (Lmin == T0 ? 1 : (Lmin == T1 ? 3 : (Lmin == T2 ? 2 : 0)));
+    L.faceid = faceid;
+    if (faceid >= 0 && Lmin >= 0.f) {
+        L.nbword = (faceid == 0) ? nb.x : (faceid == 1) ? nb.y : (faceid == 2) ? nb.z : nb.w;
+        const float4 prop = med[L.label];  // mua mus g n
+        float currweight = L.weight;
+        float Lmove = (prop.y <= kEps) ? kRMinMus : L.slen / prop.y;
+        L.isend = (Lmin > Lmove);
+        Lmove = L.isend ? Lmove : Lmin;
+        L.hit = 1;
+        const float rc = prop.w * kRC0;
+        // (int)x > maxgate-1, written without the float->int conversion
+        if ((L.ptime + Lmove * rc - S.tstart) * S.Rtstep >= (float)S.maxgate) {
+            L.faceid = -2;
+            L.hit = 0;
+            Lmove = (S.tend - L.ptime) / rc - 1e-4f;
+        }
+        L.Lmove = Lmove;
+        const float att = mmc_expf(-prop.x * Lmove);
+        L.weight *= att;
+        const int ot = S.outputtype;
+        if (S.replay) {
+            const float rw = __ldg(S.replayweight + L.pid);
+            if (ot == OT_WL || ot == OT_JACOBIAN) {
+                currweight = Lmove;
+                currweight *= rw;
+                currweight += L.weight;
+            } else if (ot == OT_WP) {
+                currweight = (L.slen0 < kEps) ? 1.f : Lmove * prop.y / L.slen0;
+                currweight *= rw;
+                currweight += L.weight;
+            }
+        }
+        L.slen -= Lmove * prop.y;
+        float ww = currweight - L.weight;
+        L.ptime += Lmove * rc;
+        float gf;
+        if (S.replay && (ot == OT_WL || ot == OT_WP))
+            gf = __ldg(S.replaytime + L.pid) * S.Rtstep;
+        else
+            gf = (L.ptime - S.tstart) * S.Rtstep;
+        // min((int)gf, maxgate-1), clamped at 0 so that no index leaves the buffer
+        int gate = (gf < (float)(S.maxgate - 1)) ? (int)gf : S.maxgate - 1;
+        gate = max(gate, 0);
+        if (ot != OT_ENERGY && ot != OT_WP && ot != OT_WL)
+            ww = (prop.x < kEps) ? (currweight * Lmove) : (ww / prop.x);
+        const unsigned newidx = (unsigned)(L.eid - 1) + (unsigned)(gate * S.ne);
+        if (L.oldidx == (unsigned)kIdUndef) L.oldidx = newidx;
+        if (newidx != L.oldidx) {
+            if (L.oldw > 0.f) deposit(S, L.oldidx, L.oldw);
+            L.oldidx = newidx;
+            L.oldw = ww;
+        } else {
+            L.oldw += ww;
+        }
+        if (L.faceid == -2 || !L.isend) {
+            deposit(S, newidx, L.oldw);
+            L.oldw = 0.f;
+        }
+        L.px = L.px + Lmove * L.vx;
+        L.py = L.py + Lmove * L.vy;
+        L.pz = L.pz + Lmove * L.vz;
+    }
+    L.slen = (L.faceid == -2) ? 0.f : L.slen;
+}
+
+// src/mmc_core.cl:1390-1402
+__device__ __forceinline__ void fixphoton(Lane& L, const SimDev& S) {
+    const int4 e = __ldg(S.elem + (L.eid - 1));
+    float cx = 0.f, cy = 0.f, cz = 0.f;
+    const int ids[4] = {e.x, e.y, e.z, e.w};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float4 p = __ldg(S.node + (ids[i] - 1));
+        cx += p.x;
+        cy += p.y;
+        cz += p.z;
+    }
+    L.px += (cx * 0.25f - L.px) * kFixPhoton;
+    L.py += (cy * 0.25f - L.py) * kFixPhoton;
+    L.pz += (cz * 0.25f - L.pz) * kFixPhoton;
+}
+
+// Fresnel / total internal reflection, src/mmc_core.cl:1247-1303.  Returns the
+// element the photon continues in (oldeid when reflected).
+__device__ __forceinline__ int reflectray(Lane& L, const SimDev& S, const float4* med, int oldeid,
+                                          int oldlabel, int eid, int newlabel, int faceid) {
+    const TetRec* R = S.rec + (oldeid - 1);
+    const int fi = (faceid == 0) ? 3 : (faceid == 1) ? 0 : (faceid == 2) ? 2 : 1;  // ifaceorder
+    const float* fx = reinterpret_cast<const float*>(&R->nx);
+    const float* fy = reinterpret_cast<const float*>(&R->ny);
+    const float* fz = reinterpret_cast<const float*>(&R->nz);
+    const float pnx = __ldg(fx + fi), pny = __ldg(fy + fi), pnz = __ldg(fz + fi);
+    const float Icos = fabsf(((L.vx * pnx) + (L.vy * pny)) + (L.vz * pnz));
+    const float n1 = (oldeid != eid) ? med[oldlabel].w : S.nout;
+    const float n2 = (eid > 0) ? med[newlabel].w : S.nout;
+    float tmp0 = n1 * n1;
+    float tmp1 = n2 * n2;
+    float tmp2 = 1.f - tmp0 / tmp1 * (1.f - Icos * Icos);
+    if (tmp2 > 0.f && !((eid <= 0) && (S.isreflect == BC_MIRROR))) {
+        float Re = tmp0 * Icos * Icos + tmp1 * tmp2;
+        tmp2 = sqrtf(tmp2);
+        float Im = 2.f * n1 * n2 * Icos * tmp2;
+        float Rtotal = (Re - Im) / (Re + Im);
+        Re = tmp1 * Icos * Icos + tmp0 * tmp2 * tmp2;
+        Rtotal = (Rtotal + (Re - Im) / (Re + Im)) * 0.5f;
+        if (rng_next(L.t0, L.t1) <= Rtotal) {
+            const float k = -2.f * Icos;
+            L.vx += k * pnx;
+            L.vy += k * pny;
+            L.vz += k * pnz;
+            eid = oldeid;
+        } else if ((S.isspecular == 2) && (eid == 0)) {
+        } else {
+            const float k = -Icos;
+            L.vx += k * pnx;
+            L.vy += k * pny;
+            L.vz += k * pnz;
+            const float q = n1 / n2;
+            L.vx = tmp2 * pnx + q * L.vx;
+            L.vy = tmp2 * pny + q * L.vy;
+            L.vz = tmp2 * pnz + q * L.vz;
+        }
+    } else {
+        const float k = -2.f * Icos;
+        L.vx += k * pnx;
+        L.vy += k * pny;
+        L.vz += k * pnz;
+        eid = oldeid;
+    }
+    const float inv = 1.f / sqrtf(L.vx * L.vx + L.vy * L.vy + L.vz * L.vz);
+    L.vx *= inv;
+    L.vy *= inv;
+    L.vz *= inv;
+    return eid;
+}
+
+// Henyey-Greenstein scatter + direction rotation, src/mmc_core.cl:1307-1377.
+__device__ __forceinline__ float next_scatter(Lane& L, float g, float& ctheta_out) {
+    const float nextslen = -mmc_logf(rng_next(L.t0, L.t1) + kEps);
+    float sphi, cphi, stheta, ctheta;
+    mmc_sincos2pi(rng_next(L.t0, L.t1), sphi, cphi);
+    if (g > kEps) {
+        float tmp0 = (1.f - g * g) / (1.f - g + 2.f * g * rng_next(L.t0, L.t1));
+        tmp0 *= tmp0;
+        tmp0 = (1.f + g * g - tmp0) / (2.f * g);
+        tmp0 = fmaxf(-1.f, fminf(tmp0, 1.f));
+        stheta = sqrtf(1.f - tmp0 * tmp0);
+        ctheta = tmp0;
+    } else {
+        ctheta = 2.f * rng_next(L.t0, L.t1) - 1.f;
+        stheta = sqrtf(1.f - ctheta * ctheta);
+    }
+    float px, py, pz;
+    if (L.vz > -1.f + kEps && L.vz < 1.f - kEps) {
+        const float tmp0 = 1.f - L.vz * L.vz;
+        float tmp1 = 1.f / sqrtf(tmp0);
+        tmp1 = stheta * tmp1;
+        px = tmp1 * (L.vx * L.vz * cphi - L.vy * sphi) + L.vx * ctheta;
+        py = tmp1 * (L.vy * L.vz * cphi + L.vx * sphi) + L.vy * ctheta;
+        pz = -tmp1 * tmp0 * cphi + L.vz * ctheta;
+    } else {
+        px = stheta * cphi;
+        py = stheta * sphi;
+        pz = (L.vz > 0.f) ? ctheta : -ctheta;
+    }
+    const float inv = 1.f / sqrtf(px * px + py * py + pz * pz);
+    L.vx = px * inv;
+    L.vy = py * inv;
+    L.vz = pz * inv;
+    ctheta_out = ctheta;
+    return nextslen;
+}
+
+__device__ __forceinline__ int finddetector(const Lane& L, const SimDev& S) {
+    for (int i = 0; i < S.detnum; i++) {
+        const float4 d = __ldg(S.det + i);
+        if ((d.x - L.px) * (d.x - L.px) + (d.y - L.py) * (d.y - L.py) + (d.z - L.pz) * (d.z - L.pz) < d.w * d.w)
+            return i + 1;
+    }
+    return 0;
+}
+
+struct Tally {
+    float eesc;
+    unsigned raytet;
+    unsigned aborted;
+    int sim;
+};
+
+__device__ __forceinline__ void flush_tally(Tally& t, const SimDev& S) {
+    if (t.sim < 0) return;
+    if (t.eesc != 0.f) atomicAdd(S.energy + 1, (double)t.eesc);
+    if (t.raytet) atomicAdd(S.counters + 0, (unsigned long long)t.raytet);
+    if (t.aborted) atomicAdd(S.counters + 1, (unsigned long long)t.aborted);
+    t.eesc = 0.f;
+    t.raytet = 0;
+    t.aborted = 0;
+}
+
+struct SingleSim {
+    const SimDev& s;
+    __device__ __forceinline__ const SimDev& operator()(int) const { return s; }
+};
+struct ManySims {
+    const SimDev* s;
+    __device__ __forceinline__ const SimDev& operator()(int i) const { return s[i]; }
+};
+
+// Shared-memory layout: media[nsims_local * nmed_stride] | ppath[reclen_max][blockDim] |
+// seed0[2][blockDim] (u64)
+template <class Sims, bool BATCHED>
+__device__ __forceinline__ void engine_body(const Sims& sims, const unsigned long long* cum, int nsims,
+                                            unsigned long long total, int nmed_stride, int reclen_max,
+                                            int want_seed, unsigned long long* work_counter) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4* smed = reinterpret_cast<float4*>(smem_raw);
+    const int nmed_rows = nsims * nmed_stride;
+    for (int i = threadIdx.x; i < nmed_rows; i += blockDim.x) {
+        const int s = i / nmed_stride, r = i % nmed_stride;
+        const SimDev& S = sims(s);
+        smed[i] = (r < S.nmedia) ? __ldg(S.media + r) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    float* ppath = reinterpret_cast<float*>(smed + nmed_rows);
+    unsigned long long* seed0 = reinterpret_cast<unsigned long long*>(ppath + (size_t)reclen_max * blockDim.x);
+    if (((uintptr_t)seed0) & 7) seed0 = reinterpret_cast<unsigned long long*>((((uintptr_t)seed0) + 7) & ~(uintptr_t)7);
+    __syncthreads();
+
+    const int tid = threadIdx.x;
+    const int bdim = blockDim.x;
+    const unsigned lane = threadIdx.x & 31;
+    Lane L;
+    L.mode = M_NEED;
+    L.sim = 0;
+    L.pid = 0;
+    L.steps = 0;
+    Tally tally{0.f, 0u, 0u, -1};
+
+#define PP(i) ppath[(size_t)(i) * bdim + tid]
+
+    while (true) {
+        // ---- (1) hand out photons to lanes that need one ----
+        const unsigned need = __ballot_sync(kFull, L.mode == M_NEED);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0;
+            if ((int)lane == leader) base = atomicAdd(work_counter, (unsigned long long)__popc(need));
+            base = __shfl_sync(kFull, base, leader);
+            if (L.mode == M_NEED) {
+                const unsigned long long gid = base + __popc(need & ((1u << lane) - 1u));
+                if (gid >= total) {
+                    L.mode = M_DONE;
+                } else {
+                    int s = 0;
+                    if (BATCHED) {
+                        int lo = 0, hi = nsims - 1;
+                        while (lo < hi) {
+                            const int mid = (lo + hi) >> 1;
+                            if (gid < cum[mid]) hi = mid; else lo = mid + 1;
+                        }
+                        s = lo;
+                    }
+                    const SimDev& S = sims(s);
+                    if (s != tally.sim) {
+                        if (tally.sim >= 0) flush_tally(tally, sims(tally.sim));
+                        tally.sim = s;
+                    }
+                    L.sim = s;
+                    L.pid = BATCHED ? (gid - (s ? cum[s - 1] : 0ull)) : gid;
+                    // ---- launch (src/mmc_core.cl:1851-1906, pencil source) ----
+                    if (S.replay) {
+                        L.t0 = __ldg(S.replayseed + 2 * L.pid);
+                        L.t1 = __ldg(S.replayseed + 2 * L.pid + 1);
+                    } else {
+                        rng_seed(S.seed, S.photon_offset + L.pid, L.t0, L.t1);
+                    }
+                    if (want_seed) {
+                        seed0[tid] = L.t0;
+                        seed0[bdim + tid] = L.t1;
+                    }
+                    L.px = S.srcpos[0];
+                    L.py = S.srcpos[1];
+                    L.pz = S.srcpos[2];
+                    L.vx = S.srcdir[0];
+                    L.vy = S.srcdir[1];
+                    L.vz = S.srcdir[2];
+                    L.eid = S.e0;
+                    L.label = __ldg(S.label + (S.e0 - 1));
+                    L.faceid = 0;
+                    L.isend = 0;
+                    L.hit = 0;
+                    L.weight = 1.f;
+                    L.ptime = 0.f;
+                    L.Lmove = 0.f;
+                    L.slen0 = 0.f;
+                    L.oldw = 0.f;
+                    L.oldidx = (unsigned)kIdUndef;
+                    L.fixcount = 0;
+                    L.steps = 0;
+                    L.slen = -mmc_logf(rng_next(L.t0, L.t1) + kEps);
+                    if (S.issavedet) {
+                        for (int i = 0; i < S.reclen; i++) PP(i) = 0.f;
+                        PP(S.reclen - 1) = L.weight;
+                    }
+                    L.mode = M_OUTER;
+                }
+            }
+        }
+        if (__all_sync(kFull, L.mode == M_DONE)) break;
+        if (L.mode == M_DONE) continue;
+
+        const SimDev& S = sims(L.sim);
+        const float4* med = smed + (BATCHED ? L.sim * nmed_stride : 0);
+        const int M = S.nmedia - 1;
+
+        // ---- (2) one ray-tet step ----
+        const bool bad_elem = (L.eid < 1 || L.eid > S.ne);  // defensive: never expected
+        if (!bad_elem) raytet_step(L, S, med);
+        L.steps++;
+        tally.raytet++;
+        bool ended = false;
+        const bool aborted = bad_elem || (L.steps > S.step_budget);
+        // after_inner: 0 = continue stepping, 1 = go to exit/scatter decision
+        int decide = 0;
+        bool cross = false;
+
+        // ---- (3) post-step control flow ----
+        if (!aborted) {
+            const int mode = L.mode;
+            if (mode == M_OUTER) {
+                if (!L.hit) {
+                    if (L.faceid == -2) {
+                        ended = true;
+                    } else if (L.fixcount++ < kMaxTrial) {
+                        fixphoton(L, S);
+                    } else {
+                        L.eid = kIdUndef;
+                        L.faceid = -1;
+                        decide = 1;
+                    }
+                } else {
+                    if (S.issavedet && L.Lmove > 0.f && L.label > 0) PP(M + L.label - 1) += L.Lmove;
+                    if (L.faceid >= 0 && !L.isend) cross = true; else decide = 1;
+                }
+            } else {  // M_INNER or M_FIXIN
+                if (S.issavedet && L.Lmove > 0.f && L.label > 0) PP(M + L.label - 1) += L.Lmove;
+                if (mode == M_INNER) {
+                    if (L.faceid == -2) {
+                        decide = 1;
+                    } else {
+                        L.fixcount = 0;
+                        if (!L.hit) {
+                            L.fixcount = 1;
+                            fixphoton(L, S);
+                            L.mode = M_FIXIN;
+                        } else if (L.faceid >= 0 && !L.isend) {
+                            cross = true;
+                        } else {
+                            decide = 1;
+                        }
+                    }
+                } else {  // M_FIXIN
+                    if (!L.hit) {
+                        if (L.fixcount++ < kMaxTrial) {
+                            fixphoton(L, S);
+                        } else {
+                            L.eid = kIdUndef;
+                            decide = 1;
+                        }
+                    } else if (L.faceid >= 0 && !L.isend) {
+                        cross = true;
+                    } else {
+                        decide = 1;
+                    }
+                }
+            }
+
+            if (cross) {
+                // face crossing, src/mmc_core.cl:1950-1993
+                const int oldeid = L.eid, oldlabel = L.label;
+                int eid = decode_nb(L.nbword);
+                int nlabel = decode_label(L.nbword);
+                if (S.isreflect) {
+                    const float nold = med[oldlabel].w;
+                    if (eid <= 0 || med[nlabel].w != nold) {
+                        if (!(eid <= 0 && (((nold == S.nout) && (S.isreflect != BC_MIRROR)) || (S.isreflect == BC_ABSORBEXT)))) {
+                            eid = reflectray(L, S, med, oldeid, oldlabel, eid, nlabel, L.faceid);
+                            if (eid == oldeid) nlabel = oldlabel;
+                        }
+                    }
+                }
+                L.eid = eid;
+                if (eid <= 0) {
+                    decide = 1;
+                } else {
+                    if (oldlabel == 0 && nlabel != 0 && !S.voidtime) L.ptime = 0.f;
+                    if (oldlabel != 0 && nlabel == 0) {
+                        L.eid = 0;
+                        decide = 1;
+                    } else {
+                        L.label = nlabel;
+                        L.mode = M_INNER;
+                    }
+                }
+            }
+
+            if (decide) {
+                // exit / roulette / scatter, src/mmc_core.cl:2033-2138
+                if (L.eid <= 0 || !L.hit) {
+                    if (L.eid != kIdUndef && S.issavedet && S.issaveexit) {
+                        PP(S.reclen - 7) = L.px;
+                        PP(S.reclen - 6) = L.py;
+                        PP(S.reclen - 5) = L.pz;
+                        PP(S.reclen - 4) = L.vx;
+                        PP(S.reclen - 3) = L.vy;
+                        PP(S.reclen - 2) = L.vz;
+                    }
+                    int detid = 0;
+                    if (S.issavedet && L.eid <= 0) {
+                        detid = finddetector(L, S);
+                        if (detid) {
+                            // ballot-compacted slot reservation: one atomic per group of detecting lanes
+                            cg::coalesced_group grp = cg::coalesced_threads();
+                            unsigned base = 0;
+                            if (grp.thread_rank() == 0) base = atomicAdd(S.detcount, grp.size());
+                            base = grp.shfl(base, 0);
+                            const unsigned slot = base + grp.thread_rank();
+                            if (slot < S.maxdet) {
+                                if (S.seeds && want_seed) {
+                                    S.seeds[2 * (size_t)slot] = seed0[tid];
+                                    S.seeds[2 * (size_t)slot + 1] = seed0[bdim + tid];
+                                }
+                                float* rec = S.detp + (size_t)slot * (S.reclen + 1);
+                                rec[0] = (float)detid;
+                                for (int i = 0; i < S.reclen; i++) rec[1 + i] = PP(i);
+                            }
+                        }
+                    }
+                    if (S.photon_det) S.photon_det[L.pid] = detid;
+                    ended = true;
+                } else {
+                    bool killed = false;
+                    if (S.roulette_on && (S.minenergy > 0.f) && (L.weight < S.minenergy)) {
+                        if (rng_next(L.t0, L.t1) * S.roulettesize <= 1.f)
+                            L.weight *= S.roulettesize;
+                        else
+                            killed = true;
+                    }
+                    if (killed) {
+                        if (S.photon_det) S.photon_det[L.pid] = 0;
+                        ended = true;
+                    } else {
+                        float ctheta;
+                        const int tp = L.label;
+                        L.slen0 = next_scatter(L, med[tp].z, ctheta);
+                        L.slen = L.slen0;
+                        if (S.issavedet && tp > 0) {
+                            if (S.ismomentum) PP(2 * M + tp - 1) += (1.f - ctheta);
+                            PP(tp - 1) += 1.f;
+                        }
+                        L.mode = M_OUTER;
+                    }
+                }
+            } else if (ended) {
+                if (S.photon_det) S.photon_det[L.pid] = 0;
+            }
+        } else {
+            ended = true;
+            tally.aborted++;
+            if (S.photon_det) S.photon_det[L.pid] = 0;
+        }
+        if (ended) {
+            tally.eesc += L.weight;
+            if (S.photon_weight) S.photon_weight[L.pid] = L.weight;
+            if (S.photon_steps) S.photon_steps[L.pid] = L.steps;
+            L.mode = M_NEED;
+        }
+    }
+#undef PP
+    if (tally.sim >= 0) flush_tally(tally, sims(tally.sim));
+}
+
+__global__ void __launch_bounds__(128, 8) photon_engine_plain(const __grid_constant__ SimDev sim,
+                                                           unsigned long long* work_counter, int reclen_max,
+                                                           int want_seed) {
+    SingleSim acc{sim};
+    engine_body<SingleSim, false>(acc, nullptr, 1, sim.nphoton, sim.nmedia, reclen_max, want_seed, work_counter);
+}
+
+__global__ void __launch_bounds__(128, 8) photon_engine_batched(const SimDev* __restrict__ sims,
+                                                             const unsigned long long* __restrict__ cum,
+                                                             int nsims, unsigned long long total,
+                                                             int nmed_stride, unsigned long long* work_counter,
+                                                             int reclen_max, int want_seed) {
+    ManySims acc{sims};
+    engine_body<ManySims, true>(acc, cum, nsims, total, nmed_stride, reclen_max, want_seed, work_counter);
+}
+
+size_t smem_bytes(int nmed_rows, int reclen_max, int threads, int want_seed) {
+    size_t b = (size_t)nmed_rows * sizeof(float4) + (size_t)reclen_max * threads * sizeof(float);
+    b = (b + 7) & ~(size_t)7;
+    if (want_seed) b += (size_t)2 * threads * sizeof(unsigned long long);
+    return b;
+}
+
+}  // namespace
+
+LaunchShape default_shape(int device, bool batched) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    int per_sm = 0;
+    const int threads = 128;
+    if (batched)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_batched, threads, 4096);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_plain, threads, 1024);
+    if (per_sm < 1) per_sm = 1;
+    return LaunchShape{sms * per_sm, threads};
+}
+
+cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
+                         cudaStream_t stream) {
+    const int want_seed = (sim.issavedet && sim.seeds) ? 1 : 0;
+    const int reclen_max = sim.issavedet ? sim.reclen : 0;
+    const size_t smem = smem_bytes(sim.nmedia, reclen_max, shape.threads, want_seed);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(photon_engine_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(unsigned long long), stream);
+    if (e != cudaSuccess) return e;
+    photon_engine_plain<<<shape.blocks, shape.threads, smem, stream>>>(sim, work_counter, reclen_max, want_seed);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
+                           unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
+                           unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream) {
+    const size_t smem = smem_bytes(nsims * nmed_stride, reclen_max, shape.threads, want_seed);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(photon_engine_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(unsigned long long), stream);
+    if (e != cudaSuccess) return e;
+    photon_engine_batched<<<shape.blocks, shape.threads, smem, stream>>>(sims, cum, nsims, total, nmed_stride,
+                                                                        work_counter, reclen_max, want_seed);
+    return cudaGetLastError();
+}
+
+}  // namespace mmcgb

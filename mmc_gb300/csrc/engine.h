@@ -1,0 +1,102 @@
+// Internal types shared by the host runtime (api.cpp, mesh.cpp) and the CUDA
+// photon engine (engine.cu).  Not part of the public C ABI (include/mmcgb.h).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mmcgb {
+
+// Output/physics enums follow the reference numbering (src/mmc_utils.h:92-110).
+enum OutputType { OT_FLUX = 0, OT_FLUENCE = 1, OT_ENERGY = 2, OT_JACOBIAN = 3, OT_WL = 4, OT_WP = 5 };
+enum Boundary { BC_NOREFLECT = 0, BC_REFLECT = 1, BC_ABSORBEXT = 2, BC_MIRROR = 3 };
+
+constexpr int kMaxMedia = 64;        // media rows (incl. background) staged in shared memory
+constexpr int kMaxSimsShared = 256;  // simulations whose media tables fit in one block's shared memory
+constexpr int kNbBits = 24;          // neighbour id bits in a packed face word
+constexpr int kMaxElem = (1 << (kNbBits - 1)) - 1;
+
+// One tetrahedron as the step kernel reads it: 80 bytes, 16-byte aligned.
+//   nx/ny/nz/nd : outward unit normals and plane offsets of the 4 faces
+//                 (face k of the reference normal table, src/mmc_mesh.c:1572-1601)
+//   nb          : for each face in neighbour order (src/mmc_highorder.cpp:50),
+//                 bits 0..23 = neighbour element (1-based, signed: <=0 is an
+//                 exterior face numbered -1,-2,...), bits 24..31 = the
+//                 neighbour's medium label (0 for exterior faces).
+struct __align__(16) TetRec {
+    float4 nx, ny, nz, nd;
+    int4 nb;
+};
+static_assert(sizeof(TetRec) == 80, "TetRec must be 80 bytes");
+
+// Per-simulation parameter block.  Plain launches pass it by value as a
+// __grid_constant__ kernel parameter; batched launches read an array of them
+// from global memory.
+struct SimDev {
+    // mesh
+    const TetRec* rec;
+    const int4* elem;      // 1-based node ids (after orientation fix)
+    const float4* node;    // xyz + pad
+    const int* label;      // medium label per element
+    int ne;
+    int e0;                // initial element (1-based)
+    int nmedia;
+    int detnum;
+    const float4* media;   // nmedia rows: mua mus g n
+    const float4* det;     // detnum rows: x y z r
+    // photons
+    unsigned long long nphoton;
+    unsigned long long photon_offset;
+    unsigned long long seed;
+    unsigned long long step_budget;
+    // source
+    float srcpos[3];
+    float srcdir[3];
+    // time gates
+    float tstart, tend, Rtstep;
+    int maxgate;
+    int roulette_on;       // (tend-tstart)*Rtstep <= 1, precomputed as the reference does
+    float minenergy, roulettesize, nout;
+    // switches
+    int isreflect, isspecular, voidtime;
+    int issavedet, issaveexit, ismomentum, issaveseed;
+    int outputtype;
+    int replay;            // replay mode (seeds from a previous run)
+    int accum_f64;
+    int reclen;            // detected-photon columns excluding the detector id
+    int nmed_ppath;        // M = nmedia-1
+    // replay inputs
+    const unsigned long long* replayseed;  // 2 words per photon
+    const float* replayweight;
+    const float* replaytime;
+    // outputs
+    float* f32a;           // ne*maxgate (accum_f64 == 0)
+    float* f32b;           // overflow half
+    double* f64;           // ne*maxgate (accum_f64 == 1)
+    float* detp;           // maxdet * (reclen+1)
+    unsigned long long* seeds;  // maxdet * 2
+    unsigned int* detcount;
+    unsigned int maxdet;
+    double* energy;        // [0] launched, [1] escaped
+    unsigned long long* counters;  // [0] ray-tet tests, [1] aborted photons
+    // optional per-photon trace (parity tests)
+    float* photon_weight;
+    unsigned int* photon_steps;
+    int* photon_det;
+};
+
+struct LaunchShape {
+    int blocks;
+    int threads;
+};
+
+// Launches the photon engine for one simulation on `stream`.
+cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
+                         cudaStream_t stream);
+// Launches the batched engine over `nsims` simulations (`sims` in device memory,
+// `cum` = inclusive prefix sums of photon counts, length nsims).
+cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
+                           unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
+                           unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream);
+LaunchShape default_shape(int device, bool batched);
+
+}  // namespace mmcgb

@@ -1,0 +1,299 @@
+// Host-side mesh preparation for the photon engine: orientation fix and
+// volumes, face neighbours, face normals/plane offsets, exterior-face
+// numbering, packed 80-byte records, and point location for the source.
+// Compiled with -ffp-contract=off: the normals feed the bit-exact parity
+// contract with the CPU oracle.
+#include "mesh.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace mmcgb {
+
+// face tables of the reference (src/mmc_mesh.c:59-107, src/mmc_highorder.cpp:50)
+const int kOut[4][3] = {{0, 3, 1}, {3, 2, 1}, {0, 2, 3}, {0, 1, 2}};
+const int kFaceMap[4] = {2, 0, 1, 3};
+const int kIFaceOrder[4] = {3, 0, 2, 1};
+const int kFaceList[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
+
+namespace {
+
+struct F3 {
+    float x, y, z;
+};
+
+inline F3 node_at(const std::vector<float>& node, int i) {
+    return F3{node[3 * (size_t)i], node[3 * (size_t)i + 1], node[3 * (size_t)i + 2]};
+}
+
+// Face neighbours (src/mmc_highorder.cpp:128-159): element faces are matched by
+// their sorted node triple; facenb[4e+j] is the element sharing face j.
+void compute_facenb(int nn, int ne, const std::vector<int>& elem, std::vector<int>& facenb) {
+    const size_t nface = (size_t)ne * 4;
+    facenb.assign(nface, 0);
+    struct Key {
+        uint64_t hi;
+        uint32_t lo;
+        uint32_t slot;
+    };
+    std::vector<Key> keys(nface);
+    const bool packed = nn < (1 << 21);
+    for (int i = 0; i < ne; i++)
+        for (int j = 0; j < 4; j++) {
+            int v[3] = {elem[4 * (size_t)i + kFaceList[j][0]], elem[4 * (size_t)i + kFaceList[j][1]],
+                        elem[4 * (size_t)i + kFaceList[j][2]]};
+            std::sort(v, v + 3);
+            Key& k = keys[4 * (size_t)i + j];
+            if (packed) {
+                k.hi = ((uint64_t)v[0] << 42) | ((uint64_t)v[1] << 21) | (uint64_t)v[2];
+                k.lo = 0;
+            } else {
+                k.hi = ((uint64_t)(uint32_t)v[0] << 32) | (uint32_t)v[1];
+                k.lo = (uint32_t)v[2];
+            }
+            k.slot = (uint32_t)(4 * (size_t)i + j);
+        }
+    std::sort(keys.begin(), keys.end(), [](const Key& a, const Key& b) {
+        if (a.hi != b.hi) return a.hi < b.hi;
+        if (a.lo != b.lo) return a.lo < b.lo;
+        return a.slot < b.slot;
+    });
+    for (size_t n = 0; n + 1 < nface; n++) {
+        const Key& a = keys[n];
+        const Key& b = keys[n + 1];
+        if (a.hi == b.hi && a.lo == b.lo) {
+            facenb[a.slot] = (int)(b.slot >> 2) + 1;
+            facenb[b.slot] = (int)(a.slot >> 2) + 1;
+            n++;
+        }
+    }
+}
+
+}  // namespace
+
+int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
+    if (d.nn <= 0 || d.ne <= 0 || !d.node || !d.elem || !d.label) {
+        err = "mesh needs nn > 0, ne > 0 and node/elem/label arrays";
+        return MMCGB_E_ARG;
+    }
+    if (d.ne > kMaxElem) {
+        err = "mesh has more elements than the packed record format holds (8,388,607)";
+        return MMCGB_E_MESH;
+    }
+    m.nn = d.nn;
+    m.ne = d.ne;
+    m.node.assign(d.node, d.node + 3 * (size_t)d.nn);
+    m.elem.assign(d.elem, d.elem + 4 * (size_t)d.ne);
+    m.label.assign(d.label, d.label + (size_t)d.ne);
+    m.evol.assign(d.ne, 0.f);
+    m.nvol.assign(d.nn, 0.f);
+    int maxlabel = 0;
+    for (int i = 0; i < d.ne; i++) {
+        if (m.label[i] < 0 || m.label[i] > 255) {
+            err = "medium labels must be in 0..255";
+            return MMCGB_E_MESH;
+        }
+        maxlabel = std::max(maxlabel, m.label[i]);
+    }
+    m.maxlabel = maxlabel;
+    // volumes and orientation (src/mmc_mesh.c:910-974): swap nodes 3,4 of a
+    // negatively oriented tet so that the face tables give outward normals
+    for (int i = 0; i < d.ne; i++) {
+        int* e = &m.elem[4 * (size_t)i];
+        for (int j = 0; j < 4; j++)
+            if (e[j] < 1 || e[j] > d.nn) {
+                err = "element " + std::to_string(i + 1) + " references a node outside 1..nn";
+                return MMCGB_E_MESH;
+            }
+        F3 n0 = node_at(m.node, e[0] - 1), n1 = node_at(m.node, e[1] - 1), n2 = node_at(m.node, e[2] - 1),
+           n3 = node_at(m.node, e[3] - 1);
+        float dx = n2.x - n3.x, dy = n2.y - n3.y, dz = n2.z - n3.z;
+        float v = n1.x * (n2.y * n3.z - n2.z * n3.y) - n1.y * (n2.x * n3.z - n2.z * n3.x) +
+                  n1.z * (n2.x * n3.y - n2.y * n3.x);
+        v += -n0.x * ((n2.y * n3.z - n2.z * n3.y) + n1.y * dz - n1.z * dy);
+        v += +n0.y * ((n2.x * n3.z - n2.z * n3.x) + n1.x * dz - n1.z * dx);
+        v += -n0.z * ((n2.x * n3.y - n2.y * n3.x) + n1.x * dy - n1.y * dx);
+        v = -v;
+        if (v < 0.f) {
+            std::swap(e[2], e[3]);
+            v = -v;
+        }
+        v *= (1.f / 6.f);
+        m.evol[i] = v;
+        if (m.label[i] == 0) continue;
+        for (int j = 0; j < 4; j++) m.nvol[e[j] - 1] += v * 0.25f;
+    }
+    if (d.facenb) {
+        m.facenb.assign(d.facenb, d.facenb + 4 * (size_t)d.ne);
+        for (size_t i = 0; i < m.facenb.size(); i++)
+            if (m.facenb[i] < 0 || m.facenb[i] > d.ne) {
+                err = "facenb entries must be 0 (exterior) or a 1-based element id";
+                return MMCGB_E_MESH;
+            }
+    } else {
+        compute_facenb(d.nn, d.ne, m.elem, m.facenb);
+    }
+    // outward unit normals and plane offsets (src/mmc_mesh.c:1572-1601)
+    m.normals.assign(16 * (size_t)d.ne, 0.f);
+    for (int i = 0; i < d.ne; i++) {
+        float* vn = &m.normals[16 * (size_t)i];
+        const int* e = &m.elem[4 * (size_t)i];
+        for (int j = 0; j < 4; j++) {
+            F3 a = node_at(m.node, e[kOut[j][0]] - 1);
+            F3 b = node_at(m.node, e[kOut[j][1]] - 1);
+            F3 c = node_at(m.node, e[kOut[j][2]] - 1);
+            F3 ab{b.x - a.x, b.y - a.y, b.z - a.z};
+            F3 ac{c.x - a.x, c.y - a.y, c.z - a.z};
+            F3 n{ab.y * ac.z - ab.z * ac.y, ab.z * ac.x - ab.x * ac.z, ab.x * ac.y - ab.y * ac.x};
+            float rn = (float)(1.f / std::sqrt((double)(n.x * n.x + n.y * n.y + n.z * n.z)));
+            n.x *= rn;
+            n.y *= rn;
+            n.z *= rn;
+            vn[j] = n.x;
+            vn[j + 4] = n.y;
+            vn[j + 8] = n.z;
+            vn[j + 12] = n.x * a.x + n.y * a.y + n.z * a.z;
+        }
+    }
+    // exterior faces numbered -1,-2,... (src/mmc_mesh.c:1466-1474)
+    int nf = 0;
+    for (size_t i = 0; i < m.facenb.size(); i++)
+        if (m.facenb[i] == 0) m.facenb[i] = -(++nf);
+    if (nf > kMaxElem + 1) {
+        err = "too many exterior faces for the packed record format";
+        return MMCGB_E_MESH;
+    }
+    m.nf = nf;
+    build_locator(m);
+    return MMCGB_OK;
+}
+
+void pack_records(const HostMesh& m, std::vector<TetRec>& rec) {
+    rec.resize(m.ne);
+    for (int i = 0; i < m.ne; i++) {
+        const float* vn = &m.normals[16 * (size_t)i];
+        TetRec& r = rec[i];
+        r.nx = make_float4(vn[0], vn[1], vn[2], vn[3]);
+        r.ny = make_float4(vn[4], vn[5], vn[6], vn[7]);
+        r.nz = make_float4(vn[8], vn[9], vn[10], vn[11]);
+        r.nd = make_float4(vn[12], vn[13], vn[14], vn[15]);
+        int w[4];
+        for (int j = 0; j < 4; j++) {
+            const int nbid = m.facenb[4 * (size_t)i + j];
+            const int lab = (nbid > 0) ? m.label[nbid - 1] : 0;
+            w[j] = (int)(((uint32_t)nbid & 0x00FFFFFFu) | ((uint32_t)lab << 24));
+        }
+        r.nb = make_int4(w[0], w[1], w[2], w[3]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// point location: the reference scans all elements and takes the first whose
+// bounding box and barycentric test enclose the point (src/mmc_mesh.c:1060-1090,
+// :1170-1205).  A uniform grid of bounding boxes gives the same answer (the
+// smallest qualifying index) without the O(ne) scan per request.
+// ---------------------------------------------------------------------------
+void build_locator(HostMesh& m) {
+    float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+    for (int i = 0; i < m.nn; i++)
+        for (int d = 0; d < 3; d++) {
+            lo[d] = std::min(lo[d], m.node[3 * (size_t)i + d]);
+            hi[d] = std::max(hi[d], m.node[3 * (size_t)i + d]);
+        }
+    int res = std::max(1, (int)std::cbrt((double)m.ne / 4.0));
+    res = std::min(res, 256);
+    LocGrid& g = m.grid;
+    g.res = res;
+    for (int d = 0; d < 3; d++) {
+        g.lo[d] = lo[d];
+        float span = hi[d] - lo[d];
+        g.inv[d] = span > 0 ? res / span : 0.f;
+    }
+    const size_t nbin = (size_t)res * res * res;
+    std::vector<uint32_t> count(nbin + 1, 0);
+    auto bin_range = [&](int e, int b0[3], int b1[3]) {
+        float mn[3] = {1e30f, 1e30f, 1e30f}, mx[3] = {-1e30f, -1e30f, -1e30f};
+        for (int j = 0; j < 4; j++)
+            for (int d = 0; d < 3; d++) {
+                float v = m.node[3 * (size_t)(m.elem[4 * (size_t)e + j] - 1) + d];
+                mn[d] = std::min(mn[d], v);
+                mx[d] = std::max(mx[d], v);
+            }
+        for (int d = 0; d < 3; d++) {
+            b0[d] = std::max(0, std::min(res - 1, (int)std::floor((mn[d] - g.lo[d]) * g.inv[d])));
+            b1[d] = std::max(0, std::min(res - 1, (int)std::floor((mx[d] - g.lo[d]) * g.inv[d])));
+        }
+    };
+    for (int e = 0; e < m.ne; e++) {
+        int b0[3], b1[3];
+        bin_range(e, b0, b1);
+        for (int z = b0[2]; z <= b1[2]; z++)
+            for (int y = b0[1]; y <= b1[1]; y++)
+                for (int x = b0[0]; x <= b1[0]; x++) count[((size_t)z * res + y) * res + x + 1]++;
+    }
+    for (size_t i = 0; i < nbin; i++) count[i + 1] += count[i];
+    g.start = count;
+    g.items.assign(count[nbin], 0);
+    std::vector<uint32_t> fill(count.begin(), count.end() - 1);
+    for (int e = 0; e < m.ne; e++) {
+        int b0[3], b1[3];
+        bin_range(e, b0, b1);
+        for (int z = b0[2]; z <= b1[2]; z++)
+            for (int y = b0[1]; y <= b1[1]; y++)
+                for (int x = b0[0]; x <= b1[0]; x++) g.items[fill[((size_t)z * res + y) * res + x]++] = (uint32_t)e;
+    }
+}
+
+static bool encloses(const HostMesh& m, int e, const float* p) {
+    const int* el = &m.elem[4 * (size_t)e];
+    double lo[3] = {1e30, 1e30, 1e30}, hi[3] = {-1e30, -1e30, -1e30};
+    for (int j = 0; j < 4; j++)
+        for (int d = 0; d < 3; d++) {
+            double v = m.node[3 * (size_t)(el[j] - 1) + d];
+            lo[d] = std::min(lo[d], v);
+            hi[d] = std::max(hi[d], v);
+        }
+    if (!(p[0] <= hi[0] && p[0] >= lo[0] && p[1] <= hi[1] && p[1] >= lo[1] && p[2] <= hi[2] && p[2] >= lo[2]))
+        return false;
+    float bary[4];
+    for (int i = 0; i < 4; i++) {
+        F3 a = node_at(m.node, el[kOut[i][0]] - 1);
+        F3 b = node_at(m.node, el[kOut[i][1]] - 1);
+        F3 c = node_at(m.node, el[kOut[i][2]] - 1);
+        F3 ab{b.x - a.x, b.y - a.y, b.z - a.z};
+        F3 ac{c.x - a.x, c.y - a.y, c.z - a.z};
+        F3 s{p[0] - a.x, p[1] - a.y, p[2] - a.z};
+        F3 n{ab.y * ac.z - ab.z * ac.y, ab.z * ac.x - ab.x * ac.z, ab.x * ac.y - ab.y * ac.x};
+        bary[kFaceMap[i]] = -(s.x * n.x + s.y * n.y + s.z * n.z);
+    }
+    for (int i = 0; i < 4; i++)
+        if (bary[i] < 0.f) return false;
+    return true;
+}
+
+int locate(const HostMesh& m, const float p[3]) {
+    const LocGrid& g = m.grid;
+    int b[3];
+    for (int d = 0; d < 3; d++) {
+        float f = (p[d] - g.lo[d]) * g.inv[d];
+        if (!(f >= -1e-3f * g.res) || !(f <= g.res * (1.f + 1e-3f))) return 0;
+        b[d] = std::max(0, std::min(g.res - 1, (int)std::floor(f)));
+    }
+    // a point on a bin boundary may belong to elements binned only in the
+    // neighbouring bin: look at every bin within one cell and take the minimum
+    int best = -1;
+    for (int z = std::max(0, b[2] - 1); z <= std::min(g.res - 1, b[2] + 1); z++)
+        for (int y = std::max(0, b[1] - 1); y <= std::min(g.res - 1, b[1] + 1); y++)
+            for (int x = std::max(0, b[0] - 1); x <= std::min(g.res - 1, b[0] + 1); x++) {
+                const size_t bin = ((size_t)z * g.res + y) * g.res + x;
+                for (uint32_t k = g.start[bin]; k < g.start[bin + 1]; k++) {
+                    const int e = (int)g.items[k];
+                    if (best >= 0 && e >= best) continue;
+                    if (encloses(m, e, p)) best = e;
+                }
+            }
+    return best >= 0 ? best + 1 : 0;
+}
+
+}  // namespace mmcgb

@@ -1,0 +1,859 @@
+/*
+ * CPU oracle: plain-C restatement of MMC's per-photon tetrahedral tracing
+ * (GPU path, branchless Badouel tracer, element-based deposit).
+ * TEST INFRASTRUCTURE ONLY -- see mmc_oracle.h.  Each routine cites the
+ * reference file:line it restates (paths inside the fangq/mmc tree).
+ *
+ * Build: gcc -O2 -ffp-contract=off -fopenmp -fPIC -shared (no -ffast-math): the
+ * float operation sequence below is the contract the CUDA engine follows, so
+ * contraction into FMAs must stay off; explicit fmaf() appears only inside the
+ * polynomial math routines, where the CUDA engine uses the same fmaf().
+ */
+#include "mmc_oracle.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <float.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ---- constants (src/mmc_core.cl:330-360, src/mmc_mesh.h:66-74) ---- */
+#define O_EPS        1e-6f              /* EPS seen by the CUDA build: src/mmc_mesh.h:70 */
+#define O_R_C0       3.335640951981520e-12f
+#define O_MAX_ACCUM  1000.f
+#define O_R_MIN_MUS  1e9f
+#define O_FIX_PHOTON 1e-3f
+#define O_MAX_TRIAL  3
+#define O_UNDEF      3.40282347e+38F    /* MMC_UNDEFINED */
+#define O_ID_UNDEF   0x7FFFFFFF
+#define O_DELTA_MUA  1e-4f
+
+enum { OT_FLUX = 0, OT_FLUENCE, OT_ENERGY, OT_JACOBIAN, OT_WL, OT_WP };
+enum { BC_NOREFLECT = 0, BC_REFLECT, BC_ABSORBEXT, BC_MIRROR };
+
+/* face tables: src/mmc_mesh.c:59 (out), :71 (facemap), :95 (faceorder),
+ * :107 (ifaceorder); face list of the neighbour search src/mmc_highorder.cpp:50 */
+static const int OUTF[4][3] = {{0, 3, 1}, {3, 2, 1}, {0, 2, 3}, {0, 1, 2}};
+static const int FACEMAP[4] = {2, 0, 1, 3};
+static const int FACEORDER[5] = {1, 3, 2, 0, -1};
+static const int IFACEORDER[4] = {3, 0, 2, 1};
+static const int FACELIST[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
+
+/* ======================================================================
+ * math: Cody-Waite argument reduction + truncated series (Cody & Waite,
+ * "Software Manual for the Elementary Functions", 1980).  Coefficients are
+ * the Taylor / atanh series terms 1/n!, 1/(2k+1).
+ * ====================================================================== */
+#define LN2_HI 0.693145751953125f          /* ln2 with its low 9 mantissa bits cleared */
+#define LN2_LO 1.42860682030941723212e-6f  /* ln2 - LN2_HI */
+#define LOG2E  1.44269504088896340736f
+
+static float bits2f(uint32_t b) { float f; memcpy(&f, &b, 4); return f; }
+static uint32_t f2bits(float f) { uint32_t b; memcpy(&b, &f, 4); return b; }
+
+float oracle_expf(float x) {
+    if (x < -104.f) return 0.f;
+    if (x > 88.7f) return INFINITY;
+    float k = rintf(x * LOG2E);
+    float r = fmaf(k, -LN2_HI, x);
+    r = fmaf(k, -LN2_LO, r);
+    /* e^r, |r| <= 0.347: Taylor to r^7 */
+    float p = 1.f / 5040.f;
+    p = fmaf(p, r, 1.f / 720.f);
+    p = fmaf(p, r, 1.f / 120.f);
+    p = fmaf(p, r, 1.f / 24.f);
+    p = fmaf(p, r, 1.f / 6.f);
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.f);
+    p = fmaf(p, r, 1.f);
+    int ki = (int)k;
+    if (ki < -125) { p *= 5.42101086242752217e-20f; ki += 64; } /* 2^-64 */
+    return p * bits2f((uint32_t)(ki + 127) << 23);
+}
+
+float oracle_logf(float x) {
+    /* x > 0, finite: x = m 2^e, m in [sqrt(1/2), sqrt(2)); log m = 2 atanh(s), s=(m-1)/(m+1) */
+    uint32_t b = f2bits(x);
+    int e = (int)((b >> 23) & 0xFF) - 127;
+    float m = bits2f((b & 0x007FFFFFu) | 0x3F800000u);
+    if (m > 1.41421356f) { m *= 0.5f; e += 1; }
+    float s = (m - 1.f) / (m + 1.f);
+    float z = s * s;
+    float p = 1.f / 11.f;
+    p = fmaf(p, z, 1.f / 9.f);
+    p = fmaf(p, z, 1.f / 7.f);
+    p = fmaf(p, z, 1.f / 5.f);
+    p = fmaf(p, z, 1.f / 3.f);
+    p = fmaf(p, z, 1.f);
+    float lm = 2.f * s * p;
+    float fe = (float)e;
+    return fmaf(fe, LN2_HI, fmaf(fe, LN2_LO, lm));
+}
+
+void oracle_sincos2pi(float u, float* s, float* c) {
+    /* sin/cos(2 pi u): quadrant from u, |x| <= pi/4 after reduction */
+    float q = rintf(u * 4.f);
+    float f = u - q * 0.25f;
+    float x = f * 6.28318530717958647692f;
+    float z = x * x;
+    float ps = 1.f / 362880.f;
+    ps = fmaf(ps, z, -1.f / 5040.f);
+    ps = fmaf(ps, z, 1.f / 120.f);
+    ps = fmaf(ps, z, -1.f / 6.f);
+    ps = fmaf(ps * z, x, x);
+    float pc = -1.f / 3628800.f;
+    pc = fmaf(pc, z, 1.f / 40320.f);
+    pc = fmaf(pc, z, -1.f / 720.f);
+    pc = fmaf(pc, z, 1.f / 24.f);
+    pc = fmaf(pc, z, -0.5f);
+    pc = fmaf(pc, z, 1.f);
+    int qi = ((int)q) & 3;
+    float sv, cv;
+    switch (qi) {
+        case 0: sv = ps; cv = pc; break;
+        case 1: sv = pc; cv = -ps; break;
+        case 2: sv = -ps; cv = -pc; break;
+        default: sv = -pc; cv = ps; break;
+    }
+    *s = sv;
+    *c = cv;
+}
+
+/* ======================================================================
+ * RNG: xorshift128+ exactly as src/mmc_core.cl:517-531 (float from the top
+ * 23 bits of the low word of s0+s1).  Per-photon initial state: splitmix64
+ * (Vigna) of (seed, photon index).
+ * ====================================================================== */
+static uint64_t splitmix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+void oracle_rng_seed(uint64_t seed, uint64_t pid, uint64_t st[2]) {
+    uint64_t base = splitmix64(seed ^ 0x6D6D63676233ull) + 2ull * pid * 0x9E3779B97F4A7C15ull;
+    st[0] = splitmix64(base);
+    st[1] = splitmix64(base + 0x9E3779B97F4A7C15ull);
+    if ((st[0] | st[1]) == 0) st[1] = 1;
+}
+
+float oracle_rng_next(uint64_t t[2]) {
+    uint64_t s1 = t[0];
+    const uint64_t s0 = t[1];
+    t[0] = s0;
+    s1 ^= s1 << 23;
+    t[1] = s1 ^ s0 ^ (s1 >> 18) ^ (s0 >> 5);
+    uint64_t r = t[1] + s0;
+    uint32_t lo = (uint32_t)r;
+    return bits2f(0x3F800000u | (lo >> 9)) - 1.0f;
+}
+
+/* ======================================================================
+ * mesh preparation
+ * ====================================================================== */
+typedef struct { float x, y, z; } f3;
+
+static f3 nodeat(const float* node, int i) { f3 r = {node[3 * i], node[3 * i + 1], node[3 * i + 2]}; return r; }
+
+typedef struct { int a, b, c; int slot; } facekey;
+
+static int cmp_face(const void* p, const void* q) {
+    const facekey* x = (const facekey*)p;
+    const facekey* y = (const facekey*)q;
+    if (x->a != y->a) return x->a < y->a ? -1 : 1;
+    if (x->b != y->b) return x->b < y->b ? -1 : 1;
+    if (x->c != y->c) return x->c < y->c ? -1 : 1;
+    return x->slot < y->slot ? -1 : (x->slot > y->slot);
+}
+
+static void sort3(int* v) {
+    int t;
+    if (v[0] > v[1]) { t = v[0]; v[0] = v[1]; v[1] = t; }
+    if (v[1] > v[2]) { t = v[1]; v[1] = v[2]; v[2] = t; }
+    if (v[0] > v[1]) { t = v[0]; v[0] = v[1]; v[1] = t; }
+}
+
+/* neighbour across face j (FACELIST order); src/mmc_highorder.cpp:128-159 */
+static void get_facenb(int ne, const int* elem, int* facenb) {
+    facekey* keys = (facekey*)malloc(sizeof(facekey) * (size_t)ne * 4);
+    for (int i = 0; i < ne; i++)
+        for (int j = 0; j < 4; j++) {
+            int v[3] = {elem[i * 4 + FACELIST[j][0]], elem[i * 4 + FACELIST[j][1]], elem[i * 4 + FACELIST[j][2]]};
+            sort3(v);
+            facekey* k = keys + i * 4 + j;
+            k->a = v[0]; k->b = v[1]; k->c = v[2]; k->slot = i * 4 + j;
+        }
+    qsort(keys, (size_t)ne * 4, sizeof(facekey), cmp_face);
+    memset(facenb, 0, sizeof(int) * (size_t)ne * 4);
+    for (size_t n = 0; n + 1 < (size_t)ne * 4; n++) {
+        facekey* x = keys + n;
+        facekey* y = keys + n + 1;
+        if (x->a == y->a && x->b == y->b && x->c == y->c) {
+            facenb[x->slot] = (y->slot >> 2) + 1;
+            facenb[y->slot] = (x->slot >> 2) + 1;
+            n++;
+        }
+    }
+    free(keys);
+}
+
+int oracle_prep_mesh(int nn, const float* node, int ne, const int* elem, const int* label,
+                     const int* facenb_in, int* ee, int* facenb, float* nrm,
+                     float* evol, float* nvol, int* nf) {
+    memcpy(ee, elem, sizeof(int) * (size_t)ne * 4);
+    memset(nvol, 0, sizeof(float) * (size_t)nn);
+    /* volumes + orientation: src/mmc_mesh.c:910-974 */
+    for (int i = 0; i < ne; i++) {
+        int* e = ee + 4 * i;
+        for (int j = 0; j < 4; j++)
+            if (e[j] < 1 || e[j] > nn) return -1;
+        f3 n0 = nodeat(node, e[0] - 1), n1 = nodeat(node, e[1] - 1), n2 = nodeat(node, e[2] - 1), n3 = nodeat(node, e[3] - 1);
+        float dx = n2.x - n3.x, dy = n2.y - n3.y, dz = n2.z - n3.z;
+        float v = n1.x * (n2.y * n3.z - n2.z * n3.y) - n1.y * (n2.x * n3.z - n2.z * n3.x) + n1.z * (n2.x * n3.y - n2.y * n3.x);
+        v += -n0.x * ((n2.y * n3.z - n2.z * n3.y) + n1.y * dz - n1.z * dy);
+        v += +n0.y * ((n2.x * n3.z - n2.z * n3.x) + n1.x * dz - n1.z * dx);
+        v += -n0.z * ((n2.x * n3.y - n2.y * n3.x) + n1.x * dy - n1.y * dx);
+        v = -v;
+        if (v < 0.f) {
+            int t = e[3]; e[3] = e[2]; e[2] = t;
+            v = -v;
+        }
+        v *= (1.f / 6.f);
+        evol[i] = v;
+        if (label[i] == 0) continue;
+        for (int j = 0; j < 4; j++) nvol[e[j] - 1] += v * 0.25f;
+    }
+    if (facenb_in) memcpy(facenb, facenb_in, sizeof(int) * (size_t)ne * 4);
+    else get_facenb(ne, ee, facenb);
+    /* outward unit normals + plane offsets: src/mmc_mesh.c:1572-1601 */
+    for (int i = 0; i < ne; i++) {
+        float* vn = nrm + 16 * i;
+        for (int j = 0; j < 4; j++) {
+            f3 a = nodeat(node, ee[4 * i + OUTF[j][0]] - 1);
+            f3 b = nodeat(node, ee[4 * i + OUTF[j][1]] - 1);
+            f3 c = nodeat(node, ee[4 * i + OUTF[j][2]] - 1);
+            f3 ab = {b.x - a.x, b.y - a.y, b.z - a.z};
+            f3 ac = {c.x - a.x, c.y - a.y, c.z - a.z};
+            f3 n = {ab.y * ac.z - ab.z * ac.y, ab.z * ac.x - ab.x * ac.z, ab.x * ac.y - ab.y * ac.x};
+            float rn = (float)(1.f / sqrt((double)(n.x * n.x + n.y * n.y + n.z * n.z)));
+            n.x *= rn; n.y *= rn; n.z *= rn;
+            vn[j] = n.x;
+            vn[j + 4] = n.y;
+            vn[j + 8] = n.z;
+            vn[j + 12] = n.x * a.x + n.y * a.y + n.z * a.z;
+        }
+    }
+    /* surface faces numbered -1,-2,...: src/mmc_mesh.c:1466-1474 */
+    int cnt = 0;
+    for (int i = 0; i < ne * 4; i++)
+        if (facenb[i] == 0) facenb[i] = -(++cnt);
+    *nf = cnt;
+    return 0;
+}
+
+/* barycentric enclosure test: src/mmc_mesh.c:1170-1205 */
+static int barycentric_inside(const float* node, const int* e, const float* p) {
+    float bary[4];
+    for (int i = 0; i < 4; i++) {
+        f3 a = nodeat(node, e[OUTF[i][0]] - 1);
+        f3 b = nodeat(node, e[OUTF[i][1]] - 1);
+        f3 c = nodeat(node, e[OUTF[i][2]] - 1);
+        f3 ab = {b.x - a.x, b.y - a.y, b.z - a.z};
+        f3 ac = {c.x - a.x, c.y - a.y, c.z - a.z};
+        f3 s = {p[0] - a.x, p[1] - a.y, p[2] - a.z};
+        f3 n = {ab.y * ac.z - ab.z * ac.y, ab.z * ac.x - ab.x * ac.z, ab.x * ac.y - ab.y * ac.x};
+        bary[FACEMAP[i]] = -(s.x * n.x + s.y * n.y + s.z * n.z);
+    }
+    for (int i = 0; i < 4; i++)
+        if (bary[i] < 0.f) return 0;
+    return 1;
+}
+
+/* linear scan, first enclosing element: src/mmc_mesh.c:1060-1090 */
+int oracle_initelem(int nn, const float* node, int ne, const int* elem, const float* p) {
+    (void)nn;
+    for (int i = 0; i < ne; i++) {
+        const int* e = elem + 4 * i;
+        double lo[3] = {1e30, 1e30, 1e30}, hi[3] = {-1e30, -1e30, -1e30};
+        for (int j = 0; j < 4; j++)
+            for (int d = 0; d < 3; d++) {
+                double v = node[3 * (e[j] - 1) + d];
+                if (v < lo[d]) lo[d] = v;
+                if (v > hi[d]) hi[d] = v;
+            }
+        if (p[0] <= hi[0] && p[0] >= lo[0] && p[1] <= hi[1] && p[1] >= lo[1] && p[2] <= hi[2] && p[2] >= lo[2])
+            if (barycentric_inside(node, e, p)) return i + 1;
+    }
+    return 0;
+}
+
+/* ======================================================================
+ * photon engine
+ * ====================================================================== */
+typedef struct {
+    int ne, nn, M;
+    const float* node;
+    const int* elem;
+    const int* type;
+    const int* facenb;
+    const float* nrm;
+    const oracle_cfg* cfg;
+    float Rtstep;
+    int maxgate;
+    float* f32a;     /* float fluence + overflow half (accum_f64 == 0) */
+    float* f32b;
+    double* f64;     /* double fluence (accum_f64 == 1) */
+    int reclen;      /* detreclen (without the det id column) */
+} engine;
+
+typedef struct {
+    float px, py, pz, vx, vy, vz, ox, oy, oz; /* p0, vec, pout */
+    int eid, faceid, isend;
+    float weight, photontimer, slen, Lmove, slen0, oldweight;
+    uint32_t oldidx;
+    uint32_t photonid;
+} ray;
+
+static void deposit(engine* g, uint32_t idx, float val) {
+    if (g->cfg->accum_f64) {
+#pragma omp atomic
+        g->f64[idx] += (double)val;
+        return;
+    }
+    /* float sums with a second buffer for running sums above MAX_ACCUM
+     * (src/mmc_core.cl:880-912); the content is moved by exchange, as the
+     * CUDA engine does */
+    float old, moved;
+#pragma omp atomic capture
+    { old = g->f32a[idx]; g->f32a[idx] += val; }
+    if (old > O_MAX_ACCUM) {
+#pragma omp atomic capture
+        { moved = g->f32a[idx]; g->f32a[idx] = 0.f; }
+        if (moved != 0.f) {
+#pragma omp atomic
+            g->f32b[idx] += moved;
+        }
+    }
+}
+
+static float medium(const engine* g, int t, int k) { return g->cfg->media[4 * t + k]; }
+
+/* one branchless Badouel step: src/mmc_core.cl:721-1226 (rtBLBadouel branch) */
+static float raytet_step(engine* g, ray* r) {
+    const oracle_cfg* cfg = g->cfg;
+    if (r->eid <= 0) return -1.f;
+    const float* N = g->nrm + 16 * (size_t)(r->eid - 1);
+    r->ox = O_UNDEF;
+    r->faceid = -1;
+    r->isend = 0;
+    float T[4], S[4];
+    for (int k = 0; k < 4; k++) {
+        S[k] = ((r->vx * N[k]) + (r->vy * N[k + 4])) + (r->vz * N[k + 8]);
+        T[k] = N[k + 12] - (((r->px * N[k]) + (r->py * N[k + 4])) + (r->pz * N[k + 8]));
+        T[k] = T[k] / S[k];
+        T[k] = (S[k] > 0.f) ? T[k] : 1e10f;
+    }
+    float Lmin = fminf(fminf(fminf(T[0], T[1]), T[2]), T[3]);
+    int faceidx = (Lmin == 1e10f) ? 4 : (Lmin == T[0] ? 0 : (Lmin == T[1] ? 1 : (Lmin == T[2] ? 2 : 3)));
+    r->faceid = FACEORDER[faceidx];
+    if (r->faceid >= 0 && Lmin >= 0.f) {
+        int type = g->type[r->eid - 1];
+        float mua = medium(g, type, 0), mus = medium(g, type, 1), nmed = medium(g, type, 3);
+        float currweight = r->weight;
+        r->Lmove = (mus <= O_EPS) ? O_R_MIN_MUS : r->slen / mus;
+        r->isend = (Lmin > r->Lmove);
+        r->Lmove = r->isend ? r->Lmove : Lmin;
+        r->ox = r->px + Lmin * r->vx;
+        r->oy = r->py + Lmin * r->vy;
+        r->oz = r->pz + Lmin * r->vz;
+        float rc = nmed * O_R_C0;
+        /* (int)x > maxgate-1 (src/mmc_core.cl:803), without the float->int conversion */
+        if ((r->photontimer + r->Lmove * rc - cfg->tstart) * g->Rtstep >= (float)g->maxgate) {
+            r->faceid = -2;
+            r->ox = O_UNDEF;
+            r->Lmove = (cfg->tend - r->photontimer) / rc - 1e-4f;
+        }
+        float totalloss = oracle_expf(-mua * r->Lmove);
+        r->weight *= totalloss;
+        int replay = (cfg->replayseed != NULL);
+        if (replay) {
+            float rw = cfg->replayweight[r->photonid];
+            if (cfg->outputtype == OT_WL || cfg->outputtype == OT_JACOBIAN) {
+                currweight = r->Lmove;
+                currweight *= rw;
+                currweight += r->weight;
+            } else if (cfg->outputtype == OT_WP) {
+                currweight = (r->slen0 < O_EPS) ? 1.f : r->Lmove * mus / r->slen0;
+                currweight *= rw;
+                currweight += r->weight;
+            }
+        }
+        r->slen -= r->Lmove * mus;
+        float ww = currweight - r->weight;
+        r->photontimer += r->Lmove * rc;
+        float gf;
+        if (replay && (cfg->outputtype == OT_WL || cfg->outputtype == OT_WP))
+            gf = cfg->replaytime[r->photonid] * g->Rtstep;
+        else
+            gf = (r->photontimer - cfg->tstart) * g->Rtstep;
+        /* MIN((int)gf, maxgate-1) of src/mmc_core.cl:835-838, kept inside the buffer */
+        int gate = (gf < (float)(g->maxgate - 1)) ? (int)gf : g->maxgate - 1;
+        if (gate < 0) gate = 0;
+        uint32_t tshift = (uint32_t)(gate * g->ne);
+        if (cfg->outputtype != OT_ENERGY && cfg->outputtype != OT_WP && cfg->outputtype != OT_WL)
+            ww = (mua < O_EPS) ? (currweight * r->Lmove) : (ww / mua);
+        uint32_t newidx = (uint32_t)(r->eid - 1) + tshift;
+        if (r->oldidx == (uint32_t)O_ID_UNDEF) r->oldidx = newidx;
+        if (newidx != r->oldidx) {
+            if (r->oldweight > 0.f) deposit(g, r->oldidx, r->oldweight);
+            r->oldidx = newidx;
+            r->oldweight = ww;
+        } else {
+            r->oldweight += ww;
+        }
+        if (r->faceid == -2 || !r->isend) {
+            deposit(g, newidx, r->oldweight);
+            r->oldweight = 0.f;
+        }
+        r->px = r->px + r->Lmove * r->vx;
+        r->py = r->py + r->Lmove * r->vy;
+        r->pz = r->pz + r->Lmove * r->vz;
+    }
+    return (r->faceid == -2) ? 0.f : r->slen;
+}
+
+/* Fresnel / TIR at a face: src/mmc_core.cl:1247-1303 */
+static void reflectray(engine* g, ray* r, int oldeid, int* eid, int faceid, uint64_t* ran) {
+    const oracle_cfg* cfg = g->cfg;
+    const float* N = g->nrm + 16 * (size_t)(oldeid - 1);
+    int fi = IFACEORDER[faceid];
+    float pnx = N[fi], pny = N[fi + 4], pnz = N[fi + 8];
+    float Icos = fabsf(((r->vx * pnx) + (r->vy * pny)) + (r->vz * pnz));
+    float n1 = (oldeid != *eid) ? medium(g, g->type[oldeid - 1], 3) : cfg->nout;
+    float n2 = (*eid > 0) ? medium(g, g->type[*eid - 1], 3) : cfg->nout;
+    float tmp0 = n1 * n1;
+    float tmp1 = n2 * n2;
+    float tmp2 = 1.f - tmp0 / tmp1 * (1.f - Icos * Icos);
+    if (tmp2 > 0.f && !((*eid <= 0) && (cfg->isreflect == BC_MIRROR))) {
+        float Re = tmp0 * Icos * Icos + tmp1 * tmp2;
+        tmp2 = sqrtf(tmp2);
+        float Im = 2.f * n1 * n2 * Icos * tmp2;
+        float Rtotal = (Re - Im) / (Re + Im);
+        Re = tmp1 * Icos * Icos + tmp0 * tmp2 * tmp2;
+        Rtotal = (Rtotal + (Re - Im) / (Re + Im)) * 0.5f;
+        if (oracle_rng_next(ran) <= Rtotal) {
+            float k = -2.f * Icos;
+            r->vx += k * pnx; r->vy += k * pny; r->vz += k * pnz;
+            *eid = oldeid;
+        } else if ((cfg->isspecular == 2) && (*eid == 0)) {
+        } else {
+            float k = -Icos;
+            r->vx += k * pnx; r->vy += k * pny; r->vz += k * pnz;
+            float q = n1 / n2;
+            r->vx = tmp2 * pnx + q * r->vx;
+            r->vy = tmp2 * pny + q * r->vy;
+            r->vz = tmp2 * pnz + q * r->vz;
+        }
+    } else {
+        float k = -2.f * Icos;
+        r->vx += k * pnx; r->vy += k * pny; r->vz += k * pnz;
+        *eid = oldeid;
+    }
+    float inv = 1.f / sqrtf(r->vx * r->vx + r->vy * r->vy + r->vz * r->vz);
+    r->vx *= inv; r->vy *= inv; r->vz *= inv;
+}
+
+/* direction update: src/mmc_core.cl:1307-1332 */
+static void rotatevector(ray* r, float stheta, float ctheta, float sphi, float cphi) {
+    float px, py, pz;
+    if (r->vz > -1.f + O_EPS && r->vz < 1.f - O_EPS) {
+        float tmp0 = 1.f - r->vz * r->vz;
+        float tmp1 = 1.f / sqrtf(tmp0);
+        tmp1 = stheta * tmp1;
+        px = tmp1 * (r->vx * r->vz * cphi - r->vy * sphi) + r->vx * ctheta;
+        py = tmp1 * (r->vy * r->vz * cphi + r->vx * sphi) + r->vy * ctheta;
+        pz = -tmp1 * tmp0 * cphi + r->vz * ctheta;
+    } else {
+        px = stheta * cphi;
+        py = stheta * sphi;
+        pz = (r->vz > 0.f) ? ctheta : -ctheta;
+    }
+    float inv = 1.f / sqrtf(px * px + py * py + pz * pz);
+    r->vx = px * inv; r->vy = py * inv; r->vz = pz * inv;
+}
+
+/* Henyey-Greenstein scatter: src/mmc_core.cl:1348-1377 */
+static float next_scatter(float gg, ray* r, uint64_t* ran, float* mom) {
+    float nextslen = -oracle_logf(oracle_rng_next(ran) + O_EPS);
+    float sphi, cphi, stheta, ctheta;
+    oracle_sincos2pi(oracle_rng_next(ran), &sphi, &cphi);
+    if (gg > O_EPS) {
+        float tmp0 = (1.f - gg * gg) / (1.f - gg + 2.f * gg * oracle_rng_next(ran));
+        tmp0 *= tmp0;
+        tmp0 = (1.f + gg * gg - tmp0) / (2.f * gg);
+        tmp0 = fmaxf(-1.f, fminf(tmp0, 1.f));
+        stheta = sqrtf(1.f - tmp0 * tmp0);
+        ctheta = tmp0;
+    } else {
+        /* cos(acos(x)) = x, sin(acos(x)) = sqrt(1-x^2) */
+        ctheta = 2.f * oracle_rng_next(ran) - 1.f;
+        stheta = sqrtf(1.f - ctheta * ctheta);
+    }
+    rotatevector(r, stheta, ctheta, sphi, cphi);
+    *mom += (1.f - ctheta);
+    return nextslen;
+}
+
+/* centroid nudge at edge/vertex hits: src/mmc_core.cl:1390-1402 */
+static void fixphoton(engine* g, ray* r) {
+    const int* e = g->elem + 4 * (size_t)(r->eid - 1);
+    float cx = 0.f, cy = 0.f, cz = 0.f;
+    for (int i = 0; i < 4; i++) {
+        const float* p = g->node + 3 * (size_t)(e[i] - 1);
+        cx += p[0]; cy += p[1]; cz += p[2];
+    }
+    r->px += (cx * 0.25f - r->px) * O_FIX_PHOTON;
+    r->py += (cy * 0.25f - r->py) * O_FIX_PHOTON;
+    r->pz += (cz * 0.25f - r->pz) * O_FIX_PHOTON;
+}
+
+static int valid_eid(const engine* g, int eid) { return eid > 0 && eid <= g->ne; }
+
+/* detector search: src/mmc_core.cl:608-621 */
+static int finddetector(const engine* g, const ray* r) {
+    const oracle_cfg* cfg = g->cfg;
+    for (int i = 0; i < cfg->detnum; i++) {
+        const float* d = cfg->detpos + 4 * i;
+        if ((d[0] - r->px) * (d[0] - r->px) + (d[1] - r->py) * (d[1] - r->py) + (d[2] - r->pz) * (d[2] - r->pz) < d[3] * d[3])
+            return i + 1;
+    }
+    return 0;
+}
+
+typedef struct {
+    double etot, eesc;
+    uint64_t raytet;
+    uint64_t aborted;
+} tallies;
+
+/* the photon life: src/mmc_core.cl:1851-2161 */
+static void onephoton(engine* g, uint64_t pidx, float* ppath, oracle_out* out, tallies* tl) {
+    const oracle_cfg* cfg = g->cfg;
+    const int M = g->M;
+    const int reclen = g->reclen;
+    uint64_t ran[2], seed0[2];
+    uint32_t photonid = (uint32_t)pidx;
+    if (cfg->replayseed) {
+        ran[0] = cfg->replayseed[2 * pidx];
+        ran[1] = cfg->replayseed[2 * pidx + 1];
+    } else {
+        oracle_rng_seed(cfg->seed, cfg->photon_offset + pidx, ran);
+    }
+    seed0[0] = ran[0]; seed0[1] = ran[1];
+    ray rr;
+    ray* r = &rr;
+    memset(r, 0, sizeof(ray));
+    r->px = cfg->srcpos[0]; r->py = cfg->srcpos[1]; r->pz = cfg->srcpos[2];
+    r->vx = cfg->srcdir[0]; r->vy = cfg->srcdir[1]; r->vz = cfg->srcdir[2];
+    r->ox = O_UNDEF;
+    r->eid = cfg->e0;
+    r->weight = 1.f;
+    r->oldidx = (uint32_t)O_ID_UNDEF;
+    r->photonid = photonid;
+    memset(ppath, 0, sizeof(float) * (size_t)reclen);
+    int fixcount = 0, oldeid = 0, detid = 0;
+    uint64_t steps = 0;
+    int aborted = 0;
+    /* pencil launch: src/mmc_core.cl:1521-1526 */
+    r->slen = -oracle_logf(oracle_rng_next(ran) + O_EPS);
+    if (cfg->issavedet) ppath[reclen - 1] = r->weight;
+    tl->etot += r->weight;
+
+#define STEP()                                                         \
+    do {                                                               \
+        r->slen = raytet_step(g, r);                                   \
+        steps++;                                                       \
+        if (steps > cfg->step_budget) { aborted = 1; goto done; }      \
+    } while (0)
+#define PPATH()                                                                       \
+    do {                                                                              \
+        if (cfg->issavedet && r->Lmove > 0.f && valid_eid(g, r->eid)) {               \
+            int tp = g->type[r->eid - 1];                                             \
+            if (tp > 0) ppath[M + tp - 1] += r->Lmove;                                \
+        }                                                                             \
+    } while (0)
+
+    while (1) {
+        STEP();
+        if (r->ox == O_UNDEF) {
+            if (r->faceid == -2) break;
+            if (fixcount++ < O_MAX_TRIAL) {
+                fixphoton(g, r);
+                continue;
+            }
+            r->eid = O_ID_UNDEF;
+            r->faceid = -1;
+        }
+        PPATH();
+        while (r->faceid >= 0 && !r->isend) {
+            r->px = r->ox; r->py = r->oy; r->pz = r->oz;
+            oldeid = r->eid;
+            r->eid = g->facenb[4 * (size_t)(r->eid - 1) + r->faceid];
+            if (cfg->isreflect) {
+                float nold = medium(g, g->type[oldeid - 1], 3);
+                if (r->eid <= 0 || medium(g, g->type[r->eid - 1], 3) != nold) {
+                    if (!(r->eid <= 0 && (((nold == cfg->nout) && (cfg->isreflect != BC_MIRROR)) || (cfg->isreflect == BC_ABSORBEXT))))
+                        reflectray(g, r, oldeid, &r->eid, r->faceid, ran);
+                }
+            }
+            if (r->eid <= 0) break;
+            if (g->type[oldeid - 1] == 0 && g->type[r->eid - 1]) {
+                if (!cfg->voidtime) r->photontimer = 0.f;
+            }
+            if (g->type[oldeid - 1] && g->type[r->eid - 1] == 0) {
+                r->eid = 0;
+                break;
+            }
+            STEP();
+            PPATH();
+            if (r->faceid == -2) break;
+            fixcount = 0;
+            while (r->ox == O_UNDEF && fixcount++ < O_MAX_TRIAL) {
+                fixphoton(g, r);
+                STEP();
+                PPATH();
+            }
+            if (r->ox == O_UNDEF) {
+                r->eid = O_ID_UNDEF;
+                break;
+            }
+        }
+        if (r->eid <= 0 || r->ox == O_UNDEF) {
+            if (r->eid != O_ID_UNDEF && cfg->issavedet && cfg->issaveexit) {
+                ppath[reclen - 7] = r->px; ppath[reclen - 6] = r->py; ppath[reclen - 5] = r->pz;
+                ppath[reclen - 4] = r->vx; ppath[reclen - 3] = r->vy; ppath[reclen - 2] = r->vz;
+            }
+            if (cfg->issavedet && r->eid <= 0) {
+                /* savedetphoton: src/mmc_core.cl:624-682 */
+                detid = finddetector(g, r);
+                if (detid) {
+                    uint32_t slot;
+#pragma omp atomic capture
+                    slot = out->detected++;
+                    if (slot < cfg->maxdetphoton) {
+                        if (out->seeds) memcpy(out->seeds + 16 * (size_t)slot, seed0, 16);
+                        if (out->detp) {
+                            float* rec = out->detp + (size_t)slot * (reclen + 1);
+                            rec[0] = (float)detid;
+                            for (int i = 0; i < reclen; i++) rec[1 + i] = ppath[i];
+                        }
+                    }
+                }
+            }
+            break;
+        }
+        /* Russian roulette: src/mmc_core.cl:2101-2114 */
+        if ((cfg->minenergy > 0.f) && (r->weight < cfg->minenergy) && ((cfg->tend - cfg->tstart) * g->Rtstep <= 1.f)) {
+            if (oracle_rng_next(ran) * cfg->roulettesize <= 1.f) {
+                r->weight *= cfg->roulettesize;
+            } else {
+                break;
+            }
+        }
+        float mom = 0.f;
+        int tp = g->type[r->eid - 1];
+        r->slen0 = next_scatter(medium(g, tp, 2), r, ran, &mom);
+        r->slen = r->slen0;
+        if (cfg->issavedet) {
+            if (cfg->ismomentum && tp > 0) ppath[2 * M + tp - 1] += mom;
+            if (tp > 0) ppath[tp - 1] += 1.f;
+        }
+    }
+done:
+#undef STEP
+#undef PPATH
+    tl->eesc += r->weight;
+    tl->raytet += steps;
+    tl->aborted += aborted;
+    if (out->photon_weight) out->photon_weight[pidx] = r->weight;
+    if (out->photon_steps) out->photon_steps[pidx] = (uint32_t)steps;
+    if (out->photon_det) out->photon_det[pidx] = detid;
+}
+
+int oracle_run(int nn, const float* node, int ne, const int* elem, const int* label,
+               const oracle_cfg* cfg, oracle_out* out, int nthreads) {
+    int* ee = (int*)malloc(sizeof(int) * (size_t)ne * 4);
+    int* fnb = (int*)malloc(sizeof(int) * (size_t)ne * 4);
+    float* nrm = (float*)malloc(sizeof(float) * (size_t)ne * 16);
+    float* evol = (float*)malloc(sizeof(float) * (size_t)ne);
+    float* nvol = (float*)malloc(sizeof(float) * (size_t)nn);
+    int nf = 0, rc = 0;
+    if (oracle_prep_mesh(nn, node, ne, elem, label, NULL, ee, fnb, nrm, evol, nvol, &nf) != 0) {
+        rc = -1;
+        goto cleanup;
+    }
+    engine g;
+    memset(&g, 0, sizeof(g));
+    g.ne = ne; g.nn = nn; g.M = cfg->nmedia - 1;
+    g.node = node; g.elem = ee; g.type = label; g.facenb = fnb; g.nrm = nrm; g.cfg = cfg;
+    g.Rtstep = 1.f / cfg->tstep;
+    g.maxgate = cfg->maxgate;
+    g.reclen = (2 + (cfg->ismomentum > 0)) * g.M + (cfg->issaveexit > 0) * 6 + 1;
+    out->reclen = g.reclen + 1;
+    size_t flen = (size_t)ne * cfg->maxgate;
+    if (cfg->accum_f64) {
+        g.f64 = out->field_raw;
+        memset(g.f64, 0, sizeof(double) * flen);
+    } else {
+        g.f32a = (float*)calloc(flen, sizeof(float));
+        g.f32b = (float*)calloc(flen, sizeof(float));
+    }
+    out->detected = 0;
+    double etot = 0, eesc = 0;
+    uint64_t raytet = 0, aborted = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+#pragma omp parallel reduction(+:etot, eesc, raytet, aborted)
+    {
+        float* ppath = (float*)calloc((size_t)g.reclen + 1, sizeof(float));
+        tallies tl = {0, 0, 0, 0};
+#pragma omp for schedule(dynamic, 64)
+        for (long long i = 0; i < (long long)cfg->nphoton; i++) onephoton(&g, (uint64_t)i, ppath, out, &tl);
+        etot += tl.etot; eesc += tl.eesc; raytet += tl.raytet; aborted += tl.aborted;
+        free(ppath);
+    }
+    out->energytot = etot;
+    out->energyesc = eesc;
+    out->raytet = raytet;
+    out->aborted = aborted;
+    if (!cfg->accum_f64) {
+        for (size_t i = 0; i < flen; i++) out->field_raw[i] = (double)g.f32a[i] + (double)g.f32b[i];
+        free(g.f32a);
+        free(g.f32b);
+    }
+cleanup:
+    free(ee); free(fnb); free(nrm); free(evol); free(nvol);
+    return rc;
+}
+
+/* ======================================================================
+ * output stage
+ * ====================================================================== */
+/* effective reflection coefficient: src/mmc_mesh.c:2305-2334 */
+static double getreff(double n_in, double n_out) {
+    double oc = asin(1.0 / n_in);
+    const double count = 1000.0;
+    const double ostep = (3.14159265358979323846 / (2.0 * count));
+    double r_phi = 0.0, r_j = 0.0;
+    for (int i = 0; i < count; i++) {
+        double o = i * ostep, coso = cos(o), r_fres, cosop, tmp;
+        if (o < oc) {
+            cosop = n_in * sin(o);
+            cosop = sqrt(1. - cosop * cosop);
+            tmp = (n_in * cosop - n_out * coso) / (n_in * cosop + n_out * coso);
+            r_fres = 0.5 * tmp * tmp;
+            tmp = (n_in * coso - n_out * cosop) / (n_in * coso + n_out * cosop);
+            r_fres += 0.5 * tmp * tmp;
+        } else {
+            r_fres = 1.f;
+        }
+        r_phi += 2.0 * sin(o) * coso * r_fres;
+        r_j += 3.0 * sin(o) * coso * coso * r_fres;
+    }
+    r_phi *= ostep;
+    r_j *= ostep;
+    return (r_phi + r_j) / (2.0 - r_phi + r_j);
+}
+
+double oracle_normalize(int nn, const float* node, int ne, const int* elem, const int* label,
+                        const oracle_cfg* cfg, const double* raw, double energytot,
+                        double energyesc, double* field) {
+    int* ee = (int*)malloc(sizeof(int) * (size_t)ne * 4);
+    int* fnb = (int*)malloc(sizeof(int) * (size_t)ne * 4);
+    float* nrm = (float*)malloc(sizeof(float) * (size_t)ne * 16);
+    float* evol = (float*)malloc(sizeof(float) * (size_t)ne);
+    float* nvol = (float*)malloc(sizeof(float) * (size_t)nn);
+    int nf = 0, prop = cfg->nmedia - 1, G = cfg->maxgate;
+    const float* med = cfg->media;
+    double normalizor = 1.0;
+    oracle_prep_mesh(nn, node, ne, elem, label, NULL, ee, fnb, nrm, evol, nvol, &nf);
+    int datalen = cfg->basisorder ? nn : ne;
+    /* surface nodal volume fix: src/mmc_mesh.c:1344-1386 (faces with no
+     * neighbour are the ones prep numbered negative) */
+    if (cfg->isnormalized == 1 && cfg->basisorder) {
+        float* Reff = (float*)calloc((size_t)prop + 1, sizeof(float));
+        if (cfg->isreflect) {
+            for (int i = 1; i <= prop; i++) {
+                for (int j = 1; j < i; j++)
+                    if (med[4 * j + 3] == med[4 * i + 3]) { Reff[i] = Reff[j]; break; }
+                if (Reff[i] == 0.f) Reff[i] = (float)getreff(med[4 * i + 3], med[3]);
+            }
+        }
+        for (int i = 0; i < ne; i++)
+            for (int j = 0; j < 4; j++)
+                if (fnb[4 * i + j] < 0) {
+                    for (int k = 0; k < 3; k++) {
+                        int nid = ee[4 * i + OUTF[IFACEORDER[j]][k]] - 1;
+                        if (nvol[nid] > 0.f && label[i] >= 0)
+                            nvol[nid] *= -(2.f / (1.0 + Reff[label[i]]));
+                    }
+                }
+        for (int i = 0; i < nn; i++)
+            if (nvol[i] < 0.f) nvol[i] = -nvol[i];
+        free(Reff);
+    }
+    /* elem -> node scatter: src/mmc_cu_host.cu:916-976 */
+    memset(field, 0, sizeof(double) * (size_t)datalen * G);
+    if (!cfg->basisorder) {
+        for (size_t i = 0; i < (size_t)ne * G; i++) field[i] = raw[i];
+    } else {
+        for (int i = 0; i < G; i++)
+            for (int j = 0; j < ne; j++) {
+                double ww = raw[(size_t)i * ne + j] * 0.25;
+                for (int k = 0; k < 4; k++) field[(size_t)i * nn + ee[4 * j + k] - 1] += ww;
+            }
+    }
+    if (cfg->isnormalized) {
+        /* src/mmc_mesh.c:2154-2279 (single source) */
+        float Etotal = (float)energytot;
+        float Eabsorb = (float)(energytot - energyesc);
+        int replay = (cfg->replayseed != NULL);
+        if (replay && (cfg->outputtype == OT_JACOBIAN || cfg->outputtype == OT_WL || cfg->outputtype == OT_WP)) {
+            normalizor = 1.f / (O_DELTA_MUA * cfg->nphoton);
+            if (cfg->outputtype == OT_WL || cfg->outputtype == OT_WP) normalizor = 1.f / Etotal;
+        } else if (cfg->outputtype == OT_ENERGY) {
+            normalizor = 1.f / Etotal;
+        } else {
+            double energydeposit = 0.0;
+            if (cfg->basisorder) {
+                for (int i = 0; i < G; i++)
+                    for (int j = 0; j < datalen; j++)
+                        if (nvol[j] > 0.f) field[(size_t)i * datalen + j] /= nvol[j];
+                for (int i = 0; i < ne; i++) {
+                    double energyelem = 0.0;
+                    for (int j = 0; j < G; j++)
+                        for (int k = 0; k < 4; k++) energyelem += field[(size_t)j * nn + ee[4 * i + k] - 1];
+                    energydeposit += energyelem * evol[i] * med[4 * label[i]];
+                }
+                normalizor = Eabsorb / (Etotal * energydeposit * 0.25f);
+            } else {
+                for (int i = 0; i < datalen; i++)
+                    for (int j = 0; j < G; j++) energydeposit += field[(size_t)j * datalen + i];
+                for (int i = 0; i < datalen; i++) {
+                    double energyelem = evol[i] * med[4 * label[i]];
+                    for (int j = 0; j < G; j++) field[(size_t)j * datalen + i] /= energyelem;
+                }
+                normalizor = Eabsorb / (Etotal * energydeposit);
+            }
+            if (cfg->outputtype == OT_FLUX) normalizor /= cfg->tstep;
+        }
+        for (size_t i = 0; i < (size_t)datalen * G; i++) field[i] *= normalizor;
+    }
+    free(ee); free(fnb); free(nrm); free(evol); free(nvol);
+    return normalizor;
+}

@@ -1,0 +1,209 @@
+"""ctypes wrapper of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, as the checker.  The product never imports it.
+The oracle restates the reference's GPU photon path in plain C; see
+oracle/mmc_oracle.h for what it follows and how it differs.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+OUTPUT_TYPES = {"flux": 0, "fluence": 1, "energy": 2, "jacobian": 3, "wl": 4, "wp": 5}
+_lib = None
+
+
+class OCfg(C.Structure):
+    _fields_ = [
+        ("nphoton", C.c_uint64), ("photon_offset", C.c_uint64), ("seed", C.c_uint64),
+        ("srcpos", C.c_float * 3), ("srcdir", C.c_float * 3), ("e0", C.c_int),
+        ("tstart", C.c_float), ("tend", C.c_float), ("tstep", C.c_float), ("maxgate", C.c_int),
+        ("isreflect", C.c_int), ("isspecular", C.c_int), ("voidtime", C.c_int),
+        ("issavedet", C.c_int), ("issaveexit", C.c_int), ("ismomentum", C.c_int),
+        ("minenergy", C.c_float), ("roulettesize", C.c_float), ("nout", C.c_float),
+        ("outputtype", C.c_int), ("basisorder", C.c_int), ("isnormalized", C.c_int),
+        ("maxdetphoton", C.c_uint32), ("nmedia", C.c_int), ("media", C.c_void_p),
+        ("detnum", C.c_int), ("detpos", C.c_void_p),
+        ("replayseed", C.c_void_p), ("replayweight", C.c_void_p), ("replaytime", C.c_void_p),
+        ("accum_f64", C.c_int), ("step_budget", C.c_uint64),
+    ]
+
+
+class OOut(C.Structure):
+    _fields_ = [
+        ("field_raw", C.c_void_p), ("detp", C.c_void_p), ("seeds", C.c_void_p),
+        ("photon_weight", C.c_void_p), ("photon_steps", C.c_void_p), ("photon_det", C.c_void_p),
+        ("detected", C.c_uint32), ("reclen", C.c_int), ("energytot", C.c_double),
+        ("energyesc", C.c_double), ("raytet", C.c_uint64), ("aborted", C.c_uint64),
+    ]
+
+
+def build(force=False):
+    src = os.path.join(HERE, "mmc_oracle.c")
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
+            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "mmc_oracle.h"))):
+        subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", LIB + ".tmp",
+                        src, "-lm"], check=True)
+        os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(LIB)
+        lib.oracle_run.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(OCfg),
+                                   C.POINTER(OOut), C.c_int]
+        lib.oracle_run.restype = C.c_int
+        lib.oracle_normalize.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(OCfg),
+                                         C.c_void_p, C.c_double, C.c_double, C.c_void_p]
+        lib.oracle_normalize.restype = C.c_double
+        lib.oracle_prep_mesh.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.POINTER(C.c_int)]
+        lib.oracle_initelem.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        lib.oracle_expf.argtypes = [C.c_float]
+        lib.oracle_expf.restype = C.c_float
+        lib.oracle_logf.argtypes = [C.c_float]
+        lib.oracle_logf.restype = C.c_float
+        lib.oracle_sincos2pi.argtypes = [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        lib.oracle_rng_seed.argtypes = [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64 * 2)]
+        lib.oracle_rng_next.argtypes = [C.POINTER(C.c_uint64 * 2)]
+        lib.oracle_rng_next.restype = C.c_float
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def _arr(node, elem, label):
+    node = np.ascontiguousarray(node, np.float32).reshape(-1, 3)
+    elem = np.ascontiguousarray(elem, np.int32).reshape(-1, 4)
+    label = np.ascontiguousarray(label, np.int32).reshape(-1)
+    return node, elem, label
+
+
+def prep_mesh(node, elem, label):
+    lib = load()
+    node, elem, label = _arr(node, elem, label)
+    nn, ne = node.shape[0], elem.shape[0]
+    ee = np.empty((ne, 4), np.int32)
+    fnb = np.empty((ne, 4), np.int32)
+    nrm = np.empty((ne, 16), np.float32)
+    evol = np.empty(ne, np.float32)
+    nvol = np.empty(nn, np.float32)
+    nf = C.c_int()
+    rc = lib.oracle_prep_mesh(nn, _p(node), ne, _p(elem), _p(label), None, _p(ee), _p(fnb), _p(nrm),
+                              _p(evol), _p(nvol), C.byref(nf))
+    if rc:
+        raise ValueError("oracle: bad mesh")
+    return dict(elem=ee, facenb=fnb, normals=nrm, evol=evol, nvol=nvol, nf=nf.value)
+
+
+def initelem(node, elem, label, p):
+    lib = load()
+    node, elem, label = _arr(node, elem, label)
+    ee = prep_mesh(node, elem, label)["elem"]
+    pp = np.asarray(p, np.float32)
+    return int(lib.oracle_initelem(node.shape[0], _p(node), ee.shape[0], _p(ee), _p(pp)))
+
+
+def _ocfg(cfg, maxgate, e0, keep):
+    c = OCfg()
+    c.nphoton = int(cfg.nphoton)
+    c.photon_offset = int(cfg.photon_offset)
+    c.seed = int(cfg.seed) & 0xFFFFFFFFFFFFFFFF
+    c.srcpos = (C.c_float * 3)(*[float(x) for x in cfg.srcpos])
+    c.srcdir = (C.c_float * 3)(*[float(x) for x in cfg.srcdir])
+    c.e0 = int(e0)
+    c.tstart = float(cfg.tstart)
+    c.tstep = float(cfg.tstep)
+    c.maxgate = int(maxgate)
+    # the per-launch window end the engine uses: tstart + tstep*maxgate (float)
+    c.tend = float(np.float32(cfg.tstart) + np.float32(cfg.tstep) * np.float32(maxgate))
+    c.isreflect, c.isspecular, c.voidtime = int(cfg.isreflect), int(cfg.isspecular), int(cfg.voidtime)
+    c.issavedet, c.issaveexit, c.ismomentum = int(cfg.issavedet), int(cfg.issaveexit), int(cfg.ismomentum)
+    c.minenergy, c.roulettesize, c.nout = float(cfg.minenergy), float(cfg.roulettesize), float(cfg.nout)
+    ot = cfg.outputtype
+    c.outputtype = OUTPUT_TYPES[ot] if isinstance(ot, str) else int(ot)
+    c.basisorder, c.isnormalized = int(cfg.basisorder), int(cfg.isnormalized)
+    c.maxdetphoton = int(cfg.maxdetphoton)
+    med = np.ascontiguousarray(cfg.media, np.float32).reshape(-1, 4)
+    keep.append(med)
+    c.nmedia, c.media = med.shape[0], _p(med)
+    if cfg.detpos is not None and len(cfg.detpos):
+        det = np.ascontiguousarray(cfg.detpos, np.float32).reshape(-1, 4)
+        keep.append(det)
+        c.detnum, c.detpos = det.shape[0], _p(det)
+    if cfg.replayseed is not None:
+        rs = np.ascontiguousarray(cfg.replayseed, np.uint64).reshape(-1, 2)
+        rw = np.ascontiguousarray(cfg.replayweight, np.float32)
+        rt = np.ascontiguousarray(cfg.replaytime, np.float32)
+        keep += [rs, rw, rt]
+        c.replayseed, c.replayweight, c.replaytime = _p(rs), _p(rw), _p(rt)
+    c.accum_f64 = int(cfg.accum_f64)
+    c.step_budget = int(cfg.step_budget) if cfg.step_budget else 100000000
+    return c
+
+
+def run(node, elem, label, cfg, nthreads=1, trace=False, normalize=True):
+    """Runs the oracle on the mesh arrays with a SimConfig; returns a dict."""
+    lib = load()
+    node, elem, label = _arr(node, elem, label)
+    nn, ne = node.shape[0], elem.shape[0]
+    maxgate = cfg.maxgate
+    e0 = cfg.e0 if cfg.e0 else initelem(node, elem, label, cfg.srcpos)
+    if e0 <= 0:
+        raise ValueError("oracle: source outside the mesh")
+    keep = []
+    c = _ocfg(cfg, maxgate, e0, keep)
+    raw = np.zeros((maxgate, ne), np.float64)
+    nmed = c.nmedia
+    reclen = 1 + (2 + (1 if cfg.ismomentum else 0)) * (nmed - 1) + (6 if cfg.issaveexit else 0) + 1
+    out = OOut()
+    detp = np.zeros((int(cfg.maxdetphoton), reclen), np.float32) if cfg.issavedet else None
+    seeds = np.zeros((int(cfg.maxdetphoton), 16), np.uint8) if cfg.issavedet and cfg.issaveseed else None
+    pw = np.zeros(int(cfg.nphoton), np.float32) if trace else None
+    ps = np.zeros(int(cfg.nphoton), np.uint32) if trace else None
+    pd = np.zeros(int(cfg.nphoton), np.int32) if trace else None
+    out.field_raw, out.detp, out.seeds = _p(raw), _p(detp), _p(seeds)
+    out.photon_weight, out.photon_steps, out.photon_det = _p(pw), _p(ps), _p(pd)
+    rc = lib.oracle_run(nn, _p(node), ne, _p(elem), _p(label), C.byref(c), C.byref(out), int(nthreads))
+    if rc:
+        raise ValueError("oracle run failed")
+    res = dict(raw=raw, detected=int(out.detected), energytot=out.energytot, energyesc=out.energyesc,
+               raytet=int(out.raytet), aborted=int(out.aborted), reclen=int(out.reclen), e0=e0,
+               photon_weight=pw, photon_steps=ps, photon_det=pd)
+    saved = min(int(out.detected), int(cfg.maxdetphoton)) if cfg.issavedet else 0
+    res["detp"] = detp[:saved] if detp is not None else None
+    res["seeds"] = seeds[:saved] if seeds is not None else None
+    if normalize:
+        datalen = nn if cfg.basisorder else ne
+        field = np.zeros((maxgate, datalen), np.float64)
+        res["normalizer"] = lib.oracle_normalize(nn, _p(node), ne, _p(elem), _p(label), C.byref(c), _p(raw),
+                                                 out.energytot, out.energyesc, _p(field))
+        res["field"] = field
+    return res
+
+
+def normalize(node, elem, label, cfg, raw, energytot, energyesc):
+    lib = load()
+    node, elem, label = _arr(node, elem, label)
+    nn, ne = node.shape[0], elem.shape[0]
+    keep = []
+    c = _ocfg(cfg, cfg.maxgate, 1, keep)
+    raw = np.ascontiguousarray(raw, np.float64)
+    datalen = nn if cfg.basisorder else ne
+    field = np.zeros((cfg.maxgate, datalen), np.float64)
+    norm = lib.oracle_normalize(nn, _p(node), ne, _p(elem), _p(label), C.byref(c), _p(raw), energytot,
+                                energyesc, _p(field))
+    return field, norm

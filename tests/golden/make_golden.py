@@ -1,0 +1,190 @@
+"""Generates the golden fixtures in tests/golden/ by running the reference MMC
+CPU engine (built from the reference sources by oracle/build_ref.sh into
+oracle/_ref/mmc).  Needs the reference tree, so it runs in the development
+container only; the fixtures it writes are committed and used everywhere.
+
+For each case the reference runs 10 times (seeds SEED0..SEED0+9), one OpenMP
+thread each (its results depend on the thread count), with the branchless
+Badouel tracer and element-based output (-M s -C 0), unnormalized (-U 0):
+
+  cube6k   homogeneous 60 mm cube, 10^3 voxels x 6 tets, mua=0.005 mus=1 g=0.01
+           n=1.37, pencil (30,30,0) +z, one 5 ns gate, 1e5 photons
+  incl48k  20^3 voxels x 6 tets at 3 mm, +/-0.6 mm jitter, r=10 mm inclusion
+           (mua=0.05 mus=5 g=0.9), 10 gates of 0.5 ns, 4 detectors R=2 mm on
+           z=0 at x=40..55, detected photons saved, 1e5 photons
+
+Stored per case: mean and standard deviation over the 10 runs of the
+per-element fluence summed over gates and of the per-gate totals, a random
+subset of (element, gate) cells, detector statistics, absorbed fraction and
+ray-tet tests per photon; plus, for seed SEED0, the normalized element output
+(-U 1) next to the raw one, which pins the normalization.
+
+  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import struct
+import subprocess
+import sys
+import tempfile
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from mmc_gb300 import meshgen  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref", "mmc")
+NRUNS = 10
+SEED0 = 20260101
+
+
+def case_defs():
+    cube = meshgen.homogeneous_cube(n=10)
+    incl = meshgen.inclusion_cube(n=20, jitter=0.6, seed=7)
+    return {
+        "cube6k": dict(mesh=cube, photons=100000, t1=5e-9, dt=5e-9, det=None),
+        "incl48k": dict(mesh=incl, photons=100000, t1=5e-9, dt=0.5e-9, det=meshgen.c1_detectors()),
+    }
+
+
+def write_json(path, name, c):
+    m = c["mesh"]
+    elem = np.c_[m.elem, m.label].tolist()
+    cfg = {
+        "Session": {"ID": name, "Photons": c["photons"], "RNGSeed": SEED0, "OutputFormat": "bin",
+                    "DoMismatch": 1},
+        "Domain": {"Media": [dict(mua=float(r[0]), mus=float(r[1]), g=float(r[2]), n=float(r[3]))
+                             for r in m.media]},
+        "Mesh": {"MeshNode": m.node.astype(np.float64).tolist(), "MeshElem": elem, "InitElem": int(c["e0"])},
+        "Forward": {"T0": 0.0, "T1": c["t1"], "Dt": c["dt"]},
+        "Optode": {"Source": {"Pos": [30.0, 30.0, 0.0], "Dir": [0.0, 0.0, 1.0]}},
+    }
+    if c["det"] is not None:
+        cfg["Optode"]["Detector"] = [{"Pos": [float(d[0]), float(d[1]), float(d[2])], "R": float(d[3])}
+                                     for d in c["det"]]
+    with open(path, "w") as f:
+        json.dump(cfg, f)
+
+
+def read_mch(path):
+    with open(path, "rb") as f:
+        buf = f.read()
+    hdr = struct.unpack("<4sIIIIIIIfIfIiI2i", buf[:64])
+    colcount, saved = hdr[4], hdr[7]
+    data = np.frombuffer(buf, np.float32, count=saved * colcount, offset=64).reshape(saved, colcount)
+    return data, dict(maxmedia=hdr[2], detnum=hdr[3], colcount=colcount, total=hdr[5], detected=hdr[6])
+
+
+def read_jdata(obj):
+    """Decodes one JData array (base64 + zlib) of the reference's JSON output."""
+    import base64
+    import zlib
+    dt = {"uint32": np.uint32, "single": np.float32, "double": np.float64, "int32": np.int32}[obj["_ArrayType_"]]
+    raw = zlib.decompress(base64.b64decode(obj["_ArrayZipData_"]))
+    return np.frombuffer(raw, dt).reshape(obj["_ArraySize_"])
+
+
+def run_ref_detp(workdir, name, seed, photons):
+    """Detected photons of one run: the reference lifecycle run by
+    oracle/ref_driver.c, which dumps cfg.exportdetected (the reference's own
+    .mch/.jdt writers take their column count from cfg.his, which the CPU path
+    leaves at 0).  Columns: detid, nscat[M], ppath[M], w0."""
+    sess = f"{name}_{seed}_det"
+    out = os.path.join(workdir, sess + ".detp")
+    cmd = [REF + "_detp", "-f", os.path.join(workdir, name + ".json"), "-c", "sse", "-M", "s", "-C", "0", "-b", "1",
+           "-U", "0", "-F", "bin", "-s", sess, "-E", str(seed), "-n", str(photons), "-d", "1"]
+    env = dict(os.environ, OMP_NUM_THREADS="1", MMCGB_DETP_OUT=out)
+    p = subprocess.run(cmd, cwd=workdir, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(p.stdout[-2000:])
+    buf = open(out, "rb").read()
+    count, cols = struct.unpack("<ii", buf[:8])
+    return np.frombuffer(buf, np.float32, count=count * cols, offset=8).reshape(count, cols)
+
+
+def run_ref(workdir, name, seed, photons, normalized=False, savedet=False):
+    sess = f"{name}_{seed}_{int(normalized)}"
+    cmd = [REF, "-f", os.path.join(workdir, name + ".json"), "-c", "sse", "-M", "s", "-C", "0", "-b", "1",
+           "-U", "1" if normalized else "0", "-F", "bin", "-s", sess, "-E", str(seed), "-n", str(photons),
+           "-D", "T", "-d", "1" if savedet else "0"]
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    p = subprocess.run(cmd, cwd=workdir, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(p.stdout[-2000:])
+    log = p.stdout
+    raw = np.fromfile(os.path.join(workdir, sess + ".bin"), np.float64)
+    tests = None
+    absorbed = None
+    for line in log.splitlines():
+        if "ray-tetrahedron tests" in line:
+            tests = float(line.split("photon/ms")[1].split()[1].strip(","))
+        if "absorbed:" in line:
+            absorbed = float(line.split("absorbed:")[1].strip().split("%")[0].split("m")[-1]) / 100.0
+    out = dict(raw=raw, tests=tests, absorbed=absorbed)
+    if savedet:
+        out["det"] = run_ref_detp(workdir, name, seed, photons)
+    return out
+
+
+def main():
+    if not os.path.exists(REF):
+        subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
+    rng = np.random.default_rng(5)
+    with tempfile.TemporaryDirectory() as wd:
+        for name, c in case_defs().items():
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+            c["e0"] = oracle.initelem(c["mesh"].node, c["mesh"].elem, c["mesh"].label, (30.0, 30.0, 0.0))
+            write_json(os.path.join(wd, name + ".json"), name, c)
+            m = c["mesh"]
+            ne = m.ne
+            G = int(round(c["t1"] / c["dt"]))
+            savedet = c["det"] is not None
+            with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+                runs = list(ex.map(lambda s: run_ref(wd, name, s, c["photons"], savedet=savedet),
+                                   [SEED0 + k for k in range(NRUNS)]))
+                norm = ex.submit(run_ref, wd, name, SEED0, c["photons"], True, False).result()
+            fields = np.stack([r["raw"].reshape(G, ne) for r in runs])  # (runs, G, ne)
+            per_elem = fields.sum(axis=1)
+            per_gate = fields.sum(axis=2)
+            cells = rng.choice(G * ne, size=min(4000, G * ne), replace=False)
+            flat = fields.reshape(NRUNS, -1)[:, cells]
+            fx = dict(
+                ne=ne, nn=m.nn, gates=G, photons=c["photons"], seeds=np.arange(NRUNS) + SEED0,
+                elem_mean=per_elem.mean(0).astype(np.float32), elem_std=per_elem.std(0, ddof=1).astype(np.float32),
+                gate_mean=per_gate.mean(0), gate_std=per_gate.std(0, ddof=1),
+                cells=cells.astype(np.int32), cell_mean=flat.mean(0).astype(np.float32),
+                cell_std=flat.std(0, ddof=1).astype(np.float32),
+                # absorbed weight per launched photon: element deposits are (w0-w1)/mua
+                absorbed=(fields.sum(axis=1) * m.media[m.label, 0][None, :].astype(np.float64)).sum(1) / c["photons"],
+                tests_per_photon=np.array([r["tests"] / c["photons"] for r in runs]),
+                raw_seed0=runs[0]["raw"].astype(np.float32) if G == 1 else np.zeros(0, np.float32),
+                norm_seed0=norm["raw"].astype(np.float32) if G == 1 else np.zeros(0, np.float32),
+            )
+            if savedet:
+                M = m.media.shape[0] - 1
+                mua = m.media[1:, 0].astype(np.float64)
+                ndet = len(c["det"])
+                counts, wsum, plen, nscat = [], [], [], []
+                for r in runs:
+                    d = r["det"]
+                    ids = d[:, 0].astype(int)
+                    pp = d[:, 1 + M:1 + 2 * M].astype(np.float64)
+                    w = d[:, -1] * np.exp(-(pp * mua).sum(1))
+                    counts.append([np.count_nonzero(ids == k + 1) for k in range(ndet)])
+                    wsum.append([w[ids == k + 1].sum() for k in range(ndet)])
+                    plen.append(pp.mean(0))
+                    nscat.append(d[:, 1:1 + M].astype(np.float64).mean(0))
+                fx.update(det_count=np.array(counts, np.float64), det_wsum=np.array(wsum),
+                          det_plen=np.array(plen), det_nscat=np.array(nscat))
+            np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **fx)
+            print(name, "ne", ne, "absorbed", fx["absorbed"].mean(), "tests/photon", fx["tests_per_photon"].mean())
+
+
+if __name__ == "__main__":
+    main()
