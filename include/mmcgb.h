@@ -170,6 +170,43 @@ int32_t mmcgb_simulate_batch(int32_t n, mmcgb_mesh* const* meshes, const mmcgb_c
 int32_t mmcgb_run(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, int32_t device,
                   mmcgb_result* res);
 
+/* ---- for callers that cannot allocate device memory ----------------------
+ * No counterpart in the reference (its CUDA host allocates every buffer per
+ * run, src/mmc_cu_host.cu:447-610).  Some callers cannot let a library call
+ * cudaMalloc: programs whose own pool already owns the free GPU memory (a
+ * framework's caching allocator), and serving loops where the device-wide
+ * synchronization of cudaMalloc/cudaFree would stall work in flight.  This
+ * entry runs one simulation of the photon engine on `stream` (a cudaStream_t,
+ * NULL = legacy default stream) into device buffers the caller owns, and
+ * allocates nothing: the work counter and the staged media/detector tables
+ * live in a fixed 8 KiB device array inside the library, held by every GPU
+ * that loads the library until the process exits.
+ *   - outputs are overwritten (zeroed first): field_raw holds the raw element
+ *     deposits, maxgate*ne doubles, gate-major (the layout of mmcgb_result.field
+ *     for basisorder 0, isnormalized 0); energy[1] = escaped weight (energy[0]
+ *     is left 0: the launched weight is nphoton); counters[0] = ray-tet tests,
+ *     counters[1] = photons stopped by the step budget; detp/detcount/seeds as
+ *     in mmcgb_result when issavedet (maxdetphoton*reclen floats, 16-byte seeds)
+ *   - limits: nmedia <= MMCGB_NOALLOC_MAX_MEDIA, detnum <= MMCGB_NOALLOC_MAX_DET,
+ *     accum_f64 = 1, no replay; anything else returns MMCGB_E_ARG
+ *   - the first call on a device looks up the array's device address; make it
+ *     before any stream capture
+ *   - all calls share the array and keep its last contents; the call clears the
+ *     work counter itself.  Calls that overlap on the GPU race on the array.
+ * The call returns after enqueueing; synchronize `stream` before reading. */
+#define MMCGB_NOALLOC_MAX_MEDIA 64
+#define MMCGB_NOALLOC_MAX_DET 256
+typedef struct mmcgb_device_out {
+    double* field_raw;       /* device, maxgate*ne */
+    float* detp;             /* device, maxdetphoton*reclen (issavedet) */
+    uint8_t* seeds;          /* device, maxdetphoton*16 (issaveseed) */
+    uint32_t* detcount;      /* device, 1 (issavedet) */
+    double* energy;          /* device, 2 */
+    uint64_t* counters;      /* device, 2 */
+} mmcgb_device_out;
+int32_t mmcgb_simulate_noalloc(mmcgb_mesh* mesh, const mmcgb_config* cfg, const mmcgb_device_out* out,
+                               void* stream);
+
 /* Fills `cfg` with the reference defaults (src/mmc_utils.c:207-363). */
 void mmcgb_config_defaults(mmcgb_config* cfg);
 

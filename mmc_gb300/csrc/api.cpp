@@ -14,17 +14,9 @@
 #include "../../include/mmcgb.h"
 #include "engine.h"
 #include "mesh.h"
+#include "mesh_handle.h"
 
 using namespace mmcgb;
-
-struct mmcgb_mesh {
-    HostMesh host;
-    int device = 0;
-    TetRec* rec = nullptr;
-    int4* elem = nullptr;
-    float4* node = nullptr;
-    int* label = nullptr;
-};
 
 namespace {
 
@@ -34,6 +26,12 @@ int fail(int code, const std::string& msg) {
     g_err = msg;
     return code;
 }
+
+}  // namespace
+
+void mmcgb::set_last_error(const std::string& msg) { g_err = msg; }
+
+namespace {
 
 int cuda_fail(cudaError_t e, const char* what) {
     return fail(MMCGB_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));

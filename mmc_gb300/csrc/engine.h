@@ -2,6 +2,7 @@
 // photon engine (engine.cu).  Not part of the public C ABI (include/mmcgb.h).
 #pragma once
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 namespace mmcgb {
@@ -98,5 +99,8 @@ cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, in
                            unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
                            unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream);
 LaunchShape default_shape(int device, bool batched);
+
+// Records the message returned by mmcgb_last_error() on this thread.
+void set_last_error(const std::string& msg);
 
 }  // namespace mmcgb

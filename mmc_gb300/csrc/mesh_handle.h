@@ -1,0 +1,14 @@
+// Definition of the opaque mmcgb_mesh handle (include/mmcgb.h): the host
+// copy of the prepared mesh plus its device-resident arrays.
+#pragma once
+#include "engine.h"
+#include "mesh.h"
+
+struct mmcgb_mesh {
+    mmcgb::HostMesh host;
+    int device = 0;
+    mmcgb::TetRec* rec = nullptr;
+    int4* elem = nullptr;
+    float4* node = nullptr;
+    int* label = nullptr;
+};
