@@ -207,6 +207,21 @@ typedef struct mmcgb_device_out {
 int32_t mmcgb_simulate_noalloc(mmcgb_mesh* mesh, const mmcgb_config* cfg, const mmcgb_device_out* out,
                                void* stream);
 
+/* ---- host-only stages (no GPU needed) ---------------------------------- */
+/* Mesh preparation alone: orientation fix and volumes (src/mmc_mesh.c:910-974),
+ * face neighbours (src/mmc_highorder.cpp:128-159), face normals and plane
+ * offsets (src/mmc_mesh.c:1572-1601), exterior-face numbering
+ * (src/mmc_mesh.c:1466-1474).  Outputs (any may be NULL): elem ne*4,
+ * facenb ne*4, normals ne*16 (nx[4] ny[4] nz[4] d[4]), evol ne, nvol nn, nf. */
+int32_t mmcgb_prepare_host(const mmcgb_mesh_desc* desc, int32_t* elem, int32_t* facenb, float* normals,
+                           float* evol, float* nvol, int32_t* nf);
+/* Output stage alone: elem->node scatter of raw element deposits
+ * (src/mmc_cu_host.cu:916-976), surface nodal-volume fix
+ * (src/mmc_mesh.c:1344-1386) and normalization (src/mmc_mesh.c:2154-2279).
+ * raw: maxgate*ne; field: maxgate*datalen (datalen = nn if basisorder). */
+int32_t mmcgb_normalize_host(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, const double* raw,
+                             double energytot, double energyesc, double* field, double* normalizer);
+
 /* Fills `cfg` with the reference defaults (src/mmc_utils.c:207-363). */
 void mmcgb_config_defaults(mmcgb_config* cfg);
 

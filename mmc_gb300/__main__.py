@@ -1,0 +1,123 @@
+"""Command line front end mirroring the reference's ``mmc`` binary for the
+photon path (src/mmc.c:58-112 and the option table of src/mmc_utils.c:103-128):
+
+    python -m mmc_gb300 -f input.json [-n photons] [-E seed|file.mch] [-s session]
+        [-C basisorder] [-U normalize] [-O x|f|e|j|l|p] [-d savedet] [-x saveexit]
+        [-q saveseed] [-m momentum] [-b reflect] [-e minenergy] [-P replaydet]
+        [-H maxdetphoton] [-F bin|dat|mch] [-G gpu] [-D T] [-M s] [--bench]
+
+Writes <session>.bin (or .dat) with the normalized output and, when detected
+photons are saved, <session>.mch -- as the reference does in standalone mode
+(src/mmc_cu_host.cu:1397-1440).  `-E file.mch` replays the photons saved in a
+previous run (src/mmc_mesh.c:815-898).
+"""
+from __future__ import annotations
+
+import argparse
+import dataclasses
+import os
+import sys
+import time
+
+import numpy as np
+
+
+def _intflag(v):
+    return int(float(v))
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="mmc_gb300", description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
+    ap.add_argument("-f", "--input", required=True)
+    ap.add_argument("-n", "--photon", type=_intflag)
+    ap.add_argument("-E", "--seed")
+    ap.add_argument("-s", "--session")
+    ap.add_argument("-C", "--basisorder", type=int)
+    ap.add_argument("-U", "--normalize", type=int)
+    ap.add_argument("-O", "--outputtype")
+    ap.add_argument("-d", "--savedet", type=int)
+    ap.add_argument("-x", "--saveexit", type=int)
+    ap.add_argument("-q", "--saveseed", type=int)
+    ap.add_argument("-m", "--momentum", type=int)
+    ap.add_argument("-b", "--reflect", type=int)
+    ap.add_argument("-e", "--minenergy", type=float)
+    ap.add_argument("-P", "--replaydet", type=int, default=0)
+    ap.add_argument("-H", "--maxdetphoton", type=_intflag)
+    ap.add_argument("-F", "--outputformat")
+    ap.add_argument("-G", "--gpu", type=int, default=1)
+    ap.add_argument("-D", "--debug", default="")
+    ap.add_argument("-M", "--method", default="s")
+    ap.add_argument("-r", "--root", default="")
+    args = ap.parse_args(argv)
+
+    from . import io
+    from .core import Mesh, simulate
+    from .io import OUTPUT_LETTERS
+
+    if args.method not in ("s", "elem", "b"):
+        ap.error("only the branchless Badouel tracer (-M s) with element deposition is implemented")
+    mesh_d, cfg, meta = io.load_input(args.input)
+    upd = {}
+    if args.photon is not None:
+        upd["nphoton"] = args.photon
+    if args.basisorder is not None:
+        upd["basisorder"] = args.basisorder
+    if args.normalize is not None:
+        upd["isnormalized"] = args.normalize
+    if args.outputtype:
+        upd["outputtype"] = OUTPUT_LETTERS[args.outputtype.lower()]
+    for k, a in (("issavedet", args.savedet), ("issaveexit", args.saveexit), ("issaveseed", args.saveseed),
+                 ("ismomentum", args.momentum), ("isreflect", args.reflect), ("minenergy", args.minenergy),
+                 ("maxdetphoton", args.maxdetphoton)):
+        if a is not None:
+            upd[k] = a
+    replay_file = None
+    if args.seed is not None:
+        if args.seed.endswith(".mch"):
+            replay_file = args.seed
+        else:
+            upd["seed"] = int(args.seed)
+    cfg = dataclasses.replace(cfg, **upd)
+    session = args.session or meta["session"]
+    fmt = (args.outputformat or meta["outputformat"]).lower()
+    outdir = args.root or os.getcwd()
+    device = max(0, args.gpu - 1)
+    mesh = Mesh(mesh_d["node"], mesh_d["elem"], mesh_d["label"], mesh_d.get("facenb"), device=device)
+
+    t0 = time.perf_counter()
+    if replay_file:
+        from . import replay as rp
+        detp, hdr, seeds = io.read_mch(replay_file)
+        if seeds is None:
+            raise SystemExit(f"{replay_file} holds no seeds (rerun the baseline with -q 1)")
+        res, idx = rp.replay(mesh, cfg, detp, seeds, cfg.outputtype if cfg.outputtype in ("wl", "wp", "wn", "jacobian")
+                             else "wl", args.replaydet, normalize=bool(cfg.isnormalized))
+        nphoton = len(idx)
+    else:
+        res = simulate(mesh, cfg)
+        nphoton = cfg.nphoton
+    dt = time.perf_counter() - t0
+    print(f"simulated {nphoton} photons in {dt * 1e3:.1f} ms ({nphoton / max(dt * 1e3, 1e-9):.2f} photon/ms), "
+          f"{res.raytet} ray-tetrahedron tests, kernel {res.kernel_ms:.1f} ms")
+    if res.energytot > 0 and not replay_file:
+        print(f"total simulated energy: {res.energytot:.0f}\tabsorbed: {100 * res.absorbed_fraction:.5f}%\t"
+              f"normalizor={res.normalizer:g}")
+    if "T" in args.debug.upper():
+        print(f"detected {res.detected} photons")
+    base = os.path.join(outdir, session)
+    if res.field is not None:
+        if fmt == "dat":
+            io.write_dat(base + ".dat", res.field)
+        else:
+            io.write_bin(base + ".bin", res.field)
+    if res.detp is not None and cfg.issavedet:
+        io.write_mch(base + ".mch", res.detp, res.seeds if cfg.issaveseed else None,
+                     maxmedia=np.asarray(cfg.media).shape[0] - 1,
+                     detnum=0 if cfg.detpos is None else len(cfg.detpos), totalphoton=nphoton,
+                     detected=res.detected, unitinmm=cfg.unitinmm, normalizer=res.normalizer)
+    mesh.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -71,7 +71,7 @@ EXPORTS = [
     "mmcgb_abi_version", "mmcgb_last_error", "mmcgb_config_defaults", "mmcgb_mesh_create",
     "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export", "mmcgb_mesh_locate",
     "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run", "mmcgb_session_begin", "mmcgb_session_launch",
-    "mmcgb_session_sync", "mmcgb_session_end",
+    "mmcgb_session_sync", "mmcgb_session_end", "mmcgb_prepare_host", "mmcgb_normalize_host",
 ]
 
 
@@ -105,7 +105,10 @@ def load():
         lib.mmcgb_session_launch.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64]
         lib.mmcgb_session_sync.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
         lib.mmcgb_session_end.argtypes = [C.c_void_p, C.c_void_p]
-        for name in ("mmcgb_session_begin", "mmcgb_session_launch", "mmcgb_session_sync", "mmcgb_session_end",
+        lib.mmcgb_prepare_host.argtypes = [C.POINTER(MeshDesc)] + [C.c_void_p] * 6
+        lib.mmcgb_normalize_host.argtypes = [C.POINTER(MeshDesc), C.POINTER(Config), C.c_void_p, C.c_double,
+                                             C.c_double, C.c_void_p, C.POINTER(C.c_double)]
+        for name in ("mmcgb_prepare_host", "mmcgb_normalize_host", "mmcgb_session_begin", "mmcgb_session_launch", "mmcgb_session_sync", "mmcgb_session_end",
                      "mmcgb_mesh_create", "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export",
                      "mmcgb_mesh_locate", "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run"):
             getattr(lib, name).restype = C.c_int32

@@ -19,11 +19,47 @@ import numpy as np
 
 from . import _native as N
 
-OUTPUT_TYPES = {"flux": 0, "fluence": 1, "energy": 2, "jacobian": 3, "wl": 4, "wp": 5}
+OUTPUT_TYPES = {"flux": 0, "fluence": 1, "energy": 2, "jacobian": 3, "wl": 4, "wp": 5, "wn": 16}
 
 
 def _ptr(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data
+
+
+def _desc(node, elem, label, facenb=None):
+    node = np.ascontiguousarray(node, dtype=np.float32).reshape(-1, 3)
+    elem = np.ascontiguousarray(elem, dtype=np.int32).reshape(-1, 4)
+    label = np.ascontiguousarray(label, dtype=np.int32).reshape(-1)
+    fnb = None if facenb is None else np.ascontiguousarray(facenb, dtype=np.int32).reshape(-1, 4)
+    d = N.MeshDesc(node.shape[0], elem.shape[0], _ptr(node), _ptr(elem), _ptr(label), _ptr(fnb))
+    return d, (node, elem, label, fnb)
+
+
+def prepare_host(node, elem, label, facenb=None):
+    """Host mesh preparation (mmcgb_prepare_host): dict of elem, facenb,
+    normals, evol, nvol, nf.  Needs no GPU."""
+    d, keep = _desc(node, elem, label, facenb)
+    ne, nn = d.ne, d.nn
+    out = dict(elem=np.empty((ne, 4), np.int32), facenb=np.empty((ne, 4), np.int32),
+               normals=np.empty((ne, 16), np.float32), evol=np.empty(ne, np.float32), nvol=np.empty(nn, np.float32))
+    nf = C.c_int32()
+    N.check(N.load().mmcgb_prepare_host(C.byref(d), _ptr(out["elem"]), _ptr(out["facenb"]), _ptr(out["normals"]),
+                                        _ptr(out["evol"]), _ptr(out["nvol"]), C.byref(nf)))
+    out["nf"] = nf.value
+    return out
+
+
+def normalize_host(node, elem, label, cfg: "SimConfig", raw, energytot: float, energyesc: float):
+    """Output stage on the host (mmcgb_normalize_host): returns (field, normalizer)."""
+    d, keep = _desc(node, elem, label)
+    c, ckeep = cfg.to_c()
+    raw = np.ascontiguousarray(raw, np.float64)
+    datalen = d.nn if cfg.basisorder else d.ne
+    field = np.zeros((cfg.maxgate, datalen), np.float64)
+    norm = C.c_double()
+    N.check(N.load().mmcgb_normalize_host(C.byref(d), C.byref(c), _ptr(raw), float(energytot), float(energyesc),
+                                          _ptr(field), C.byref(norm)))
+    return field, norm.value
 
 
 class Mesh:

@@ -564,6 +564,36 @@ int32_t mmcgb_simulate_batch(int32_t n, mmcgb_mesh* const* meshes, const mmcgb_c
     return rc;
 }
 
+int32_t mmcgb_prepare_host(const mmcgb_mesh_desc* desc, int32_t* elem, int32_t* facenb, float* normals, float* evol,
+                           float* nvol, int32_t* nf) {
+    if (!desc) return fail(MMCGB_E_ARG, "null argument");
+    HostMesh h;
+    std::string err;
+    int rc = prepare_mesh(*desc, h, err);
+    if (rc) return fail(rc, err);
+    if (elem) std::memcpy(elem, h.elem.data(), sizeof(int) * h.elem.size());
+    if (facenb) std::memcpy(facenb, h.facenb.data(), sizeof(int) * h.facenb.size());
+    if (normals) std::memcpy(normals, h.normals.data(), sizeof(float) * h.normals.size());
+    if (evol) std::memcpy(evol, h.evol.data(), sizeof(float) * h.evol.size());
+    if (nvol) std::memcpy(nvol, h.nvol.data(), sizeof(float) * h.nvol.size());
+    if (nf) *nf = h.nf;
+    return MMCGB_OK;
+}
+
+int32_t mmcgb_normalize_host(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, const double* raw,
+                             double energytot, double energyesc, double* field, double* normalizer) {
+    if (!desc || !cfg || !raw || !field) return fail(MMCGB_E_ARG, "null argument");
+    HostMesh h;
+    std::string err;
+    int rc = prepare_mesh(*desc, h, err);
+    if (rc) return fail(rc, err);
+    if (cfg->nmedia < 2 || !cfg->media || h.maxlabel > cfg->nmedia - 1) return fail(MMCGB_E_ARG, "media table does not cover the mesh labels");
+    if (!(cfg->tstep > 0.f)) return fail(MMCGB_E_ARG, "tstep must be positive");
+    const double n = normalize_output(h, *cfg, gates_of(*cfg), raw, energytot, energyesc, field);
+    if (normalizer) *normalizer = n;
+    return MMCGB_OK;
+}
+
 int32_t mmcgb_run(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, int32_t device, mmcgb_result* res) {
     mmcgb_mesh* m = nullptr;
     int rc = mmcgb_mesh_create(desc, device, &m);

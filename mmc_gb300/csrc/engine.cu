@@ -127,6 +127,13 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
         L.slen -= Lmove * prop.y;
         float ww = currweight - L.weight;
         L.ptime += Lmove * rc;
+        if (ot == OT_WN) {  // scatter counts are deposited at the scattering events only
+            L.px = L.px + Lmove * L.vx;
+            L.py = L.py + Lmove * L.vy;
+            L.pz = L.pz + Lmove * L.vz;
+            L.slen = (L.faceid == -2) ? 0.f : L.slen;
+            return;
+        }
         float gf;
         if (S.replay && (ot == OT_WL || ot == OT_WP))
             gf = __ldg(S.replaytime + L.pid) * S.Rtstep;
@@ -543,6 +550,12 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                         if (S.photon_det) S.photon_det[L.pid] = 0;
                         ended = true;
                     } else {
+                        if (S.replay && S.outputtype == OT_WN) {
+                            const float gf = __ldg(S.replaytime + L.pid) * S.Rtstep;
+                            int gate = (gf < (float)(S.maxgate - 1)) ? (int)gf : S.maxgate - 1;
+                            gate = max(gate, 0);
+                            deposit(S, (unsigned)(L.eid - 1) + (unsigned)(gate * S.ne), __ldg(S.replayweight + L.pid));
+                        }
                         float ctheta;
                         const int tp = L.label;
                         L.slen0 = next_scatter(L, med[tp].z, ctheta);

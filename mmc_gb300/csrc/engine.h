@@ -8,7 +8,11 @@
 namespace mmcgb {
 
 // Output/physics enums follow the reference numbering (src/mmc_utils.h:92-110).
-enum OutputType { OT_FLUX = 0, OT_FLUENCE = 1, OT_ENERGY = 2, OT_JACOBIAN = 3, OT_WL = 4, OT_WP = 5 };
+enum OutputType { OT_FLUX = 0, OT_FLUENCE = 1, OT_ENERGY = 2, OT_JACOBIAN = 3, OT_WL = 4, OT_WP = 5,
+                  // replay only, no reference counterpart: replay weight deposited once per
+                  // scattering event in the element where it happens (the scatter-count term of
+                  // the mus derivative of a detected photon's likelihood)
+                  OT_WN = 16 };
 enum Boundary { BC_NOREFLECT = 0, BC_REFLECT = 1, BC_ABSORBEXT = 2, BC_MIRROR = 3 };
 
 constexpr int kMaxMedia = 64;        // media rows (incl. background) staged in shared memory

@@ -95,9 +95,10 @@ double normalize_output(const HostMesh& m, const mmcgb_config& cfg, int G, const
     const float Etotal = (float)energytot;
     const float Eabsorb = (float)(energytot - energyesc);
     const bool replay = cfg.replayseed != nullptr;
-    if (replay && (cfg.outputtype == OT_JACOBIAN || cfg.outputtype == OT_WL || cfg.outputtype == OT_WP)) {
+    if (replay && (cfg.outputtype == OT_JACOBIAN || cfg.outputtype == OT_WL || cfg.outputtype == OT_WP ||
+                   cfg.outputtype == OT_WN)) {
         normalizor = 1.f / (1e-4f * (float)cfg.nphoton);
-        if (cfg.outputtype == OT_WL || cfg.outputtype == OT_WP) normalizor = 1.f / Etotal;
+        if (cfg.outputtype != OT_JACOBIAN) normalizor = 1.f / Etotal;
     } else if (cfg.outputtype == OT_ENERGY) {
         normalizor = 1.f / Etotal;
     } else {

@@ -1,0 +1,179 @@
+"""File formats of the reference's front ends.
+
+* JSON input (``mmc -f input.json``; the subset the photon path reads,
+  src/mmc_utils.c:1566-2392): Session, Domain.Media, Mesh (MeshNode/MeshElem
+  inline, or MeshID naming node_/elem_/prop_/facenb_<ID>.dat files),
+  Forward (T0/T1/Dt/N0), Optode.Source (Pos/Dir), Optode.Detector[{Pos, R}].
+* ``.mch`` detected-photon history: 64-byte header (magic "MCXH", version 1,
+  src/mmc_utils.h:168-184), float32 records, then 16-byte RNG seeds
+  (src/mmc_mesh.c:1978-2010).
+* ``.bin`` output: raw float64 [gate][datalen] (src/mmc_utils.c:966-990).
+* ``.dat`` output: text "index value" per line (src/mmc_mesh.c:1759-1813).
+"""
+from __future__ import annotations
+
+import json
+import os
+import struct
+from typing import Optional
+
+import numpy as np
+
+from .core import SimConfig
+
+MCH_HEADER = struct.Struct("<4sIIIIIIIfIfIiI2i")  # 64 bytes
+OUTPUT_LETTERS = {"x": "flux", "f": "fluence", "e": "energy", "j": "jacobian", "l": "wl", "p": "wp", "n": "wn"}
+OUTPUT_NAMES = {"flux": "flux", "fluence": "fluence", "energy": "energy", "jacobian": "jacobian", "wl": "wl",
+                "wp": "wp", "wn": "wn"}
+
+
+# ---------------------------------------------------------------------------
+# .dat meshes (src/mmc_mesh.c:563-780): a "1 count" header line, then rows
+# ---------------------------------------------------------------------------
+def _read_table(path, ncols, skip_index=True):
+    with open(path) as f:
+        head = f.readline().split()
+        n = int(head[1])
+        rows = np.loadtxt(f, max_rows=n, ndmin=2)
+    return rows[:, 1:1 + ncols] if skip_index else rows[:, :ncols]
+
+
+def read_dat_mesh(mesh_id: str, root: str):
+    node = _read_table(os.path.join(root, f"node_{mesh_id}.dat"), 3).astype(np.float32)
+    el = _read_table(os.path.join(root, f"elem_{mesh_id}.dat"), 5)
+    elem = el[:, :4].astype(np.int32)
+    label = el[:, 4].astype(np.int32) if el.shape[1] > 4 else np.ones(len(el), np.int32)
+    out = dict(node=node, elem=elem, label=label)
+    fnb = os.path.join(root, f"facenb_{mesh_id}.dat")
+    if os.path.exists(fnb):
+        out["facenb"] = _read_table(fnb, 4, skip_index=False).astype(np.int32)
+    prop = os.path.join(root, f"prop_{mesh_id}.dat")
+    if os.path.exists(prop):
+        p = _read_table(prop, 4).astype(np.float32)
+        out["media"] = np.vstack([[0.0, 0.0, 1.0, 1.0], p]).astype(np.float32)
+    return out
+
+
+def _media_from_json(media):
+    rows = []
+    for m in media:
+        if isinstance(m, dict):
+            rows.append([m.get("mua", 0.0), m.get("mus", 0.0), m.get("g", 1.0), m.get("n", 1.0)])
+        else:
+            rows.append(list(m)[:4])
+    return np.asarray(rows, np.float32)
+
+
+def load_input(path: str):
+    """Reads a reference JSON input; returns (mesh dict, SimConfig, meta)."""
+    with open(path) as f:
+        cfgj = json.load(f)
+    root = os.path.dirname(os.path.abspath(path))
+    ses = cfgj.get("Session", {})
+    dom = cfgj.get("Domain", {})
+    msh = cfgj.get("Mesh", {})
+    fwd = cfgj.get("Forward", {})
+    opt = cfgj.get("Optode", {})
+    if "MeshNode" in msh:
+        node = np.asarray(msh["MeshNode"], np.float32).reshape(-1, 3)
+        el = np.asarray(msh["MeshElem"], np.int64)
+        elem = el[:, :4].astype(np.int32)
+        label = el[:, 4].astype(np.int32) if el.shape[1] > 4 else np.ones(len(el), np.int32)
+        mesh = dict(node=node, elem=elem, label=label)
+    elif "MeshID" in msh:
+        mesh = read_dat_mesh(str(msh["MeshID"]), root)
+    else:
+        raise ValueError("input has neither Mesh.MeshNode/MeshElem nor Mesh.MeshID")
+    if "Media" in dom:
+        media = _media_from_json(dom["Media"])
+    elif "media" in mesh:
+        media = mesh["media"]
+    else:
+        raise ValueError("input has no Domain.Media and no prop_<ID>.dat")
+    unit = float(msh.get("LengthUnit", dom.get("LengthUnit", 1.0)))
+    if unit != 1.0:
+        mesh["node"] = (mesh["node"] * unit).astype(np.float32)
+    src = opt.get("Source", {})
+    dets = opt.get("Detector", [])
+    detpos = None
+    if dets:
+        detpos = np.array([[*d["Pos"][:3], d.get("R", 1.0)] for d in dets], np.float32)
+    srcdir = np.asarray(src.get("Dir", [0.0, 0.0, 1.0]), np.float64)[:3]
+    srcdir = srcdir / np.linalg.norm(srcdir)
+    stype = str(src.get("Type", "pencil")).lower()
+    if stype not in ("pencil", ""):
+        raise ValueError(f"source type '{stype}' is not implemented (pencil only)")
+    t0 = float(fwd.get("T0", 0.0))
+    t1 = float(fwd.get("T1", 5e-9))
+    dt = float(fwd.get("Dt", t1 - t0))
+    otype = ses.get("OutputType", "x")
+    otype = OUTPUT_LETTERS.get(str(otype).lower(), OUTPUT_NAMES.get(str(otype).lower(), "flux"))
+    cfg = SimConfig(
+        media=media, nphoton=int(float(ses.get("Photons", 1e6))), seed=int(ses.get("RNGSeed", 0x623F9A9E)),
+        srcpos=tuple(float(x) for x in src.get("Pos", [0, 0, 0])[:3]), srcdir=tuple(float(x) for x in srcdir),
+        e0=int(msh.get("InitElem", 0)), tstart=t0, tend=t1, tstep=dt,
+        isreflect=int(ses.get("DoMismatch", 1)), isspecular=int(ses.get("DoSpecular", 0)),
+        issavedet=int(ses.get("DoPartialPath", 1 if dets else 0)), issaveseed=int(ses.get("DoSaveSeed", 0)),
+        issaveexit=int(ses.get("DoSaveExit", 0)), isnormalized=int(ses.get("DoNormalize", 1)),
+        basisorder=int(ses.get("BasisOrder", 1)), outputtype=otype, nout=float(fwd.get("N0", 1.0)),
+        detpos=detpos, unitinmm=unit)
+    meta = dict(session=str(ses.get("ID", "default")), outputformat=str(ses.get("OutputFormat", "bin")),
+                saveweight=int(ses.get("DoSaveVolume", 1)), root=root)
+    return mesh, cfg, meta
+
+
+# ---------------------------------------------------------------------------
+# .mch
+# ---------------------------------------------------------------------------
+def write_mch(path: str, detp: np.ndarray, seeds: Optional[np.ndarray], maxmedia: int, detnum: int,
+              totalphoton: int, detected: int, unitinmm: float = 1.0, normalizer: float = 1.0,
+              savedetflag: int = 0):
+    detp = np.ascontiguousarray(detp, np.float32)
+    n, cols = detp.shape if detp.ndim == 2 else (0, 0)
+    seedbyte = 16 if seeds is not None else 0
+    hdr = MCH_HEADER.pack(b"MCXH", 1, maxmedia, detnum, cols, int(totalphoton) & 0xFFFFFFFF, int(detected), n,
+                          float(unitinmm), seedbyte, float(normalizer), 1, 1, savedetflag, 0, 0)
+    with open(path, "wb") as f:
+        f.write(hdr)
+        f.write(detp.tobytes())
+        if seeds is not None:
+            f.write(np.ascontiguousarray(seeds, np.uint8).reshape(n, 16).tobytes())
+
+
+def read_mch(path: str):
+    """Returns (records (n, cols) float32, header dict, seeds (n, 16) uint8 or None)."""
+    with open(path, "rb") as f:
+        buf = f.read()
+    h = MCH_HEADER.unpack(buf[:64])
+    if h[0] != b"MCXH":
+        raise ValueError(f"{path}: not an mch file")
+    keys = ["magic", "version", "maxmedia", "detnum", "colcount", "totalphoton", "detected", "savedphoton",
+            "unitinmm", "seedbyte", "normalizer", "srcnum", "respin", "savedetflag"]
+    hd = dict(zip(keys, h[:14]))
+    n, cols = hd["savedphoton"], hd["colcount"]
+    detp = np.frombuffer(buf, np.float32, count=n * cols, offset=64).reshape(n, cols).copy()
+    seeds = None
+    if hd["seedbyte"]:
+        off = 64 + n * cols * 4
+        seeds = np.frombuffer(buf, np.uint8, count=n * hd["seedbyte"], offset=off).reshape(n, hd["seedbyte"]).copy()
+    return detp, hd, seeds
+
+
+# ---------------------------------------------------------------------------
+# fluence outputs
+# ---------------------------------------------------------------------------
+def write_bin(path: str, field: np.ndarray):
+    np.ascontiguousarray(field, np.float64).tofile(path)
+
+
+def read_bin(path: str, gates: int):
+    d = np.fromfile(path, np.float64)
+    return d.reshape(gates, -1)
+
+
+def write_dat(path: str, field: np.ndarray):
+    field = np.asarray(field, np.float64)
+    with open(path, "w") as f:
+        for g in range(field.shape[0]):
+            for j, v in enumerate(field[g]):
+                f.write(f"{j + 1}\t{v:e}\n")

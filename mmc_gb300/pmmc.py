@@ -1,0 +1,121 @@
+"""pmmc-compatible Python interface: ``run(cfg: dict) -> dict``.
+
+Mirrors the reference binding ``pmmc.run`` (src/pmmc.cpp:903-1351, key
+parsing :117-890) for the photon path: the same input keys and the same
+output keys and array layouts (``flux`` as [datalen, maxgate], ``detp`` as
+[columns, ndetected], ``seeds`` as [16, ndetected]; these are transposed views
+of the row-major arrays the engine returns).  Errors raise ``ValueError`` for
+bad inputs and ``RuntimeError`` for engine failures, as pmmc does.
+"""
+from __future__ import annotations
+
+import dataclasses
+import time
+
+import numpy as np
+
+from . import _native
+from .core import Mesh, SimConfig, simulate
+
+_SCALARS_INT = ["nphoton", "isreflect", "isspecular", "ismomentum", "issaveexit", "issavedet", "issaveseed",
+                "basisorder", "isnormalized", "maxdetphoton", "voidtime", "e0"]
+_SCALARS_FLOAT = ["tstart", "tstep", "tend", "roulettesize", "minenergy", "unitinmm", "nout"]
+_METHODS = {"plucker": None, "havel": None, "badouel": None, "elem": "elem", "grid": None}
+_OUTPUTS = {"flux", "fluence", "energy", "jacobian", "wl", "wp", "wn"}
+
+
+def version() -> str:
+    from . import __version__
+    return f"mmc_gb300 {__version__}"
+
+
+def gpuinfo():
+    import torch
+    return [dict(name=torch.cuda.get_device_name(i), id=i + 1) for i in range(torch.cuda.device_count())]
+
+
+def _parse(cfg: dict):
+    for req in ("node", "elem", "prop", "srcpos"):
+        if req not in cfg:
+            raise ValueError(f"cfg.{req} is required")
+    node = np.asarray(cfg["node"], np.float32)
+    elem = np.asarray(cfg["elem"])
+    if elem.ndim != 2 or elem.shape[1] not in (4, 5):
+        raise ValueError("the 'elem' field must have 4 columns (labels in 'elemprop') or 5")
+    if elem.shape[1] == 5 and "elemprop" not in cfg:
+        label = elem[:, 4].astype(np.int32)
+    else:
+        label = np.asarray(cfg.get("elemprop", np.ones(len(elem))), np.int32).reshape(-1)
+    elem = elem[:, :4].astype(np.int32)
+    prop = np.asarray(cfg["prop"], np.float32).reshape(-1, 4)
+    method = str(cfg.get("method", "elem")).lower()
+    if method not in _METHODS:
+        raise ValueError(f"unknown method '{method}'")
+    if _METHODS[method] is None:
+        raise ValueError(f"method '{method}' is not implemented (use 'elem': branchless Badouel, element deposit)")
+    srctype = str(cfg.get("srctype", "pencil")).lower()
+    if srctype != "pencil":
+        raise ValueError(f"srctype '{srctype}' is not implemented (pencil only)")
+    kw = dict(media=prop, srcpos=tuple(np.asarray(cfg["srcpos"], np.float64).ravel()[:3]))
+    if "srcdir" in cfg:
+        d = np.asarray(cfg["srcdir"], np.float64).ravel()[:3]
+        kw["srcdir"] = tuple(d / np.linalg.norm(d))
+    for k in _SCALARS_INT:
+        if k in cfg:
+            kw[k] = int(cfg[k])
+    for k in _SCALARS_FLOAT:
+        if k in cfg:
+            kw[k] = float(cfg[k])
+    if "outputtype" in cfg:
+        ot = str(cfg["outputtype"]).lower()
+        if ot not in _OUTPUTS:
+            raise ValueError("the specified output type is not supported")
+        kw["outputtype"] = ot
+    if "detpos" in cfg:
+        kw["detpos"] = np.asarray(cfg["detpos"], np.float32).reshape(-1, 4)
+    seeds = None
+    if "seed" in cfg:
+        s = cfg["seed"]
+        if np.isscalar(s):
+            kw["seed"] = int(s)
+        else:
+            seeds = np.asarray(s, np.uint8)
+            if seeds.shape[0] != 16:
+                raise ValueError("the row number of cfg.seed does not match RNG seed byte-length")
+    if "tend" in kw and "tstep" not in kw:
+        kw["tstep"] = kw["tend"] - kw.get("tstart", 0.0)
+    return node, elem, label, cfg.get("facenb"), SimConfig(**kw), seeds
+
+
+def run(cfg: dict) -> dict:
+    node, elem, label, facenb, sc, seeds = _parse(cfg)
+    device = max(0, int(cfg.get("gpuid", 1)) - 1) if np.isscalar(cfg.get("gpuid", 1)) else 0
+    t0 = time.perf_counter()
+    try:
+        mesh = Mesh(node, elem, label, facenb, device=device)
+        if seeds is not None:
+            from . import replay as rp
+            detp = np.asarray(cfg.get("detphotons"), np.float32)
+            if detp is None or detp.ndim != 2:
+                raise ValueError("you give cfg.seed for replay, but did not specify cfg.detphotons")
+            res, idx = rp.replay(mesh, sc, detp.T.copy(), seeds.T.copy(),
+                                 sc.outputtype if sc.outputtype in ("wl", "wp", "wn", "jacobian") else "wl",
+                                 int(cfg.get("replaydet", 0)), normalize=bool(sc.isnormalized))
+            nph = len(idx)
+        else:
+            res = simulate(mesh, sc)
+            nph = sc.nphoton
+        mesh.close()
+    except _native.MmcgbError as e:
+        if e.code == 1:
+            raise ValueError(str(e)) from e
+        raise RuntimeError(str(e)) from e
+    out = {"flux": res.field.T, "stat": dict(runtime=(time.perf_counter() - t0) * 1e3, nphoton=nph,
+                                             energytot=res.energytot, energyabs=res.energytot - res.energyesc,
+                                             normalizer=res.normalizer, raytet=res.raytet,
+                                             kernel_ms=res.kernel_ms)}
+    if sc.issavedet and res.detp is not None and len(res.detp):
+        out["detp"] = res.detp.T
+        if sc.issaveseed and res.seeds is not None:
+            out["seeds"] = res.seeds.T
+    return out

@@ -23,7 +23,11 @@ case "$(uname -m)" in
     *) echo "reference CPU engine needs SSE4.1 (x86-64); host is $(uname -m)" >&2; exit 3 ;;
 esac
 mkdir -p "$OUT/obj"
-CFLAGS="-O3 -fopenmp -ffast-math -fno-strict-aliasing -w -DMMC_USE_SSE -DHAVE_SSE2 -msse -msse2 -msse3 -mssse3 -msse4.1 -DMMC_XORSHIFT -DUSE_OS_TIMER -I$SRC -I$SRC/zmat/easylzma -I$SRC/ubj -include $HERE/ref_shim.h"
+# The reference's own Makefile adds -ffast-math; it is left out here so the
+# binary follows the IEEE semantics of the reference source, which the oracle
+# pins bit for bit (volumes of jittered tets cancel badly and fast-math
+# reassociation moves them by ~1e-3).
+CFLAGS="-O3 -fopenmp -fno-strict-aliasing -w -DMMC_USE_SSE -DHAVE_SSE2 -msse -msse2 -msse3 -mssse3 -msse4.1 -DMMC_XORSHIFT -DUSE_OS_TIMER -I$SRC -I$SRC/zmat/easylzma -I$SRC/ubj -include $HERE/ref_shim.h"
 ZFLAGS="-DNO_LZMA -DNO_LZ4 -DNO_BLOSC2 -DNO_ZSTD"
 CSRCS="mmc mmc_host mmc_utils mmc_mesh mmc_raytrace mmc_rand_xorshift128p mmc_tictoc mmc_bench cjson/cJSON ubj/ubjw"
 CXXSRCS="mmc_highorder mmc_neurojson"

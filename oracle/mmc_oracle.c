@@ -29,7 +29,7 @@
 #define O_ID_UNDEF   0x7FFFFFFF
 #define O_DELTA_MUA  1e-4f
 
-enum { OT_FLUX = 0, OT_FLUENCE, OT_ENERGY, OT_JACOBIAN, OT_WL, OT_WP };
+enum { OT_FLUX = 0, OT_FLUENCE, OT_ENERGY, OT_JACOBIAN, OT_WL, OT_WP, OT_WN = 16 };
 enum { BC_NOREFLECT = 0, BC_REFLECT, BC_ABSORBEXT, BC_MIRROR };
 
 /* face tables: src/mmc_mesh.c:59 (out), :71 (facemap), :95 (faceorder),
@@ -393,6 +393,12 @@ static float raytet_step(engine* g, ray* r) {
         r->slen -= r->Lmove * mus;
         float ww = currweight - r->weight;
         r->photontimer += r->Lmove * rc;
+        if (cfg->outputtype == OT_WN) { /* deposits happen at scattering events only */
+            r->px = r->px + r->Lmove * r->vx;
+            r->py = r->py + r->Lmove * r->vy;
+            r->pz = r->pz + r->Lmove * r->vz;
+            return (r->faceid == -2) ? 0.f : r->slen;
+        }
         float gf;
         if (replay && (cfg->outputtype == OT_WL || cfg->outputtype == OT_WP))
             gf = cfg->replaytime[r->photonid] * g->Rtstep;
@@ -662,6 +668,13 @@ static void onephoton(engine* g, uint64_t pidx, float* ppath, oracle_out* out, t
                 break;
             }
         }
+        if (cfg->replayseed && cfg->outputtype == OT_WN) {
+            /* replay weight once per scattering event, in the element where it happens */
+            float gf = cfg->replaytime[r->photonid] * g->Rtstep;
+            int gate = (gf < (float)(g->maxgate - 1)) ? (int)gf : g->maxgate - 1;
+            if (gate < 0) gate = 0;
+            deposit(g, (uint32_t)(r->eid - 1) + (uint32_t)(gate * g->ne), cfg->replayweight[r->photonid]);
+        }
         float mom = 0.f;
         int tp = g->type[r->eid - 1];
         r->slen0 = next_scatter(medium(g, tp, 2), r, ran, &mom);
@@ -823,9 +836,10 @@ double oracle_normalize(int nn, const float* node, int ne, const int* elem, cons
         float Etotal = (float)energytot;
         float Eabsorb = (float)(energytot - energyesc);
         int replay = (cfg->replayseed != NULL);
-        if (replay && (cfg->outputtype == OT_JACOBIAN || cfg->outputtype == OT_WL || cfg->outputtype == OT_WP)) {
+        if (replay && (cfg->outputtype == OT_JACOBIAN || cfg->outputtype == OT_WL || cfg->outputtype == OT_WP ||
+                       cfg->outputtype == OT_WN)) {
             normalizor = 1.f / (O_DELTA_MUA * cfg->nphoton);
-            if (cfg->outputtype == OT_WL || cfg->outputtype == OT_WP) normalizor = 1.f / Etotal;
+            if (cfg->outputtype != OT_JACOBIAN) normalizor = 1.f / Etotal;
         } else if (cfg->outputtype == OT_ENERGY) {
             normalizor = 1.f / Etotal;
         } else {

@@ -15,7 +15,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
-OUTPUT_TYPES = {"flux": 0, "fluence": 1, "energy": 2, "jacobian": 3, "wl": 4, "wp": 5}
+OUTPUT_TYPES = {"flux": 0, "fluence": 1, "energy": 2, "jacobian": 3, "wl": 4, "wp": 5, "wn": 16}
 _lib = None
 
 

@@ -13,6 +13,10 @@ Badouel tracer and element-based output (-M s -C 0), unnormalized (-U 0):
            (mua=0.05 mus=5 g=0.9), 10 gates of 0.5 ns, 4 detectors R=2 mm on
            z=0 at x=40..55, detected photons saved, 1e5 photons
 
+Six more runs with fresh seeds calibrate the null: their coverage of the
+10-run statistics (fraction of cells within 3 sigma, mean z) is stored, and a
+candidate must score like a fresh reference run does.
+
 Stored per case: mean and standard deviation over the 10 runs of the
 per-element fluence summed over gates and of the per-gate totals, a random
 subset of (element, gate) cells, detector statistics, absorbed fraction and
@@ -40,6 +44,7 @@ from mmc_gb300 import meshgen  # noqa: E402
 
 REF = os.path.join(ROOT, "oracle", "_ref", "mmc")
 NRUNS = 10
+NNULL = 6
 SEED0 = 20260101
 
 
@@ -107,6 +112,52 @@ def run_ref_detp(workdir, name, seed, photons):
     return np.frombuffer(buf, np.float32, count=count * cols, offset=8).reshape(count, cols)
 
 
+def run_ref_mesh(workdir, name):
+    """The reference's prepared mesh (after mmc_prep) dumped by oracle/ref_driver.c."""
+    out = os.path.join(workdir, name + ".meshdump")
+    norm_in = os.path.join(workdir, name + ".nin")
+    with open(norm_in, "wb") as f:  # a normalize-only run so no photons are simulated
+        f.write(np.zeros(2, np.float64).tobytes())
+    cmd = [REF + "_detp", "-f", os.path.join(workdir, name + ".json"), "-c", "sse", "-M", "s", "-C", "0", "-b", "1",
+           "-n", "1"]
+    env = dict(os.environ, OMP_NUM_THREADS="1", MMCGB_MESH_OUT=out)
+    p = subprocess.run(cmd, cwd=workdir, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(p.stdout[-2000:])
+    buf = open(out, "rb").read()
+    nn, ne, nf = struct.unpack("<iii", buf[:12])
+    o = 12
+    def take(dt, n):
+        nonlocal o
+        a = np.frombuffer(buf, dt, count=n, offset=o)
+        o += a.nbytes
+        return a
+    elem = take(np.int32, ne * 4).reshape(ne, 4)
+    facenb = take(np.int32, ne * 4).reshape(ne, 4)
+    evol = take(np.float32, ne)
+    nvol = take(np.float32, nn)
+    normals = take(np.float32, ne * 16).reshape(ne, 16)
+    return dict(nn=nn, ne=ne, nf=nf, elem=elem, facenb=facenb, evol=evol, nvol=nvol, normals=normals)
+
+
+def run_ref_normalize(workdir, name, raw, eabs, etot, basisorder):
+    """The reference's output stage (elem->node scatter + mesh_normalize) applied
+    to a given raw element field, through oracle/ref_driver.c."""
+    fin = os.path.join(workdir, f"{name}_{basisorder}.nin")
+    fout = os.path.join(workdir, f"{name}_{basisorder}.nout")
+    with open(fin, "wb") as f:
+        f.write(np.array([eabs, etot], np.float64).tobytes())
+        f.write(np.ascontiguousarray(raw, np.float64).tobytes())
+    cmd = [REF + "_detp", "-f", os.path.join(workdir, name + ".json"), "-c", "sse", "-M", "s", "-C", str(basisorder),
+           "-b", "1", "-U", "1", "-n", "1"]
+    env = dict(os.environ, OMP_NUM_THREADS="1", MMCGB_NORM_IN=fin, MMCGB_NORM_OUT=fout)
+    p = subprocess.run(cmd, cwd=workdir, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(p.stdout[-2000:])
+    data = np.fromfile(fout, np.float64)
+    return data[:-1], data[-1]
+
+
 def run_ref(workdir, name, seed, photons, normalized=False, savedet=False):
     sess = f"{name}_{seed}_{int(normalized)}"
     cmd = [REF, "-f", os.path.join(workdir, name + ".json"), "-c", "sse", "-M", "s", "-C", "0", "-b", "1",
@@ -149,6 +200,9 @@ def main():
                 runs = list(ex.map(lambda s: run_ref(wd, name, s, c["photons"], savedet=savedet),
                                    [SEED0 + k for k in range(NRUNS)]))
                 norm = ex.submit(run_ref, wd, name, SEED0, c["photons"], True, False).result()
+                # null calibration: fresh reference runs scored against the 10-run statistics
+                nulls = list(ex.map(lambda s: run_ref(wd, name, s, c["photons"]),
+                                    [SEED0 + 1000 + k for k in range(NNULL)]))
             fields = np.stack([r["raw"].reshape(G, ne) for r in runs])  # (runs, G, ne)
             per_elem = fields.sum(axis=1)
             per_gate = fields.sum(axis=2)
@@ -166,6 +220,14 @@ def main():
                 raw_seed0=runs[0]["raw"].astype(np.float32) if G == 1 else np.zeros(0, np.float32),
                 norm_seed0=norm["raw"].astype(np.float32) if G == 1 else np.zeros(0, np.float32),
             )
+            sys.path.insert(0, os.path.dirname(HERE))
+            import golden_checks as gc
+            nf = [np.array([r["raw"].reshape(G, ne).sum(0) for r in nulls]),
+                  np.array([r["raw"].reshape(-1)[cells] for r in nulls])]
+            st = [[gc.zstats(x, fx["elem_mean"], fx["elem_std"]) for x in nf[0]],
+                  [gc.zstats(x, fx["cell_mean"], fx["cell_std"]) for x in nf[1]]]
+            fx.update(null_elem_frac=np.array([t[0] for t in st[0]]), null_elem_meanz=np.array([t[1] for t in st[0]]),
+                      null_cell_frac=np.array([t[0] for t in st[1]]), null_cell_meanz=np.array([t[1] for t in st[1]]))
             if savedet:
                 M = m.media.shape[0] - 1
                 mua = m.media[1:, 0].astype(np.float64)
@@ -183,6 +245,22 @@ def main():
                 fx.update(det_count=np.array(counts, np.float64), det_wsum=np.array(wsum),
                           det_plen=np.array(plen), det_nscat=np.array(nscat))
             np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **fx)
+            # pins of the host stages: prepared mesh and output normalization
+            md = run_ref_mesh(wd, name)
+            sub = np.sort(rng.choice(ne, size=min(ne, 3000), replace=False)).astype(np.int32)
+            pin = dict(nn=md["nn"], ne=md["ne"], nf=md["nf"], sub=sub, elem=md["elem"][sub], facenb=md["facenb"][sub],
+                       evol=md["evol"][sub], normals=md["normals"][sub], nvol=md["nvol"])
+            raw = np.random.default_rng(123).random((G, ne)) * 100.0
+            eabs, etot = 0.27 * c["photons"], float(c["photons"])
+            nsub = np.sort(rng.choice(m.nn, size=min(m.nn, 2000), replace=False)).astype(np.int32)
+            pin["nsub"] = nsub
+            for bo in (0, 1):
+                w, norm = run_ref_normalize(wd, name, raw, eabs, etot, bo)
+                w = w.reshape(G, -1)[:, sub if bo == 0 else nsub]
+                pin[f"norm{bo}_field"] = w.astype(np.float64)
+                pin[f"norm{bo}_normalizer"] = norm
+            pin["norm_eabs"], pin["norm_etot"] = eabs, etot
+            np.savez_compressed(os.path.join(HERE, f"{name}_pins.npz"), **pin)
             print(name, "ne", ne, "absorbed", fx["absorbed"].mean(), "tests/photon", fx["tests_per_photon"].mean())
 
 

@@ -1,0 +1,115 @@
+"""Statistical parity checks against the reference golden fixtures
+(tests/golden/*.npz, made by tests/golden/make_golden.py from 10 runs of the
+reference CPU engine).  Shared by the oracle tests (CPU) and the engine tests
+(GPU).
+
+A single run with the fixture's photon count is an independent sample; its
+difference from the 10-run mean has variance sigma^2 (1 + 1/10), sigma being
+the run-to-run spread of the reference.  With sigma estimated from 10 runs,
+z = diff / (s sqrt(1.1)) follows Student's t with 9 degrees of freedom, so a
+Gaussian run would put 98.5% of the well-sampled cells inside 3 sigma (not the
+99.7% of a known sigma), and sparsely visited cells have heavier tails still.
+So the thresholds are calibrated on the reference itself: the fixtures hold
+the coverage and mean z of six fresh reference runs scored the same way, and a
+candidate run passes when it scores like them (see _zcheck); aggregate
+quantities must lie within 3 sigma.
+"""
+import os
+
+import numpy as np
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+INFLATE = np.sqrt(1.0 + 1.0 / 10.0)
+
+
+def load(name):
+    return dict(np.load(os.path.join(HERE, name + ".npz")))
+
+
+def case_mesh_and_config(name, nphoton=None, seed=4242):
+    from mmc_gb300 import meshgen
+    from mmc_gb300.core import SimConfig
+    fx = load(name)
+    if name == "cube6k":
+        m = meshgen.homogeneous_cube(n=10)
+        cfg = SimConfig(media=m.media, nphoton=nphoton or int(fx["photons"]), seed=seed, srcpos=(30.0, 30.0, 0.0),
+                        srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=5e-9, basisorder=0, isnormalized=0)
+    elif name == "incl48k":
+        m = meshgen.inclusion_cube(n=20, jitter=0.6, seed=7)
+        cfg = SimConfig(media=m.media, nphoton=nphoton or int(fx["photons"]), seed=seed, srcpos=(30.0, 30.0, 0.0),
+                        srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=0.5e-9, basisorder=0, isnormalized=0, issavedet=1,
+                        detpos=meshgen.c1_detectors(), maxdetphoton=200000)
+    else:
+        raise KeyError(name)
+    return m, cfg, fx
+
+
+def zstats(x, mean, std, rel_noise_max=0.25):
+    """(fraction of well-sampled cells with |z| < 3, mean z, cell count)."""
+    ok = (mean > 0) & (std > 0) & (std < rel_noise_max * mean)
+    z = (x[ok] - mean[ok]) / (std[ok] * INFLATE)
+    return float(np.mean(np.abs(z) < 3.0)), float(np.mean(z)) if z.size else 0.0, int(ok.sum())
+
+
+def _zcheck(what, x, mean, std, nmin, null_frac, null_meanz):
+    """Coverage and bias of one run against the thresholds set by fresh
+    reference runs (the null): coverage no lower than the worst fresh run
+    minus 0.5%, |mean z| no larger than the largest fresh-run value + 0.1."""
+    f, mz, n = zstats(x, mean, std)
+    need = float(np.min(null_frac)) - 0.005
+    mz_max = float(np.max(np.abs(null_meanz))) + 0.1
+    if n < nmin or f < need or abs(mz) > mz_max:
+        return [f"{what}: {f:.4f} of {n} cells within 3 sigma (need {need:.4f}), mean z {mz:+.3f} "
+                f"(limit {mz_max:.3f})"]
+    return []
+
+
+def check_field(raw, fx, media, label, photons):
+    """raw: (gates, ne) element deposits of one run."""
+    msgs = []
+    msgs += _zcheck("per-element", raw.sum(0), fx["elem_mean"], fx["elem_std"], 100,
+                    fx["null_elem_frac"], fx["null_elem_meanz"])
+    msgs += _zcheck("(element,gate) cells", raw.reshape(-1)[fx["cells"]], fx["cell_mean"], fx["cell_std"], 50,
+                    fx["null_cell_frac"], fx["null_cell_meanz"])
+    gm, gs = fx["gate_mean"], fx["gate_std"]
+    gz = np.abs(raw.sum(1) - gm) / (gs * INFLATE)
+    if np.any(gz[gm > 0] > 4.0):
+        msgs.append(f"per-gate totals z = {np.round(gz, 2)}")
+    absorbed = float((raw.sum(0) * media[label, 0].astype(np.float64)).sum() / photons)
+    a = fx["absorbed"]
+    if abs(absorbed - a.mean()) > 3 * a.std(ddof=1) * INFLATE:
+        msgs.append(f"absorbed fraction {absorbed:.5f} vs reference {a.mean():.5f} +- {a.std(ddof=1):.5f}")
+    return msgs
+
+
+def check_tests_per_photon(tpp, fx, rel=0.01):
+    ref = float(fx["tests_per_photon"].mean())
+    return [] if abs(tpp - ref) <= rel * ref else [f"ray-tet tests/photon {tpp:.2f} vs reference {ref:.2f}"]
+
+
+def check_detectors(detp, media, fx):
+    msgs = []
+    M = media.shape[0] - 1
+    mua = media[1:, 0].astype(np.float64)
+    ids = detp[:, 0].astype(int)
+    pp = detp[:, 1 + M:1 + 2 * M].astype(np.float64)
+    w = detp[:, -1] * np.exp(-(pp * mua).sum(1))
+    ndet = fx["det_count"].shape[1]
+    for k in range(ndet):
+        cnt = np.count_nonzero(ids == k + 1)
+        cm, cs = fx["det_count"][:, k].mean(), fx["det_count"][:, k].std(ddof=1)
+        if abs(cnt - cm) > 3.5 * max(cs, 1.0) * INFLATE:
+            msgs.append(f"detector {k + 1}: {cnt} photons vs reference {cm:.1f} +- {cs:.1f}")
+        ws = w[ids == k + 1].sum()
+        wm, wsd = fx["det_wsum"][:, k].mean(), fx["det_wsum"][:, k].std(ddof=1)
+        if abs(ws - wm) > 3.5 * max(wsd, 1e-12) * INFLATE:
+            msgs.append(f"detector {k + 1}: weight {ws:.4g} vs reference {wm:.4g} +- {wsd:.3g}")
+    plen = pp.mean(0)
+    pm, ps = fx["det_plen"].mean(0), fx["det_plen"].std(0, ddof=1)
+    if np.any(np.abs(plen - pm) > 3.5 * ps * INFLATE + 1e-9):
+        msgs.append(f"mean partial path {plen} vs reference {pm} +- {ps}")
+    ns = detp[:, 1:1 + M].astype(np.float64).mean(0)
+    nm, nsd = fx["det_nscat"].mean(0), fx["det_nscat"].std(0, ddof=1)
+    if np.any(np.abs(ns - nm) > 3.5 * nsd * INFLATE + 1e-9):
+        msgs.append(f"mean scatter count {ns} vs reference {nm} +- {nsd}")
+    return msgs

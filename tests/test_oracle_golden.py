@@ -1,0 +1,35 @@
+"""The CPU oracle against the reference golden fixtures (statistical parity),
+at the fixtures' own photon counts: this pins the oracle, which in turn checks
+the CUDA engine photon by photon."""
+import os
+
+import pytest
+
+import golden_checks as gc
+
+NTHREADS = os.cpu_count() or 4
+
+
+@pytest.mark.parametrize("name", ["cube6k", "incl48k"])
+def test_oracle_matches_reference_runs(oracle_mod, name):
+    m, cfg, fx = gc.case_mesh_and_config(name)
+    r = oracle_mod.run(m.node, m.elem, m.label, cfg, nthreads=NTHREADS, normalize=False)
+    msgs = gc.check_field(r["raw"], fx, m.media, m.label, cfg.nphoton)
+    msgs += gc.check_tests_per_photon(r["raytet"] / cfg.nphoton, fx)
+    if cfg.issavedet:
+        msgs += gc.check_detectors(r["detp"], m.media, fx)
+    assert r["aborted"] == 0
+    assert not msgs, "\n".join(msgs)
+
+
+def test_oracle_detects_a_planted_error(oracle_mod):
+    """The statistical check has power: a 5% change of the absorption
+    coefficient, planted in the oracle's input, must fail it."""
+    import dataclasses
+    import numpy as np
+    m, cfg, fx = gc.case_mesh_and_config("cube6k")
+    media = m.media.copy()
+    media[1, 0] *= 1.05
+    r = oracle_mod.run(m.node, m.elem, m.label, dataclasses.replace(cfg, media=media), nthreads=NTHREADS,
+                       normalize=False)
+    assert gc.check_field(r["raw"], fx, m.media, m.label, cfg.nphoton)
