@@ -179,7 +179,16 @@ def main():
     ap.add_argument("--photons-per-step", type=int, default=PHOTONS_PER_STEP)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--exact", action="store_true",
+                    help="IEEE arithmetic (photon-for-photon reproducible on the CPU) instead of fast math")
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "serving", "replay"],
+                    help="plain: the 1.3M-tet benchmark (default); batched / serving / replay: the batched, "
+                         "continuous-batching and differentiation workloads (one JSON line each)")
+    ap.add_argument("--requests", type=int, default=64, help="serving: number of requests")
     args = ap.parse_args()
+    if args.workload != "plain":
+        from mmc_gb300 import workloads
+        return workloads.run(args)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -206,6 +215,7 @@ def main():
     torch.cuda.set_device(local_rank)
     nps = args.photons_per_step
     m, cfg = workload_config(nps)
+    cfg = dataclasses.replace(cfg, fast_math=0 if args.exact else 1)
     mesh = Mesh(m.node, m.elem, m.label, device=local_rank)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local_rank}")
 
@@ -280,7 +290,8 @@ def main():
         line = {
             "metric": "photons/ms", "value": value, "unit": "photons/ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 fluence accumulation)",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (f64 fluence accumulation, %s)" % ("IEEE" if args.exact else "fast math"),
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "ne": mesh.ne, "nn": mesh.nn, "photons_per_step": nps,
                        "job_photons": JOB_PHOTONS, "gates": 50, "detectors": 4, "savedet": True,

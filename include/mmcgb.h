@@ -101,6 +101,9 @@ typedef struct mmcgb_config {
     uint64_t step_budget;    /* max ray-tet tests per photon, 0 = 100,000,000 */
     int32_t threads;         /* threads per block, 0 = auto */
     int32_t blocks;          /* persistent blocks, 0 = auto */
+    int32_t fast_math;       /* 1: hardware-approximate division/exp/log/sincos and fused
+                                multiply-adds (as the reference's -use_fast_math build);
+                                0: IEEE arithmetic, photon-for-photon reproducible on the CPU */
 } mmcgb_config;
 
 /* Outputs.  Pointers may be NULL to skip an output; counts are always set. */
@@ -158,6 +161,13 @@ typedef struct mmcgb_session mmcgb_session;
 int32_t mmcgb_session_begin(mmcgb_mesh* mesh, const mmcgb_config* cfg, mmcgb_result* trace,
                             mmcgb_session** out);
 int32_t mmcgb_session_launch(mmcgb_session* s, uint64_t photon_offset, uint64_t nphoton);
+/* One persistent launch over several sessions (same device, same fast_math):
+ * session i simulates photons [offsets[i], offsets[i]+counts[i]) of its run.
+ * Photons are handed out from one pool, so sessions of very different sizes
+ * keep every SM busy to the end.  Used for batched runs and for the waves of
+ * the continuous-batching server. */
+int32_t mmcgb_session_launch_batch(int32_t n, mmcgb_session* const* sessions, const uint64_t* offsets,
+                                   const uint64_t* counts);
 int32_t mmcgb_session_sync(mmcgb_session* s, float* last_kernel_ms);
 int32_t mmcgb_session_end(mmcgb_session* s, mmcgb_result* res);
 

@@ -53,7 +53,7 @@ class Config(C.Structure):
         ("detnum", C.c_int32), ("detpos", C.c_void_p),
         ("replayseed", C.c_void_p), ("replayweight", C.c_void_p), ("replaytime", C.c_void_p),
         ("accum_f64", C.c_int32), ("step_budget", C.c_uint64),
-        ("threads", C.c_int32), ("blocks", C.c_int32),
+        ("threads", C.c_int32), ("blocks", C.c_int32), ("fast_math", C.c_int32),
     ]
 
 
@@ -72,6 +72,7 @@ EXPORTS = [
     "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export", "mmcgb_mesh_locate",
     "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run", "mmcgb_session_begin", "mmcgb_session_launch",
     "mmcgb_session_sync", "mmcgb_session_end", "mmcgb_prepare_host", "mmcgb_normalize_host",
+    "mmcgb_session_launch_batch",
 ]
 
 
@@ -108,7 +109,9 @@ def load():
         lib.mmcgb_prepare_host.argtypes = [C.POINTER(MeshDesc)] + [C.c_void_p] * 6
         lib.mmcgb_normalize_host.argtypes = [C.POINTER(MeshDesc), C.POINTER(Config), C.c_void_p, C.c_double,
                                              C.c_double, C.c_void_p, C.POINTER(C.c_double)]
-        for name in ("mmcgb_prepare_host", "mmcgb_normalize_host", "mmcgb_session_begin", "mmcgb_session_launch", "mmcgb_session_sync", "mmcgb_session_end",
+        lib.mmcgb_session_launch_batch.argtypes = [C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
+                                                   C.POINTER(C.c_uint64)]
+        for name in ("mmcgb_session_launch_batch", "mmcgb_prepare_host", "mmcgb_normalize_host", "mmcgb_session_begin", "mmcgb_session_launch", "mmcgb_session_sync", "mmcgb_session_end",
                      "mmcgb_mesh_create", "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export",
                      "mmcgb_mesh_locate", "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run"):
             getattr(lib, name).restype = C.c_int32

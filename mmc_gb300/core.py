@@ -94,6 +94,11 @@ class Mesh:
         return self._node
 
     @property
+    def elem(self):
+        """Element node ids as given (before the orientation fix)."""
+        return self._elem
+
+    @property
     def label(self):
         return self._label
 
@@ -159,6 +164,7 @@ class SimConfig:
     step_budget: int = 0
     threads: int = 0
     blocks: int = 0
+    fast_math: int = 1
     save_field: bool = True
 
     @property
@@ -203,6 +209,7 @@ class SimConfig:
         c.accum_f64 = int(self.accum_f64)
         c.step_budget = int(self.step_budget)
         c.threads, c.blocks = int(self.threads), int(self.blocks)
+        c.fast_math = int(self.fast_math)
         return c, keep
 
 
@@ -336,3 +343,12 @@ class Session:
                 N.load().mmcgb_session_end(self._h, None)
             except Exception:
                 pass
+
+
+def launch_batch(sessions, offsets, counts):
+    """One persistent launch over several sessions (mmcgb_session_launch_batch)."""
+    n = len(sessions)
+    h = (C.c_void_p * n)(*[s._h for s in sessions])
+    o = (C.c_uint64 * n)(*[int(x) for x in offsets])
+    k = (C.c_uint64 * n)(*[int(x) for x in counts])
+    N.check(N.load().mmcgb_session_launch_batch(n, h, o, k))

@@ -211,6 +211,7 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     S.outputtype = c.outputtype;
     S.replay = c.replayseed ? 1 : 0;
     S.accum_f64 = f64 ? 1 : 0;
+    S.fast_math = c.fast_math ? 1 : 0;
     S.reclen = reclen_dev;
     S.nmed_ppath = M;
     S.replayseed = B.rseed;
@@ -301,6 +302,7 @@ struct mmcgb_session {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     unsigned long long launched = 0;
     int launches = 0;
+    bool timed = false;  // ev0/ev1 bracket this session's last launch
     LaunchShape shape{0, 0};
 };
 
@@ -342,6 +344,7 @@ void mmcgb_config_defaults(mmcgb_config* c) {
     c->outputtype = MMCGB_OUT_FLUX;
     c->maxdetphoton = 1000000;
     c->accum_f64 = 1;
+    c->fast_math = 1;
 }
 
 int32_t mmcgb_mesh_create(const mmcgb_mesh_desc* desc, int32_t device, mmcgb_mesh** out) {
@@ -449,6 +452,77 @@ int32_t mmcgb_session_launch(mmcgb_session* s, uint64_t photon_offset, uint64_t 
     CK(cudaEventRecord(s->ev1, s->stream));
     s->launched += nphoton;
     s->launches++;
+    s->timed = true;
+    return MMCGB_OK;
+}
+
+int32_t mmcgb_session_launch_batch(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets,
+                                   const uint64_t* counts) {
+    if (n <= 0 || !ss || !offsets || !counts) return fail(MMCGB_E_ARG, "null or empty batch");
+    mmcgb_session* s0 = ss[0];
+    if (!s0) return fail(MMCGB_E_ARG, "null session");
+    const int device = s0->mesh->device;
+    const int fast = s0->cfg.fast_math ? 1 : 0;
+    std::vector<SimDev> sims(n);
+    std::vector<unsigned long long> cum(n);
+    unsigned long long total = 0;
+    int nmed_stride = 0, reclen_max = 0, want_seed = 0;
+    for (int i = 0; i < n; i++) {
+        mmcgb_session* s = ss[i];
+        if (!s || s->mesh->device != device) return fail(MMCGB_E_ARG, "batched sessions must live on one device");
+        if ((s->cfg.fast_math ? 1 : 0) != fast) return fail(MMCGB_E_ARG, "batched sessions must share fast_math");
+        if (s->cfg.replayseed && (offsets[i] != 0 || counts[i] != s->cfg.nphoton))
+            return fail(MMCGB_E_ARG, "replay sessions run all replayed photons in one launch");
+        if ((s->P.buf.pw || s->P.buf.ps || s->P.buf.pd) && counts[i] > s->cfg.nphoton)
+            return fail(MMCGB_E_ARG, "per-photon trace buffers hold cfg.nphoton photons");
+        sims[i] = s->P.sim;
+        sims[i].nphoton = counts[i];
+        sims[i].photon_offset = s->cfg.photon_offset + offsets[i];
+        nmed_stride = std::max(nmed_stride, s->cfg.nmedia);
+        if (s->cfg.issavedet) reclen_max = std::max(reclen_max, s->P.sim.reclen);
+        if (s->cfg.issavedet && s->P.sim.seeds) want_seed = 1;
+        total += counts[i];
+        cum[i] = total;
+    }
+    if ((size_t)n * nmed_stride * sizeof(float4) > 40 * 1024)
+        return fail(MMCGB_E_ARG, "batch media tables exceed shared memory; split the batch");
+    CK(cudaSetDevice(device));
+    cudaStream_t st = s0->stream;
+    // order the batch after every session's earlier work, and every session's later work after it
+    std::vector<cudaEvent_t> evs;
+    for (int i = 1; i < n; i++) {
+        if (ss[i]->stream == st) continue;
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        evs.push_back(e);
+        CK(cudaEventRecord(e, ss[i]->stream));
+        CK(cudaStreamWaitEvent(st, e, 0));
+    }
+    SimDev* dsims = nullptr;
+    unsigned long long* dcum = nullptr;
+    CK(cudaMallocAsync((void**)&dsims, sizeof(SimDev) * n, st));
+    CK(cudaMallocAsync((void**)&dcum, sizeof(unsigned long long) * n, st));
+    CK(cudaMemcpyAsync(dsims, sims.data(), sizeof(SimDev) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dcum, cum.data(), sizeof(unsigned long long) * n, cudaMemcpyHostToDevice, st));
+    LaunchShape shape = default_shape(device, true);
+    if (s0->cfg.threads > 0) shape.threads = std::max(32, std::min(s0->cfg.threads, 128) / 32 * 32);
+    if (s0->cfg.blocks > 0) shape.blocks = s0->cfg.blocks;
+    CK(cudaEventRecord(s0->ev0, st));
+    CK(launch_batched(dsims, dcum, n, total, nmed_stride, reclen_max, want_seed, s0->work, shape, st, fast));
+    CK(cudaEventRecord(s0->ev1, st));
+    CK(cudaFreeAsync(dsims, st));
+    CK(cudaFreeAsync(dcum, st));
+    cudaEvent_t done;
+    CK(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+    CK(cudaEventRecord(done, st));
+    for (int i = 0; i < n; i++) {
+        ss[i]->launched += counts[i];
+        ss[i]->launches++;
+        ss[i]->timed = (i == 0);  // the batch is timed on the first session's events
+        if (ss[i]->stream != st) CK(cudaStreamWaitEvent(ss[i]->stream, done, 0));
+    }
+    for (cudaEvent_t e : evs) cudaEventDestroy(e);
+    cudaEventDestroy(done);
     return MMCGB_OK;
 }
 
@@ -458,7 +532,7 @@ int32_t mmcgb_session_sync(mmcgb_session* s, float* last_kernel_ms) {
     CK(cudaStreamSynchronize(s->stream));
     if (last_kernel_ms) {
         *last_kernel_ms = 0.f;
-        if (s->launches) CK(cudaEventElapsedTime(last_kernel_ms, s->ev0, s->ev1));
+        if (s->timed) CK(cudaEventElapsedTime(last_kernel_ms, s->ev0, s->ev1));
     }
     return MMCGB_OK;
 }
@@ -470,7 +544,7 @@ int32_t mmcgb_session_end(mmcgb_session* s, mmcgb_result* res) {
     if (res) {
         rc = finish_sim(s->mesh, s->cfg, s->P, res, s->stream, s->launched);
         float ms = 0.f;
-        if (s->launches && cudaEventElapsedTime(&ms, s->ev0, s->ev1) == cudaSuccess) res->kernel_ms = ms;
+        if (s->timed && cudaEventElapsedTime(&ms, s->ev0, s->ev1) == cudaSuccess) res->kernel_ms = ms;
     } else {
         s->P.buf.release();
     }
@@ -516,6 +590,10 @@ int32_t mmcgb_simulate_batch(int32_t n, mmcgb_mesh* const* meshes, const mmcgb_c
         nmed_stride = std::max(nmed_stride, cfgs[i].nmedia);
         if (cfgs[i].issavedet) reclen_max = std::max(reclen_max, P[i].sim.reclen);
         if (cfgs[i].issavedet && cfgs[i].issaveseed) want_seed = 1;
+        if ((cfgs[i].fast_math != 0) != (cfgs[0].fast_math != 0)) {
+            rc = fail(MMCGB_E_ARG, "batched simulations must share fast_math");
+            break;
+        }
         total += cfgs[i].nphoton;
         cum[i] = total;
     }
@@ -538,7 +616,9 @@ int32_t mmcgb_simulate_batch(int32_t n, mmcgb_mesh* const* meshes, const mmcgb_c
         if (cfgs[0].threads > 0) shape.threads = std::max(32, std::min(cfgs[0].threads, 128) / 32 * 32);
         if (cfgs[0].blocks > 0) shape.blocks = cfgs[0].blocks;
         if (e == cudaSuccess) e = cudaEventRecord(ev0, stream);
-        if (e == cudaSuccess) e = launch_batched(dsims, dcum, n, total, nmed_stride, reclen_max, want_seed, work, shape, stream);
+        if (e == cudaSuccess)
+            e = launch_batched(dsims, dcum, n, total, nmed_stride, reclen_max, want_seed, work, shape, stream,
+                               cfgs[0].fast_math ? 1 : 0);
         if (e == cudaSuccess) e = cudaEventRecord(ev1, stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) rc = cuda_fail(e, "batched photon engine");

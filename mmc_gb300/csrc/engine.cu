@@ -31,18 +31,53 @@ constexpr int kMaxTrial = 3;
 constexpr int kIdUndef = 0x7FFFFFFF;
 constexpr unsigned kFull = 0xFFFFFFFFu;
 
-enum Mode : int { M_NEED = 0, M_OUTER = 1, M_INNER = 2, M_FIXIN = 3, M_DONE = 4 };
+enum Mode : int { M_NEED = 0, M_OUTER = 1, M_INNER = 2, M_FIXIN = 3, M_DONE = 4, M_SCAT = 5 };
+
+// Scattering runs at the top of the trip after the step that ends inside an
+// element (roulette, then the scatter), ahead of that lane's next step.  The
+// scatter may be batched across lanes: a lane parks until kScatBatch lanes of
+// its warp are parked or one has waited kMaxWait trips.  Measured on GB300,
+// batching (8 lanes / 4 trips) was 4% slower than scattering at once, so the
+// batch size is 1.  Each photon performs the same operations in either case.
+constexpr int kScatBatch = 1;
+constexpr int kMaxWait = 4;
 
 struct Lane {
     float px, py, pz, vx, vy, vz;
     float weight, ptime, slen, Lmove, slen0, oldw;
     unsigned oldidx;
     int eid, faceid, isend, hit, label, nbword;
-    int fixcount, mode;
+    int fixcount, mode, wait;
     unsigned steps;
     unsigned long long t0, t1;
     unsigned long long pid;  // photon index inside its simulation
     int sim;
+};
+
+// Arithmetic policies.  Exact: IEEE division and square root, the project's
+// polynomial exp/log/sincos, no contraction -- bit-identical to the CPU
+// oracle.  Fast: hardware approximations (__fdividef, __expf, __logf,
+// __sincosf, rsqrtf) and fused multiply-adds, as the reference's CUDA build
+// gets from -use_fast_math; validated statistically.
+struct ExactMath {
+    static constexpr bool kFast = false;
+    static __device__ __forceinline__ float div(float a, float b) { return a / b; }
+    static __device__ __forceinline__ float exp(float x) { return mmc_expf(x); }
+    static __device__ __forceinline__ float log(float x) { return mmc_logf(x); }
+    static __device__ __forceinline__ void sincos2pi(float u, float& s, float& c) { mmc_sincos2pi(u, s, c); }
+    static __device__ __forceinline__ float rsqrt(float x) { return 1.f / sqrtf(x); }
+    static __device__ __forceinline__ float mad(float a, float b, float c) { return a * b + c; }
+};
+struct FastMath {
+    static constexpr bool kFast = true;
+    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+    static __device__ __forceinline__ float exp(float x) { return __expf(x); }
+    static __device__ __forceinline__ float log(float x) { return __logf(x); }
+    static __device__ __forceinline__ void sincos2pi(float u, float& s, float& c) {
+        __sincosf(u * 6.28318530717958647692f, &s, &c);
+    }
+    static __device__ __forceinline__ float rsqrt(float x) { return rsqrtf(x); }
+    static __device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
 };
 
 __device__ __forceinline__ int decode_nb(int w) { return (w << 8) >> 8; }
@@ -67,6 +102,7 @@ __device__ __forceinline__ void deposit(const SimDev& S, unsigned idx, float val
 }
 
 // One branchless Badouel step with fused deposit.  Requires 1 <= L.eid <= ne.
+template <class MP>
 __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const float4* med) {
     const TetRec* R = S.rec + (L.eid - 1);
     const float4 nx = __ldg(&R->nx);
@@ -77,18 +113,18 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
     L.hit = 0;
     L.faceid = -1;
     L.isend = 0;
-    float S0 = ((L.vx * nx.x) + (L.vy * ny.x)) + (L.vz * nz.x);
-    float S1 = ((L.vx * nx.y) + (L.vy * ny.y)) + (L.vz * nz.y);
-    float S2 = ((L.vx * nx.z) + (L.vy * ny.z)) + (L.vz * nz.z);
-    float S3 = ((L.vx * nx.w) + (L.vy * ny.w)) + (L.vz * nz.w);
-    float T0 = nd.x - (((L.px * nx.x) + (L.py * ny.x)) + (L.pz * nz.x));
-    float T1 = nd.y - (((L.px * nx.y) + (L.py * ny.y)) + (L.pz * nz.y));
-    float T2 = nd.z - (((L.px * nx.z) + (L.py * ny.z)) + (L.pz * nz.z));
-    float T3 = nd.w - (((L.px * nx.w) + (L.py * ny.w)) + (L.pz * nz.w));
-    T0 = (S0 > 0.f) ? (T0 / S0) : 1e10f;
-    T1 = (S1 > 0.f) ? (T1 / S1) : 1e10f;
-    T2 = (S2 > 0.f) ? (T2 / S2) : 1e10f;
-    T3 = (S3 > 0.f) ? (T3 / S3) : 1e10f;
+    float S0 = MP::mad(L.vz, nz.x, MP::mad(L.vy, ny.x, L.vx * nx.x));
+    float S1 = MP::mad(L.vz, nz.y, MP::mad(L.vy, ny.y, L.vx * nx.y));
+    float S2 = MP::mad(L.vz, nz.z, MP::mad(L.vy, ny.z, L.vx * nx.z));
+    float S3 = MP::mad(L.vz, nz.w, MP::mad(L.vy, ny.w, L.vx * nx.w));
+    float T0 = nd.x - MP::mad(L.pz, nz.x, MP::mad(L.py, ny.x, L.px * nx.x));
+    float T1 = nd.y - MP::mad(L.pz, nz.y, MP::mad(L.py, ny.y, L.px * nx.y));
+    float T2 = nd.z - MP::mad(L.pz, nz.z, MP::mad(L.py, ny.z, L.px * nx.z));
+    float T3 = nd.w - MP::mad(L.pz, nz.w, MP::mad(L.py, ny.w, L.px * nx.w));
+    T0 = (S0 > 0.f) ? MP::div(T0, S0) : 1e10f;
+    T1 = (S1 > 0.f) ? MP::div(T1, S1) : 1e10f;
+    T2 = (S2 > 0.f) ? MP::div(T2, S2) : 1e10f;
+    T3 = (S3 > 0.f) ? MP::div(T3, S3) : 1e10f;
     const float Lmin = fminf(fminf(fminf(T0, T1), T2), T3);
     // faceorder {1,3,2,0,-1} (src/mmc_mesh.c:95)
     int faceid = (Lmin == 1e10f) ? -1 : (Lmin == T0 ? 1 : (Lmin == T1 ? 3 : (Lmin == T2 ? 2 : 0)));
@@ -97,7 +133,7 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
         L.nbword = (faceid == 0) ? nb.x : (faceid == 1) ? nb.y : (faceid == 2) ? nb.z : nb.w;
         const float4 prop = med[L.label];  // mua mus g n
         float currweight = L.weight;
-        float Lmove = (prop.y <= kEps) ? kRMinMus : L.slen / prop.y;
+        float Lmove = (prop.y <= kEps) ? kRMinMus : MP::div(L.slen, prop.y);
         L.isend = (Lmin > Lmove);
         Lmove = L.isend ? Lmove : Lmin;
         L.hit = 1;
@@ -106,10 +142,10 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
         if ((L.ptime + Lmove * rc - S.tstart) * S.Rtstep >= (float)S.maxgate) {
             L.faceid = -2;
             L.hit = 0;
-            Lmove = (S.tend - L.ptime) / rc - 1e-4f;
+            Lmove = MP::div(S.tend - L.ptime, rc) - 1e-4f;
         }
         L.Lmove = Lmove;
-        const float att = mmc_expf(-prop.x * Lmove);
+        const float att = MP::exp(-prop.x * Lmove);
         L.weight *= att;
         const int ot = S.outputtype;
         if (S.replay) {
@@ -119,7 +155,7 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
                 currweight *= rw;
                 currweight += L.weight;
             } else if (ot == OT_WP) {
-                currweight = (L.slen0 < kEps) ? 1.f : Lmove * prop.y / L.slen0;
+                currweight = (L.slen0 < kEps) ? 1.f : MP::div(Lmove * prop.y, L.slen0);
                 currweight *= rw;
                 currweight += L.weight;
             }
@@ -128,9 +164,9 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
         float ww = currweight - L.weight;
         L.ptime += Lmove * rc;
         if (ot == OT_WN) {  // scatter counts are deposited at the scattering events only
-            L.px = L.px + Lmove * L.vx;
-            L.py = L.py + Lmove * L.vy;
-            L.pz = L.pz + Lmove * L.vz;
+            L.px = MP::mad(Lmove, L.vx, L.px);
+            L.py = MP::mad(Lmove, L.vy, L.py);
+            L.pz = MP::mad(Lmove, L.vz, L.pz);
             L.slen = (L.faceid == -2) ? 0.f : L.slen;
             return;
         }
@@ -143,7 +179,7 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
         int gate = (gf < (float)(S.maxgate - 1)) ? (int)gf : S.maxgate - 1;
         gate = max(gate, 0);
         if (ot != OT_ENERGY && ot != OT_WP && ot != OT_WL)
-            ww = (prop.x < kEps) ? (currweight * Lmove) : (ww / prop.x);
+            ww = (prop.x < kEps) ? (currweight * Lmove) : MP::div(ww, prop.x);
         const unsigned newidx = (unsigned)(L.eid - 1) + (unsigned)(gate * S.ne);
         if (L.oldidx == (unsigned)kIdUndef) L.oldidx = newidx;
         if (newidx != L.oldidx) {
@@ -157,9 +193,9 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
             deposit(S, newidx, L.oldw);
             L.oldw = 0.f;
         }
-        L.px = L.px + Lmove * L.vx;
-        L.py = L.py + Lmove * L.vy;
-        L.pz = L.pz + Lmove * L.vz;
+        L.px = MP::mad(Lmove, L.vx, L.px);
+        L.py = MP::mad(Lmove, L.vy, L.py);
+        L.pz = MP::mad(Lmove, L.vz, L.pz);
     }
     L.slen = (L.faceid == -2) ? 0.f : L.slen;
 }
@@ -183,6 +219,7 @@ __device__ __forceinline__ void fixphoton(Lane& L, const SimDev& S) {
 
 // Fresnel / total internal reflection, src/mmc_core.cl:1247-1303.  Returns the
 // element the photon continues in (oldeid when reflected).
+template <class MP>
 __device__ __forceinline__ int reflectray(Lane& L, const SimDev& S, const float4* med, int oldeid,
                                           int oldlabel, int eid, int newlabel, int faceid) {
     const TetRec* R = S.rec + (oldeid - 1);
@@ -196,14 +233,14 @@ __device__ __forceinline__ int reflectray(Lane& L, const SimDev& S, const float4
     const float n2 = (eid > 0) ? med[newlabel].w : S.nout;
     float tmp0 = n1 * n1;
     float tmp1 = n2 * n2;
-    float tmp2 = 1.f - tmp0 / tmp1 * (1.f - Icos * Icos);
+    float tmp2 = 1.f - MP::div(tmp0, tmp1) * (1.f - Icos * Icos);
     if (tmp2 > 0.f && !((eid <= 0) && (S.isreflect == BC_MIRROR))) {
         float Re = tmp0 * Icos * Icos + tmp1 * tmp2;
         tmp2 = sqrtf(tmp2);
         float Im = 2.f * n1 * n2 * Icos * tmp2;
-        float Rtotal = (Re - Im) / (Re + Im);
+        float Rtotal = MP::div(Re - Im, Re + Im);
         Re = tmp1 * Icos * Icos + tmp0 * tmp2 * tmp2;
-        Rtotal = (Rtotal + (Re - Im) / (Re + Im)) * 0.5f;
+        Rtotal = (Rtotal + MP::div(Re - Im, Re + Im)) * 0.5f;
         if (rng_next(L.t0, L.t1) <= Rtotal) {
             const float k = -2.f * Icos;
             L.vx += k * pnx;
@@ -216,7 +253,7 @@ __device__ __forceinline__ int reflectray(Lane& L, const SimDev& S, const float4
             L.vx += k * pnx;
             L.vy += k * pny;
             L.vz += k * pnz;
-            const float q = n1 / n2;
+            const float q = MP::div(n1, n2);
             L.vx = tmp2 * pnx + q * L.vx;
             L.vy = tmp2 * pny + q * L.vy;
             L.vz = tmp2 * pnz + q * L.vz;
@@ -228,7 +265,7 @@ __device__ __forceinline__ int reflectray(Lane& L, const SimDev& S, const float4
         L.vz += k * pnz;
         eid = oldeid;
     }
-    const float inv = 1.f / sqrtf(L.vx * L.vx + L.vy * L.vy + L.vz * L.vz);
+    const float inv = MP::rsqrt(L.vx * L.vx + L.vy * L.vy + L.vz * L.vz);
     L.vx *= inv;
     L.vy *= inv;
     L.vz *= inv;
@@ -236,14 +273,15 @@ __device__ __forceinline__ int reflectray(Lane& L, const SimDev& S, const float4
 }
 
 // Henyey-Greenstein scatter + direction rotation, src/mmc_core.cl:1307-1377.
+template <class MP>
 __device__ __forceinline__ float next_scatter(Lane& L, float g, float& ctheta_out) {
-    const float nextslen = -mmc_logf(rng_next(L.t0, L.t1) + kEps);
+    const float nextslen = -MP::log(rng_next(L.t0, L.t1) + kEps);
     float sphi, cphi, stheta, ctheta;
-    mmc_sincos2pi(rng_next(L.t0, L.t1), sphi, cphi);
+    MP::sincos2pi(rng_next(L.t0, L.t1), sphi, cphi);
     if (g > kEps) {
-        float tmp0 = (1.f - g * g) / (1.f - g + 2.f * g * rng_next(L.t0, L.t1));
+        float tmp0 = MP::div(1.f - g * g, 1.f - g + 2.f * g * rng_next(L.t0, L.t1));
         tmp0 *= tmp0;
-        tmp0 = (1.f + g * g - tmp0) / (2.f * g);
+        tmp0 = MP::div(1.f + g * g - tmp0, 2.f * g);
         tmp0 = fmaxf(-1.f, fminf(tmp0, 1.f));
         stheta = sqrtf(1.f - tmp0 * tmp0);
         ctheta = tmp0;
@@ -254,7 +292,7 @@ __device__ __forceinline__ float next_scatter(Lane& L, float g, float& ctheta_ou
     float px, py, pz;
     if (L.vz > -1.f + kEps && L.vz < 1.f - kEps) {
         const float tmp0 = 1.f - L.vz * L.vz;
-        float tmp1 = 1.f / sqrtf(tmp0);
+        float tmp1 = MP::rsqrt(tmp0);
         tmp1 = stheta * tmp1;
         px = tmp1 * (L.vx * L.vz * cphi - L.vy * sphi) + L.vx * ctheta;
         py = tmp1 * (L.vy * L.vz * cphi + L.vx * sphi) + L.vy * ctheta;
@@ -264,7 +302,7 @@ __device__ __forceinline__ float next_scatter(Lane& L, float g, float& ctheta_ou
         py = stheta * sphi;
         pz = (L.vz > 0.f) ? ctheta : -ctheta;
     }
-    const float inv = 1.f / sqrtf(px * px + py * py + pz * pz);
+    const float inv = MP::rsqrt(px * px + py * py + pz * pz);
     L.vx = px * inv;
     L.vy = py * inv;
     L.vz = pz * inv;
@@ -309,7 +347,7 @@ struct ManySims {
 
 // Shared-memory layout: media[nsims_local * nmed_stride] | ppath[reclen_max][blockDim] |
 // seed0[2][blockDim] (u64)
-template <class Sims, bool BATCHED>
+template <class MP, class Sims, bool BATCHED>
 __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned long long* cum, int nsims,
                                             unsigned long long total, int nmed_stride, int reclen_max,
                                             int want_seed, unsigned long long* work_counter) {
@@ -397,7 +435,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                     L.oldidx = (unsigned)kIdUndef;
                     L.fixcount = 0;
                     L.steps = 0;
-                    L.slen = -mmc_logf(rng_next(L.t0, L.t1) + kEps);
+                    L.slen = -MP::log(rng_next(L.t0, L.t1) + kEps);
                     if (S.issavedet) {
                         for (int i = 0; i < S.reclen; i++) PP(i) = 0.f;
                         PP(S.reclen - 1) = L.weight;
@@ -407,7 +445,53 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
             }
         }
         if (__all_sync(kFull, L.mode == M_DONE)) break;
-        if (L.mode == M_DONE) continue;
+
+        // ---- (1b) deferred roulette + scatter, src/mmc_core.cl:2101-2134 ----
+        const unsigned parked = __ballot_sync(kFull, L.mode == M_SCAT);
+        if (parked) {
+            const bool fire = (__popc(parked) >= kScatBatch) ||
+                              __any_sync(kFull, L.mode == M_SCAT && L.wait >= kMaxWait);
+            if (L.mode == M_SCAT) {
+                if (!fire) {
+                    L.wait++;
+                } else {
+                    const SimDev& S = sims(L.sim);
+                    const float4* med = smed + (BATCHED ? L.sim * nmed_stride : 0);
+                    bool killed = false;
+                    if (S.roulette_on && (S.minenergy > 0.f) && (L.weight < S.minenergy)) {
+                        if (rng_next(L.t0, L.t1) * S.roulettesize <= 1.f)
+                            L.weight *= S.roulettesize;
+                        else
+                            killed = true;
+                    }
+                    if (killed) {
+                        if (S.photon_det) S.photon_det[L.pid] = 0;
+                        tally.eesc += L.weight;
+                        if (S.photon_weight) S.photon_weight[L.pid] = L.weight;
+                        if (S.photon_steps) S.photon_steps[L.pid] = L.steps;
+                        L.mode = M_NEED;
+                    } else {
+                        if (S.replay && S.outputtype == OT_WN) {
+                            const float gf = __ldg(S.replaytime + L.pid) * S.Rtstep;
+                            int gate = (gf < (float)(S.maxgate - 1)) ? (int)gf : S.maxgate - 1;
+                            gate = max(gate, 0);
+                            deposit(S, (unsigned)(L.eid - 1) + (unsigned)(gate * S.ne), __ldg(S.replayweight + L.pid));
+                        }
+                        float ctheta;
+                        const int tp = L.label;
+                        L.slen0 = next_scatter<MP>(L, med[tp].z, ctheta);
+                        L.slen = L.slen0;
+                        if (S.issavedet && tp > 0) {
+                            const int M = S.nmedia - 1;
+                            if (S.ismomentum) PP(2 * M + tp - 1) += (1.f - ctheta);
+                            PP(tp - 1) += 1.f;
+                        }
+                        L.mode = M_OUTER;
+                    }
+                }
+            }
+        }
+        if (L.mode == M_DONE || L.mode == M_SCAT || L.mode == M_NEED) continue;
 
         const SimDev& S = sims(L.sim);
         const float4* med = smed + (BATCHED ? L.sim * nmed_stride : 0);
@@ -415,7 +499,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
 
         // ---- (2) one ray-tet step ----
         const bool bad_elem = (L.eid < 1 || L.eid > S.ne);  // defensive: never expected
-        if (!bad_elem) raytet_step(L, S, med);
+        if (!bad_elem) raytet_step<MP>(L, S, med);
         L.steps++;
         tally.raytet++;
         bool ended = false;
@@ -484,7 +568,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                     const float nold = med[oldlabel].w;
                     if (eid <= 0 || med[nlabel].w != nold) {
                         if (!(eid <= 0 && (((nold == S.nout) && (S.isreflect != BC_MIRROR)) || (S.isreflect == BC_ABSORBEXT)))) {
-                            eid = reflectray(L, S, med, oldeid, oldlabel, eid, nlabel, L.faceid);
+                            eid = reflectray<MP>(L, S, med, oldeid, oldlabel, eid, nlabel, L.faceid);
                             if (eid == oldeid) nlabel = oldlabel;
                         }
                     }
@@ -539,33 +623,8 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                     if (S.photon_det) S.photon_det[L.pid] = detid;
                     ended = true;
                 } else {
-                    bool killed = false;
-                    if (S.roulette_on && (S.minenergy > 0.f) && (L.weight < S.minenergy)) {
-                        if (rng_next(L.t0, L.t1) * S.roulettesize <= 1.f)
-                            L.weight *= S.roulettesize;
-                        else
-                            killed = true;
-                    }
-                    if (killed) {
-                        if (S.photon_det) S.photon_det[L.pid] = 0;
-                        ended = true;
-                    } else {
-                        if (S.replay && S.outputtype == OT_WN) {
-                            const float gf = __ldg(S.replaytime + L.pid) * S.Rtstep;
-                            int gate = (gf < (float)(S.maxgate - 1)) ? (int)gf : S.maxgate - 1;
-                            gate = max(gate, 0);
-                            deposit(S, (unsigned)(L.eid - 1) + (unsigned)(gate * S.ne), __ldg(S.replayweight + L.pid));
-                        }
-                        float ctheta;
-                        const int tp = L.label;
-                        L.slen0 = next_scatter(L, med[tp].z, ctheta);
-                        L.slen = L.slen0;
-                        if (S.issavedet && tp > 0) {
-                            if (S.ismomentum) PP(2 * M + tp - 1) += (1.f - ctheta);
-                            PP(tp - 1) += 1.f;
-                        }
-                        L.mode = M_OUTER;
-                    }
+                    L.mode = M_SCAT;  // roulette + scatter run batched at the top of a later trip
+                    L.wait = 0;
                 }
             } else if (ended) {
                 if (S.photon_det) S.photon_det[L.pid] = 0;
@@ -586,20 +645,22 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
     if (tally.sim >= 0) flush_tally(tally, sims(tally.sim));
 }
 
+template <class MP>
 __global__ void __launch_bounds__(128, 8) photon_engine_plain(const __grid_constant__ SimDev sim,
-                                                           unsigned long long* work_counter, int reclen_max,
-                                                           int want_seed) {
+                                                              unsigned long long* work_counter, int reclen_max,
+                                                              int want_seed) {
     SingleSim acc{sim};
-    engine_body<SingleSim, false>(acc, nullptr, 1, sim.nphoton, sim.nmedia, reclen_max, want_seed, work_counter);
+    engine_body<MP, SingleSim, false>(acc, nullptr, 1, sim.nphoton, sim.nmedia, reclen_max, want_seed, work_counter);
 }
 
+template <class MP>
 __global__ void __launch_bounds__(128, 8) photon_engine_batched(const SimDev* __restrict__ sims,
-                                                             const unsigned long long* __restrict__ cum,
-                                                             int nsims, unsigned long long total,
-                                                             int nmed_stride, unsigned long long* work_counter,
-                                                             int reclen_max, int want_seed) {
+                                                                const unsigned long long* __restrict__ cum,
+                                                                int nsims, unsigned long long total,
+                                                                int nmed_stride, unsigned long long* work_counter,
+                                                                int reclen_max, int want_seed) {
     ManySims acc{sims};
-    engine_body<ManySims, true>(acc, cum, nsims, total, nmed_stride, reclen_max, want_seed, work_counter);
+    engine_body<MP, ManySims, true>(acc, cum, nsims, total, nmed_stride, reclen_max, want_seed, work_counter);
 }
 
 size_t smem_bytes(int nmed_rows, int reclen_max, int threads, int want_seed) {
@@ -617,41 +678,60 @@ LaunchShape default_shape(int device, bool batched) {
     int per_sm = 0;
     const int threads = 128;
     if (batched)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_batched, threads, 4096);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_batched<FastMath>, threads, 4096);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_plain, threads, 1024);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_plain<FastMath>, threads, 1024);
     if (per_sm < 1) per_sm = 1;
     return LaunchShape{sms * per_sm, threads};
 }
 
-cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
-                         cudaStream_t stream) {
+template <class MP>
+static cudaError_t launch_plain_t(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
+                                  cudaStream_t stream) {
     const int want_seed = (sim.issavedet && sim.seeds) ? 1 : 0;
     const int reclen_max = sim.issavedet ? sim.reclen : 0;
     const size_t smem = smem_bytes(sim.nmedia, reclen_max, shape.threads, want_seed);
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(photon_engine_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(photon_engine_plain<MP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
-    photon_engine_plain<<<shape.blocks, shape.threads, smem, stream>>>(sim, work_counter, reclen_max, want_seed);
+    (void)cudaGetLastError();  // the launch check below must see this launch's status only
+    photon_engine_plain<MP><<<shape.blocks, shape.threads, smem, stream>>>(sim, work_counter, reclen_max, want_seed);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
+                         cudaStream_t stream) {
+    return sim.fast_math ? launch_plain_t<FastMath>(sim, work_counter, shape, stream)
+                         : launch_plain_t<ExactMath>(sim, work_counter, shape, stream);
+}
+
+template <class MP>
+static cudaError_t launch_batched_t(const SimDev* sims, const unsigned long long* cum, int nsims,
+                                    unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
+                                    unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream) {
+    const size_t smem = smem_bytes(nsims * nmed_stride, reclen_max, shape.threads, want_seed);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(photon_engine_batched<MP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(unsigned long long), stream);
+    if (e != cudaSuccess) return e;
+    (void)cudaGetLastError();  // the launch check below must see this launch's status only
+    photon_engine_batched<MP><<<shape.blocks, shape.threads, smem, stream>>>(sims, cum, nsims, total, nmed_stride,
+                                                                            work_counter, reclen_max, want_seed);
     return cudaGetLastError();
 }
 
 cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
                            unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
-                           unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream) {
-    const size_t smem = smem_bytes(nsims * nmed_stride, reclen_max, shape.threads, want_seed);
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(photon_engine_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
-    cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(unsigned long long), stream);
-    if (e != cudaSuccess) return e;
-    photon_engine_batched<<<shape.blocks, shape.threads, smem, stream>>>(sims, cum, nsims, total, nmed_stride,
-                                                                        work_counter, reclen_max, want_seed);
-    return cudaGetLastError();
+                           unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream, int fast_math) {
+    return fast_math ? launch_batched_t<FastMath>(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
+                                                  work_counter, shape, stream)
+                     : launch_batched_t<ExactMath>(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
+                                                   work_counter, shape, stream);
 }
 
 }  // namespace mmcgb

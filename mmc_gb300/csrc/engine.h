@@ -67,6 +67,7 @@ struct SimDev {
     int outputtype;
     int replay;            // replay mode (seeds from a previous run)
     int accum_f64;
+    int fast_math;         // 1: hardware-approximate math, 0: bit-exact with the CPU oracle
     int reclen;            // detected-photon columns excluding the detector id
     int nmed_ppath;        // M = nmedia-1
     // replay inputs
@@ -101,7 +102,8 @@ cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, La
 // `cum` = inclusive prefix sums of photon counts, length nsims).
 cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
                            unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
-                           unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream);
+                           unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream,
+                           int fast_math);
 LaunchShape default_shape(int device, bool batched);
 
 // Records the message returned by mmcgb_last_error() on this thread.

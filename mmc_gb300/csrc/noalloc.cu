@@ -159,6 +159,7 @@ extern "C" int32_t mmcgb_simulate_noalloc(mmcgb_mesh* mesh, const mmcgb_config* 
     S.issaveseed = (c->issavedet && c->issaveseed) ? 1 : 0;
     S.outputtype = c->outputtype;
     S.accum_f64 = 1;
+    S.fast_math = c->fast_math ? 1 : 0;
     S.reclen = reclen;
     S.nmed_ppath = M;
     S.f64 = out->field_raw;

@@ -1,0 +1,182 @@
+"""The batched, serving and differentiation benchmark workloads
+(``python bench.py --workload batched|serving|replay``).  Each prints one JSON
+line.  Meshes are the seeded synthetic recipes of mmc_gb300.meshgen.
+
+batched  256 simulations on the 4-layer shell mesh (1.296M tets): random
+         per-layer mua (log-uniform 1e-3..1e-1), mus' (0.5..3), g (0.8..0.95),
+         a source 0.5 mm inside the r=25 mm surface at a random angle pointing
+         inward, photons log-uniform 1e5..1e7, element fluence, 10 gates of
+         0.5 ns.  One persistent launch for all vs one plain launch each
+         (device time); the autotuner picks the launch shape.
+serving  Poisson arrivals (200/s) over three resident meshes (162k-tet cube,
+         1.3M-tet inclusion cube, 0.6 mm shell mesh with 6.0M tets): photons
+         log-uniform 1e5..1e8, per-layer properties as above, a random surface
+         pencil source, 1-8 detectors, 10 gates, float32 fluence.  p50/p99
+         latency and photons/ms, against the same requests run one at a time.
+replay   shell mesh, pencil (30,30,5.5) +z, 8 detectors R=1.5 mm on the shell
+         surface at polar angles 10..80 deg, 1e7 photons with seeds; L =
+         sum_d c_d log W_d; forward and replay (backward) throughput.
+"""
+from __future__ import annotations
+
+import dataclasses
+import json
+import time
+
+import numpy as np
+
+from mmc_gb300 import meshgen
+from mmc_gb300.autotune import autotune
+from mmc_gb300.core import Mesh, Session, SimConfig, launch_batch, simulate
+
+CENTER = np.array([30.0, 30.0, 30.0])
+
+
+def _random_media(rng, base):
+    media = base.copy()
+    k = media.shape[0] - 1
+    g = rng.uniform(0.8, 0.95, k)
+    musp = rng.uniform(0.5, 3.0, k)
+    media[1:, 0] = 10 ** rng.uniform(-3, -1, k)
+    media[1:, 1] = musp / (1 - g)
+    media[1:, 2] = g
+    return media.astype(np.float32)
+
+
+def _surface_source(rng, radius=24.5):
+    u = rng.normal(size=3)
+    u /= np.linalg.norm(u)
+    return tuple(CENTER + radius * u), tuple(-u)
+
+
+def run_batched(args):
+    m = meshgen.shell_mesh(n=60, jitter=0.25, seed=4321)
+    mesh = Mesh(m.node, m.elem, m.label)
+    rng = np.random.default_rng(2026)
+    cfgs = []
+    for i in range(256):
+        pos, d = _surface_source(rng)
+        cfgs.append(SimConfig(media=_random_media(rng, m.media), nphoton=int(10 ** rng.uniform(5, 7)), seed=i + 1,
+                              srcpos=pos, srcdir=d, tend=5e-9, tstep=0.5e-9, basisorder=0, isnormalized=1))
+    tune = autotune(mesh, cfgs[0], trial_photons=1_000_000)
+    cfgs = [dataclasses.replace(c, threads=tune["threads"], blocks=tune["blocks"], accum_f64=tune["accum_f64"])
+            for c in cfgs]
+    total = sum(c.nphoton for c in cfgs)
+    # one plain launch per simulation (device time of each launch)
+    serial_ms = 0.0
+    for c in cfgs:
+        s = Session(mesh, c)
+        s.launch(0, c.nphoton)
+        serial_ms += s.sync()
+        s.end(collect=False)
+    # all simulations in one persistent launch
+    sess = [Session(mesh, c) for c in cfgs]
+    launch_batch(sess, [0] * len(cfgs), [c.nphoton for c in cfgs])
+    batched_ms = sess[0].sync()
+    t0 = time.perf_counter()
+    results = [s.end() for s in sess]
+    readback_s = time.perf_counter() - t0
+    absorbed = float(np.mean([r.absorbed_fraction for r in results]))
+    line = {"metric": "aggregate photons/ms, 256 batched simulations", "value": total / batched_ms,
+            "unit": "photons/ms", "n_gpus": 1, "higher_is_better": True, "workload": "batched-256-shells",
+            "serial_plain_photons_per_ms": total / serial_ms, "speedup_vs_serial_plain": serial_ms / batched_ms,
+            "batched_kernel_ms": batched_ms, "serial_kernel_ms": serial_ms, "photons": total,
+            "readback_and_normalize_s": readback_s, "mean_absorbed_fraction": absorbed,
+            "autotune": {k: v for k, v in tune.items() if k != "trials"}, "data": "synthetic",
+            "config": {"mesh": "4-layer shells 1.296M tets", "sims": 256, "gates": 10}}
+    print(json.dumps(line), flush=True)
+
+
+def run_serving(args):
+    from mmc_gb300.serving import Request, Server
+    rng = np.random.default_rng(7)
+    meshes = {}
+    recipes = {"cube162k": meshgen.homogeneous_cube(n=30),
+               "incl1.3M": meshgen.inclusion_cube(n=60, jitter=0.25, seed=12345),
+               "shell6M": meshgen.shell_mesh(n=100, jitter=0.15, seed=99)}
+    for k, mm in recipes.items():
+        meshes[k] = (Mesh(mm.node, mm.elem, mm.label), mm)
+    keys = list(meshes)
+    reqs = []
+    t = 0.0
+    for i in range(args.requests):
+        key = keys[rng.integers(len(keys))]
+        mm = meshes[key][1]
+        t += rng.exponential(1.0 / 200.0)
+        if key == "shell6M":
+            pos, d = _surface_source(rng)
+            media = _random_media(rng, mm.media)
+        else:  # surface pencil on the z=0 face pointing into the cube
+            pos, d = (float(rng.uniform(10, 50)), float(rng.uniform(10, 50)), 0.0), (0.0, 0.0, 1.0)
+            media = mm.media.copy()
+            media[1:, 0] = 10 ** rng.uniform(-3, -1, len(media) - 1)
+        ndet = int(rng.integers(1, 9))
+        det = []
+        for j in range(ndet):
+            if key == "shell6M":
+                p, _ = _surface_source(rng, 25.0)
+            else:
+                p = (float(rng.uniform(5, 55)), float(rng.uniform(5, 55)), 0.0)
+            det.append([*p, 2.0])
+        cfg = SimConfig(media=media, nphoton=int(10 ** rng.uniform(5, 8)), seed=1000 + i, srcpos=pos, srcdir=d,
+                        tend=5e-9, tstep=0.5e-9, issavedet=1, detpos=np.array(det, np.float32),
+                        maxdetphoton=200_000, basisorder=0, isnormalized=1, accum_f64=0)
+        reqs.append(Request(mesh=key, cfg=cfg, arrival=t))
+    # continuous batching
+    srv = Server({k: v[0] for k, v in meshes.items()}, wave_photons=8_000_000, min_share=100_000)
+    t0 = time.perf_counter()
+    for r in reqs:
+        r.arrival += t0
+    srv.run(arrivals=reqs, deadline=t0 + 1800)
+    st = srv.stats()
+    # the same requests one at a time, in arrival order (plain launches)
+    service = []
+    for r in reqs:
+        s0 = time.perf_counter()
+        simulate(meshes[r.mesh][0], r.cfg)
+        service.append(time.perf_counter() - s0)
+    fin, lat = 0.0, []
+    arr = [r.arrival - t0 for r in reqs]
+    for a, s in zip(arr, service):
+        fin = max(fin, a) + s
+        lat.append(fin - a)
+    photons = sum(r.cfg.nphoton for r in reqs)
+    serial_rate = photons / (max(fin - arr[0], 1e-9) * 1e3)
+    line = {"metric": "served photons/ms (continuous batching)", "value": st["photons_per_ms"], "unit": "photons/ms",
+            "n_gpus": 1, "higher_is_better": True, "workload": "serving-3-meshes",
+            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "requests": st["requests"], "waves": st["waves"],
+            "mean_wave_ms": st["mean_wave_ms"], "serial_plain_photons_per_ms": serial_rate,
+            "speedup_vs_serial_plain": st["photons_per_ms"] / serial_rate,
+            "serial_p50_ms": float(np.percentile(np.array(lat) * 1e3, 50)),
+            "serial_p99_ms": float(np.percentile(np.array(lat) * 1e3, 99)), "photons": photons, "data": "synthetic",
+            "config": {"arrival_rate_hz": 200, "photons": "log-uniform 1e5-1e8", "gates": 10, "fluence": "float32"}}
+    print(json.dumps(line), flush=True)
+
+
+def run_replay(args):
+    from mmc_gb300 import replay as rp
+    m = meshgen.shell_mesh(n=60, jitter=0.25, seed=4321)
+    mesh = Mesh(m.node, m.elem, m.label)
+    th = np.deg2rad(np.arange(10, 90, 10))
+    det = np.array([[*(CENTER + 25.0 * np.array([np.sin(a), 0.0, -np.cos(a)])), 1.5] for a in th], np.float32)
+    cfg = SimConfig(media=m.media, nphoton=10_000_000, seed=31, srcpos=(30.0, 30.0, 5.5), tend=5e-9, tstep=5e-9,
+                    issavedet=1, issaveseed=1, detpos=det, maxdetphoton=5_000_000, basisorder=0, isnormalized=0)
+    c = np.random.default_rng(3).normal(size=len(det))
+    t0 = time.perf_counter()
+    fwd = simulate(mesh, cfg)
+    t1 = time.perf_counter()
+    L, W, gmua, gmus = rp.loss_and_grads(mesh, cfg, fwd.detp, fwd.seeds, c)
+    t2 = time.perf_counter()
+    nrep = len(fwd.detp)
+    line = {"metric": "replay (backward) photons/ms", "value": 2 * nrep / ((t2 - t1) * 1e3), "unit": "photons/ms",
+            "n_gpus": 1, "higher_is_better": True, "workload": "replay-8-detectors",
+            "forward_photons_per_ms": cfg.nphoton / ((t1 - t0) * 1e3), "forward_kernel_ms": fwd.kernel_ms,
+            "detected": int(fwd.detected), "replayed": nrep, "loss": L,
+            "detector_weights": [float(x) for x in W], "backward_s": t2 - t1,
+            "grad_mua_norm": float(np.linalg.norm(gmua)), "grad_mus_norm": float(np.linalg.norm(gmus)),
+            "data": "synthetic", "config": {"mesh": "4-layer shells 1.296M tets", "photons": 10_000_000}}
+    print(json.dumps(line), flush=True)
+
+
+def run(args):
+    {"batched": run_batched, "serving": run_serving, "replay": run_replay}[args.workload](args)

@@ -1,0 +1,68 @@
+"""Batched launches: several simulations (different meshes, optical
+properties, sources, photon counts) share one persistent launch.  Each photon
+stream depends only on its simulation's seed and photon index, so every
+simulation must give the same deposits and detected records alone and in the
+mix (float64 accumulation: equal up to the order of the additions)."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from mmc_gb300 import meshgen
+from mmc_gb300.core import Mesh, Session, SimConfig, launch_batch, simulate, simulate_batch
+
+pytestmark = pytest.mark.gpu
+
+
+def _rows(r):
+    return sorted(map(bytes, np.concatenate([r.detp.view(np.uint8).reshape(len(r.detp), -1), r.seeds], 1)))
+
+
+def _cases():
+    a = meshgen.inclusion_cube(n=16, jitter=0.5, seed=4)
+    b = meshgen.shell_mesh(n=20, jitter=0.5, seed=5)
+    ma, mb = Mesh(a.node, a.elem, a.label), Mesh(b.node, b.elem, b.label)
+    det = np.array([[40, 30, 0, 3], [45, 30, 0, 3]], np.float32)
+    sh_media = b.media.copy()
+    sh_media[1:, 0] *= 1.7
+    cfgs = [
+        SimConfig(media=a.media, nphoton=30000, seed=1, srcpos=(30, 30, 0), tend=5e-9, tstep=0.5e-9,
+                  issavedet=1, issaveseed=1, detpos=det, maxdetphoton=50000, basisorder=0, isnormalized=0),
+        SimConfig(media=sh_media, nphoton=7000, seed=2, srcpos=(30, 30, 5.6), srcdir=(0, 0, 1), tend=5e-9,
+                  tstep=0.5e-9, issavedet=1, issaveseed=1, detpos=np.array([[30, 30, 5, 4]], np.float32),
+                  maxdetphoton=50000, basisorder=0, isnormalized=0),
+        SimConfig(media=a.media, nphoton=120000, seed=3, srcpos=(30, 30, 0), tend=5e-9, tstep=1e-9,
+                  issavedet=1, issaveseed=1, detpos=det, maxdetphoton=50000, basisorder=0, isnormalized=0),
+    ]
+    return [ma, mb, ma], cfgs
+
+
+def test_batch_equals_individual_runs(gpu_ready):
+    meshes, cfgs = _cases()
+    alone = [simulate(m, c) for m, c in zip(meshes, cfgs)]
+    mixed = simulate_batch(meshes, cfgs)
+    for a, b in zip(alone, mixed):
+        np.testing.assert_allclose(b.field, a.field, rtol=1e-9, atol=1e-12)
+        assert a.raytet == b.raytet and a.detected == b.detected
+        assert _rows(a) == _rows(b)
+        assert b.energyesc == pytest.approx(a.energyesc, rel=1e-9)
+
+
+def test_session_waves_equal_individual_runs(gpu_ready):
+    """Sessions advanced in several shared waves (the serving loop's launch
+    pattern) reproduce their one-shot results."""
+    meshes, cfgs = _cases()
+    alone = [simulate(m, c) for m, c in zip(meshes, cfgs)]
+    sess = [Session(m, c) for m, c in zip(meshes, cfgs)]
+    done = [0] * len(cfgs)
+    quantum = 20000
+    while any(d < c.nphoton for d, c in zip(done, cfgs)):
+        live = [i for i, c in enumerate(cfgs) if done[i] < c.nphoton]
+        counts = [min(quantum, cfgs[i].nphoton - done[i]) for i in live]
+        launch_batch([sess[i] for i in live], [done[i] for i in live], counts)
+        for i, k in zip(live, counts):
+            done[i] += k
+    res = [s.end() for s in sess]
+    for a, b in zip(alone, res):
+        np.testing.assert_allclose(b.field, a.field, rtol=1e-9, atol=1e-12)
+        assert a.raytet == b.raytet and _rows(a) == _rows(b)

@@ -18,7 +18,7 @@ C0_SRC = dict(srcpos=(30.0, 30.0, 0.0), srcdir=(0.0, 0.0, 1.0))
 
 
 def _cfg(m, **kw):
-    base = dict(media=m.media, nphoton=4000, seed=1648335518, basisorder=0, **C0_SRC)
+    base = dict(media=m.media, nphoton=4000, seed=1648335518, basisorder=0, fast_math=0, **C0_SRC)
     base.update(kw)
     return SimConfig(**base)
 

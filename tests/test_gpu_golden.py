@@ -9,11 +9,11 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("name", ["cube6k", "incl48k"])
-@pytest.mark.parametrize("accum_f64", [1, 0])
-def test_engine_matches_reference_runs(gpu_ready, name, accum_f64):
+@pytest.mark.parametrize("accum_f64,fast_math", [(1, 0), (0, 0), (1, 1), (0, 1)])
+def test_engine_matches_reference_runs(gpu_ready, name, accum_f64, fast_math):
     import dataclasses
     m, cfg, fx = gc.case_mesh_and_config(name, seed=9001)
-    cfg = dataclasses.replace(cfg, accum_f64=accum_f64)
+    cfg = dataclasses.replace(cfg, accum_f64=accum_f64, fast_math=fast_math)
     mesh = Mesh(m.node, m.elem, m.label)
     r = simulate(mesh, cfg)
     msgs = gc.check_field(r.field, fx, m.media, m.label, cfg.nphoton)

@@ -1,0 +1,129 @@
+"""Replay and the replay Jacobians.
+
+* Replay identity (the reference's own check, matlab/mmcjmua.m:55-60): the
+  detected photons, re-traced from their saved seeds, are detected again with
+  identical records.
+* dL/dmua and dL/dmus of L = sum_d c_d log W_d from one replay pair, against
+  central finite differences (+-1%) with common random numbers on element
+  groups (each group relabelled as its own copy of its layer's medium).
+  Changing mua does not change photon paths, so the mua difference quotient is
+  smooth and must match closely; changing mus changes paths, so that check is
+  statistical.
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from mmc_gb300 import io, meshgen
+from mmc_gb300 import replay as rp
+from mmc_gb300.core import Mesh, SimConfig, simulate
+
+pytestmark = pytest.mark.gpu
+
+CENTER = np.array([30.0, 30.0, 30.0])
+
+
+def _det():
+    th = np.deg2rad([10.0, 20.0, 30.0, 40.0])
+    return np.array([[*(CENTER + 25.0 * np.array([np.sin(a), 0.0, -np.cos(a)])), 3.0] for a in th], np.float32)
+
+
+@pytest.fixture(scope="module")
+def grouped(gpu_ready):
+    """Shell mesh (2 mm voxels) with 8 element groups near the surface under the
+    detectors, each relabelled 5..12 with a copy of its layer's medium."""
+    m = meshgen.shell_mesh(n=30, jitter=0.3, seed=6)
+    cen = meshgen.centroids(m.node, m.elem)
+    rng = np.random.default_rng(11)
+    label = m.label.copy()
+    media = [row for row in m.media]
+    groups = []
+    for g in range(8):
+        a = np.deg2rad(rng.uniform(5, 40))
+        p = CENTER + rng.uniform(21.0, 24.0) * np.array([np.sin(a), 0.0, -np.cos(a)])
+        near = np.nonzero((np.linalg.norm(cen - p, axis=1) < 3.0) & (label >= 1) & (label <= 4))[0]
+        lay = np.bincount(label[near]).argmax()
+        sel = near[label[near] == lay]
+        new = len(media)
+        media.append(m.media[lay].copy())
+        label[sel] = new
+        groups.append(new)
+    media = np.array(media, np.float32)
+    mesh = Mesh(m.node, m.elem, label)
+    return m, mesh, label, media, groups
+
+
+def _cfg(media, n, **kw):
+    base = dict(media=media, nphoton=n, seed=5, srcpos=(30.0, 30.0, 5.5), tend=5e-9, tstep=5e-9, issavedet=1,
+                issaveseed=1, detpos=_det(), maxdetphoton=2_000_000, basisorder=0, isnormalized=0, minenergy=0.0)
+    base.update(kw)
+    return SimConfig(**base)
+
+
+def _loss(res, media, c):
+    w = rp.detected_weight(res.detp, media).astype(np.float64)
+    ids = res.detp[:, 0].astype(int)
+    W = np.array([w[ids == d + 1].sum() for d in range(len(c))])
+    return float(np.sum(c * np.log(W)))
+
+
+def test_replay_reproduces_detected_photons(grouped, tmp_path):
+    m, mesh, label, media, groups = grouped
+    cfg = _cfg(media, 200_000)
+    fwd = simulate(mesh, cfg)
+    assert fwd.detected > 100
+    # through the .mch file, as a reference user would
+    path = str(tmp_path / "run.mch")
+    io.write_mch(path, fwd.detp, fwd.seeds, maxmedia=len(media) - 1, detnum=4, totalphoton=cfg.nphoton,
+                 detected=fwd.detected)
+    detp, hdr, seeds = io.read_mch(path)
+    assert hdr["savedphoton"] == fwd.detected and seeds.shape == (fwd.detected, 16)
+    s, w, t, idx = rp.replay_inputs(detp, seeds, media, 0, cfg.tstart, cfg.tend)
+    rcfg = dataclasses.replace(cfg, nphoton=len(idx), replayseed=s, replayweight=w, replaytime=t, outputtype="wl")
+    rep = simulate(mesh, rcfg)
+    rows = lambda d: sorted(map(bytes, d.view(np.uint8).reshape(len(d), -1)))
+    assert rep.detected == len(idx)
+    assert rows(rep.detp) == rows(detp[idx])
+    # wl = replay weight x path length: summed over elements it equals sum_p w_p * (total path of p)
+    M = len(media) - 1
+    total_path = detp[idx][:, 1 + M:1 + 2 * M].astype(np.float64).sum(1)
+    assert rep.field.sum() == pytest.approx(float((w.astype(np.float64) * total_path).sum()), rel=1e-4)
+
+
+def test_mua_gradient_matches_central_differences(grouped):
+    m, mesh, label, media, groups = grouped
+    c = np.array([0.7, -1.2, 0.4, 1.1])
+    cfg = _cfg(media, 300_000)
+    fwd = simulate(mesh, cfg)
+    L, W, gmua, gmus = rp.loss_and_grads(mesh, cfg, fwd.detp, fwd.seeds, c)
+    for g in groups:
+        dm = 0.01 * media[g, 0]
+        mp, mm = media.copy(), media.copy()
+        mp[g, 0] += dm
+        mm[g, 0] -= dm
+        fd = (_loss(simulate(mesh, dataclasses.replace(cfg, media=mp)), mp, c)
+              - _loss(simulate(mesh, dataclasses.replace(cfg, media=mm)), mm, c)) / (2 * dm)
+        an = float(gmua[label == g].sum())
+        assert an == pytest.approx(fd, rel=2e-3, abs=1e-6 * max(1.0, abs(L))), (g, an, fd)
+
+
+def test_mus_gradient_agrees_with_central_differences(grouped):
+    m, mesh, label, media, groups = grouped
+    c = np.array([0.7, -1.2, 0.4, 1.1])
+    cfg = _cfg(media, 1_000_000)
+    fwd = simulate(mesh, cfg)
+    L, W, gmua, gmus = rp.loss_and_grads(mesh, cfg, fwd.detp, fwd.seeds, c)
+    an, fd = [], []
+    for g in groups:
+        ds = 0.01 * media[g, 1]
+        mp, mm = media.copy(), media.copy()
+        mp[g, 1] += ds
+        mm[g, 1] -= ds
+        fd.append((_loss(simulate(mesh, dataclasses.replace(cfg, media=mp)), mp, c)
+                   - _loss(simulate(mesh, dataclasses.replace(cfg, media=mm)), mm, c)) / (2 * ds))
+        an.append(float(gmus[label == g].sum()))
+    an, fd = np.array(an), np.array(fd)
+    # paths change with mus, so the difference quotients are noisy: compare the pattern over groups
+    assert np.corrcoef(an, fd)[0, 1] > 0.8
+    assert np.sign(an).tolist() == np.sign(fd).tolist() or np.abs(an - fd).max() < 0.5 * np.abs(fd).max()
