@@ -169,6 +169,10 @@ int32_t mmcgb_session_launch(mmcgb_session* s, uint64_t photon_offset, uint64_t 
 int32_t mmcgb_session_launch_batch(int32_t n, mmcgb_session* const* sessions, const uint64_t* offsets,
                                    const uint64_t* counts);
 int32_t mmcgb_session_sync(mmcgb_session* s, float* last_kernel_ms);
+/* The session's CUDA stream (a cudaStream_t): callers may record events on it
+ * to pipeline work, e.g. to know when a batched launch led by this session
+ * has finished.  Valid until mmcgb_session_end. */
+void* mmcgb_session_stream(mmcgb_session* s);
 int32_t mmcgb_session_end(mmcgb_session* s, mmcgb_result* res);
 
 /* `n` simulations sharing one persistent launch; meshes may differ.  Each

@@ -72,7 +72,7 @@ EXPORTS = [
     "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export", "mmcgb_mesh_locate",
     "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run", "mmcgb_session_begin", "mmcgb_session_launch",
     "mmcgb_session_sync", "mmcgb_session_end", "mmcgb_prepare_host", "mmcgb_normalize_host",
-    "mmcgb_session_launch_batch",
+    "mmcgb_session_launch_batch", "mmcgb_session_stream",
 ]
 
 
@@ -109,6 +109,8 @@ def load():
         lib.mmcgb_prepare_host.argtypes = [C.POINTER(MeshDesc)] + [C.c_void_p] * 6
         lib.mmcgb_normalize_host.argtypes = [C.POINTER(MeshDesc), C.POINTER(Config), C.c_void_p, C.c_double,
                                              C.c_double, C.c_void_p, C.POINTER(C.c_double)]
+        lib.mmcgb_session_stream.argtypes = [C.c_void_p]
+        lib.mmcgb_session_stream.restype = C.c_void_p
         lib.mmcgb_session_launch_batch.argtypes = [C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
                                                    C.POINTER(C.c_uint64)]
         for name in ("mmcgb_session_launch_batch", "mmcgb_prepare_host", "mmcgb_normalize_host", "mmcgb_session_begin", "mmcgb_session_launch", "mmcgb_session_sync", "mmcgb_session_end",

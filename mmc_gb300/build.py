@@ -58,9 +58,9 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
     os.makedirs(BUILDDIR, exist_ok=True)
     out = os.path.join(LIBDIR, "libmmcgb.so")
-    headers = [os.path.join(CSRC, h) for h in ("engine.h", "mesh.h", "mesh_handle.h", "devmath.cuh")]
+    headers = [os.path.join(CSRC, h) for h in ("engine.h", "mesh.h", "mesh_handle.h", "devmath.cuh", "output_dev.h")]
     headers.append(os.path.join(ROOT, "include", "mmcgb.h"))
-    cu = ["engine.cu", "noalloc.cu"]
+    cu = ["engine.cu", "noalloc.cu", "output.cu"]
     cpp = ["mesh.cpp", "output.cpp", "api.cpp"]
     srcs = [os.path.join(CSRC, f) for f in cu + cpp]
     if not force and not _stale(out, srcs + headers):

@@ -236,13 +236,18 @@ class SimResult:
         return (self.energytot - self.energyesc) / self.energytot if self.energytot else 0.0
 
 
-def _alloc_result(mesh: Mesh, cfg: SimConfig, trace: bool):
+def _alloc_result(mesh: Mesh, cfg: SimConfig, trace: bool, out: Optional[np.ndarray] = None):
     G = cfg.maxgate
     datalen = mesh.nn if cfg.basisorder else mesh.ne
     nmed = np.asarray(cfg.media).reshape(-1, 4).shape[0]
     reclen = 1 + (2 + (1 if cfg.ismomentum else 0)) * (nmed - 1) + (6 if cfg.issaveexit else 0) + 1
     arrs = {}
-    arrs["field"] = np.zeros((G, datalen), np.float64) if cfg.save_field else None
+    if out is not None:
+        if out.dtype != np.float64 or out.shape != (G, datalen) or not out.flags.c_contiguous:
+            raise ValueError(f"out must be a C-contiguous float64 array of shape {(G, datalen)}")
+        arrs["field"] = out
+    else:
+        arrs["field"] = np.empty((G, datalen), np.float64) if cfg.save_field else None
     if cfg.issavedet:
         arrs["detp"] = np.zeros((int(cfg.maxdetphoton), reclen), np.float32)
         arrs["seeds"] = np.zeros((int(cfg.maxdetphoton), 16), np.uint8) if cfg.issaveseed else None
@@ -272,11 +277,13 @@ def _make_result(r: N.Result, arrs) -> SimResult:
                      photon_steps=arrs["photon_steps"], photon_det=arrs["photon_det"])
 
 
-def simulate(mesh: Mesh, cfg: SimConfig, trace: bool = False) -> SimResult:
-    """Runs one simulation on a resident mesh (mmcgb_simulate)."""
+def simulate(mesh: Mesh, cfg: SimConfig, trace: bool = False, out: Optional[np.ndarray] = None) -> SimResult:
+    """Runs one simulation on a resident mesh (mmcgb_simulate).  `out`: an
+    optional preallocated (maxgate, datalen) float64 array for the field (for
+    example pinned host memory reused across calls)."""
     lib = N.load()
     c, keep = cfg.to_c()
-    r, arrs = _alloc_result(mesh, cfg, trace)
+    r, arrs = _alloc_result(mesh, cfg, trace, out)
     N.check(lib.mmcgb_simulate(mesh.handle, C.byref(c), C.byref(r)))
     del keep
     return _make_result(r, arrs)
@@ -320,6 +327,11 @@ class Session:
     def launch(self, photon_offset: int, nphoton: int):
         N.check(N.load().mmcgb_session_launch(self._h, int(photon_offset), int(nphoton)))
 
+    @property
+    def stream(self) -> int:
+        """The session's cudaStream_t as an integer handle."""
+        return int(N.load().mmcgb_session_stream(self._h) or 0)
+
     def sync(self) -> float:
         ms = C.c_float()
         N.check(N.load().mmcgb_session_sync(self._h, C.byref(ms)))
@@ -352,3 +364,11 @@ def launch_batch(sessions, offsets, counts):
     o = (C.c_uint64 * n)(*[int(x) for x in offsets])
     k = (C.c_uint64 * n)(*[int(x) for x in counts])
     N.check(N.load().mmcgb_session_launch_batch(n, h, o, k))
+
+
+def pinned_empty(shape, dtype=np.float64) -> np.ndarray:
+    """A page-locked host array (through torch's pinned allocator): device to
+    host copies into it run at the interconnect's full rate."""
+    import torch
+    t = torch.empty(int(np.prod(shape)), dtype=getattr(torch, np.dtype(dtype).name), pin_memory=True)
+    return t.numpy().reshape(shape)  # the array's base holds the tensor, keeping the allocation alive

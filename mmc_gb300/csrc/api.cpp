@@ -15,6 +15,7 @@
 #include "engine.h"
 #include "mesh.h"
 #include "mesh_handle.h"
+#include "output_dev.h"
 
 using namespace mmcgb;
 
@@ -243,20 +244,40 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
     CK(cudaMemcpyAsync(energy, B.energy, sizeof(energy), cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(counters, B.counters, sizeof(counters), cudaMemcpyDeviceToHost, stream));
     const size_t saved = std::min<size_t>(detected, c.issavedet ? c.maxdetphoton : 0);
-    std::vector<double> raw;
-    std::vector<float> raw32;
-    const bool f64 = c.accum_f64 != 0;
-    const bool direct = res->field && f64 && !c.basisorder;  // raw layout == element output layout
+    double normalizer = 1.0;
     if (res->field) {
-        if (direct) {
-            CK(cudaMemcpyAsync(res->field, B.f64, sizeof(double) * P.flen, cudaMemcpyDeviceToHost, stream));
-        } else if (f64) {
-            raw.resize(P.flen);
-            CK(cudaMemcpyAsync(raw.data(), B.f64, sizeof(double) * P.flen, cudaMemcpyDeviceToHost, stream));
-        } else {
-            raw32.resize(2 * P.flen);
-            CK(cudaMemcpyAsync(raw32.data(), B.f32, sizeof(float) * 2 * P.flen, cudaMemcpyDeviceToHost, stream));
+        // output stage on the device, then one copy of the final field
+        const size_t datalen = c.basisorder ? (size_t)mesh->host.nn : (size_t)mesh->host.ne;
+        const size_t nout = datalen * P.maxgate;
+        double* dout = nullptr;
+        float* dnvol = nullptr;
+        CK(cudaStreamSynchronize(stream));  // energies are needed by the normalization
+        CK(cudaMallocAsync((void**)&dout, sizeof(double) * nout, stream));
+        if (c.basisorder) {
+            const std::vector<float> nv = surface_fixed_nvol(mesh->host, c);
+            CK(cudaMallocAsync((void**)&dnvol, sizeof(float) * nv.size(), stream));
+            CK(cudaMemcpyAsync(dnvol, nv.data(), sizeof(float) * nv.size(), cudaMemcpyHostToDevice, stream));
+            CK(cudaStreamSynchronize(stream));  // nv is a host temporary
         }
+        DeviceOutputArgs A;
+        A.host = &mesh->host;
+        A.cfg = &c;
+        A.maxgate = P.maxgate;
+        A.energytot = (double)launched;
+        A.energyesc = energy[1];
+        A.f64 = B.f64;
+        A.f32a = B.f32;
+        A.f32b = B.f32 ? B.f32 + P.flen : nullptr;
+        A.elem = mesh->elem;
+        A.label = mesh->label;
+        A.evol = mesh->evol;
+        A.nvol = dnvol;
+        A.media = B.media;
+        A.out = dout;
+        CK(device_output(A, stream, &normalizer));
+        CK(cudaMemcpyAsync(res->field, dout, sizeof(double) * nout, cudaMemcpyDeviceToHost, stream));
+        CK(cudaFreeAsync(dout, stream));
+        if (dnvol) CK(cudaFreeAsync(dnvol, stream));
     }
     if (res->detp && saved) CK(cudaMemcpyAsync(res->detp, B.detp, sizeof(float) * P.reclen * saved, cudaMemcpyDeviceToHost, stream));
     if (res->seeds && saved && B.seeds) CK(cudaMemcpyAsync(res->seeds, B.seeds, 16 * saved, cudaMemcpyDeviceToHost, stream));
@@ -273,20 +294,7 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
     res->energyesc = energy[1];
     res->raytet = counters[0];
     res->aborted = counters[1];
-    res->normalizer = 1.0;
-    if (res->field) {
-        const double* src;
-        if (direct) {
-            src = res->field;
-        } else if (f64) {
-            src = raw.data();
-        } else {
-            raw.resize(P.flen);
-            for (size_t i = 0; i < P.flen; i++) raw[i] = (double)raw32[i] + (double)raw32[i + P.flen];
-            src = raw.data();
-        }
-        res->normalizer = normalize_output(mesh->host, c, P.maxgate, src, res->energytot, res->energyesc, res->field);
-    }
+    res->normalizer = normalizer;
     if (res->aborted) return fail(MMCGB_E_BUDGET, "some photons exceeded the per-photon step budget");
     return MMCGB_OK;
 }
@@ -313,6 +321,8 @@ void free_mesh_device(mmcgb_mesh* m) {
     if (m->elem) cudaFree(m->elem);
     if (m->node) cudaFree(m->node);
     if (m->label) cudaFree(m->label);
+    if (m->evol) cudaFree(m->evol);
+    m->evol = nullptr;
     m->rec = nullptr;
     m->elem = nullptr;
     m->node = nullptr;
@@ -366,6 +376,8 @@ int32_t mmcgb_mesh_create(const mmcgb_mesh_desc* desc, int32_t device, mmcgb_mes
         (e = cudaMalloc((void**)&m->elem, sizeof(int4) * m->host.ne)) != cudaSuccess ||
         (e = cudaMalloc((void**)&m->node, sizeof(float4) * m->host.nn)) != cudaSuccess ||
         (e = cudaMalloc((void**)&m->label, sizeof(int) * m->host.ne)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&m->evol, sizeof(float) * m->host.ne)) != cudaSuccess ||
+        (e = cudaMemcpy(m->evol, m->host.evol.data(), sizeof(float) * m->host.ne, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(m->rec, rec.data(), sizeof(TetRec) * rec.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(m->elem, m->host.elem.data(), sizeof(int4) * m->host.ne, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(m->node, node.data(), sizeof(float4) * m->host.nn, cudaMemcpyHostToDevice)) != cudaSuccess ||
@@ -525,6 +537,8 @@ int32_t mmcgb_session_launch_batch(int32_t n, mmcgb_session* const* ss, const ui
     cudaEventDestroy(done);
     return MMCGB_OK;
 }
+
+void* mmcgb_session_stream(mmcgb_session* s) { return s ? (void*)s->stream : nullptr; }
 
 int32_t mmcgb_session_sync(mmcgb_session* s, float* last_kernel_ms) {
     if (!s) return fail(MMCGB_E_ARG, "null session");

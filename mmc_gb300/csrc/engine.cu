@@ -60,7 +60,6 @@ struct Lane {
 // __sincosf, rsqrtf) and fused multiply-adds, as the reference's CUDA build
 // gets from -use_fast_math; validated statistically.
 struct ExactMath {
-    static constexpr bool kFast = false;
     static __device__ __forceinline__ float div(float a, float b) { return a / b; }
     static __device__ __forceinline__ float exp(float x) { return mmc_expf(x); }
     static __device__ __forceinline__ float log(float x) { return mmc_logf(x); }
@@ -69,7 +68,6 @@ struct ExactMath {
     static __device__ __forceinline__ float mad(float a, float b, float c) { return a * b + c; }
 };
 struct FastMath {
-    static constexpr bool kFast = true;
     static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
     static __device__ __forceinline__ float exp(float x) { return __expf(x); }
     static __device__ __forceinline__ float log(float x) { return __logf(x); }

@@ -11,4 +11,5 @@ struct mmcgb_mesh {
     int4* elem = nullptr;
     float4* node = nullptr;
     int* label = nullptr;
+    float* evol = nullptr;
 };

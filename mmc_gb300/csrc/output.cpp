@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "mesh.h"
+#include "output_dev.h"
 
 namespace mmcgb {
 
@@ -42,12 +43,10 @@ double effective_reflection(double n_in, double n_out) {
 
 }  // namespace
 
-double normalize_output(const HostMesh& m, const mmcgb_config& cfg, int G, const double* raw,
-                        double energytot, double energyesc, double* field) {
+std::vector<float> surface_fixed_nvol(const HostMesh& m, const mmcgb_config& cfg) {
     const int nn = m.nn, ne = m.ne;
     const int prop = cfg.nmedia - 1;
     const float* med = cfg.media;
-    const int datalen = cfg.basisorder ? nn : ne;
     std::vector<float> nvol(m.nvol);
     if (cfg.isnormalized == 1 && cfg.basisorder) {
         std::vector<float> Reff(prop + 1, 0.f);
@@ -72,6 +71,15 @@ double normalize_output(const HostMesh& m, const mmcgb_config& cfg, int G, const
         for (int i = 0; i < nn; i++)
             if (nvol[i] < 0.f) nvol[i] = -nvol[i];
     }
+    return nvol;
+}
+
+double normalize_output(const HostMesh& m, const mmcgb_config& cfg, int G, const double* raw,
+                        double energytot, double energyesc, double* field) {
+    const int nn = m.nn, ne = m.ne;
+    const float* med = cfg.media;
+    const int datalen = cfg.basisorder ? nn : ne;
+    const std::vector<float> nvol = surface_fixed_nvol(m, cfg);
     const size_t total = (size_t)datalen * G;
     if (!cfg.basisorder) {
         if (field != raw) std::memcpy(field, raw, sizeof(double) * total);

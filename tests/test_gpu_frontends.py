@@ -1,0 +1,67 @@
+"""Front ends on the GPU: the command line (JSON in, .bin/.mch out, .mch
+replay) and the pmmc-style run(dict)."""
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from mmc_gb300 import io, meshgen, pmmc
+from mmc_gb300.core import Mesh, SimConfig, simulate
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_cli_run_and_replay(gpu_ready, tmp_path):
+    m = meshgen.inclusion_cube(n=12, jitter=0.4, seed=3)
+    cfg = {"Session": {"ID": "cli", "Photons": 20000, "RNGSeed": 5, "BasisOrder": 0, "DoSaveSeed": 1},
+           "Domain": {"Media": m.media.tolist()},
+           "Mesh": {"MeshNode": m.node.tolist(), "MeshElem": np.c_[m.elem, m.label].tolist()},
+           "Forward": {"T0": 0.0, "T1": 5e-9, "Dt": 1e-9},
+           "Optode": {"Source": {"Pos": [30, 30, 0], "Dir": [0, 0, 1]},
+                      "Detector": [{"Pos": [40, 30, 0], "R": 3}, {"Pos": [45, 30, 0], "R": 3}]}}
+    (tmp_path / "in.json").write_text(json.dumps(cfg))
+    env = dict(os.environ, PYTHONPATH=ROOT)
+    r = subprocess.run([sys.executable, "-m", "mmc_gb300", "-f", "in.json", "-s", "base", "-d", "1", "-q", "1"],
+                       cwd=tmp_path, env=env, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    field = io.read_bin(str(tmp_path / "base.bin"), 5)
+    detp, hdr, seeds = io.read_mch(str(tmp_path / "base.mch"))
+    assert field.shape == (5, m.ne) and hdr["savedphoton"] > 0 and seeds is not None
+    # same run through the Python API
+    mesh = Mesh(m.node, m.elem, m.label)
+    ref = simulate(mesh, SimConfig(media=m.media, nphoton=20000, seed=5, srcpos=(30, 30, 0), tend=5e-9, tstep=1e-9,
+                                   basisorder=0, issavedet=1, issaveseed=1,
+                                   detpos=np.array([[40, 30, 0, 3], [45, 30, 0, 3]], np.float32)))
+    np.testing.assert_allclose(field, ref.field, rtol=1e-9)
+    # replay of detector 1 from the .mch file (-E file.mch -P 1 -O l)
+    r = subprocess.run([sys.executable, "-m", "mmc_gb300", "-f", "in.json", "-s", "rep", "-E", "base.mch", "-P", "1",
+                        "-O", "l", "-d", "1", "-U", "0"], cwd=tmp_path, env=env, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    rep = io.read_bin(str(tmp_path / "rep.bin"), 5)
+    assert rep.sum() > 0
+    d2, h2, _ = io.read_mch(str(tmp_path / "rep.mch"))
+    assert h2["savedphoton"] == int((detp[:, 0] == 1).sum())
+
+
+def test_pmmc_run_matches_api(gpu_ready):
+    m = meshgen.inclusion_cube(n=10, jitter=0.4, seed=2)
+    cfg = dict(node=m.node, elem=m.elem, elemprop=m.label, prop=m.media, srcpos=[30, 30, 0], srcdir=[0, 0, 1],
+               nphoton=30000, seed=11, tstart=0.0, tend=5e-9, tstep=1e-9, issavedet=1, issaveseed=1,
+               detpos=[[40, 30, 0, 3]], basisorder=1, outputtype="flux")
+    out = pmmc.run(cfg)
+    assert out["flux"].shape == (m.nn, 5)                       # [datalen, maxgate], as pmmc
+    assert out["detp"].shape[0] == 1 + 2 * 2 + 1               # [columns, ndetected]
+    assert out["seeds"].shape[0] == 16
+    mesh = Mesh(m.node, m.elem, m.label)
+    ref = simulate(mesh, SimConfig(media=m.media, nphoton=30000, seed=11, srcpos=(30, 30, 0), tend=5e-9, tstep=1e-9,
+                                   basisorder=1, issavedet=1, issaveseed=1, detpos=np.array([[40, 30, 0, 3]], np.float32)))
+    np.testing.assert_allclose(out["flux"], ref.field.T, rtol=1e-9)
+    # replay through pmmc with the seed matrix
+    rep = pmmc.run(dict(cfg, seed=out["seeds"], detphotons=out["detp"], outputtype="wl", isnormalized=0))
+    assert rep["flux"].sum() > 0
+    with pytest.raises(ValueError):
+        pmmc.run(dict(cfg, prop=m.media[:1]))

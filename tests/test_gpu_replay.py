@@ -3,12 +3,13 @@
 * Replay identity (the reference's own check, matlab/mmcjmua.m:55-60): the
   detected photons, re-traced from their saved seeds, are detected again with
   identical records.
-* dL/dmua and dL/dmus of L = sum_d c_d log W_d from one replay pair, against
-  central finite differences (+-1%) with common random numbers on element
-  groups (each group relabelled as its own copy of its layer's medium).
-  Changing mua does not change photon paths, so the mua difference quotient is
-  smooth and must match closely; changing mus changes paths, so that check is
-  statistical.
+* dL/dmua and dL/dmus of L = sum_d c_d log W_d from one replay pair, on
+  element groups (each group relabelled as its own copy of its layer's
+  medium).  Changing mua does not change photon paths, so the mua gradient
+  must match central finite differences (+-1%, common random numbers) closely.
+  The summed mus Jacobian of a group must equal the medium derivative built
+  from the saved per-medium scattering counts and path lengths; that
+  derivative is checked against finite differences statistically.
 """
 import dataclasses
 
@@ -29,29 +30,32 @@ def _det():
     return np.array([[*(CENTER + 25.0 * np.array([np.sin(a), 0.0, -np.cos(a)])), 3.0] for a in th], np.float32)
 
 
-@pytest.fixture(scope="module")
-def grouped(gpu_ready):
-    """Shell mesh (2 mm voxels) with 8 element groups near the surface under the
-    detectors, each relabelled 5..12 with a copy of its layer's medium."""
-    m = meshgen.shell_mesh(n=30, jitter=0.3, seed=6)
+def _make_groups(m, ngroups, radius, layers, seed):
     cen = meshgen.centroids(m.node, m.elem)
-    rng = np.random.default_rng(11)
+    rng = np.random.default_rng(seed)
     label = m.label.copy()
     media = [row for row in m.media]
     groups = []
-    for g in range(8):
+    for g in range(ngroups):
         a = np.deg2rad(rng.uniform(5, 40))
         p = CENTER + rng.uniform(21.0, 24.0) * np.array([np.sin(a), 0.0, -np.cos(a)])
-        near = np.nonzero((np.linalg.norm(cen - p, axis=1) < 3.0) & (label >= 1) & (label <= 4))[0]
+        near = np.nonzero((np.linalg.norm(cen - p, axis=1) < radius) & np.isin(label, layers))[0]
         lay = np.bincount(label[near]).argmax()
         sel = near[label[near] == lay]
         new = len(media)
         media.append(m.media[lay].copy())
         label[sel] = new
         groups.append(new)
-    media = np.array(media, np.float32)
-    mesh = Mesh(m.node, m.elem, label)
-    return m, mesh, label, media, groups
+    return label, np.array(media, np.float32), groups
+
+
+@pytest.fixture(scope="module")
+def grouped(gpu_ready):
+    """Shell mesh (2 mm voxels) with 8 element groups near the surface under the
+    detectors, each relabelled 5..12 with a copy of its layer's medium."""
+    m = meshgen.shell_mesh(n=30, jitter=0.3, seed=6)
+    label, media, groups = _make_groups(m, 8, 3.0, [1, 2, 3, 4], 11)
+    return m, Mesh(m.node, m.elem, label), label, media, groups
 
 
 def _cfg(media, n, **kw):
@@ -108,22 +112,65 @@ def test_mua_gradient_matches_central_differences(grouped):
         assert an == pytest.approx(fd, rel=2e-3, abs=1e-6 * max(1.0, abs(L))), (g, an, fd)
 
 
-def test_mus_gradient_agrees_with_central_differences(grouped):
-    m, mesh, label, media, groups = grouped
+def _medium_mus_lr(detp, media, c, g):
+    """dL/dmus of medium g from the detected records alone: each record holds
+    the photon's scattering count and path length per medium, so
+    dW_d/dmus_g = sum_p w_p (nscat_pg / mus_g - ppath_pg)."""
+    M = len(media) - 1
+    w = rp.detected_weight(detp, media).astype(np.float64)
+    ids = detp[:, 0].astype(int)
+    a = detp[:, g].astype(np.float64) / float(media[g, 1]) - detp[:, M + g].astype(np.float64)
+    return float(sum(c[d] * (w[ids == d + 1] * a[ids == d + 1]).sum() / w[ids == d + 1].sum() for d in range(len(c))))
+
+
+@pytest.fixture(scope="module")
+def scattering_groups(gpu_ready):
+    """Six large element groups (6 mm spheres) in the two strongly scattering
+    layers (mus 8.6 and 7.8 /mm) under the detectors."""
+    m = meshgen.shell_mesh(n=30, jitter=0.3, seed=6)
+    label, media, groups = _make_groups(m, 6, 6.0, [3, 4], 12)
+    return Mesh(m.node, m.elem, label), label, media, groups
+
+
+def test_mus_jacobian_sums_to_medium_derivative(scattering_groups):
+    """The replayed per-element J_mus = wn/mus - wl, summed over a group, is the
+    medium derivative computed from the saved scattering counts and partial
+    path lengths of the same detected photons."""
+    mesh, label, media, groups = scattering_groups
     c = np.array([0.7, -1.2, 0.4, 1.1])
-    cfg = _cfg(media, 1_000_000)
+    cfg = _cfg(media, 500_000)
     fwd = simulate(mesh, cfg)
     L, W, gmua, gmus = rp.loss_and_grads(mesh, cfg, fwd.detp, fwd.seeds, c)
-    an, fd = [], []
     for g in groups:
-        ds = 0.01 * media[g, 1]
-        mp, mm = media.copy(), media.copy()
-        mp[g, 1] += ds
-        mm[g, 1] -= ds
-        fd.append((_loss(simulate(mesh, dataclasses.replace(cfg, media=mp)), mp, c)
-                   - _loss(simulate(mesh, dataclasses.replace(cfg, media=mm)), mm, c)) / (2 * ds))
-        an.append(float(gmus[label == g].sum()))
-    an, fd = np.array(an), np.array(fd)
-    # paths change with mus, so the difference quotients are noisy: compare the pattern over groups
-    assert np.corrcoef(an, fd)[0, 1] > 0.8
-    assert np.sign(an).tolist() == np.sign(fd).tolist() or np.abs(an - fd).max() < 0.5 * np.abs(fd).max()
+        lr = _medium_mus_lr(fwd.detp, media, c, g)
+        assert float(gmus[label == g].sum()) == pytest.approx(lr, rel=1e-3, abs=1e-4 * abs(lr) + 1e-9), g
+
+
+def test_mus_gradient_agrees_with_central_differences(scattering_groups):
+    """Changing mus moves the scattering points, so paths past the first
+    changed segment are re-randomized even with common random numbers and the
+    difference quotient is noisy; the likelihood-ratio estimate is noisy too.
+    Both are averaged over independent seeds and compared within four
+    combined standard errors, with the errors required to be small against
+    the signal so that the comparison has power."""
+    mesh, label, media, groups = scattering_groups
+    c = np.array([0.7, -1.2, 0.4, 1.1])
+    K = 4
+    an = np.zeros((K, len(groups)))
+    fd = np.zeros((K, len(groups)))
+    for k in range(K):
+        cfg = _cfg(media, 1_000_000, seed=100 + k, issaveseed=0)
+        fwd = simulate(mesh, cfg)
+        for j, g in enumerate(groups):
+            an[k, j] = _medium_mus_lr(fwd.detp, media, c, g)
+            ds = 0.05 * media[g, 1]
+            mp, mm = media.copy(), media.copy()
+            mp[g, 1] += ds
+            mm[g, 1] -= ds
+            fd[k, j] = (_loss(simulate(mesh, dataclasses.replace(cfg, media=mp)), mp, c)
+                        - _loss(simulate(mesh, dataclasses.replace(cfg, media=mm)), mm, c)) / (2 * ds)
+    se = np.sqrt(an.var(0, ddof=1) / K + fd.var(0, ddof=1) / K)
+    print("dL/dmus likelihood ratio:", an.mean(0), "central differences:", fd.mean(0), "se:", se)
+    assert np.all(np.abs(an.mean(0) - fd.mean(0)) < 4 * se + 1e-3 * np.abs(fd.mean(0)))
+    assert np.median(se) < 0.5 * np.abs(fd.mean(0)).max()
+    assert np.corrcoef(an.mean(0), fd.mean(0))[0, 1] > 0.8

@@ -1,0 +1,84 @@
+"""File formats and front-end parsing (no GPU): .mch round trip, JSON input
+(inline mesh and MeshID .dat files), pmmc dict parsing, .bin/.dat writers."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from mmc_gb300 import io, meshgen, pmmc
+
+
+def test_mch_roundtrip(tmp_path):
+    rng = np.random.default_rng(0)
+    detp = rng.random((37, 6)).astype(np.float32)
+    seeds = rng.integers(0, 255, (37, 16), dtype=np.uint8)
+    p = str(tmp_path / "a.mch")
+    io.write_mch(p, detp, seeds, maxmedia=2, detnum=4, totalphoton=1000, detected=40, unitinmm=1.0)
+    d, h, s = io.read_mch(p)
+    assert h["magic"] == b"MCXH" and h["version"] == 1 and h["colcount"] == 6 and h["savedphoton"] == 37
+    assert h["detected"] == 40 and h["seedbyte"] == 16 and os.path.getsize(p) == 64 + 37 * 6 * 4 + 37 * 16
+    assert np.array_equal(d, detp) and np.array_equal(s, seeds)
+
+
+def _write_case(tmp_path, inline=True):
+    m = meshgen.inclusion_cube(n=4, jitter=0.3, seed=1)
+    cfg = {"Session": {"ID": "t", "Photons": 1234, "RNGSeed": 77, "DoMismatch": 1, "BasisOrder": 0},
+           "Domain": {"Media": [{"mua": 0, "mus": 0, "g": 1, "n": 1}, {"mua": 0.005, "mus": 1, "g": 0.01, "n": 1.37},
+                                {"mua": 0.05, "mus": 5, "g": 0.9, "n": 1.37}]},
+           "Forward": {"T0": 0.0, "T1": 5e-9, "Dt": 1e-9},
+           "Optode": {"Source": {"Pos": [30, 30, 0], "Dir": [0, 0, 1]},
+                      "Detector": [{"Pos": [40, 30, 0], "R": 2}]}}
+    if inline:
+        cfg["Mesh"] = {"MeshNode": m.node.tolist(), "MeshElem": np.c_[m.elem, m.label].tolist(), "InitElem": 0}
+    else:
+        cfg["Mesh"] = {"MeshID": "x"}
+        with open(tmp_path / "node_x.dat", "w") as f:
+            f.write(f"1\t{m.nn}\n")
+            for i, p in enumerate(m.node):
+                f.write(f"{i + 1}\t{p[0]:.8e}\t{p[1]:.8e}\t{p[2]:.8e}\n")
+        with open(tmp_path / "elem_x.dat", "w") as f:
+            f.write(f"1\t{m.ne}\n")
+            for i, (e, lab) in enumerate(zip(m.elem, m.label)):
+                f.write(f"{i + 1}\t{e[0]}\t{e[1]}\t{e[2]}\t{e[3]}\t{lab}\n")
+    p = tmp_path / "in.json"
+    p.write_text(json.dumps(cfg))
+    return str(p), m
+
+
+@pytest.mark.parametrize("inline", [True, False])
+def test_json_input(tmp_path, inline):
+    path, m = _write_case(tmp_path, inline)
+    mesh, cfg, meta = io.load_input(path)
+    np.testing.assert_allclose(mesh["node"], m.node, rtol=1e-6)
+    assert np.array_equal(mesh["elem"], m.elem) and np.array_equal(mesh["label"], m.label)
+    assert cfg.nphoton == 1234 and cfg.seed == 77 and cfg.maxgate == 5 and cfg.basisorder == 0
+    assert cfg.issavedet == 1 and cfg.detpos.shape == (1, 4) and meta["session"] == "t"
+    assert cfg.media.shape == (3, 4)
+
+
+def test_pmmc_dict_parsing():
+    m = meshgen.homogeneous_cube(n=3)
+    node, elem, label, fnb, sc, seeds = pmmc._parse(dict(
+        node=m.node, elem=m.elem, elemprop=m.label, prop=m.media, srcpos=[30, 30, 0], srcdir=[0, 0, 2],
+        nphoton=1e4, tstart=0, tend=5e-9, tstep=1e-9, issavedet=1, detpos=[[40, 30, 0, 2]], outputtype="fluence",
+        method="elem", seed=99))
+    assert sc.nphoton == 10000 and sc.seed == 99 and sc.outputtype == "fluence" and sc.maxgate == 5
+    assert np.allclose(sc.srcdir, (0, 0, 1)) and seeds is None
+    with pytest.raises(ValueError):
+        pmmc._parse(dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[1, 1, 1], method="plucker"))
+    with pytest.raises(ValueError):
+        pmmc._parse(dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[1, 1, 1], srctype="disk"))
+    # a uint8 [16, N] seed matrix selects replay
+    *_, s2 = pmmc._parse(dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[30, 30, 0],
+                              seed=np.zeros((16, 5), np.uint8)))
+    assert s2.shape == (16, 5)
+
+
+def test_bin_and_dat_writers(tmp_path):
+    f = np.arange(12, dtype=np.float64).reshape(3, 4)
+    io.write_bin(str(tmp_path / "a.bin"), f)
+    assert np.array_equal(io.read_bin(str(tmp_path / "a.bin"), 3), f)
+    io.write_dat(str(tmp_path / "a.dat"), f)
+    lines = open(tmp_path / "a.dat").read().split("\n")
+    assert lines[0].split("\t")[0] == "1" and len([x for x in lines if x]) == 12
