@@ -601,8 +601,10 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                     if (S.issavedet && L.eid <= 0) {
                         detid = finddetector(L, S);
                         if (detid) {
-                            // ballot-compacted slot reservation: one atomic per group of detecting lanes
-                            cg::coalesced_group grp = cg::coalesced_threads();
+                            // ballot-compacted slot reservation: one atomic per group of detecting
+                            // lanes of the same simulation (a batched warp mixes simulations)
+                            cg::coalesced_group grp = BATCHED ? cg::labeled_partition(cg::coalesced_threads(), L.sim)
+                                                              : cg::coalesced_threads();
                             unsigned base = 0;
                             if (grp.thread_rank() == 0) base = atomicAdd(S.detcount, grp.size());
                             base = grp.shfl(base, 0);
