@@ -4,9 +4,9 @@ heterogeneous cube (60^3 voxels at 1 mm, 6 tets/voxel, orientation-safe
 of 0.1 ns; 4 detectors R=2 mm saving per-medium partial paths and scatter
 counts; 1e8 photons per job).
 
-A step simulates 1e7 photons (one tenth of the 1e8-photon job) with the mesh
-and all buffers resident on the GPU; the default 10 timed steps are the whole
-job.  L2 is flushed (256 MB write) before every timed step.
+A step is the whole 1e8-photon job, one persistent launch with the mesh and
+all buffers resident on the GPU (each step traces a new photon range of the
+same seed).  L2 is flushed (256 MB write) before every timed step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -28,7 +28,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 BYTES_PER_STEP = 92  # 64 B face planes + 16 B neighbour ids + 4 B label + 8 B fluence RMW per ray-tet test
-PHOTONS_PER_STEP = 10_000_000
+PHOTONS_PER_STEP = 100_000_000
 JOB_PHOTONS = 100_000_000
 WORKLOAD = "inclusion-cube-1.3M-tets"
 

@@ -168,6 +168,23 @@ int32_t mmcgb_session_launch(mmcgb_session* s, uint64_t photon_offset, uint64_t 
  * the continuous-batching server. */
 int32_t mmcgb_session_launch_batch(int32_t n, mmcgb_session* const* sessions, const uint64_t* offsets,
                                    const uint64_t* counts);
+/* As mmcgb_session_launch_batch, but enqueued on the caller's CUDA stream
+ * `stream` (a cudaStream_t), ordered after each session's setup but not
+ * against the sessions' launches: several such launches may be in flight at once and
+ * accumulate into the same sessions concurrently (every accumulation is
+ * atomic).  Each session's later work (mmcgb_session_sync/_end, freeing its
+ * buffers) is ordered after the launch, so ending a session early is safe.
+ * Pipelined serving waves use it: the next wave's blocks take over the SMs
+ * while the current wave's last photons drain.  No counterpart in the
+ * reference. */
+int32_t mmcgb_session_launch_batch_on(int32_t n, mmcgb_session* const* sessions, const uint64_t* offsets,
+                                      const uint64_t* counts, void* stream);
+/* The reference's respin loop (src/mmc_cu_host.cu:656-906: `repeats` launches
+ * accumulating into one set of buffers) as one CUDA graph: launch k traces
+ * photons [photon_offset + k*nphoton, photon_offset + (k+1)*nphoton).  The
+ * graph is captured on the session's stream; later calls of the same shape
+ * update the instantiated graph in place instead of instantiating again. */
+int32_t mmcgb_session_launch_repeat(mmcgb_session* s, uint64_t photon_offset, uint64_t nphoton, int32_t repeats);
 int32_t mmcgb_session_sync(mmcgb_session* s, float* last_kernel_ms);
 /* The session's CUDA stream (a cudaStream_t): callers may record events on it
  * to pipeline work, e.g. to know when a batched launch led by this session

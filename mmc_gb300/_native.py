@@ -72,7 +72,8 @@ EXPORTS = [
     "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export", "mmcgb_mesh_locate",
     "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run", "mmcgb_session_begin", "mmcgb_session_launch",
     "mmcgb_session_sync", "mmcgb_session_end", "mmcgb_prepare_host", "mmcgb_normalize_host",
-    "mmcgb_session_launch_batch", "mmcgb_session_stream",
+    "mmcgb_session_launch_batch", "mmcgb_session_stream", "mmcgb_session_launch_batch_on",
+    "mmcgb_session_launch_repeat",
 ]
 
 
@@ -113,7 +114,10 @@ def load():
         lib.mmcgb_session_stream.restype = C.c_void_p
         lib.mmcgb_session_launch_batch.argtypes = [C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
                                                    C.POINTER(C.c_uint64)]
-        for name in ("mmcgb_session_launch_batch", "mmcgb_prepare_host", "mmcgb_normalize_host", "mmcgb_session_begin", "mmcgb_session_launch", "mmcgb_session_sync", "mmcgb_session_end",
+        lib.mmcgb_session_launch_batch_on.argtypes = [C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
+                                                      C.POINTER(C.c_uint64), C.c_void_p]
+        lib.mmcgb_session_launch_repeat.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32]
+        for name in ("mmcgb_session_launch_batch", "mmcgb_session_launch_batch_on", "mmcgb_session_launch_repeat", "mmcgb_prepare_host", "mmcgb_normalize_host", "mmcgb_session_begin", "mmcgb_session_launch", "mmcgb_session_sync", "mmcgb_session_end",
                      "mmcgb_mesh_create", "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export",
                      "mmcgb_mesh_locate", "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run"):
             getattr(lib, name).restype = C.c_int32

@@ -30,12 +30,19 @@ def _signature(mesh: Mesh, cfg: SimConfig):
             tuple(map(tuple, __import__("numpy").asarray(cfg.media).round(6).tolist())))
 
 
-def autotune(mesh: Mesh, cfg: SimConfig, trial_photons: int = 1_000_000,
-             threads: Iterable[int] = (64, 128), blocks_per_sm: Iterable[int] = (4, 6, 8),
+def autotune(mesh: Mesh, cfg: SimConfig, photons_per_lane: int = 32,
+             threads: Iterable[int] = (64, 128), blocks_per_sm: Iterable[int] = (6, 8),
              accum: Iterable[int] = (1, 0), repeats: int = 2, use_cache: bool = True) -> dict:
     """Returns {'threads', 'blocks', 'accum_f64', 'photons_per_ms', 'trials'} and
-    leaves `cfg` unchanged; apply with dataclasses.replace(cfg, **choice)."""
-    key = (_signature(mesh, cfg), trial_photons, tuple(threads), tuple(blocks_per_sm), tuple(accum))
+    leaves `cfg` unchanged; apply with dataclasses.replace(cfg, **choice).
+
+    Each trial launch gives every lane of the candidate grid the same number
+    of photons (`photons_per_lane`): a launch ends with the drain of its last
+    photons in flight, and a fixed photon count would favour small grids,
+    whose lanes each run more photons past that drain.  The persistent grid
+    hands photons out dynamically, so the grid size also sets the photons per
+    thread (launch photons / lanes)."""
+    key = (_signature(mesh, cfg), photons_per_lane, tuple(threads), tuple(blocks_per_sm), tuple(accum))
     if use_cache and key in _cache:
         return _cache[key]
     sms = _sm_count(mesh.device)
@@ -44,6 +51,7 @@ def autotune(mesh: Mesh, cfg: SimConfig, trial_photons: int = 1_000_000,
     for th, bps, acc in itertools.product(threads, blocks_per_sm, accum):
         # same resident warps per SM for each thread count
         blocks = sms * bps * (128 // th)
+        trial_photons = blocks * th * photons_per_lane
         c = dataclasses.replace(cfg, nphoton=trial_photons, threads=th, blocks=blocks, accum_f64=acc,
                                 save_field=False)
         s = Session(mesh, c)
@@ -55,7 +63,8 @@ def autotune(mesh: Mesh, cfg: SimConfig, trial_photons: int = 1_000_000,
             ms.append(s.sync())
         s.end(collect=False)
         rate = trial_photons / min(ms)
-        trials.append(dict(threads=th, blocks=blocks, accum_f64=acc, photons_per_ms=rate))
+        trials.append(dict(threads=th, blocks=blocks, accum_f64=acc, photons_per_ms=rate,
+                           photons_per_thread=photons_per_lane))
         if best is None or rate > best["photons_per_ms"]:
             best = trials[-1]
     out = dict(best, trials=trials)

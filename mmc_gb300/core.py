@@ -327,6 +327,11 @@ class Session:
     def launch(self, photon_offset: int, nphoton: int):
         N.check(N.load().mmcgb_session_launch(self._h, int(photon_offset), int(nphoton)))
 
+    def launch_repeat(self, photon_offset: int, nphoton: int, repeats: int):
+        """`repeats` launches of `nphoton` photons as one CUDA graph
+        (mmcgb_session_launch_repeat); sync() then times the whole graph."""
+        N.check(N.load().mmcgb_session_launch_repeat(self._h, int(photon_offset), int(nphoton), int(repeats)))
+
     @property
     def stream(self) -> int:
         """The session's cudaStream_t as an integer handle."""
@@ -357,13 +362,20 @@ class Session:
                 pass
 
 
-def launch_batch(sessions, offsets, counts):
-    """One persistent launch over several sessions (mmcgb_session_launch_batch)."""
+def launch_batch(sessions, offsets, counts, stream: Optional[int] = None):
+    """One persistent launch over several sessions (mmcgb_session_launch_batch).
+    With `stream` (a cudaStream_t handle, e.g. torch.cuda.Stream().cuda_stream)
+    the launch is enqueued there with no ordering against the sessions' own
+    streams (mmcgb_session_launch_batch_on): the caller waits for that stream
+    before syncing or ending the sessions."""
     n = len(sessions)
     h = (C.c_void_p * n)(*[s._h for s in sessions])
     o = (C.c_uint64 * n)(*[int(x) for x in offsets])
     k = (C.c_uint64 * n)(*[int(x) for x in counts])
-    N.check(N.load().mmcgb_session_launch_batch(n, h, o, k))
+    if stream is None:
+        N.check(N.load().mmcgb_session_launch_batch(n, h, o, k))
+    else:
+        N.check(N.load().mmcgb_session_launch_batch_on(n, h, o, k, C.c_void_p(int(stream))))
 
 
 def pinned_empty(shape, dtype=np.float64) -> np.ndarray:

@@ -308,10 +308,14 @@ struct mmcgb_session {
     cudaStream_t stream = nullptr;
     unsigned long long* work = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ready = nullptr;  // recorded after the session's buffers are set up
     unsigned long long launched = 0;
     int launches = 0;
     bool timed = false;  // ev0/ev1 bracket this session's last launch
     LaunchShape shape{0, 0};
+    cudaGraphExec_t gexec = nullptr;  // respin graph (mmcgb_session_launch_repeat) and its shape
+    uint64_t g_nphoton = 0;
+    int g_repeats = 0;
 };
 
 namespace {
@@ -392,6 +396,7 @@ int32_t mmcgb_mesh_create(const mmcgb_mesh_desc* desc, int32_t device, mmcgb_mes
 int32_t mmcgb_mesh_destroy(mmcgb_mesh* m) {
     if (!m) return MMCGB_OK;
     cudaSetDevice(m->device);
+    cudaDeviceSynchronize();  // no launch still reading the records outlives them
     free_mesh_device(m);
     delete m;
     return MMCGB_OK;
@@ -433,12 +438,16 @@ int32_t mmcgb_session_begin(mmcgb_mesh* mesh, const mmcgb_config* cfg, mmcgb_res
         cudaError_t e = cudaMallocAsync((void**)&s->work, sizeof(unsigned long long), s->stream);
         if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
         if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ready, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(s->ready, s->stream);
         if (e != cudaSuccess) rc = cuda_fail(e, "session setup");
     }
     if (rc) {
         s->P.buf.release();
         if (s->work) cudaFreeAsync(s->work, s->stream);
         cudaStreamSynchronize(s->stream);
+        for (cudaEvent_t ev : {s->ev0, s->ev1, s->ready})
+            if (ev) cudaEventDestroy(ev);
         cudaStreamDestroy(s->stream);
         return rc;
     }
@@ -468,8 +477,16 @@ int32_t mmcgb_session_launch(mmcgb_session* s, uint64_t photon_offset, uint64_t 
     return MMCGB_OK;
 }
 
-int32_t mmcgb_session_launch_batch(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets,
-                                   const uint64_t* counts) {
+}  // extern "C"
+
+namespace {
+
+// One persistent launch over several sessions.  `ordered`: on the first
+// session's stream, after every session's earlier work and before its later
+// work, timed with the first session's events.  Otherwise on `st` with its own
+// work counter and no ordering against the sessions' streams.
+int batch_launch(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets, const uint64_t* counts,
+                 cudaStream_t st, bool ordered) {
     if (n <= 0 || !ss || !offsets || !counts) return fail(MMCGB_E_ARG, "null or empty batch");
     mmcgb_session* s0 = ss[0];
     if (!s0) return fail(MMCGB_E_ARG, "null session");
@@ -499,10 +516,12 @@ int32_t mmcgb_session_launch_batch(int32_t n, mmcgb_session* const* ss, const ui
     if ((size_t)n * nmed_stride * sizeof(float4) > 40 * 1024)
         return fail(MMCGB_E_ARG, "batch media tables exceed shared memory; split the batch");
     CK(cudaSetDevice(device));
-    cudaStream_t st = s0->stream;
+    if (ordered) st = s0->stream;
     // order the batch after every session's earlier work, and every session's later work after it
     std::vector<cudaEvent_t> evs;
-    for (int i = 1; i < n; i++) {
+    // unordered: only after each session's setup (buffer allocation and zeroing, table uploads)
+    for (int i = 0; !ordered && i < n; i++) CK(cudaStreamWaitEvent(st, ss[i]->ready, 0));
+    for (int i = 1; ordered && i < n; i++) {
         if (ss[i]->stream == st) continue;
         cudaEvent_t e;
         CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -512,29 +531,103 @@ int32_t mmcgb_session_launch_batch(int32_t n, mmcgb_session* const* ss, const ui
     }
     SimDev* dsims = nullptr;
     unsigned long long* dcum = nullptr;
+    unsigned long long* work = ordered ? s0->work : nullptr;
     CK(cudaMallocAsync((void**)&dsims, sizeof(SimDev) * n, st));
     CK(cudaMallocAsync((void**)&dcum, sizeof(unsigned long long) * n, st));
+    if (!ordered) CK(cudaMallocAsync((void**)&work, sizeof(unsigned long long), st));
     CK(cudaMemcpyAsync(dsims, sims.data(), sizeof(SimDev) * n, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dcum, cum.data(), sizeof(unsigned long long) * n, cudaMemcpyHostToDevice, st));
     LaunchShape shape = default_shape(device, true);
     if (s0->cfg.threads > 0) shape.threads = std::max(32, std::min(s0->cfg.threads, 128) / 32 * 32);
     if (s0->cfg.blocks > 0) shape.blocks = s0->cfg.blocks;
-    CK(cudaEventRecord(s0->ev0, st));
-    CK(launch_batched(dsims, dcum, n, total, nmed_stride, reclen_max, want_seed, s0->work, shape, st, fast));
-    CK(cudaEventRecord(s0->ev1, st));
+    if (ordered) CK(cudaEventRecord(s0->ev0, st));
+    CK(launch_batched(dsims, dcum, n, total, nmed_stride, reclen_max, want_seed, work, shape, st, fast));
+    if (ordered) CK(cudaEventRecord(s0->ev1, st));
     CK(cudaFreeAsync(dsims, st));
     CK(cudaFreeAsync(dcum, st));
-    cudaEvent_t done;
+    if (!ordered) CK(cudaFreeAsync(work, st));
+    // every session's later work (sync, output stage, freeing its buffers) waits for this launch;
+    // unordered launches never wait on the session streams, so they still overlap one another
+    cudaEvent_t done = nullptr;
     CK(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
     CK(cudaEventRecord(done, st));
     for (int i = 0; i < n; i++) {
         ss[i]->launched += counts[i];
         ss[i]->launches++;
-        ss[i]->timed = (i == 0);  // the batch is timed on the first session's events
+        ss[i]->timed = ordered && (i == 0);  // the batch is timed on the first session's events
         if (ss[i]->stream != st) CK(cudaStreamWaitEvent(ss[i]->stream, done, 0));
     }
     for (cudaEvent_t e : evs) cudaEventDestroy(e);
-    cudaEventDestroy(done);
+    if (done) cudaEventDestroy(done);
+    return MMCGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t mmcgb_session_launch_batch(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets,
+                                   const uint64_t* counts) {
+    return batch_launch(n, ss, offsets, counts, nullptr, true);
+}
+
+int32_t mmcgb_session_launch_batch_on(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets,
+                                      const uint64_t* counts, void* stream) {
+    if (!stream) return fail(MMCGB_E_ARG, "null stream");
+    return batch_launch(n, ss, offsets, counts, (cudaStream_t)stream, false);
+}
+
+int32_t mmcgb_session_launch_repeat(mmcgb_session* s, uint64_t photon_offset, uint64_t nphoton, int32_t repeats) {
+    if (!s) return fail(MMCGB_E_ARG, "null session");
+    if (repeats < 1 || nphoton == 0) return fail(MMCGB_E_ARG, "repeats and nphoton must be positive");
+    if (s->cfg.replayseed) return fail(MMCGB_E_ARG, "replay sessions run all replayed photons in one launch");
+    if ((s->P.buf.pw || s->P.buf.ps || s->P.buf.pd) && nphoton * (uint64_t)repeats > s->cfg.nphoton)
+        return fail(MMCGB_E_ARG, "per-photon trace buffers hold cfg.nphoton photons");
+    CK(cudaSetDevice(s->mesh->device));
+    CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < repeats && e == cudaSuccess; k++) {
+        SimDev sim = s->P.sim;
+        sim.nphoton = nphoton;
+        sim.photon_offset = s->cfg.photon_offset + photon_offset + (uint64_t)k * nphoton;
+        e = launch_plain(sim, s->work, s->shape, s->stream);
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(s->stream, &g);
+    if (e == cudaSuccess) e = ec;
+    if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(e, "respin graph capture");
+    }
+    if (s->gexec && (s->g_nphoton != nphoton || s->g_repeats != repeats)) {
+        cudaGraphExecDestroy(s->gexec);
+        s->gexec = nullptr;
+    }
+    if (s->gexec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(s->gexec, g, &info) != cudaSuccess) {
+            (void)cudaGetLastError();
+            cudaGraphExecDestroy(s->gexec);
+            s->gexec = nullptr;
+        }
+    }
+    if (!s->gexec) {
+        e = cudaGraphInstantiate(&s->gexec, g, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            s->gexec = nullptr;
+            return cuda_fail(e, "respin graph instantiation");
+        }
+        s->g_nphoton = nphoton;
+        s->g_repeats = repeats;
+    }
+    cudaGraphDestroy(g);
+    CK(cudaEventRecord(s->ev0, s->stream));
+    CK(cudaGraphLaunch(s->gexec, s->stream));
+    CK(cudaEventRecord(s->ev1, s->stream));
+    s->launched += nphoton * (uint64_t)repeats;
+    s->launches += repeats;
+    s->timed = true;
     return MMCGB_OK;
 }
 
@@ -564,8 +657,10 @@ int32_t mmcgb_session_end(mmcgb_session* s, mmcgb_result* res) {
     }
     if (s->work) cudaFreeAsync(s->work, s->stream);
     cudaStreamSynchronize(s->stream);
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
     cudaEventDestroy(s->ev0);
     cudaEventDestroy(s->ev1);
+    if (s->ready) cudaEventDestroy(s->ready);
     cudaStreamDestroy(s->stream);
     delete s;
     return rc;

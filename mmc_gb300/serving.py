@@ -2,14 +2,18 @@
 
 Requests (a resident mesh, optical properties, source, detectors, photon
 count) arrive at any time.  The server runs the GPU in waves: every wave is
-one persistent launch (mmcgb_session_launch_batch) in which each admitted
-request advances by its share of a per-wave photon budget.  Between waves it
-admits waiting requests while the free device memory, less a reserve, covers
-their fluence and detector buffers, and finishes the requests whose photons
-are all traced (readback + normalization).  A request that arrives while
-others are on the GPU therefore joins at the next wave boundary and shares
-the device with them; the engine's per-photon random streams make each
-result identical to running the request alone (tests/test_gpu_serving.py).
+one persistent launch over all admitted requests, in which each request
+advances by its share of a per-wave photon budget.  Waves are pipelined: up
+to `depth` of them are in flight on separate CUDA streams
+(mmcgb_session_launch_batch_on), so the next wave's blocks take over the SMs
+while the current wave's last photons drain, and the host plans the next wave
+while the device works.  When a wave completes the server admits waiting
+requests while the free device memory, less a reserve, covers their fluence
+and detector buffers, and hands requests whose photons are all traced to a
+background thread (output stage + readback).  A request that arrives while
+others are on the GPU therefore joins within a wave or two and shares the
+device with them; the engine's per-photon random streams make each result
+identical to running the request alone (tests/test_gpu_serving.py).
 
 The meshes stay resident (one upload each); nothing about a request is
 uploaded except its small parameter block and tables.
@@ -55,21 +59,27 @@ def device_bytes(mesh: Mesh, cfg: SimConfig) -> int:
 
 class Server:
     def __init__(self, meshes: Dict[str, Mesh], wave_photons: int = 4_000_000, min_share: int = 50_000,
-                 max_active: int = 128, memory_budget: Optional[int] = None, reserve: int = 2 << 30):
+                 max_active: int = 128, memory_budget: Optional[int] = None, reserve: int = 2 << 30,
+                 depth: int = 2):
         import torch
         self.meshes = meshes
         self.wave_photons = int(wave_photons)
         self.min_share = int(min_share)
         self.max_active = int(max_active)
+        self.depth = max(1, int(depth))
         dev = next(iter(meshes.values())).device
         free, _ = torch.cuda.mem_get_info(dev)
         self.budget = int(memory_budget) if memory_budget else max(0, free - reserve)
         self.in_use = 0
         self.pending: deque = deque()
-        self.active: List[tuple] = []  # (request, session, done)
+        # active entries: [request, session, photons assigned to waves, device bytes, waves in flight]
+        self.active: List[list] = []
         self.completed: List[Request] = []
         self.waves = 0
         self.wave_ms: List[float] = []
+        self._streams = [torch.cuda.Stream(device=dev) for _ in range(self.depth)]
+        self._inflight: deque = deque()  # (event, [(entry, count)], launch time)
+        self._last_done: Optional[float] = None
         self._lock = threading.Lock()
         self._next_id = 0
         # readback + normalization of finished requests overlaps the next wave
@@ -95,38 +105,57 @@ class Server:
                 break  # wait for memory to free up (FIFO: no overtaking)
             self.pending.popleft()
             try:
-                sess = Session(mesh, dataclasses.replace(req.cfg, basisorder=req.cfg.basisorder))
+                sess = Session(mesh, req.cfg)
             except Exception as e:  # reported per request; the server keeps going
                 req.error, req.finished = str(e), time.perf_counter()
                 self.completed.append(req)
                 continue
             req.admitted = time.perf_counter()
             self.in_use += need
-            self.active.append([req, sess, 0, need])
+            self.active.append([req, sess, 0, need, 0])
 
-    def step(self) -> bool:
-        """Admits, runs one wave, finishes completed requests.  Returns False
-        when there is nothing to do."""
-        with self._lock:
-            self._admit()
-        if not self.active:
+    def _launch_wave(self) -> bool:
+        import torch
+        live = [a for a in self.active if a[2] < a[0].cfg.nphoton]
+        if not live:
             return False
-        live = self.active
         share = max(self.min_share, self.wave_photons // len(live))
         counts = [min(share, a[0].cfg.nphoton - a[2]) for a in live]
-        t0 = time.perf_counter()
-        launch_batch([a[1] for a in live], [a[2] for a in live], counts)
-        live[0][1].sync()
-        self.wave_ms.append((time.perf_counter() - t0) * 1e3)
-        self.waves += 1
-        still = []
+        st = self._streams[self.waves % self.depth]
+        launch_batch([a[1] for a in live], [a[2] for a in live], counts, stream=st.cuda_stream)
+        ev = torch.cuda.Event()
+        ev.record(st)
         for a, k in zip(live, counts):
             a[2] += k
-            if a[2] >= a[0].cfg.nphoton:
+            a[4] += 1
+        self._inflight.append((ev, list(zip(live, counts)), time.perf_counter()))
+        self.waves += 1
+        return True
+
+    def _complete_wave(self):
+        ev, members, t_launch = self._inflight.popleft()
+        ev.synchronize()
+        now = time.perf_counter()
+        # device time per wave, seen from the host: the gap between consecutive completions
+        self.wave_ms.append((now - max(t_launch, self._last_done or t_launch)) * 1e3)
+        self._last_done = now
+        for a, _ in members:
+            a[4] -= 1
+            if a[2] >= a[0].cfg.nphoton and a[4] == 0:
+                self.active = [x for x in self.active if x is not a]
                 self._finishing.append(self._finisher.submit(self._finish, a))
-            else:
-                still.append(a)
-        self.active = still
+
+    def step(self) -> bool:
+        """Admits, keeps up to `depth` waves in flight, completes the oldest
+        one and finishes requests whose photons are all traced.  Returns
+        False when there is nothing to do."""
+        with self._lock:
+            self._admit()
+        while len(self._inflight) < self.depth and self._launch_wave():
+            pass
+        if not self._inflight:
+            return False
+        self._complete_wave()
         self._reap(block=False)
         return True
 
@@ -156,6 +185,14 @@ class Server:
         `arrivals`: requests with `arrival` times in the future (perf_counter
         clock) that are submitted when their time comes."""
         sched = sorted(arrivals or [], key=lambda r: r.arrival)
+        try:
+            self._serve(sched, deadline)
+        finally:
+            for st in self._streams:  # no wave outlives the loop, whatever ended it
+                st.synchronize()
+        return self.completed
+
+    def _serve(self, sched, deadline):
         i = 0
         while True:
             now = time.perf_counter()

@@ -66,3 +66,40 @@ def test_session_waves_equal_individual_runs(gpu_ready):
     for a, b in zip(alone, res):
         np.testing.assert_allclose(b.field, a.field, rtol=1e-9, atol=1e-12)
         assert a.raytet == b.raytet and _rows(a) == _rows(b)
+
+
+def test_overlapping_waves_on_two_streams(gpu_ready):
+    """Waves enqueued on two caller streams with no ordering between them
+    (mmcgb_session_launch_batch_on) run concurrently into the same sessions;
+    once both streams are synchronized every session equals its solo run."""
+    import torch
+    meshes, cfgs = _cases()
+    alone = [simulate(m, c) for m, c in zip(meshes, cfgs)]
+    sess = [Session(m, c) for m, c in zip(meshes, cfgs)]
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    half = [c.nphoton // 2 for c in cfgs]
+    launch_batch(sess, [0] * len(cfgs), half, stream=streams[0].cuda_stream)
+    launch_batch(sess, half, [c.nphoton - h for c, h in zip(cfgs, half)], stream=streams[1].cuda_stream)
+    for st in streams:
+        st.synchronize()
+    res = [s.end() for s in sess]
+    for a, b in zip(alone, res):
+        np.testing.assert_allclose(b.field, a.field, rtol=1e-9, atol=1e-12)
+        assert a.raytet == b.raytet and _rows(a) == _rows(b)
+
+
+def test_respin_graph_equals_one_launch(gpu_ready):
+    """The respin loop as a CUDA graph (mmcgb_session_launch_repeat), also
+    after an in-place update of the graph for a new photon range, equals one
+    launch of all the photons."""
+    meshes, cfgs = _cases()
+    m, c = meshes[2], cfgs[2]
+    n = c.nphoton // 4
+    alone = simulate(m, dataclasses.replace(c, nphoton=4 * n))
+    s = Session(m, dataclasses.replace(c, nphoton=4 * n))
+    s.launch_repeat(0, n, 2)
+    assert s.sync() > 0
+    s.launch_repeat(2 * n, n, 2)  # same shape: the instantiated graph is updated in place
+    r = s.end()
+    np.testing.assert_allclose(r.field, alone.field, rtol=1e-9, atol=1e-12)
+    assert r.raytet == alone.raytet and _rows(r) == _rows(alone)
