@@ -4,9 +4,10 @@ heterogeneous cube (60^3 voxels at 1 mm, 6 tets/voxel, orientation-safe
 of 0.1 ns; 4 detectors R=2 mm saving per-medium partial paths and scatter
 counts; 1e8 photons per job).
 
-A step is the whole 1e8-photon job, one persistent launch with the mesh and
-all buffers resident on the GPU (each step traces a new photon range of the
-same seed).  L2 is flushed (256 MB write) before every timed step.
+A step is the whole 1e8-photon job with the mesh and all buffers resident on
+the GPU (each step traces a new photon range of the same seed), traced
+gate-phased: one persistent launch per window of time gates, photons parked
+between windows.  L2 is flushed (256 MB write) before every timed step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -298,6 +299,7 @@ def main():
             "config": {"workload": WORKLOAD, "ne": mesh.ne, "nn": mesh.nn, "photons_per_step": nps,
                        "job_photons": JOB_PHOTONS, "gates": 50, "detectors": 4, "savedet": True,
                        "l2": "flushed (256 MB write) before each timed step",
+                       "tracing": "gate-phased (automatic window: the live gate planes fill ~60% of L2)",
                        "steps_per_photon": steps_per_photon, "detected": res.detected,
                        "absorbed_fraction": res.absorbed_fraction, "wall_s": wall},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

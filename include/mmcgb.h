@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define MMCGB_ABI_VERSION 1
+#define MMCGB_ABI_VERSION 2
 
 typedef enum mmcgb_status {
     MMCGB_OK = 0,
@@ -104,6 +104,13 @@ typedef struct mmcgb_config {
     int32_t fast_math;       /* 1: hardware-approximate division/exp/log/sincos and fused
                                 multiply-adds (as the reference's -use_fast_math build);
                                 0: IEEE arithmetic, photon-for-photon reproducible on the CPU */
+    int32_t phased;          /* gate-phased tracing of a launch (one launch per window of k time
+                                gates, photons parked between windows, so only k+1 gate planes of
+                                the fluence take deposits at a time; same results photon for
+                                photon): 0 = auto (when >= 8 gates, fluence >= 64 MB, >= 4e6
+                                photons per launch and queue memory available; k sized so the
+                                k+1 live planes fill ~60% of the L2), k >= 1 = window of k gates
+                                whenever possible (not for replay), -1 = never */
 } mmcgb_config;
 
 /* Outputs.  Pointers may be NULL to skip an output; counts are always set. */

@@ -53,7 +53,7 @@ class Config(C.Structure):
         ("detnum", C.c_int32), ("detpos", C.c_void_p),
         ("replayseed", C.c_void_p), ("replayweight", C.c_void_p), ("replaytime", C.c_void_p),
         ("accum_f64", C.c_int32), ("step_budget", C.c_uint64),
-        ("threads", C.c_int32), ("blocks", C.c_int32), ("fast_math", C.c_int32),
+        ("threads", C.c_int32), ("blocks", C.c_int32), ("fast_math", C.c_int32), ("phased", C.c_int32),
     ]
 
 
@@ -121,7 +121,7 @@ def load():
                      "mmcgb_mesh_create", "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export",
                      "mmcgb_mesh_locate", "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run"):
             getattr(lib, name).restype = C.c_int32
-        if lib.mmcgb_abi_version() != 1:
+        if lib.mmcgb_abi_version() != 2:
             raise NativeLibraryError("libmmcgb ABI version mismatch")
         _lib = lib
         return lib

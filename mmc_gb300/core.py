@@ -165,6 +165,7 @@ class SimConfig:
     threads: int = 0
     blocks: int = 0
     fast_math: int = 1
+    phased: int = 0
     save_field: bool = True
 
     @property
@@ -210,6 +211,7 @@ class SimConfig:
         c.step_budget = int(self.step_budget)
         c.threads, c.blocks = int(self.threads), int(self.blocks)
         c.fast_math = int(self.fast_math)
+        c.phased = int(self.phased)
         return c, keep
 
 

@@ -316,6 +316,10 @@ struct mmcgb_session {
     cudaGraphExec_t gexec = nullptr;  // respin graph (mmcgb_session_launch_repeat) and its shape
     uint64_t g_nphoton = 0;
     int g_repeats = 0;
+    PhaseQueue pq[2] = {};            // gate-phased tracing queues, capacity pq_cap photons each
+    void* pq_mem = nullptr;
+    uint64_t pq_cap = 0;
+    int pq_span = 0;                  // gates per phased launch
 };
 
 namespace {
@@ -458,6 +462,77 @@ int32_t mmcgb_session_begin(mmcgb_mesh* mesh, const mmcgb_config* cfg, mmcgb_res
     return MMCGB_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Whether a launch of `nphoton` photons of this session runs gate-phased
+// (mmcgb_config.phased); sets up the queues and the window when it does.
+// Automatic windows keep the live gate planes (window + 1 of them) within
+// about 60% of the L2: measured on the 1.296M-tet, 50-gate benchmark
+// (10.4 MB planes), windows of 5-10 gates trace 1e8 photons at 74.7k-75.3k
+// photons/ms against 59.4k in one launch; 17 gates drop to 71.5k, 1 gate
+// (parking every photon at every gate) to 59.9k.  Returns a status.
+int phased_setup(mmcgb_session* s, uint64_t nphoton, bool* use) {
+    *use = false;
+    const mmcgb_config& c = s->cfg;
+    if (c.phased < 0 || c.replayseed || s->P.maxgate < 2) return MMCGB_OK;
+    const size_t per = phase_bytes_per_photon(s->P.sim);
+    const size_t need = per * nphoton + 4096;
+    const size_t plane = (size_t)s->mesh->host.ne * (c.accum_f64 ? 8 : 4);
+    if (c.phased > 0) {
+        s->pq_span = c.phased;
+    } else {
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, s->mesh->device);
+        s->pq_span = std::max(1, (int)(0.6 * (double)l2 / (double)plane) - 1);
+    }
+    if (c.phased == 0) {
+        const size_t fluence = (size_t)s->mesh->host.ne * s->P.maxgate * 8;
+        if (s->P.maxgate < 8 || fluence < ((size_t)64 << 20) || nphoton < 4000000ull ||
+            s->pq_span >= s->P.maxgate)
+            return MMCGB_OK;
+        if (nphoton > s->pq_cap) {
+            size_t free_b = 0, total_b = 0;
+            if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || need > free_b / 2) {
+                (void)cudaGetLastError();
+                return MMCGB_OK;  // not enough room for the queues: trace in one launch
+            }
+        }
+    }
+    if (nphoton > s->pq_cap) {
+        if (s->pq_mem) CK(cudaFreeAsync(s->pq_mem, s->stream));
+        s->pq_mem = nullptr;
+        s->pq_cap = 0;
+        cudaError_t e = cudaMallocAsync(&s->pq_mem, need, s->stream);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            return fail(MMCGB_E_NOMEM, "no device memory for the gate-phased queues");
+        }
+        s->pq_cap = nphoton;
+        const SimDev& sim = s->P.sim;
+        const bool want_seed = sim.issavedet && sim.seeds;
+        char* p = static_cast<char*>(s->pq_mem);
+        auto take = [&](size_t bytes) {
+            char* r = p;
+            p += (bytes + 255) & ~(size_t)255;
+            return r;
+        };
+        for (int i = 0; i < 2; i++) {
+            s->pq[i].rec = reinterpret_cast<PState*>(take(sizeof(PState) * nphoton));
+            s->pq[i].ppath = sim.issavedet ? reinterpret_cast<float*>(take(sizeof(float) * sim.reclen * nphoton)) : nullptr;
+            s->pq[i].seed0 = want_seed ? reinterpret_cast<unsigned long long*>(take(16 * nphoton)) : nullptr;
+            s->pq[i].count = reinterpret_cast<unsigned long long*>(take(sizeof(unsigned long long)));
+        }
+    }
+    *use = true;
+    return MMCGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int32_t mmcgb_session_launch(mmcgb_session* s, uint64_t photon_offset, uint64_t nphoton) {
     if (!s) return fail(MMCGB_E_ARG, "null session");
     if (s->cfg.replayseed && (photon_offset != 0 || nphoton != s->cfg.nphoton))
@@ -468,8 +543,14 @@ int32_t mmcgb_session_launch(mmcgb_session* s, uint64_t photon_offset, uint64_t 
     SimDev sim = s->P.sim;
     sim.nphoton = nphoton;
     sim.photon_offset = s->cfg.photon_offset + photon_offset;
+    bool phased = false;
+    const int rc = phased_setup(s, nphoton, &phased);
+    if (rc) return rc;
     CK(cudaEventRecord(s->ev0, s->stream));
-    CK(launch_plain(sim, s->work, s->shape, s->stream));
+    if (phased)
+        CK(launch_phased(sim, s->work, s->shape, s->stream, s->pq, s->pq_span));
+    else
+        CK(launch_plain(sim, s->work, s->shape, s->stream));
     CK(cudaEventRecord(s->ev1, s->stream));
     s->launched += nphoton;
     s->launches++;
@@ -541,7 +622,10 @@ int batch_launch(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets, c
     if (s0->cfg.threads > 0) shape.threads = std::max(32, std::min(s0->cfg.threads, 128) / 32 * 32);
     if (s0->cfg.blocks > 0) shape.blocks = s0->cfg.blocks;
     if (ordered) CK(cudaEventRecord(s0->ev0, st));
-    CK(launch_batched(dsims, dcum, n, total, nmed_stride, reclen_max, want_seed, work, shape, st, fast));
+    if (n == 1)  // a single simulation takes the plain kernel (its parameter block in constant memory)
+        CK(launch_plain(sims[0], work, s0->shape, st));
+    else
+        CK(launch_batched(dsims, dcum, n, total, nmed_stride, reclen_max, want_seed, work, shape, st, fast));
     if (ordered) CK(cudaEventRecord(s0->ev1, st));
     CK(cudaFreeAsync(dsims, st));
     CK(cudaFreeAsync(dcum, st));
@@ -656,6 +740,7 @@ int32_t mmcgb_session_end(mmcgb_session* s, mmcgb_result* res) {
         s->P.buf.release();
     }
     if (s->work) cudaFreeAsync(s->work, s->stream);
+    if (s->pq_mem) cudaFreeAsync(s->pq_mem, s->stream);
     cudaStreamSynchronize(s->stream);
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
     cudaEventDestroy(s->ev0);

@@ -12,6 +12,7 @@
 // Compile with -fmad=false: the float sequence is the contract shared with the
 // CPU oracle, and explicit fmaf() appears only in devmath.cuh.
 #include <cooperative_groups.h>
+#include <algorithm>
 #include <cstdio>
 #include "devmath.cuh"
 #include "engine.h"
@@ -345,10 +346,10 @@ struct ManySims {
 
 // Shared-memory layout: media[nsims_local * nmed_stride] | ppath[reclen_max][blockDim] |
 // seed0[2][blockDim] (u64)
-template <class MP, class Sims, bool BATCHED>
+template <class MP, class Sims, bool BATCHED, bool PHASED>
 __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned long long* cum, int nsims,
                                             unsigned long long total, int nmed_stride, int reclen_max,
-                                            int want_seed, unsigned long long* work_counter) {
+                                            int want_seed, unsigned long long* work_counter, const PhaseArgs& pa) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float4* smed = reinterpret_cast<float4*>(smem_raw);
     const int nmed_rows = nsims * nmed_stride;
@@ -403,6 +404,50 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                     }
                     L.sim = s;
                     L.pid = BATCHED ? (gid - (s ? cum[s - 1] : 0ull)) : gid;
+                    if (PHASED && pa.phase > 0) {
+                        // ---- resume a photon parked at the end of the previous gate ----
+                        // queue traffic is read once: streaming loads keep it from displacing
+                        // the tet records and the live gate planes in L2
+                        const PState* q = pa.in.rec + gid;
+                        PState r;
+                        r.pos = __ldcs(&q->pos);
+                        r.dir = __ldcs(&q->dir);
+                        r.len = __ldcs(&q->len);
+                        r.elem = __ldcs(&q->elem);
+                        r.meta = __ldcs(&q->meta);
+                        r.rng = __ldcs(&q->rng);
+                        L.px = r.pos.x;
+                        L.py = r.pos.y;
+                        L.pz = r.pos.z;
+                        L.ptime = r.pos.w;
+                        L.vx = r.dir.x;
+                        L.vy = r.dir.y;
+                        L.vz = r.dir.z;
+                        L.weight = r.dir.w;
+                        L.slen = r.len.x;
+                        L.slen0 = r.len.y;
+                        L.oldw = r.len.z;
+                        L.oldidx = __float_as_uint(r.len.w);
+                        L.eid = r.elem.x;
+                        L.label = r.elem.y;
+                        L.mode = r.elem.z;
+                        L.fixcount = r.elem.w;
+                        L.steps = r.meta.x;
+                        L.pid = ((unsigned long long)r.meta.z << 32) | r.meta.y;
+                        L.t0 = ((unsigned long long)r.rng.y << 32) | r.rng.x;
+                        L.t1 = ((unsigned long long)r.rng.w << 32) | r.rng.z;
+                        L.Lmove = 0.f;
+                        L.faceid = 0;
+                        L.isend = 0;
+                        L.hit = 0;
+                        L.wait = 0;
+                        if (S.issavedet)
+                            for (int i = 0; i < S.reclen; i++) PP(i) = __ldcs(pa.in.ppath + gid * S.reclen + i);
+                        if (want_seed) {
+                            seed0[tid] = __ldcs(pa.in.seed0 + 2 * gid);
+                            seed0[bdim + tid] = __ldcs(pa.in.seed0 + 2 * gid + 1);
+                        }
+                    } else {
                     // ---- launch (src/mmc_core.cl:1851-1906, pencil source) ----
                     if (S.replay) {
                         L.t0 = __ldg(S.replayseed + 2 * L.pid);
@@ -439,10 +484,44 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                         PP(S.reclen - 1) = L.weight;
                     }
                     L.mode = M_OUTER;
+                    }
                 }
             }
         }
         if (__all_sync(kFull, L.mode == M_DONE)) break;
+
+        // ---- (1a) gate-phased runs: park photons whose time reached the next gate ----
+        if (PHASED && !pa.last) {
+            const SimDev& S = sims(0);
+            const bool live = (L.mode == M_OUTER || L.mode == M_INNER || L.mode == M_FIXIN || L.mode == M_SCAT);
+            if (live && (L.ptime - S.tstart) * S.Rtstep >= (float)(pa.phase + pa.span)) {
+                cg::coalesced_group grp = cg::coalesced_threads();
+                unsigned long long base = 0;
+                if (grp.thread_rank() == 0) base = atomicAdd(pa.out.count, (unsigned long long)grp.size());
+                base = grp.shfl(base, 0);
+                const unsigned long long slot = base + grp.thread_rank();
+                // each photon is parked at most once per gate, so slot < cap; checked all the same
+                if (slot < pa.cap) {
+                    PState* q = pa.out.rec + slot;  // streaming stores: written once, read once
+                    __stcs(&q->pos, make_float4(L.px, L.py, L.pz, L.ptime));
+                    __stcs(&q->dir, make_float4(L.vx, L.vy, L.vz, L.weight));
+                    __stcs(&q->len, make_float4(L.slen, L.slen0, L.oldw, __uint_as_float(L.oldidx)));
+                    __stcs(&q->elem, make_int4(L.eid, L.label, L.mode, L.fixcount));
+                    __stcs(&q->meta, make_uint4(L.steps, (unsigned)L.pid, (unsigned)(L.pid >> 32), 0u));
+                    __stcs(&q->rng, make_uint4((unsigned)L.t0, (unsigned)(L.t0 >> 32), (unsigned)L.t1,
+                                               (unsigned)(L.t1 >> 32)));
+                    if (S.issavedet)
+                        for (int i = 0; i < S.reclen; i++) __stcs(pa.out.ppath + slot * S.reclen + i, PP(i));
+                    if (want_seed) {
+                        __stcs(pa.out.seed0 + 2 * slot, seed0[tid]);
+                        __stcs(pa.out.seed0 + 2 * slot + 1, seed0[bdim + tid]);
+                    }
+                } else {
+                    tally.aborted++;
+                }
+                L.mode = M_NEED;
+            }
+        }
 
         // ---- (1b) deferred roulette + scatter, src/mmc_core.cl:2101-2134 ----
         const unsigned parked = __ballot_sync(kFull, L.mode == M_SCAT);
@@ -650,7 +729,22 @@ __global__ void __launch_bounds__(128, 8) photon_engine_plain(const __grid_const
                                                               unsigned long long* work_counter, int reclen_max,
                                                               int want_seed) {
     SingleSim acc{sim};
-    engine_body<MP, SingleSim, false>(acc, nullptr, 1, sim.nphoton, sim.nmedia, reclen_max, want_seed, work_counter);
+    const PhaseArgs none{};
+    engine_body<MP, SingleSim, false, false>(acc, nullptr, 1, sim.nphoton, sim.nmedia, reclen_max, want_seed,
+                                             work_counter, none);
+}
+
+template <class MP>
+__global__ void __launch_bounds__(128, 8) photon_engine_phased(const __grid_constant__ SimDev sim,
+                                                               const __grid_constant__ PhaseArgs pa,
+                                                               unsigned long long* work_counter, int reclen_max,
+                                                               int want_seed) {
+    SingleSim acc{sim};
+    // gate 0 launches the run's photons; later gates resume the ones parked by the previous launch
+    unsigned long long total = sim.nphoton;
+    if (pa.phase > 0) total = min(*pa.in.count, pa.cap);
+    engine_body<MP, SingleSim, false, true>(acc, nullptr, 1, total, sim.nmedia, reclen_max, want_seed,
+                                            work_counter, pa);
 }
 
 template <class MP>
@@ -660,7 +754,9 @@ __global__ void __launch_bounds__(128, 8) photon_engine_batched(const SimDev* __
                                                                 int nmed_stride, unsigned long long* work_counter,
                                                                 int reclen_max, int want_seed) {
     ManySims acc{sims};
-    engine_body<MP, ManySims, true>(acc, cum, nsims, total, nmed_stride, reclen_max, want_seed, work_counter);
+    const PhaseArgs none{};
+    engine_body<MP, ManySims, true, false>(acc, cum, nsims, total, nmed_stride, reclen_max, want_seed, work_counter,
+                                           none);
 }
 
 size_t smem_bytes(int nmed_rows, int reclen_max, int threads, int want_seed) {
@@ -706,6 +802,48 @@ cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, La
                          cudaStream_t stream) {
     return sim.fast_math ? launch_plain_t<FastMath>(sim, work_counter, shape, stream)
                          : launch_plain_t<ExactMath>(sim, work_counter, shape, stream);
+}
+
+size_t phase_bytes_per_photon(const SimDev& sim) {
+    const int want_seed = (sim.issavedet && sim.seeds) ? 1 : 0;
+    return 2 * (sizeof(PState) + (sim.issavedet ? (size_t)sim.reclen * sizeof(float) : 0) +
+                (want_seed ? 2 * sizeof(unsigned long long) : 0));
+}
+
+template <class MP>
+static cudaError_t launch_phased_t(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
+                                   cudaStream_t stream, const PhaseQueue q[2], int span) {
+    const int want_seed = (sim.issavedet && sim.seeds) ? 1 : 0;
+    const int reclen_max = sim.issavedet ? sim.reclen : 0;
+    const size_t smem = smem_bytes(sim.nmedia, reclen_max, shape.threads, want_seed);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(photon_engine_phased<MP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    span = std::max(1, span);
+    for (int g = 0, k = 0; g < sim.maxgate; g += span, k++) {
+        PhaseArgs pa;
+        pa.phase = g;
+        pa.span = span;
+        pa.last = (g + span >= sim.maxgate) ? 1 : 0;
+        pa.in = q[(k + 1) & 1];  // written by the previous launch
+        pa.out = q[k & 1];
+        pa.cap = sim.nphoton;
+        cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(unsigned long long), stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(pa.out.count, 0, sizeof(unsigned long long), stream);
+        if (e != cudaSuccess) return e;
+        (void)cudaGetLastError();
+        photon_engine_phased<MP><<<shape.blocks, shape.threads, smem, stream>>>(sim, pa, work_counter, reclen_max,
+                                                                               want_seed);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
+                          cudaStream_t stream, const PhaseQueue q[2], int span) {
+    return sim.fast_math ? launch_phased_t<FastMath>(sim, work_counter, shape, stream, q, span)
+                         : launch_phased_t<ExactMath>(sim, work_counter, shape, stream, q, span);
 }
 
 template <class MP>

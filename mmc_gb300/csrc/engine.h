@@ -95,6 +95,46 @@ struct LaunchShape {
     int threads;
 };
 
+// Gate-phased tracing.  Launch g of a phased run traces every live photon
+// while its time lies in gate g; a photon whose time reaches gate g+1 is parked
+// as a PState record (plus its partial-path columns and saved seed) in the
+// queue that launch g+1 resumes from.  Only one or two gate planes of the
+// fluence then receive deposits at a time.  A parked photon keeps exactly
+// the state the step loop carries from one trip to the next, so its sequence
+// of operations (and random numbers) is the same as in one unbroken launch.
+struct __align__(16) PState {
+    float4 pos;   // px py pz ptime
+    float4 dir;   // vx vy vz weight
+    float4 len;   // slen slen0 oldw, oldidx bits
+    int4 elem;    // eid label mode fixcount
+    uint4 meta;   // steps, pid (low, high), unused
+    uint4 rng;    // xorshift128+ state t0 (low, high), t1 (low, high)
+};
+static_assert(sizeof(PState) == 96, "PState must be 96 bytes");
+
+struct PhaseQueue {
+    PState* rec;                // capacity records
+    float* ppath;               // reclen floats per record (saved detections only)
+    unsigned long long* seed0;  // 2 words per record (saved seeds only)
+    unsigned long long* count;  // records written
+};
+
+struct PhaseArgs {
+    int phase;   // first gate g traced by this launch
+    int span;    // gates per launch: photons are parked when their time reaches gate g + span
+    int last;    // 1: the last launch, photons run to their end
+    PhaseQueue in, out;
+    unsigned long long cap;
+};
+
+// Bytes of queue storage per photon of a phased launch (both queues).
+size_t phase_bytes_per_photon(const SimDev& sim);
+// Enqueues a phased run of `sim` on `stream`: one launch per `span` gates,
+// queues q[0], q[1] (capacity sim.nphoton each) used alternately.  No host
+// synchronization between the launches.
+cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
+                          cudaStream_t stream, const PhaseQueue q[2], int span);
+
 // Launches the photon engine for one simulation on `stream`.
 cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
                          cudaStream_t stream);

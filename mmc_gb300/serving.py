@@ -2,8 +2,8 @@
 
 Requests (a resident mesh, optical properties, source, detectors, photon
 count) arrive at any time.  The server runs the GPU in waves: every wave is
-one persistent launch over all admitted requests, in which each request
-advances by its share of a per-wave photon budget.  Waves are pipelined: up
+one persistent launch over admitted requests, composed shortest remaining
+work first within a per-wave photon budget.  Waves are pipelined: up
 to `depth` of them are in flight on separate CUDA streams
 (mmcgb_session_launch_batch_on), so the next wave's blocks take over the SMs
 while the current wave's last photons drain, and the host plans the next wave
@@ -60,13 +60,14 @@ def device_bytes(mesh: Mesh, cfg: SimConfig) -> int:
 class Server:
     def __init__(self, meshes: Dict[str, Mesh], wave_photons: int = 4_000_000, min_share: int = 50_000,
                  max_active: int = 128, memory_budget: Optional[int] = None, reserve: int = 2 << 30,
-                 depth: int = 2):
+                 depth: int = 2, max_wave_requests: int = 16):
         import torch
         self.meshes = meshes
         self.wave_photons = int(wave_photons)
         self.min_share = int(min_share)
         self.max_active = int(max_active)
         self.depth = max(1, int(depth))
+        self.max_wave_requests = max(1, int(max_wave_requests))
         dev = next(iter(meshes.values())).device
         free, _ = torch.cuda.mem_get_info(dev)
         self.budget = int(memory_budget) if memory_budget else max(0, free - reserve)
@@ -115,12 +116,26 @@ class Server:
             self.active.append([req, sess, 0, need, 0])
 
     def _launch_wave(self) -> bool:
+        """Composes the next wave shortest-remaining-first: requests in order
+        of untraced photons take their remainder (at least `min_share`) until
+        the wave's photon budget or `max_wave_requests` is reached.  Small
+        requests thus finish in one wave, and a wave mixes few requests, so
+        their fluence buffers and meshes compete less for the L2."""
         import torch
         live = [a for a in self.active if a[2] < a[0].cfg.nphoton]
         if not live:
             return False
-        share = max(self.min_share, self.wave_photons // len(live))
-        counts = [min(share, a[0].cfg.nphoton - a[2]) for a in live]
+        live.sort(key=lambda a: (a[0].cfg.nphoton - a[2], a[0].rid))
+        budget = self.wave_photons
+        picked, counts = [], []
+        for a in live:
+            if len(picked) >= self.max_wave_requests or budget <= 0:
+                break
+            k = min(a[0].cfg.nphoton - a[2], max(budget, self.min_share))
+            picked.append(a)
+            counts.append(k)
+            budget -= k
+        live = picked
         st = self._streams[self.waves % self.depth]
         launch_batch([a[1] for a in live], [a[2] for a in live], counts, stream=st.cuda_stream)
         ev = torch.cuda.Event()

@@ -33,9 +33,11 @@ def _compare_photons(gpu, ora):
                              f"{gpu.photon_steps[bad[:5]]} oracle {ora['photon_steps'][bad[:5]]}")
 
 
-def test_per_photon_bitexact_homogeneous(gpu_ready, oracle_mod, small_cube):
+@pytest.mark.parametrize("phased", [-1, 1, 3])
+def test_per_photon_bitexact_homogeneous(gpu_ready, oracle_mod, small_cube, phased):
+    """phased=1 traces gate by gate (10 gates), parking photons between launches."""
     m = small_cube
-    cfg = _cfg(m, nphoton=5000)
+    cfg = _cfg(m, nphoton=5000, phased=phased, tstep=5e-9 if phased < 0 else 0.5e-9)
     mesh = Mesh(m.node, m.elem, m.label)
     g = simulate(mesh, cfg, trace=True)
     o = oracle_mod.run(m.node, m.elem, m.label, cfg, nthreads=4, trace=True)
@@ -45,20 +47,22 @@ def test_per_photon_bitexact_homogeneous(gpu_ready, oracle_mod, small_cube):
     assert abs(g.energyesc - o["energyesc"]) <= 1e-9 * o["energyesc"]
 
 
-def test_fluence_matches_oracle(gpu_ready, oracle_mod, small_cube):
+@pytest.mark.parametrize("phased", [-1, 1, 3])
+def test_fluence_matches_oracle(gpu_ready, oracle_mod, small_cube, phased):
     m = small_cube
-    cfg = _cfg(m, nphoton=20000, isnormalized=0)
+    cfg = _cfg(m, nphoton=20000, isnormalized=0, phased=phased, tstep=0.5e-9)
     mesh = Mesh(m.node, m.elem, m.label)
     g = simulate(mesh, cfg)
     o = oracle_mod.run(m.node, m.elem, m.label, cfg, nthreads=4)
     np.testing.assert_allclose(g.field, o["raw"], rtol=1e-9, atol=1e-12)
 
 
-def test_detected_records_bitexact(gpu_ready, oracle_mod, small_inclusion):
+@pytest.mark.parametrize("phased", [-1, 1, 3])
+def test_detected_records_bitexact(gpu_ready, oracle_mod, small_inclusion, phased):
     m = small_inclusion
     det = meshgen.c1_detectors()
     cfg = _cfg(m, nphoton=20000, tend=5e-9, tstep=0.5e-9, issavedet=1, issaveseed=1, issaveexit=1,
-               ismomentum=1, detpos=det, maxdetphoton=100000)
+               ismomentum=1, detpos=det, maxdetphoton=100000, phased=phased)
     mesh = Mesh(m.node, m.elem, m.label)
     g = simulate(mesh, cfg, trace=True)
     o = oracle_mod.run(m.node, m.elem, m.label, cfg, nthreads=4, trace=True)
