@@ -54,8 +54,9 @@ def peaks():
 
 
 def profiled_traffic():
-    """DRAM bytes per photon of the engine kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "engine_inclusion_cube.md")
+    """DRAM bytes per photon of the engine's launches (all gate windows of a
+    step) from the committed ncu summary, measured on a 5e6-photon step."""
+    path = os.path.join(ROOT, "profiles", "photon_engine_phased_inclusion_cube.md")
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_photon:"):
@@ -257,6 +258,10 @@ def main():
     steps_per_photon = res.raytet / ((args.warmup + args.steps) * nps)
     raytet_per_launch = steps_per_photon * nps
     avg_ms = float(np.mean(kernel_ms))
+    # engine launches per step: one per window of gates (the library's automatic window)
+    l2 = getattr(torch.cuda.get_device_properties(local_rank), "L2_cache_size", 0) or (126 << 20)
+    span = max(1, int(0.6 * l2 / (mesh.ne * 8)) - 1)
+    launches_per_step = -(-cfg.maxgate // span) if (span < cfg.maxgate and nps >= 4_000_000) else 1
     achieved = raytet_per_launch * BYTES_PER_STEP / (avg_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
     tpp = profiled_traffic()
@@ -306,10 +311,11 @@ def main():
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": (tpp * nps) if tpp else None,
                          "bytes_per_test": BYTES_PER_STEP, "tests_per_launch": raytet_per_launch,
-                         "avg_launch_ms": avg_ms},
+                         "avg_launch_ms": avg_ms, "launches_per_step": launches_per_step,
+                         "note": "per step: the step's phased launches together"},
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * launches_per_step,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
