@@ -109,7 +109,7 @@ typedef struct mmcgb_config {
                                 the fluence take deposits at a time; same results photon for
                                 photon): 0 = auto (when >= 8 gates, fluence >= 64 MB, >= 4e6
                                 photons per launch and queue memory available; k sized so the
-                                k+1 live planes fill ~60% of the L2), k >= 1 = window of k gates
+                                k+1 live planes fill ~90% of the L2), k >= 1 = window of k gates
                                 whenever possible (not for replay), -1 = never */
 } mmcgb_config;
 

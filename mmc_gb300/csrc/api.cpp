@@ -317,6 +317,8 @@ struct mmcgb_session {
     uint64_t g_nphoton = 0;
     int g_repeats = 0;
     PhaseQueue pq[2] = {};            // gate-phased tracing queues, capacity pq_cap photons each
+    unsigned* pq_order = nullptr;     // spatial resume order (pq_cap entries), null beyond 2^32 photons
+    unsigned* pq_bucket = nullptr;    // 2 * kBuckets counters
     void* pq_mem = nullptr;
     uint64_t pq_cap = 0;
     int pq_span = 0;                  // gates per phased launch
@@ -377,8 +379,17 @@ int32_t mmcgb_mesh_create(const mmcgb_mesh_desc* desc, int32_t device, mmcgb_mes
     std::vector<TetRec> rec;
     pack_records(m->host, rec);
     std::vector<float4> node(m->host.nn);
-    for (int i = 0; i < m->host.nn; i++)
+    for (int a = 0; a < 3; a++) {
+        m->lo[a] = m->host.nn ? m->host.node[a] : 0.f;
+        m->hi[a] = m->lo[a];
+    }
+    for (int i = 0; i < m->host.nn; i++) {
         node[i] = make_float4(m->host.node[3 * (size_t)i], m->host.node[3 * (size_t)i + 1], m->host.node[3 * (size_t)i + 2], 0.f);
+        for (int a = 0; a < 3; a++) {
+            m->lo[a] = std::min(m->lo[a], m->host.node[3 * (size_t)i + a]);
+            m->hi[a] = std::max(m->hi[a], m->host.node[3 * (size_t)i + a]);
+        }
+    }
     cudaError_t e;
     if ((e = cudaMalloc((void**)&m->rec, sizeof(TetRec) * rec.size())) != cudaSuccess ||
         (e = cudaMalloc((void**)&m->elem, sizeof(int4) * m->host.ne)) != cudaSuccess ||
@@ -469,23 +480,26 @@ namespace {
 // Whether a launch of `nphoton` photons of this session runs gate-phased
 // (mmcgb_config.phased); sets up the queues and the window when it does.
 // Automatic windows keep the live gate planes (window + 1 of them) within
-// about 60% of the L2: measured on the 1.296M-tet, 50-gate benchmark
-// (10.4 MB planes), windows of 5-10 gates trace 1e8 photons at 74.7k-75.3k
-// photons/ms against 59.4k in one launch; 17 gates drop to 71.5k, 1 gate
-// (parking every photon at every gate) to 59.9k.  Returns a status.
+// about 90% of the L2: measured on the 1.296M-tet, 50-gate benchmark
+// (10.4 MB planes, photons resumed in spatial order), windows of 6 and 10
+// gates trace 1e8 photons at 77.7k and 78.2k photons/ms against 59.4k in one
+// launch; before the spatial order, 5, 10 and 17 gates ran at 74.7k, 75.3k
+// and 71.5k, and 1 gate (parking every photon at every gate) at 59.9k.
+// Returns a status.
 int phased_setup(mmcgb_session* s, uint64_t nphoton, bool* use) {
     *use = false;
     const mmcgb_config& c = s->cfg;
     if (c.phased < 0 || c.replayseed || s->P.maxgate < 2) return MMCGB_OK;
-    const size_t per = phase_bytes_per_photon(s->P.sim);
-    const size_t need = per * nphoton + 4096;
+    const bool sorted = nphoton <= 0xFFFFFFFFull;
+    const size_t per = phase_bytes_per_photon(s->P.sim) + (sorted ? sizeof(unsigned) : 0);
+    const size_t need = per * nphoton + sizeof(unsigned) * 2 * kBuckets + 4096;
     const size_t plane = (size_t)s->mesh->host.ne * (c.accum_f64 ? 8 : 4);
     if (c.phased > 0) {
         s->pq_span = c.phased;
     } else {
         int l2 = 0;
         cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, s->mesh->device);
-        s->pq_span = std::max(1, (int)(0.6 * (double)l2 / (double)plane) - 1);
+        s->pq_span = std::max(1, (int)(0.9 * (double)l2 / (double)plane) - 1);
     }
     if (c.phased == 0) {
         const size_t fluence = (size_t)s->mesh->host.ne * s->P.maxgate * 8;
@@ -524,6 +538,8 @@ int phased_setup(mmcgb_session* s, uint64_t nphoton, bool* use) {
             s->pq[i].seed0 = want_seed ? reinterpret_cast<unsigned long long*>(take(16 * nphoton)) : nullptr;
             s->pq[i].count = reinterpret_cast<unsigned long long*>(take(sizeof(unsigned long long)));
         }
+        s->pq_order = sorted ? reinterpret_cast<unsigned*>(take(sizeof(unsigned) * nphoton)) : nullptr;
+        s->pq_bucket = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * 2 * kBuckets));
     }
     *use = true;
     return MMCGB_OK;
@@ -548,7 +564,8 @@ int32_t mmcgb_session_launch(mmcgb_session* s, uint64_t photon_offset, uint64_t 
     if (rc) return rc;
     CK(cudaEventRecord(s->ev0, s->stream));
     if (phased)
-        CK(launch_phased(sim, s->work, s->shape, s->stream, s->pq, s->pq_span));
+        CK(launch_phased(sim, s->work, s->shape, s->stream, s->pq, s->pq_span, s->pq_order, s->pq_bucket,
+                         s->mesh->lo, s->mesh->hi));
     else
         CK(launch_plain(sim, s->work, s->shape, s->stream));
     CK(cudaEventRecord(s->ev1, s->stream));

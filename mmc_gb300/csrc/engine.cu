@@ -80,6 +80,58 @@ struct FastMath {
 };
 
 __device__ __forceinline__ int decode_nb(int w) { return (w << 8) >> 8; }
+
+// Morton index of the bounding-box grid cell holding p (cells clamped to the grid).
+__device__ __forceinline__ unsigned spatial_key(float px, float py, float pz, const PhaseArgs& pa) {
+    const int n = (1 << kSortBits) - 1;
+    const unsigned x = (unsigned)min(max((int)((px - pa.lo[0]) * pa.scale[0]), 0), n);
+    const unsigned y = (unsigned)min(max((int)((py - pa.lo[1]) * pa.scale[1]), 0), n);
+    const unsigned z = (unsigned)min(max((int)((pz - pa.lo[2]) * pa.scale[2]), 0), n);
+    unsigned key = 0;
+#pragma unroll
+    for (int b = 0; b < kSortBits; b++)
+        key |= (((x >> b) & 1u) << (3 * b)) | (((y >> b) & 1u) << (3 * b + 1)) | (((z >> b) & 1u) << (3 * b + 2));
+    return key;
+}
+
+// Exclusive prefix sum of the kBuckets counts into `offset` (one block of 1024 threads).
+__global__ void __launch_bounds__(1024) k_bucket_scan(const unsigned* count, unsigned* offset) {
+    __shared__ unsigned part[1024];
+    constexpr int per = kBuckets / 1024;
+    const int t = threadIdx.x;
+    unsigned v[per], s = 0;
+#pragma unroll
+    for (int i = 0; i < per; i++) {
+        v[i] = count[t * per + i];
+        s += v[i];
+    }
+    part[t] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {  // Hillis-Steele inclusive scan of the per-thread sums
+        const unsigned add = (t >= o) ? part[t - o] : 0u;
+        __syncthreads();
+        part[t] += add;
+        __syncthreads();
+    }
+    unsigned base = part[t] - s;
+#pragma unroll
+    for (int i = 0; i < per; i++) {
+        offset[t * per + i] = base;
+        base += v[i];
+    }
+}
+
+// order[offset[key] + rank] = i for every parked record i (bucketed, order within a bucket arbitrary).
+__global__ void k_bucket_order(const PState* rec, const unsigned long long* count, unsigned long long cap,
+                               unsigned* offset, unsigned* order) {
+    const unsigned long long n = min(*count, cap);
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned key = rec[i].meta.w;
+        const unsigned slot = atomicAdd(offset + key, 1u);
+        if (slot < n) order[slot] = (unsigned)i;
+    }
+}
 __device__ __forceinline__ int decode_label(int w) { return (int)((unsigned)w >> 24); }
 
 __device__ __forceinline__ void deposit(const SimDev& S, unsigned idx, float val) {
@@ -408,7 +460,8 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                         // ---- resume a photon parked at the end of the previous gate ----
                         // queue traffic is read once: streaming loads keep it from displacing
                         // the tet records and the live gate planes in L2
-                        const PState* q = pa.in.rec + gid;
+                        const unsigned long long qi = pa.order ? (unsigned long long)pa.order[gid] : gid;
+                        const PState* q = pa.in.rec + qi;
                         PState r;
                         r.pos = __ldcs(&q->pos);
                         r.dir = __ldcs(&q->dir);
@@ -442,10 +495,10 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                         L.hit = 0;
                         L.wait = 0;
                         if (S.issavedet)
-                            for (int i = 0; i < S.reclen; i++) PP(i) = __ldcs(pa.in.ppath + gid * S.reclen + i);
+                            for (int i = 0; i < S.reclen; i++) PP(i) = __ldcs(pa.in.ppath + qi * S.reclen + i);
                         if (want_seed) {
-                            seed0[tid] = __ldcs(pa.in.seed0 + 2 * gid);
-                            seed0[bdim + tid] = __ldcs(pa.in.seed0 + 2 * gid + 1);
+                            seed0[tid] = __ldcs(pa.in.seed0 + 2 * qi);
+                            seed0[bdim + tid] = __ldcs(pa.in.seed0 + 2 * qi + 1);
                         }
                     } else {
                     // ---- launch (src/mmc_core.cl:1851-1906, pencil source) ----
@@ -502,12 +555,14 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                 const unsigned long long slot = base + grp.thread_rank();
                 // each photon is parked at most once per gate, so slot < cap; checked all the same
                 if (slot < pa.cap) {
+                    const unsigned key = spatial_key(L.px, L.py, L.pz, pa);
+                    atomicAdd(pa.bcount + key, 1u);
                     PState* q = pa.out.rec + slot;  // streaming stores: written once, read once
                     __stcs(&q->pos, make_float4(L.px, L.py, L.pz, L.ptime));
                     __stcs(&q->dir, make_float4(L.vx, L.vy, L.vz, L.weight));
                     __stcs(&q->len, make_float4(L.slen, L.slen0, L.oldw, __uint_as_float(L.oldidx)));
                     __stcs(&q->elem, make_int4(L.eid, L.label, L.mode, L.fixcount));
-                    __stcs(&q->meta, make_uint4(L.steps, (unsigned)L.pid, (unsigned)(L.pid >> 32), 0u));
+                    __stcs(&q->meta, make_uint4(L.steps, (unsigned)L.pid, (unsigned)(L.pid >> 32), key));
                     __stcs(&q->rng, make_uint4((unsigned)L.t0, (unsigned)(L.t0 >> 32), (unsigned)L.t1,
                                                (unsigned)(L.t1 >> 32)));
                     if (S.issavedet)
@@ -812,7 +867,8 @@ size_t phase_bytes_per_photon(const SimDev& sim) {
 
 template <class MP>
 static cudaError_t launch_phased_t(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
-                                   cudaStream_t stream, const PhaseQueue q[2], int span) {
+                                   cudaStream_t stream, const PhaseQueue q[2], int span, unsigned* order,
+                                   unsigned* bscratch, const float lo[3], const float hi[3]) {
     const int want_seed = (sim.issavedet && sim.seeds) ? 1 : 0;
     const int reclen_max = sim.issavedet ? sim.reclen : 0;
     const size_t smem = smem_bytes(sim.nmedia, reclen_max, shape.threads, want_seed);
@@ -829,21 +885,36 @@ static cudaError_t launch_phased_t(const SimDev& sim, unsigned long long* work_c
         pa.in = q[(k + 1) & 1];  // written by the previous launch
         pa.out = q[k & 1];
         pa.cap = sim.nphoton;
+        pa.order = (k > 0 && order) ? order : nullptr;
+        pa.bcount = bscratch;
+        for (int a = 0; a < 3; a++) {
+            pa.lo[a] = lo[a];
+            pa.scale[a] = (hi[a] > lo[a]) ? (float)(1 << kSortBits) / (hi[a] - lo[a]) : 0.f;
+        }
         cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(unsigned long long), stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(pa.out.count, 0, sizeof(unsigned long long), stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(bscratch, 0, sizeof(unsigned) * kBuckets, stream);
         if (e != cudaSuccess) return e;
         (void)cudaGetLastError();
         photon_engine_phased<MP><<<shape.blocks, shape.threads, smem, stream>>>(sim, pa, work_counter, reclen_max,
                                                                                want_seed);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (!pa.last && order) {  // resume order of the photons just parked
+            k_bucket_scan<<<1, 1024, 0, stream>>>(bscratch, bscratch + kBuckets);
+            k_bucket_order<<<shape.blocks, 256, 0, stream>>>(pa.out.rec, pa.out.count, pa.cap, bscratch + kBuckets,
+                                                            order);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
     }
     return cudaSuccess;
 }
 
 cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
-                          cudaStream_t stream, const PhaseQueue q[2], int span) {
-    return sim.fast_math ? launch_phased_t<FastMath>(sim, work_counter, shape, stream, q, span)
-                         : launch_phased_t<ExactMath>(sim, work_counter, shape, stream, q, span);
+                          cudaStream_t stream, const PhaseQueue q[2], int span, unsigned* order,
+                          unsigned* bscratch, const float lo[3], const float hi[3]) {
+    return sim.fast_math
+               ? launch_phased_t<FastMath>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi)
+               : launch_phased_t<ExactMath>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi);
 }
 
 template <class MP>

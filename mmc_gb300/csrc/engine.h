@@ -119,12 +119,24 @@ struct PhaseQueue {
     unsigned long long* count;  // records written
 };
 
+// Parked photons are resumed in spatial order: each is keyed by the cell of a
+// 16x16x16 grid over the mesh's bounding box that holds it (Morton order of
+// the cells), and between launches the queue is bucketed by key.  At any
+// moment the SMs then work on photons of a few neighbouring cells, whose
+// records and gate-plane entries stay in L2 together.
+constexpr int kSortBits = 4;                            // per axis
+constexpr int kBuckets = 1 << (3 * kSortBits);          // 4096
+
 struct PhaseArgs {
     int phase;   // first gate g traced by this launch
     int span;    // gates per launch: photons are parked when their time reaches gate g + span
     int last;    // 1: the last launch, photons run to their end
     PhaseQueue in, out;
     unsigned long long cap;
+    const unsigned* order;   // resume order of `in` (nullptr: queue order)
+    unsigned* bcount;        // kBuckets photon counts of `out` by spatial key
+    float lo[3];             // bounding box origin of the mesh
+    float scale[3];          // grid cells per mm along each axis
 };
 
 // Bytes of queue storage per photon of a phased launch (both queues).
@@ -132,8 +144,11 @@ size_t phase_bytes_per_photon(const SimDev& sim);
 // Enqueues a phased run of `sim` on `stream`: one launch per `span` gates,
 // queues q[0], q[1] (capacity sim.nphoton each) used alternately.  No host
 // synchronization between the launches.
+// `order` (sim.nphoton entries) and `bscratch` (2*kBuckets entries) hold the
+// spatial resume order between launches; `lo`/`hi` bound the mesh.
 cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
-                          cudaStream_t stream, const PhaseQueue q[2], int span);
+                          cudaStream_t stream, const PhaseQueue q[2], int span, unsigned* order,
+                          unsigned* bscratch, const float lo[3], const float hi[3]);
 
 // Launches the photon engine for one simulation on `stream`.
 cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,

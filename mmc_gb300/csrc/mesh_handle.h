@@ -12,4 +12,6 @@ struct mmcgb_mesh {
     float4* node = nullptr;
     int* label = nullptr;
     float* evol = nullptr;
+    float lo[3] = {0.f, 0.f, 0.f};  // bounding box of the nodes
+    float hi[3] = {0.f, 0.f, 0.f};
 };
