@@ -153,7 +153,9 @@ __device__ __forceinline__ void deposit(const SimDev& S, unsigned idx, float val
 }
 
 // One branchless Badouel step with fused deposit.  Requires 1 <= L.eid <= ne.
-template <class MP>
+// REPLAY: the kernel may run replay simulations (output types wl, wp, wn and
+// the Jacobian); kernels for forward runs are compiled without those branches.
+template <class MP, bool REPLAY>
 __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const float4* med) {
     const TetRec* R = S.rec + (L.eid - 1);
     const float4 nx = __ldg(&R->nx);
@@ -199,7 +201,7 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
         const float att = MP::exp(-prop.x * Lmove);
         L.weight *= att;
         const int ot = S.outputtype;
-        if (S.replay) {
+        if (REPLAY && S.replay) {
             const float rw = __ldg(S.replayweight + L.pid);
             if (ot == OT_WL || ot == OT_JACOBIAN) {
                 currweight = Lmove;
@@ -214,7 +216,7 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
         L.slen -= Lmove * prop.y;
         float ww = currweight - L.weight;
         L.ptime += Lmove * rc;
-        if (ot == OT_WN) {  // scatter counts are deposited at the scattering events only
+        if (REPLAY && ot == OT_WN) {  // scatter counts are deposited at the scattering events only
             L.px = MP::mad(Lmove, L.vx, L.px);
             L.py = MP::mad(Lmove, L.vy, L.py);
             L.pz = MP::mad(Lmove, L.vz, L.pz);
@@ -222,14 +224,14 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
             return;
         }
         float gf;
-        if (S.replay && (ot == OT_WL || ot == OT_WP))
+        if (REPLAY && S.replay && (ot == OT_WL || ot == OT_WP))
             gf = __ldg(S.replaytime + L.pid) * S.Rtstep;
         else
             gf = (L.ptime - S.tstart) * S.Rtstep;
         // min((int)gf, maxgate-1), clamped at 0 so that no index leaves the buffer
         int gate = (gf < (float)(S.maxgate - 1)) ? (int)gf : S.maxgate - 1;
         gate = max(gate, 0);
-        if (ot != OT_ENERGY && ot != OT_WP && ot != OT_WL)
+        if (ot != OT_ENERGY && !(REPLAY && (ot == OT_WP || ot == OT_WL)))
             ww = (prop.x < kEps) ? (currweight * Lmove) : MP::div(ww, prop.x);
         const unsigned newidx = (unsigned)(L.eid - 1) + (unsigned)(gate * S.ne);
         if (L.oldidx == (unsigned)kIdUndef) L.oldidx = newidx;
@@ -398,7 +400,7 @@ struct ManySims {
 
 // Shared-memory layout: media[nsims_local * nmed_stride] | ppath[reclen_max][blockDim] |
 // seed0[2][blockDim] (u64)
-template <class MP, class Sims, bool BATCHED, bool PHASED>
+template <class MP, class Sims, bool BATCHED, bool PHASED, bool REPLAY>
 __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned long long* cum, int nsims,
                                             unsigned long long total, int nmed_stride, int reclen_max,
                                             int want_seed, unsigned long long* work_counter, const PhaseArgs& pa) {
@@ -425,7 +427,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
     L.steps = 0;
     Tally tally{0.f, 0u, 0u, -1};
 
-#define PP(i) ppath[(size_t)(i) * bdim + tid]
+#define PP(i) ppath[(i) * bdim + tid]
 
     while (true) {
         // ---- (1) hand out photons to lanes that need one ----
@@ -502,7 +504,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                         }
                     } else {
                     // ---- launch (src/mmc_core.cl:1851-1906, pencil source) ----
-                    if (S.replay) {
+                    if (REPLAY && S.replay) {
                         L.t0 = __ldg(S.replayseed + 2 * L.pid);
                         L.t1 = __ldg(S.replayseed + 2 * L.pid + 1);
                     } else {
@@ -603,7 +605,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                         if (S.photon_steps) S.photon_steps[L.pid] = L.steps;
                         L.mode = M_NEED;
                     } else {
-                        if (S.replay && S.outputtype == OT_WN) {
+                        if (REPLAY && S.replay && S.outputtype == OT_WN) {
                             const float gf = __ldg(S.replaytime + L.pid) * S.Rtstep;
                             int gate = (gf < (float)(S.maxgate - 1)) ? (int)gf : S.maxgate - 1;
                             gate = max(gate, 0);
@@ -631,7 +633,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
 
         // ---- (2) one ray-tet step ----
         const bool bad_elem = (L.eid < 1 || L.eid > S.ne);  // defensive: never expected
-        if (!bad_elem) raytet_step<MP>(L, S, med);
+        if (!bad_elem) raytet_step<MP, REPLAY>(L, S, med);
         L.steps++;
         tally.raytet++;
         bool ended = false;
@@ -779,14 +781,14 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
     if (tally.sim >= 0) flush_tally(tally, sims(tally.sim));
 }
 
-template <class MP>
+template <class MP, bool REPLAY>
 __global__ void __launch_bounds__(128, 8) photon_engine_plain(const __grid_constant__ SimDev sim,
                                                               unsigned long long* work_counter, int reclen_max,
                                                               int want_seed) {
     SingleSim acc{sim};
     const PhaseArgs none{};
-    engine_body<MP, SingleSim, false, false>(acc, nullptr, 1, sim.nphoton, sim.nmedia, reclen_max, want_seed,
-                                             work_counter, none);
+    engine_body<MP, SingleSim, false, false, REPLAY>(acc, nullptr, 1, sim.nphoton, sim.nmedia, reclen_max,
+                                                     want_seed, work_counter, none);
 }
 
 template <class MP>
@@ -798,11 +800,11 @@ __global__ void __launch_bounds__(128, 8) photon_engine_phased(const __grid_cons
     // gate 0 launches the run's photons; later gates resume the ones parked by the previous launch
     unsigned long long total = sim.nphoton;
     if (pa.phase > 0) total = min(*pa.in.count, pa.cap);
-    engine_body<MP, SingleSim, false, true>(acc, nullptr, 1, total, sim.nmedia, reclen_max, want_seed,
-                                            work_counter, pa);
+    engine_body<MP, SingleSim, false, true, false>(acc, nullptr, 1, total, sim.nmedia, reclen_max, want_seed,
+                                                   work_counter, pa);
 }
 
-template <class MP>
+template <class MP, bool REPLAY>
 __global__ void __launch_bounds__(128, 8) photon_engine_batched(const SimDev* __restrict__ sims,
                                                                 const unsigned long long* __restrict__ cum,
                                                                 int nsims, unsigned long long total,
@@ -810,8 +812,8 @@ __global__ void __launch_bounds__(128, 8) photon_engine_batched(const SimDev* __
                                                                 int reclen_max, int want_seed) {
     ManySims acc{sims};
     const PhaseArgs none{};
-    engine_body<MP, ManySims, true, false>(acc, cum, nsims, total, nmed_stride, reclen_max, want_seed, work_counter,
-                                           none);
+    engine_body<MP, ManySims, true, false, REPLAY>(acc, cum, nsims, total, nmed_stride, reclen_max, want_seed,
+                                                   work_counter, none);
 }
 
 size_t smem_bytes(int nmed_rows, int reclen_max, int threads, int want_seed) {
@@ -829,34 +831,39 @@ LaunchShape default_shape(int device, bool batched) {
     int per_sm = 0;
     const int threads = 128;
     if (batched)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_batched<FastMath>, threads, 4096);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_batched<FastMath, true>, threads, 4096);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_plain<FastMath>, threads, 1024);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_plain<FastMath, false>, threads, 1024);
     if (per_sm < 1) per_sm = 1;
     return LaunchShape{sms * per_sm, threads};
 }
 
-template <class MP>
+template <class MP, bool REPLAY>
 static cudaError_t launch_plain_t(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
                                   cudaStream_t stream) {
     const int want_seed = (sim.issavedet && sim.seeds) ? 1 : 0;
     const int reclen_max = sim.issavedet ? sim.reclen : 0;
     const size_t smem = smem_bytes(sim.nmedia, reclen_max, shape.threads, want_seed);
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(photon_engine_plain<MP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(photon_engine_plain<MP, REPLAY>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     (void)cudaGetLastError();  // the launch check below must see this launch's status only
-    photon_engine_plain<MP><<<shape.blocks, shape.threads, smem, stream>>>(sim, work_counter, reclen_max, want_seed);
+    photon_engine_plain<MP, REPLAY><<<shape.blocks, shape.threads, smem, stream>>>(sim, work_counter, reclen_max,
+                                                                                  want_seed);
     return cudaGetLastError();
 }
 
 cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
                          cudaStream_t stream) {
-    return sim.fast_math ? launch_plain_t<FastMath>(sim, work_counter, shape, stream)
-                         : launch_plain_t<ExactMath>(sim, work_counter, shape, stream);
+    if (sim.replay)
+        return sim.fast_math ? launch_plain_t<FastMath, true>(sim, work_counter, shape, stream)
+                             : launch_plain_t<ExactMath, true>(sim, work_counter, shape, stream);
+    return sim.fast_math ? launch_plain_t<FastMath, false>(sim, work_counter, shape, stream)
+                         : launch_plain_t<ExactMath, false>(sim, work_counter, shape, stream);
 }
 
 size_t phase_bytes_per_photon(const SimDev& sim) {
@@ -923,14 +930,16 @@ static cudaError_t launch_batched_t(const SimDev* sims, const unsigned long long
                                     unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream) {
     const size_t smem = smem_bytes(nsims * nmed_stride, reclen_max, shape.threads, want_seed);
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(photon_engine_batched<MP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(photon_engine_batched<MP, true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     (void)cudaGetLastError();  // the launch check below must see this launch's status only
-    photon_engine_batched<MP><<<shape.blocks, shape.threads, smem, stream>>>(sims, cum, nsims, total, nmed_stride,
-                                                                            work_counter, reclen_max, want_seed);
+    // batches may mix forward and replay simulations: the batched kernel keeps the replay branches
+    photon_engine_batched<MP, true><<<shape.blocks, shape.threads, smem, stream>>>(
+        sims, cum, nsims, total, nmed_stride, work_counter, reclen_max, want_seed);
     return cudaGetLastError();
 }
 
