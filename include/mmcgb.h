@@ -70,9 +70,13 @@ typedef struct mmcgb_config {
     uint64_t nphoton;        /* photons to launch (replay: replayed photons) */
     uint64_t photon_offset;  /* index of the first photon (sharded runs) */
     uint64_t seed;           /* RNG seed */
-    float srcpos[3];         /* pencil source position (mm) */
+    float srcpos[3];         /* source position (mm) */
     float srcdir[3];         /* unit launch direction */
-    int32_t srctype;         /* 0 = pencil (the only source type implemented) */
+    int32_t srctype;         /* the reference's source types (src/mmc_utils.h:101-105): 0 pencil,
+                                1 isotropic, 2 cone, 3 gaussian, 4 planar, 5 pattern, 6 fourier,
+                                7 arcsine, 8 disk, 9 fourierx, 10 fourierx2d, 11 zgaussian, 12 line,
+                                13 slit, 14 pencilarray, 15 pattern3d, 16 hyperboloid, 17 ring;
+                                parameters in srcparam1/srcparam2/focus/srcpattern below */
     int32_t e0;              /* initial element, 1-based; 0 = locate it */
     float tstart, tend, tstep;  /* time gates (s) */
     int32_t isreflect;       /* 0 no mismatch, 1 Fresnel, 2 absorbing exterior, 3 mirror */
@@ -111,6 +115,14 @@ typedef struct mmcgb_config {
                                 photons per launch and queue memory available; k sized so the
                                 k+1 live planes fill ~90% of the L2), k >= 1 = window of k gates
                                 whenever possible (not for replay), -1 = never */
+    float srcparam1[4];      /* source parameters 1 and 2, as the reference's cfg->srcparam1/2
+                                (src/mmc_utils.h:219-220), e.g. disk radius, area-source edge
+                                vectors with the pattern size in w, Fourier wave numbers */
+    float srcparam2[4];
+    float focus;             /* focal length (the reference's srcdir.w): 0 none, > 0 converging,
+                                < 0 diverging; NaN random direction, -inf Lambertian */
+    const float* srcpattern; /* pattern source weights: srcparam1.w x srcparam2.w values (type 5)
+                                or srcparam1.x x .y x .z (type 15), row-major, else NULL */
 } mmcgb_config;
 
 /* Outputs.  Pointers may be NULL to skip an output; counts are always set. */
@@ -130,6 +142,7 @@ typedef struct mmcgb_result {
     double normalizer;
     uint64_t raytet;         /* ray-tetrahedron tests */
     uint64_t aborted;        /* photons stopped by the step budget */
+    uint64_t outside;        /* photons whose launch position lies in no element (an error) */
     float kernel_ms;         /* device time of the photon kernel */
 } mmcgb_result;
 
@@ -221,8 +234,8 @@ int32_t mmcgb_run(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, int32_t 
  * that loads the library until the process exits.
  *   - outputs are overwritten (zeroed first): field_raw holds the raw element
  *     deposits, maxgate*ne doubles, gate-major (the layout of mmcgb_result.field
- *     for basisorder 0, isnormalized 0); energy[1] = escaped weight (energy[0]
- *     is left 0: the launched weight is nphoton); counters[0] = ray-tet tests,
+ *     for basisorder 0, isnormalized 0); energy[0] = launched weight, energy[1] =
+ *     escaped weight; counters[0] = ray-tet tests,
  *     counters[1] = photons stopped by the step budget; detp/detcount/seeds as
  *     in mmcgb_result when issavedet (maxdetphoton*reclen floats, 16-byte seeds)
  *   - limits: nmedia <= MMCGB_NOALLOC_MAX_MEDIA, detnum <= MMCGB_NOALLOC_MAX_DET,

@@ -20,6 +20,10 @@ import numpy as np
 from . import _native as N
 
 OUTPUT_TYPES = {"flux": 0, "fluence": 1, "energy": 2, "jacobian": 3, "wl": 4, "wp": 5, "wn": 16}
+# the reference's source type names and numbers (src/mmc_utils.h:101-105)
+SOURCE_TYPES = {"pencil": 0, "isotropic": 1, "cone": 2, "gaussian": 3, "planar": 4, "pattern": 5, "fourier": 6,
+                "arcsine": 7, "disk": 8, "fourierx": 9, "fourierx2d": 10, "zgaussian": 11, "line": 12, "slit": 13,
+                "pencilarray": 14, "pattern3d": 15, "hyperboloid": 16, "ring": 17}
 
 
 def _ptr(a: Optional[np.ndarray]):
@@ -166,6 +170,11 @@ class SimConfig:
     blocks: int = 0
     fast_math: int = 1
     phased: int = 0
+    srctype: object = "pencil"                  # name or the reference's number (SOURCE_TYPES)
+    srcparam1: Sequence[float] = (0.0, 0.0, 0.0, 0.0)
+    srcparam2: Sequence[float] = (0.0, 0.0, 0.0, 0.0)
+    focus: float = 0.0                          # the reference's srcdir.w
+    srcpattern: Optional[np.ndarray] = None     # pattern / pattern3d weights
     save_field: bool = True
 
     @property
@@ -180,7 +189,15 @@ class SimConfig:
         c.seed = int(self.seed) & 0xFFFFFFFFFFFFFFFF
         c.srcpos = (C.c_float * 3)(*[float(x) for x in self.srcpos])
         c.srcdir = (C.c_float * 3)(*[float(x) for x in self.srcdir])
-        c.srctype = 0
+        st = self.srctype
+        c.srctype = SOURCE_TYPES[st] if isinstance(st, str) else int(st)
+        c.srcparam1 = (C.c_float * 4)(*[float(x) for x in self.srcparam1])
+        c.srcparam2 = (C.c_float * 4)(*[float(x) for x in self.srcparam2])
+        c.focus = float(self.focus)
+        if self.srcpattern is not None:
+            pat = np.ascontiguousarray(self.srcpattern, dtype=np.float32).reshape(-1)
+            keep["pattern"] = pat
+            c.srcpattern = _ptr(pat)
         c.e0 = int(self.e0)
         c.tstart, c.tend, c.tstep = float(self.tstart), float(self.tend), float(self.tstep)
         c.isreflect, c.isspecular, c.voidtime = int(self.isreflect), int(self.isspecular), int(self.voidtime)

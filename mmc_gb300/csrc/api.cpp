@@ -46,8 +46,31 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 int gates_of(const mmcgb_config& c) { return (int)((c.tend - c.tstart) / c.tstep + 0.5f); }
 
+// Source types whose photons all start at srcpos in the initial element (the
+// reference returns early from the launch for them, src/mmc_raytrace.c:2353-2357,
+// :2483-2485); the others are located per photon.
+bool point_source(int t) { return t == 0 || t == 1 || t == 2 || t == 7; }
+
+size_t pattern_len(const mmcgb_config& c) {
+    if (c.srctype == 5) return (size_t)std::max(0, (int)c.srcparam1[3]) * (size_t)std::max(0, (int)c.srcparam2[3]);
+    if (c.srctype == 15)
+        return (size_t)std::max(0, (int)c.srcparam1[0]) * (size_t)std::max(0, (int)c.srcparam1[1]) *
+               (size_t)std::max(0, (int)c.srcparam1[2]);
+    return 0;
+}
+
 int validate(const HostMesh& m, const mmcgb_config& c, std::string& err) {
-    if (c.srctype != 0) { err = "only the pencil source (srctype 0) is implemented"; return MMCGB_E_ARG; }
+    if (c.srctype < 0 || c.srctype > 17) { err = "srctype must be 0..17"; return MMCGB_E_ARG; }
+    if ((c.srctype == 5 || c.srctype == 15) && (!c.srcpattern || pattern_len(c) == 0)) {
+        err = "pattern sources need srcpattern and a positive pattern size in srcparam1/srcparam2";
+        return MMCGB_E_ARG;
+    }
+    if (c.srctype == 14 && (!(c.srcparam1[3] > 1.f) || !(c.srcparam2[3] > 1.f))) {
+        err = "pencil-array sources need at least 2 beams along each edge (srcparam1.w, srcparam2.w)";
+        return MMCGB_E_ARG;
+    }
+    for (int k = 0; k < 4; k++)
+        if (!std::isfinite(c.srcparam1[k]) || !std::isfinite(c.srcparam2[k])) { err = "source parameters must be finite"; return MMCGB_E_ARG; }
     if (!(c.tstep > 0.f) || !(c.tend > c.tstart)) { err = "time gates need tstep > 0 and tend > tstart"; return MMCGB_E_ARG; }
     if (gates_of(c) < 1) { err = "time window holds no gate"; return MMCGB_E_ARG; }
     if (c.nmedia < 2 || c.nmedia > kMaxMedia || !c.media) { err = "media table needs 2..64 rows (row 0 = background)"; return MMCGB_E_ARG; }
@@ -75,6 +98,7 @@ struct SimBuffers {
     unsigned int* detcount = nullptr;
     double* energy = nullptr;
     unsigned long long* counters = nullptr;
+    float* pattern = nullptr;
     unsigned long long* rseed = nullptr;
     float* rweight = nullptr;
     float* rtime = nullptr;
@@ -131,7 +155,9 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     } else {
         e0 = locate(m, c.srcpos);
     }
-    if (e0 <= 0) return fail(MMCGB_E_SOURCE, "initial element does not enclose the source");
+    // point sources start in e0; the others are located per photon and may lie outside the mesh
+    if (e0 <= 0 && point_source(c.srctype)) return fail(MMCGB_E_SOURCE, "initial element does not enclose the source");
+    if (e0 < 0) e0 = 0;
 
     P.maxgate = gates_of(c);
     const int M = c.nmedia - 1;
@@ -153,7 +179,12 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     if (c.issaveseed) CK(B.alloc(&B.seeds, maxdet * 2));
     CK(B.alloc(&B.detcount, 1));
     CK(B.alloc(&B.energy, 2));
-    CK(B.alloc(&B.counters, 2));
+    CK(B.alloc(&B.counters, 3));
+    const size_t plen = pattern_len(c);
+    if (plen) {
+        CK(B.alloc(&B.pattern, plen));
+        CK(cudaMemcpyAsync(B.pattern, c.srcpattern, sizeof(float) * plen, cudaMemcpyHostToDevice, stream));
+    }
     if (c.replayseed) {
         CK(B.alloc(&B.rseed, 2 * c.nphoton));
         CK(B.alloc(&B.rweight, c.nphoton));
@@ -171,7 +202,7 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     else CK(cudaMemsetAsync(B.f32, 0, sizeof(float) * 2 * P.flen, stream));
     CK(cudaMemsetAsync(B.detcount, 0, sizeof(unsigned), stream));
     CK(cudaMemsetAsync(B.energy, 0, sizeof(double) * 2, stream));
-    CK(cudaMemsetAsync(B.counters, 0, sizeof(unsigned long long) * 2, stream));
+    CK(cudaMemsetAsync(B.counters, 0, sizeof(unsigned long long) * 3, stream));
 
     SimDev& S = P.sim;
     std::memset(&S, 0, sizeof(S));
@@ -192,6 +223,18 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     for (int k = 0; k < 3; k++) {
         S.srcpos[k] = c.srcpos[k];
         S.srcdir[k] = c.srcdir[k];
+    }
+    S.srctype = c.srctype;
+    S.srcp1 = make_float4(c.srcparam1[0], c.srcparam1[1], c.srcparam1[2], c.srcparam1[3]);
+    S.srcp2 = make_float4(c.srcparam2[0], c.srcparam2[1], c.srcparam2[2], c.srcparam2[3]);
+    S.focus = c.focus;
+    S.srcpattern = B.pattern;
+    S.loc_start = mesh->loc_start;
+    S.loc_items = mesh->loc_items;
+    S.loc_res = m.grid.res;
+    for (int k = 0; k < 3; k++) {
+        S.loc_lo[k] = m.grid.lo[k];
+        S.loc_inv[k] = m.grid.inv[k];
     }
     // per-launch time window (src/mmc_cu_host.cu:642-662): all gates in one launch
     S.tstart = c.tstart;
@@ -227,6 +270,7 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     S.maxdet = (unsigned)maxdet;
     S.energy = B.energy;
     S.counters = B.counters;
+    S.ncounters = 3;
     S.photon_weight = B.pw;
     S.photon_steps = B.ps;
     S.photon_det = B.pd;
@@ -239,7 +283,7 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
     SimBuffers& B = P.buf;
     unsigned detected = 0;
     double energy[2] = {0, 0};
-    unsigned long long counters[2] = {0, 0};
+    unsigned long long counters[3] = {0, 0, 0};
     CK(cudaMemcpyAsync(&detected, B.detcount, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(energy, B.energy, sizeof(energy), cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(counters, B.counters, sizeof(counters), cudaMemcpyDeviceToHost, stream));
@@ -263,7 +307,7 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
         A.host = &mesh->host;
         A.cfg = &c;
         A.maxgate = P.maxgate;
-        A.energytot = (double)launched;
+        A.energytot = energy[0];
         A.energyesc = energy[1];
         A.f64 = B.f64;
         A.f32a = B.f32;
@@ -290,11 +334,15 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
     res->saved = (uint32_t)saved;
     res->reclen = P.reclen;
     res->maxgate = P.maxgate;
-    res->energytot = (double)launched;  // every photon launches with weight 1
+    (void)launched;
+    res->energytot = energy[0];  // launched weight, summed on the device (source weights may be < 1)
     res->energyesc = energy[1];
     res->raytet = counters[0];
     res->aborted = counters[1];
+    res->outside = counters[2];
     res->normalizer = normalizer;
+    if (res->outside)
+        return fail(MMCGB_E_SOURCE, std::to_string(res->outside) + " photons were launched at positions no element encloses");
     if (res->aborted) return fail(MMCGB_E_BUDGET, "some photons exceeded the per-photon step budget");
     return MMCGB_OK;
 }
@@ -332,7 +380,11 @@ void free_mesh_device(mmcgb_mesh* m) {
     if (m->node) cudaFree(m->node);
     if (m->label) cudaFree(m->label);
     if (m->evol) cudaFree(m->evol);
+    if (m->loc_start) cudaFree(m->loc_start);
+    if (m->loc_items) cudaFree(m->loc_items);
     m->evol = nullptr;
+    m->loc_start = nullptr;
+    m->loc_items = nullptr;
     m->rec = nullptr;
     m->elem = nullptr;
     m->node = nullptr;
@@ -400,7 +452,13 @@ int32_t mmcgb_mesh_create(const mmcgb_mesh_desc* desc, int32_t device, mmcgb_mes
         (e = cudaMemcpy(m->rec, rec.data(), sizeof(TetRec) * rec.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(m->elem, m->host.elem.data(), sizeof(int4) * m->host.ne, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(m->node, node.data(), sizeof(float4) * m->host.nn, cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMemcpy(m->label, m->host.label.data(), sizeof(int) * m->host.ne, cudaMemcpyHostToDevice)) != cudaSuccess) {
+        (e = cudaMemcpy(m->label, m->host.label.data(), sizeof(int) * m->host.ne, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&m->loc_start, sizeof(unsigned) * m->host.grid.start.size())) != cudaSuccess ||
+        (e = cudaMalloc((void**)&m->loc_items, sizeof(unsigned) * std::max<size_t>(1, m->host.grid.items.size()))) != cudaSuccess ||
+        (e = cudaMemcpy(m->loc_start, m->host.grid.start.data(), sizeof(unsigned) * m->host.grid.start.size(),
+                        cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(m->loc_items, m->host.grid.items.data(), sizeof(unsigned) * m->host.grid.items.size(),
+                        cudaMemcpyHostToDevice)) != cudaSuccess) {
         free_mesh_device(m.get());
         return cuda_fail(e, "mesh upload");
     }
@@ -593,7 +651,7 @@ int batch_launch(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets, c
     std::vector<SimDev> sims(n);
     std::vector<unsigned long long> cum(n);
     unsigned long long total = 0;
-    int nmed_stride = 0, reclen_max = 0, want_seed = 0;
+    int nmed_stride = 0, reclen_max = 0, want_seed = 0, want_io = 0;
     for (int i = 0; i < n; i++) {
         mmcgb_session* s = ss[i];
         if (!s || s->mesh->device != device) return fail(MMCGB_E_ARG, "batched sessions must live on one device");
@@ -608,6 +666,7 @@ int batch_launch(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets, c
         nmed_stride = std::max(nmed_stride, s->cfg.nmedia);
         if (s->cfg.issavedet) reclen_max = std::max(reclen_max, s->P.sim.reclen);
         if (s->cfg.issavedet && s->P.sim.seeds) want_seed = 1;
+        if (s->P.sim.srctype != 0 || s->P.sim.e0 <= 0) want_io = 1;
         total += counts[i];
         cum[i] = total;
     }
@@ -642,7 +701,7 @@ int batch_launch(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets, c
     if (n == 1)  // a single simulation takes the plain kernel (its parameter block in constant memory)
         CK(launch_plain(sims[0], work, s0->shape, st));
     else
-        CK(launch_batched(dsims, dcum, n, total, nmed_stride, reclen_max, want_seed, work, shape, st, fast));
+        CK(launch_batched(dsims, dcum, n, total, nmed_stride, reclen_max, want_seed, work, shape, st, fast, want_io));
     if (ordered) CK(cudaEventRecord(s0->ev1, st));
     CK(cudaFreeAsync(dsims, st));
     CK(cudaFreeAsync(dcum, st));
@@ -792,7 +851,7 @@ int32_t mmcgb_simulate_batch(int32_t n, mmcgb_mesh* const* meshes, const mmcgb_c
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     std::vector<Prepared> P(n);
     int rc = MMCGB_OK;
-    int nmed_stride = 0, reclen_max = 0, want_seed = 0;
+    int nmed_stride = 0, reclen_max = 0, want_seed = 0, want_io = 0;
     std::vector<unsigned long long> cum(n);
     unsigned long long total = 0;
     for (int i = 0; i < n && rc == MMCGB_OK; i++) {
@@ -801,6 +860,7 @@ int32_t mmcgb_simulate_batch(int32_t n, mmcgb_mesh* const* meshes, const mmcgb_c
         nmed_stride = std::max(nmed_stride, cfgs[i].nmedia);
         if (cfgs[i].issavedet) reclen_max = std::max(reclen_max, P[i].sim.reclen);
         if (cfgs[i].issavedet && cfgs[i].issaveseed) want_seed = 1;
+        if (P[i].sim.srctype != 0 || P[i].sim.e0 <= 0) want_io = 1;
         if ((cfgs[i].fast_math != 0) != (cfgs[0].fast_math != 0)) {
             rc = fail(MMCGB_E_ARG, "batched simulations must share fast_math");
             break;
@@ -829,7 +889,7 @@ int32_t mmcgb_simulate_batch(int32_t n, mmcgb_mesh* const* meshes, const mmcgb_c
         if (e == cudaSuccess) e = cudaEventRecord(ev0, stream);
         if (e == cudaSuccess)
             e = launch_batched(dsims, dcum, n, total, nmed_stride, reclen_max, want_seed, work, shape, stream,
-                               cfgs[0].fast_math ? 1 : 0);
+                               cfgs[0].fast_math ? 1 : 0, want_io);
         if (e == cudaSuccess) e = cudaEventRecord(ev1, stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) rc = cuda_fail(e, "batched photon engine");

@@ -325,23 +325,10 @@ __device__ __forceinline__ int reflectray(Lane& L, const SimDev& S, const float4
     return eid;
 }
 
-// Henyey-Greenstein scatter + direction rotation, src/mmc_core.cl:1307-1377.
+// Rotates the direction by polar angle (stheta, ctheta) and azimuth (sphi,
+// cphi) about itself, then renormalizes (rotatevector, src/mmc_core.cl:1345-1377).
 template <class MP>
-__device__ __forceinline__ float next_scatter(Lane& L, float g, float& ctheta_out) {
-    const float nextslen = -MP::log(rng_next(L.t0, L.t1) + kEps);
-    float sphi, cphi, stheta, ctheta;
-    MP::sincos2pi(rng_next(L.t0, L.t1), sphi, cphi);
-    if (g > kEps) {
-        float tmp0 = MP::div(1.f - g * g, 1.f - g + 2.f * g * rng_next(L.t0, L.t1));
-        tmp0 *= tmp0;
-        tmp0 = MP::div(1.f + g * g - tmp0, 2.f * g);
-        tmp0 = fmaxf(-1.f, fminf(tmp0, 1.f));
-        stheta = sqrtf(1.f - tmp0 * tmp0);
-        ctheta = tmp0;
-    } else {
-        ctheta = 2.f * rng_next(L.t0, L.t1) - 1.f;
-        stheta = sqrtf(1.f - ctheta * ctheta);
-    }
+__device__ __forceinline__ void rotate_dir(Lane& L, float stheta, float ctheta, float sphi, float cphi) {
     float px, py, pz;
     if (L.vz > -1.f + kEps && L.vz < 1.f - kEps) {
         const float tmp0 = 1.f - L.vz * L.vz;
@@ -359,6 +346,26 @@ __device__ __forceinline__ float next_scatter(Lane& L, float g, float& ctheta_ou
     L.vx = px * inv;
     L.vy = py * inv;
     L.vz = pz * inv;
+}
+
+// Henyey-Greenstein scatter + direction rotation, src/mmc_core.cl:1307-1377.
+template <class MP>
+__device__ __forceinline__ float next_scatter(Lane& L, float g, float& ctheta_out) {
+    const float nextslen = -MP::log(rng_next(L.t0, L.t1) + kEps);
+    float sphi, cphi, stheta, ctheta;
+    MP::sincos2pi(rng_next(L.t0, L.t1), sphi, cphi);
+    if (g > kEps) {
+        float tmp0 = MP::div(1.f - g * g, 1.f - g + 2.f * g * rng_next(L.t0, L.t1));
+        tmp0 *= tmp0;
+        tmp0 = MP::div(1.f + g * g - tmp0, 2.f * g);
+        tmp0 = fmaxf(-1.f, fminf(tmp0, 1.f));
+        stheta = sqrtf(1.f - tmp0 * tmp0);
+        ctheta = tmp0;
+    } else {
+        ctheta = 2.f * rng_next(L.t0, L.t1) - 1.f;
+        stheta = sqrtf(1.f - ctheta * ctheta);
+    }
+    rotate_dir<MP>(L, stheta, ctheta, sphi, cphi);
     ctheta_out = ctheta;
     return nextslen;
 }
@@ -372,21 +379,344 @@ __device__ __forceinline__ int finddetector(const Lane& L, const SimDev& S) {
     return 0;
 }
 
+// ---- photon sources ---------------------------------------------------------
+// Source types, numbered as the reference's TSrcType (src/mmc_utils.h:101-105).
+enum SrcType : int {
+    ST_PENCIL = 0, ST_ISOTROPIC = 1, ST_CONE = 2, ST_GAUSSIAN = 3, ST_PLANAR = 4, ST_PATTERN = 5,
+    ST_FOURIER = 6, ST_ARCSINE = 7, ST_DISK = 8, ST_FOURIERX = 9, ST_FOURIER2D = 10, ST_ZGAUSSIAN = 11,
+    ST_LINE = 12, ST_SLIT = 13, ST_PENCILARRAY = 14, ST_PATTERN3D = 15, ST_HYPERBOLOID = 16, ST_RING = 17
+};
+
+constexpr float kPi = 3.14159265358979323846f;
+
+// Whether element e (0-based) encloses p: the barycentric test of the
+// reference's source-element search, src/mmc_raytrace.c:2599-2652 (face
+// normals from node cross products, unnormalized, tolerance -1e-4).
+__device__ __forceinline__ float face_bary(const float4& a, const float4& b, const float4& c, float px, float py,
+                                           float pz) {
+    const float abx = b.x - a.x, aby = b.y - a.y, abz = b.z - a.z;
+    const float acx = c.x - a.x, acy = c.y - a.y, acz = c.z - a.z;
+    const float sx = px - a.x, sy = py - a.y, sz = pz - a.z;
+    const float nx = aby * acz - abz * acy, ny = abz * acx - abx * acz, nz = abx * acy - aby * acx;
+    return -((sx * nx + sy * ny) + sz * nz);
+}
+
+__device__ __forceinline__ bool src_encloses(const SimDev& S, int e, float px, float py, float pz) {
+    const int4 el = __ldg(S.elem + e);
+    const float4 n0 = __ldg(S.node + (el.x - 1)), n1 = __ldg(S.node + (el.y - 1));
+    const float4 n2 = __ldg(S.node + (el.z - 1)), n3 = __ldg(S.node + (el.w - 1));
+    // faces out[i] = {0,3,1} {3,2,1} {0,2,3} {0,1,2} (src/mmc_mesh.c:59-64), facemap {2,0,1,3}
+    const float b2 = face_bary(n0, n3, n1, px, py, pz);
+    const float b0 = face_bary(n3, n2, n1, px, py, pz);
+    const float b1 = face_bary(n0, n2, n3, px, py, pz);
+    const float b3 = face_bary(n0, n1, n2, px, py, pz);
+    return !(b0 < -1e-4f || b1 < -1e-4f || b2 < -1e-4f || b3 < -1e-4f);
+}
+
+// The lowest-index element enclosing p among the bounding-box grid cell that
+// holds p, else among its 26 neighbours (cells hold every element whose
+// bounding box overlaps them).  Returns a 1-based id, 0 when none does.
+__device__ int src_locate(const SimDev& S, float px, float py, float pz) {
+    const int res = S.loc_res;
+    const float fx = (px - S.loc_lo[0]) * S.loc_inv[0];
+    const float fy = (py - S.loc_lo[1]) * S.loc_inv[1];
+    const float fz = (pz - S.loc_lo[2]) * S.loc_inv[2];
+    const float lo = -1e-3f * res, hi = res * (1.f + 1e-3f);
+    if (!(fx >= lo) || !(fx <= hi) || !(fy >= lo) || !(fy <= hi) || !(fz >= lo) || !(fz <= hi)) return 0;
+    const int bx = min(res - 1, max(0, (int)floorf(fx)));
+    const int by = min(res - 1, max(0, (int)floorf(fy)));
+    const int bz = min(res - 1, max(0, (int)floorf(fz)));
+    for (int pass = 0; pass < 2; pass++) {
+        int best = 0x7FFFFFFF;
+        for (int z = max(0, bz - pass); z <= min(res - 1, bz + pass); z++)
+            for (int y = max(0, by - pass); y <= min(res - 1, by + pass); y++)
+                for (int x = max(0, bx - pass); x <= min(res - 1, bx + pass); x++) {
+                    const size_t cell = ((size_t)z * res + y) * res + x;
+                    const unsigned k1 = __ldg(S.loc_start + cell + 1);
+                    for (unsigned k = __ldg(S.loc_start + cell); k < k1; k++) {
+                        const int e = (int)__ldg(S.loc_items + k);
+                        if (e < best && src_encloses(S, e, px, py, pz)) best = e;
+                    }
+                }
+        if (best != 0x7FFFFFFF) return best + 1;
+    }
+    return 0;
+}
+
+// Sets the launch state of a new photon (position, direction, weight, first
+// scattering length, element, label), following the reference's CPU launch
+// (launchphoton, src/mmc_raytrace.c:2346-2671; the device version,
+// src/mmc_core.cl:1416-1834, differs only where noted in the oracle).  A
+// source whose launch position varies is located per photon: the initial
+// element first, then the bounding-box grid.  Returns false when no element
+// encloses the launch position.
+template <class MP>
+__device__ __forceinline__ bool launch_photon(Lane& L, const SimDev& S) {
+    L.px = S.srcpos[0];
+    L.py = S.srcpos[1];
+    L.pz = S.srcpos[2];
+    L.vx = S.srcdir[0];
+    L.vy = S.srcdir[1];
+    L.vz = S.srcdir[2];
+    L.weight = 1.f;
+    L.eid = S.e0;
+    float ox = L.px, oy = L.py, oz = L.pz;  // origin: the focus is measured from here
+    bool canfocus = true;
+    L.slen = -MP::log(rng_next(L.t0, L.t1) + kEps);
+    const float4 p1 = S.srcp1, p2 = S.srcp2;
+    const int st = S.srctype;
+    if (st == ST_PENCIL) {
+        if (L.eid > 0) {
+            L.label = __ldg(S.label + (L.eid - 1));
+            return true;
+        }
+    } else if (st == ST_PLANAR || st == ST_PATTERN || st == ST_PATTERN3D || st == ST_FOURIER || st == ST_PENCILARRAY) {
+        const float rx = rng_next(L.t0, L.t1);
+        const float ry = rng_next(L.t0, L.t1);
+        if (st == ST_PATTERN3D) {
+            const float rz = rng_next(L.t0, L.t1);
+            L.px = S.srcpos[0] + rx * p1.x;
+            L.py = S.srcpos[1] + ry * p1.y;
+            L.pz = S.srcpos[2] + rz * p1.z;
+            const int nx = (int)p1.x, ny = (int)p1.y, nz = (int)p1.z;
+            const int ix = min((int)(rx * nx), nx - 1), iy = min((int)(ry * ny), ny - 1),
+                      iz = min((int)(rz * nz), nz - 1);
+            L.weight = __ldg(S.srcpattern + ((size_t)iz * ny + iy) * nx + ix);
+            ox += p1.x * 0.5f;
+            oy += p1.y * 0.5f;
+            oz += p1.z * 0.5f;
+        } else if (st == ST_PENCILARRAY) {
+            const float fx = floorf(rx * p1.w), fy = floorf(ry * p2.w);
+            L.px = S.srcpos[0] + fx * p1.x / (p1.w - 1.f) + fy * p2.x / (p2.w - 1.f);
+            L.py = S.srcpos[1] + fx * p1.y / (p1.w - 1.f) + fy * p2.y / (p2.w - 1.f);
+            L.pz = S.srcpos[2] + fx * p1.z / (p1.w - 1.f) + fy * p2.z / (p2.w - 1.f);
+            ox += (p1.x + p2.x) * 0.5f;
+            oy += (p1.y + p2.y) * 0.5f;
+            oz += (p1.z + p2.z) * 0.5f;
+        } else {
+            L.px = S.srcpos[0] + rx * p1.x + ry * p2.x;
+            L.py = S.srcpos[1] + rx * p1.y + ry * p2.y;
+            L.pz = S.srcpos[2] + rx * p1.z + ry * p2.z;
+            if (st == ST_PATTERN) {
+                const int nx = (int)p1.w, ny = (int)p2.w;
+                const int idx = min((int)(ry * ny), ny - 1) * nx + min((int)(rx * nx), nx - 1);
+                L.weight = __ldg(S.srcpattern + idx);
+            } else if (st == ST_FOURIER) {
+                float sv, cv;
+                MP::sincos2pi(floorf(p1.w) * rx + floorf(p2.w) * ry + p1.w - floorf(p1.w), sv, cv);
+                L.weight = (cv * (1.f - p2.w + floorf(p2.w)) + 1.f) * 0.5f;
+            }
+            ox += (p1.x + p2.x) * 0.5f;
+            oy += (p1.y + p2.y) * 0.5f;
+            oz += (p1.z + p2.z) * 0.5f;
+        }
+    } else if (st == ST_FOURIERX || st == ST_FOURIER2D) {
+        const float rx = rng_next(L.t0, L.t1);
+        const float ry = rng_next(L.t0, L.t1);
+        const float w = p1.w * (1.f / sqrtf(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z));
+        const float v2x = w * (S.srcdir[1] * p1.z - S.srcdir[2] * p1.y);
+        const float v2y = w * (S.srcdir[2] * p1.x - S.srcdir[0] * p1.z);
+        const float v2z = w * (S.srcdir[0] * p1.y - S.srcdir[1] * p1.x);
+        L.px = S.srcpos[0] + rx * p1.x + ry * v2x;
+        L.py = S.srcpos[1] + rx * p1.y + ry * v2y;
+        L.pz = S.srcpos[2] + rx * p1.z + ry * v2z;
+        float s1, c1, s2, c2;
+        if (st == ST_FOURIER2D) {
+            MP::sincos2pi(p2.x * rx + p2.z, s1, c1);
+            MP::sincos2pi(p2.y * ry + p2.w, s2, c2);
+            L.weight = (s1 * s2 + 1.f) * 0.5f;
+        } else {
+            MP::sincos2pi(p2.x * rx + p2.y * ry + p2.z, s1, c1);
+            L.weight = (c1 * (1.f - p2.w) + 1.f) * 0.5f;
+        }
+        ox += (p1.x + v2x) * 0.5f;
+        oy += (p1.y + v2y) * 0.5f;
+        oz += (p1.z + v2z) * 0.5f;
+    } else if (st == ST_DISK || st == ST_RING || st == ST_GAUSSIAN) {
+        float sphi, cphi;
+        if (st == ST_RING && (p1.z > 0.f || p1.w > 0.f)) {  // azimuth range [min, max] in radians
+            const float phi = fabsf(p1.z - p1.w) * rng_next(L.t0, L.t1) + fminf(p1.z, p1.w);
+            MP::sincos2pi(phi * (0.5f / kPi), sphi, cphi);
+        } else {
+            MP::sincos2pi(rng_next(L.t0, L.t1), sphi, cphi);
+        }
+        float r0;
+        if (st == ST_DISK || st == ST_RING) {  // radii p1.y (inner) to p1.x (outer), uniform in area
+            r0 = sqrtf(rng_next(L.t0, L.t1) * fabsf(p1.x * p1.x - p1.y * p1.y) + p1.y * p1.y);
+        } else if (fabsf(S.focus) < 1e-5f || fabsf(p1.y) < 1e-5f) {  // waist p1.x
+            // (+EPS: a draw of exactly 0 would put the photon at infinity)
+            r0 = sqrtf(-MP::log(rng_next(L.t0, L.t1) + kEps)) * p1.x;
+        } else {  // waist p1.x, wavelength p1.y, focus: widened by the Rayleigh range
+            const float z0 = p1.x * p1.x * kPi / p1.y;
+            r0 = sqrtf(-MP::log(rng_next(L.t0, L.t1) + kEps) * (1.f + (S.focus * S.focus / (z0 * z0)))) * p1.x;
+        }
+        const float dx = S.srcdir[0], dy = S.srcdir[1], dz = S.srcdir[2];
+        if (dz > -1.f + kEps && dz < 1.f - kEps) {
+            const float tmp0 = 1.f - dz * dz;
+            const float tmp1 = r0 / sqrtf(tmp0);
+            L.px = S.srcpos[0] + tmp1 * (dx * dz * cphi - dy * sphi);
+            L.py = S.srcpos[1] + tmp1 * (dy * dz * cphi + dx * sphi);
+            L.pz = S.srcpos[2] - tmp1 * tmp0 * cphi;
+        } else {
+            L.px += r0 * cphi;
+            L.py += r0 * sphi;
+        }
+    } else if (st == ST_CONE || st == ST_ISOTROPIC || st == ST_ARCSINE) {
+        float sphi, cphi, stheta, ctheta;
+        MP::sincos2pi(rng_next(L.t0, L.t1), sphi, cphi);
+        if (st == ST_CONE) {
+            // polar angle within the half angle p1.x: uniform in angle (p1.y > 0) or in solid
+            // angle, sampled by inversion instead of the reference's rejection loop
+            const float u = rng_next(L.t0, L.t1);
+            if (p1.y > 0.f) {
+                MP::sincos2pi(u * p1.x * (0.5f / kPi), stheta, ctheta);
+            } else {
+                float sa, ca;
+                MP::sincos2pi(p1.x * (0.5f / kPi), sa, ca);
+                ctheta = 1.f - u * (1.f - ca);
+                stheta = sqrtf(fmaxf(0.f, 1.f - ctheta * ctheta));
+            }
+        } else if (st == ST_ISOTROPIC) {  // cos(acos(2u-1)) = 2u-1
+            ctheta = 2.f * rng_next(L.t0, L.t1) - 1.f;
+            stheta = sqrtf(fmaxf(0.f, 1.f - ctheta * ctheta));
+        } else {  // arcsine: polar angle uniform in [0, pi)
+            MP::sincos2pi(0.5f * rng_next(L.t0, L.t1), stheta, ctheta);
+        }
+        rotate_dir<MP>(L, stheta, ctheta, sphi, cphi);
+        canfocus = false;
+        if (L.eid > 0) {
+            L.label = __ldg(S.label + (L.eid - 1));
+            return true;
+        }
+    } else if (st == ST_ZGAUSSIAN) {  // polar angle Gaussian with sigma p1.x
+        float sphi, cphi, stheta, ctheta;
+        MP::sincos2pi(rng_next(L.t0, L.t1), sphi, cphi);
+        const float u1 = rng_next(L.t0, L.t1);
+        const float u2 = rng_next(L.t0, L.t1);
+        const float ang = sqrtf(-2.f * MP::log(u1 + kEps)) * (1.f - 2.f * u2) * p1.x;
+        MP::sincos2pi(ang * (0.5f / kPi), stheta, ctheta);
+        rotate_dir<MP>(L, stheta, ctheta, sphi, cphi);
+        canfocus = false;
+    } else if (st == ST_HYPERBOLOID) {  // hyperboloid Gaussian beam: waist p1.x, p1.y/p1.z tilt
+        float sphi, cphi;
+        MP::sincos2pi(rng_next(L.t0, L.t1), sphi, cphi);
+        const float r0 = sqrtf(0.5f * -MP::log(rng_next(L.t0, L.t1) + kEps)) * p1.x;
+        const float tilt = (p1.z > 0.f) ? (-p1.y / p1.z) : 0.f;
+        float bx = -r0 * sphi, by = r0 * cphi, bz = p1.z;
+        const float nb = 1.f / sqrtf(bx * bx + by * by + bz * bz);
+        bx *= nb;
+        by *= nb;
+        bz *= nb;
+        const float qx = r0 * (cphi - tilt * sphi), qy = r0 * (sphi + tilt * cphi);
+        const float dx = S.srcdir[0], dy = S.srcdir[1], dz = S.srcdir[2];
+        if (dz > -1.f + kEps && dz < 1.f - kEps) {
+            const float sint = sqrtf(1.f - dz * dz);
+            const float isint = 1.f / sint;
+            const float cb = dx * isint, sb = dy * isint;
+            L.px = S.srcpos[0] + qx * cb * dz - qy * sb;
+            L.py = S.srcpos[1] + qx * sb * dz + qy * cb;
+            L.pz = S.srcpos[2] - qx * sint;
+            L.vx = bx * cb * dz - by * sb + bz * cb * sint;
+            L.vy = bx * sb * dz + by * cb + bz * sb * sint;
+            L.vz = -bx * sint + bz * dz;
+        } else {
+            L.px = S.srcpos[0] + qx;
+            L.py = S.srcpos[1] + qy;
+            L.pz = S.srcpos[2];
+            L.vx = bx;
+            L.vy = by;
+            L.vz = (dz > 0.f) ? bz : -bz;
+        }
+        const float nv = 1.f / sqrtf(L.vx * L.vx + L.vy * L.vy + L.vz * L.vz);
+        L.vx *= nv;
+        L.vy *= nv;
+        L.vz *= nv;
+        canfocus = false;
+    } else if (st == ST_LINE || st == ST_SLIT) {  // segment srcpos .. srcpos + p1.xyz
+        float t = rng_next(L.t0, L.t1);
+        L.px += t * p1.x;
+        L.py += t * p1.y;
+        L.pz += t * p1.z;
+        if (st == ST_LINE) {  // direction perpendicular to the launch direction, random
+            t = 1.f - 2.f * rng_next(L.t0, L.t1);
+            const float s = 1.f - 2.f * rng_next(L.t0, L.t1);
+            const float sign = (rng_next(L.t0, L.t1) > 0.5f) ? 1.f : -1.f;
+            const float p = sqrtf(1.f - L.vx * L.vx - L.vy * L.vy) * sign;
+            const float vx = L.vy * p - L.vz * s, vy = L.vz * t - L.vx * p, vz = L.vx * s - L.vy * t;
+            L.vx = vx;
+            L.vy = vy;
+            L.vz = vz;
+        }
+        ox += p1.x * 0.5f;
+        oy += p1.y * 0.5f;
+        oz += p1.z * 0.5f;
+        canfocus = (st == ST_SLIT);
+    }
+    if (canfocus) {
+        const float f = S.focus;
+        if (f != f) {  // NaN: a uniformly random direction about the launch direction
+            float sphi, cphi;
+            MP::sincos2pi(rng_next(L.t0, L.t1), sphi, cphi);
+            const float ctheta = 2.f * rng_next(L.t0, L.t1) - 1.f;
+            rotate_dir<MP>(L, sqrtf(fmaxf(0.f, 1.f - ctheta * ctheta)), ctheta, sphi, cphi);
+        } else if (f < 0.f && isinf(f)) {  // -inf: Lambertian (cosine) emission
+            float sphi, cphi;
+            MP::sincos2pi(rng_next(L.t0, L.t1), sphi, cphi);
+            const float stheta = sqrtf(rng_next(L.t0, L.t1));
+            rotate_dir<MP>(L, stheta, sqrtf(1.f - stheta * stheta), sphi, cphi);
+        } else if (f != 0.f) {  // converging (f > 0) or diverging (f < 0) beam
+            ox += f * L.vx;
+            oy += f * L.vy;
+            oz += f * L.vz;
+            float vx, vy, vz;
+            if (f < 0.f) {
+                vx = L.px - ox;
+                vy = L.py - oy;
+                vz = L.pz - oz;
+            } else {
+                vx = ox - L.px;
+                vy = oy - L.py;
+                vz = oz - L.pz;
+            }
+            const float rn = 1.f / sqrtf(vx * vx + vy * vy + vz * vz);
+            L.vx = vx * rn;
+            L.vy = vy * rn;
+            L.vz = vz * rn;
+        }
+    }
+    L.px = L.px + L.vx * kEps;
+    L.py = L.py + L.vy * kEps;
+    L.pz = L.pz + L.vz * kEps;
+    int e = 0;
+    if (L.eid > 0 && src_encloses(S, L.eid - 1, L.px, L.py, L.pz)) e = L.eid;
+    else if (S.loc_start) e = src_locate(S, L.px, L.py, L.pz);
+    if (e <= 0) return false;
+    L.eid = e;
+    L.label = __ldg(S.label + (e - 1));
+    return true;
+}
+
 struct Tally {
     float eesc;
+    float etot;
     unsigned raytet;
     unsigned aborted;
+    unsigned outside;
     int sim;
 };
 
 __device__ __forceinline__ void flush_tally(Tally& t, const SimDev& S) {
     if (t.sim < 0) return;
+    if (t.etot != 0.f) atomicAdd(S.energy + 0, (double)t.etot);
     if (t.eesc != 0.f) atomicAdd(S.energy + 1, (double)t.eesc);
     if (t.raytet) atomicAdd(S.counters + 0, (unsigned long long)t.raytet);
     if (t.aborted) atomicAdd(S.counters + 1, (unsigned long long)t.aborted);
+    if (t.outside && S.ncounters > 2) atomicAdd(S.counters + 2, (unsigned long long)t.outside);
+    t.etot = 0.f;
     t.eesc = 0.f;
     t.raytet = 0;
     t.aborted = 0;
+    t.outside = 0;
 }
 
 struct SingleSim {
@@ -400,7 +730,7 @@ struct ManySims {
 
 // Shared-memory layout: media[nsims_local * nmed_stride] | ppath[reclen_max][blockDim] |
 // seed0[2][blockDim] (u64)
-template <class MP, class Sims, bool BATCHED, bool PHASED, bool REPLAY>
+template <class MP, class Sims, bool BATCHED, bool PHASED, bool REPLAY, bool SRC>
 __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned long long* cum, int nsims,
                                             unsigned long long total, int nmed_stride, int reclen_max,
                                             int want_seed, unsigned long long* work_counter, const PhaseArgs& pa) {
@@ -425,7 +755,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
     L.sim = 0;
     L.pid = 0;
     L.steps = 0;
-    Tally tally{0.f, 0u, 0u, -1};
+    Tally tally{0.f, 0.f, 0u, 0u, 0u, -1};
 
 #define PP(i) ppath[(i) * bdim + tid]
 
@@ -514,18 +844,9 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                         seed0[tid] = L.t0;
                         seed0[bdim + tid] = L.t1;
                     }
-                    L.px = S.srcpos[0];
-                    L.py = S.srcpos[1];
-                    L.pz = S.srcpos[2];
-                    L.vx = S.srcdir[0];
-                    L.vy = S.srcdir[1];
-                    L.vz = S.srcdir[2];
-                    L.eid = S.e0;
-                    L.label = __ldg(S.label + (S.e0 - 1));
                     L.faceid = 0;
                     L.isend = 0;
                     L.hit = 0;
-                    L.weight = 1.f;
                     L.ptime = 0.f;
                     L.Lmove = 0.f;
                     L.slen0 = 0.f;
@@ -533,12 +854,37 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                     L.oldidx = (unsigned)kIdUndef;
                     L.fixcount = 0;
                     L.steps = 0;
-                    L.slen = -MP::log(rng_next(L.t0, L.t1) + kEps);
+                    bool placed;
+                    if (!SRC || (S.srctype == ST_PENCIL && S.e0 > 0)) {  // the pencil branch of launch_photon
+                        L.px = S.srcpos[0];
+                        L.py = S.srcpos[1];
+                        L.pz = S.srcpos[2];
+                        L.vx = S.srcdir[0];
+                        L.vy = S.srcdir[1];
+                        L.vz = S.srcdir[2];
+                        L.weight = 1.f;
+                        L.eid = S.e0;
+                        L.slen = -MP::log(rng_next(L.t0, L.t1) + kEps);
+                        L.label = __ldg(S.label + (S.e0 - 1));
+                        placed = true;
+                    } else {
+                        placed = launch_photon<MP>(L, S);
+                    }
+                    tally.etot += L.weight;
                     if (S.issavedet) {
                         for (int i = 0; i < S.reclen; i++) PP(i) = 0.f;
                         PP(S.reclen - 1) = L.weight;
                     }
-                    L.mode = M_OUTER;
+                    if (placed) {
+                        L.mode = M_OUTER;
+                    } else {  // launch position in no element: counted, reported as an error
+                        tally.outside++;
+                        tally.eesc += L.weight;
+                        if (S.photon_det) S.photon_det[L.pid] = 0;
+                        if (S.photon_weight) S.photon_weight[L.pid] = L.weight;
+                        if (S.photon_steps) S.photon_steps[L.pid] = 0;
+                        L.mode = M_NEED;
+                    }
                     }
                 }
             }
@@ -781,17 +1127,17 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
     if (tally.sim >= 0) flush_tally(tally, sims(tally.sim));
 }
 
-template <class MP, bool REPLAY>
+template <class MP, bool REPLAY, bool SRC>
 __global__ void __launch_bounds__(128, 8) photon_engine_plain(const __grid_constant__ SimDev sim,
                                                               unsigned long long* work_counter, int reclen_max,
                                                               int want_seed) {
     SingleSim acc{sim};
     const PhaseArgs none{};
-    engine_body<MP, SingleSim, false, false, REPLAY>(acc, nullptr, 1, sim.nphoton, sim.nmedia, reclen_max,
-                                                     want_seed, work_counter, none);
+    engine_body<MP, SingleSim, false, false, REPLAY, SRC>(acc, nullptr, 1, sim.nphoton, sim.nmedia, reclen_max,
+                                                          want_seed, work_counter, none);
 }
 
-template <class MP>
+template <class MP, bool SRC>
 __global__ void __launch_bounds__(128, 8) photon_engine_phased(const __grid_constant__ SimDev sim,
                                                                const __grid_constant__ PhaseArgs pa,
                                                                unsigned long long* work_counter, int reclen_max,
@@ -800,11 +1146,11 @@ __global__ void __launch_bounds__(128, 8) photon_engine_phased(const __grid_cons
     // gate 0 launches the run's photons; later gates resume the ones parked by the previous launch
     unsigned long long total = sim.nphoton;
     if (pa.phase > 0) total = min(*pa.in.count, pa.cap);
-    engine_body<MP, SingleSim, false, true, false>(acc, nullptr, 1, total, sim.nmedia, reclen_max, want_seed,
-                                                   work_counter, pa);
+    engine_body<MP, SingleSim, false, true, false, SRC>(acc, nullptr, 1, total, sim.nmedia, reclen_max, want_seed,
+                                                        work_counter, pa);
 }
 
-template <class MP, bool REPLAY>
+template <class MP, bool SRC>
 __global__ void __launch_bounds__(128, 8) photon_engine_batched(const SimDev* __restrict__ sims,
                                                                 const unsigned long long* __restrict__ cum,
                                                                 int nsims, unsigned long long total,
@@ -812,8 +1158,8 @@ __global__ void __launch_bounds__(128, 8) photon_engine_batched(const SimDev* __
                                                                 int reclen_max, int want_seed) {
     ManySims acc{sims};
     const PhaseArgs none{};
-    engine_body<MP, ManySims, true, false, REPLAY>(acc, cum, nsims, total, nmed_stride, reclen_max, want_seed,
-                                                   work_counter, none);
+    engine_body<MP, ManySims, true, false, true, SRC>(acc, cum, nsims, total, nmed_stride, reclen_max, want_seed,
+                                                      work_counter, none);
 }
 
 size_t smem_bytes(int nmed_rows, int reclen_max, int threads, int want_seed) {
@@ -823,6 +1169,11 @@ size_t smem_bytes(int nmed_rows, int reclen_max, int threads, int want_seed) {
     return b;
 }
 
+// Kernels compiled with the general source launch (SRC) serve simulations
+// whose source is not a pencil beam starting in a known element; the others
+// carry only the pencil launch, which keeps the step loop's registers free.
+bool general_source(const SimDev& s) { return s.srctype != ST_PENCIL || s.e0 <= 0; }
+
 }  // namespace
 
 LaunchShape default_shape(int device, bool batched) {
@@ -831,39 +1182,48 @@ LaunchShape default_shape(int device, bool batched) {
     int per_sm = 0;
     const int threads = 128;
     if (batched)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_batched<FastMath, true>, threads, 4096);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_batched<FastMath, false>, threads, 4096);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_plain<FastMath, false>, threads, 1024);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_plain<FastMath, false, false>, threads,
+                                                      1024);
     if (per_sm < 1) per_sm = 1;
     return LaunchShape{sms * per_sm, threads};
 }
 
-template <class MP, bool REPLAY>
+template <class MP, bool REPLAY, bool SRC>
 static cudaError_t launch_plain_t(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
                                   cudaStream_t stream) {
     const int want_seed = (sim.issavedet && sim.seeds) ? 1 : 0;
     const int reclen_max = sim.issavedet ? sim.reclen : 0;
     const size_t smem = smem_bytes(sim.nmedia, reclen_max, shape.threads, want_seed);
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(photon_engine_plain<MP, REPLAY>,
+        cudaError_t e = cudaFuncSetAttribute(photon_engine_plain<MP, REPLAY, SRC>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     (void)cudaGetLastError();  // the launch check below must see this launch's status only
-    photon_engine_plain<MP, REPLAY><<<shape.blocks, shape.threads, smem, stream>>>(sim, work_counter, reclen_max,
-                                                                                  want_seed);
+    photon_engine_plain<MP, REPLAY, SRC><<<shape.blocks, shape.threads, smem, stream>>>(sim, work_counter,
+                                                                                       reclen_max, want_seed);
     return cudaGetLastError();
 }
 
 cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
                          cudaStream_t stream) {
-    if (sim.replay)
-        return sim.fast_math ? launch_plain_t<FastMath, true>(sim, work_counter, shape, stream)
-                             : launch_plain_t<ExactMath, true>(sim, work_counter, shape, stream);
-    return sim.fast_math ? launch_plain_t<FastMath, false>(sim, work_counter, shape, stream)
-                         : launch_plain_t<ExactMath, false>(sim, work_counter, shape, stream);
+    const bool src = general_source(sim);
+    if (sim.replay) {
+        if (src)
+            return sim.fast_math ? launch_plain_t<FastMath, true, true>(sim, work_counter, shape, stream)
+                                 : launch_plain_t<ExactMath, true, true>(sim, work_counter, shape, stream);
+        return sim.fast_math ? launch_plain_t<FastMath, true, false>(sim, work_counter, shape, stream)
+                             : launch_plain_t<ExactMath, true, false>(sim, work_counter, shape, stream);
+    }
+    if (src)
+        return sim.fast_math ? launch_plain_t<FastMath, false, true>(sim, work_counter, shape, stream)
+                             : launch_plain_t<ExactMath, false, true>(sim, work_counter, shape, stream);
+    return sim.fast_math ? launch_plain_t<FastMath, false, false>(sim, work_counter, shape, stream)
+                         : launch_plain_t<ExactMath, false, false>(sim, work_counter, shape, stream);
 }
 
 size_t phase_bytes_per_photon(const SimDev& sim) {
@@ -872,7 +1232,7 @@ size_t phase_bytes_per_photon(const SimDev& sim) {
                 (want_seed ? 2 * sizeof(unsigned long long) : 0));
 }
 
-template <class MP>
+template <class MP, bool SRC>
 static cudaError_t launch_phased_t(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
                                    cudaStream_t stream, const PhaseQueue q[2], int span, unsigned* order,
                                    unsigned* bscratch, const float lo[3], const float hi[3]) {
@@ -880,7 +1240,8 @@ static cudaError_t launch_phased_t(const SimDev& sim, unsigned long long* work_c
     const int reclen_max = sim.issavedet ? sim.reclen : 0;
     const size_t smem = smem_bytes(sim.nmedia, reclen_max, shape.threads, want_seed);
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(photon_engine_phased<MP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(photon_engine_phased<MP, SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
         if (e != cudaSuccess) return e;
     }
     span = std::max(1, span);
@@ -903,8 +1264,8 @@ static cudaError_t launch_phased_t(const SimDev& sim, unsigned long long* work_c
         if (e == cudaSuccess) e = cudaMemsetAsync(bscratch, 0, sizeof(unsigned) * kBuckets, stream);
         if (e != cudaSuccess) return e;
         (void)cudaGetLastError();
-        photon_engine_phased<MP><<<shape.blocks, shape.threads, smem, stream>>>(sim, pa, work_counter, reclen_max,
-                                                                               want_seed);
+        photon_engine_phased<MP, SRC><<<shape.blocks, shape.threads, smem, stream>>>(sim, pa, work_counter,
+                                                                                    reclen_max, want_seed);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if (!pa.last && order) {  // resume order of the photons just parked
             k_bucket_scan<<<1, 1024, 0, stream>>>(bscratch, bscratch + kBuckets);
@@ -919,18 +1280,22 @@ static cudaError_t launch_phased_t(const SimDev& sim, unsigned long long* work_c
 cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
                           cudaStream_t stream, const PhaseQueue q[2], int span, unsigned* order,
                           unsigned* bscratch, const float lo[3], const float hi[3]) {
+    if (general_source(sim))
+        return sim.fast_math
+                   ? launch_phased_t<FastMath, true>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi)
+                   : launch_phased_t<ExactMath, true>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi);
     return sim.fast_math
-               ? launch_phased_t<FastMath>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi)
-               : launch_phased_t<ExactMath>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi);
+               ? launch_phased_t<FastMath, false>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi)
+               : launch_phased_t<ExactMath, false>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi);
 }
 
-template <class MP>
+template <class MP, bool SRC>
 static cudaError_t launch_batched_t(const SimDev* sims, const unsigned long long* cum, int nsims,
                                     unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
                                     unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream) {
     const size_t smem = smem_bytes(nsims * nmed_stride, reclen_max, shape.threads, want_seed);
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(photon_engine_batched<MP, true>,
+        cudaError_t e = cudaFuncSetAttribute(photon_engine_batched<MP, SRC>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
@@ -938,18 +1303,24 @@ static cudaError_t launch_batched_t(const SimDev* sims, const unsigned long long
     if (e != cudaSuccess) return e;
     (void)cudaGetLastError();  // the launch check below must see this launch's status only
     // batches may mix forward and replay simulations: the batched kernel keeps the replay branches
-    photon_engine_batched<MP, true><<<shape.blocks, shape.threads, smem, stream>>>(
+    photon_engine_batched<MP, SRC><<<shape.blocks, shape.threads, smem, stream>>>(
         sims, cum, nsims, total, nmed_stride, work_counter, reclen_max, want_seed);
     return cudaGetLastError();
 }
 
 cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
                            unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
-                           unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream, int fast_math) {
-    return fast_math ? launch_batched_t<FastMath>(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
-                                                  work_counter, shape, stream)
-                     : launch_batched_t<ExactMath>(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
-                                                   work_counter, shape, stream);
+                           unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream, int fast_math,
+                           int general_src) {
+    if (general_src)
+        return fast_math ? launch_batched_t<FastMath, true>(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
+                                                            work_counter, shape, stream)
+                         : launch_batched_t<ExactMath, true>(sims, cum, nsims, total, nmed_stride, reclen_max,
+                                                             want_seed, work_counter, shape, stream);
+    return fast_math ? launch_batched_t<FastMath, false>(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
+                                                         work_counter, shape, stream)
+                     : launch_batched_t<ExactMath, false>(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
+                                                          work_counter, shape, stream);
 }
 
 }  // namespace mmcgb

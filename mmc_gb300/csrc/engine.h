@@ -53,9 +53,19 @@ struct SimDev {
     unsigned long long photon_offset;
     unsigned long long seed;
     unsigned long long step_budget;
-    // source
+    // source (the reference's TSrcType codes, src/mmc_utils.h:101-105)
     float srcpos[3];
     float srcdir[3];
+    int srctype;
+    float4 srcp1, srcp2;   // srcparam1, srcparam2
+    float focus;
+    const float* srcpattern;
+    // bounding-box grid of the mesh (per-photon source element search):
+    // cell (x,y,z) lists the elements whose bounding boxes overlap it
+    const unsigned* loc_start;  // res^3 + 1 offsets
+    const unsigned* loc_items;  // 0-based element ids
+    int loc_res;
+    float loc_lo[3], loc_inv[3];
     // time gates
     float tstart, tend, Rtstep;
     int maxgate;
@@ -82,8 +92,9 @@ struct SimDev {
     unsigned long long* seeds;  // maxdet * 2
     unsigned int* detcount;
     unsigned int maxdet;
-    double* energy;        // [0] launched, [1] escaped
-    unsigned long long* counters;  // [0] ray-tet tests, [1] aborted photons
+    double* energy;        // [0] launched weight, [1] escaped weight
+    unsigned long long* counters;  // [0] ray-tet tests, [1] aborted photons, [2] photons launched outside
+    int ncounters;         // entries of `counters` (2 for callers that give two)
     // optional per-photon trace (parity tests)
     float* photon_weight;
     unsigned int* photon_steps;
@@ -158,7 +169,7 @@ cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, La
 cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
                            unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
                            unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream,
-                           int fast_math);
+                           int fast_math, int general_src);
 LaunchShape default_shape(int device, bool batched);
 
 // Records the message returned by mmcgb_last_error() on this thread.

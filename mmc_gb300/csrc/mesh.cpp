@@ -90,8 +90,12 @@ int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
     m.nvol.assign(d.nn, 0.f);
     int maxlabel = 0;
     for (int i = 0; i < d.ne; i++) {
+        // -1 marks the reference's source-element candidates, which it then treats as
+        // void (mesh_srcdetelem, src/mmc_mesh.c:390-425); sources are located here by a
+        // search over all elements, so such a tet is simply void
+        if (m.label[i] == -1) m.label[i] = 0;
         if (m.label[i] < 0 || m.label[i] > 255) {
-            err = "medium labels must be in 0..255";
+            err = "medium labels must be in -1..255 (-2, wide-field detector elements, is not supported)";
             return MMCGB_E_MESH;
         }
         maxlabel = std::max(maxlabel, m.label[i]);

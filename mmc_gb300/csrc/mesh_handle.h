@@ -12,6 +12,8 @@ struct mmcgb_mesh {
     float4* node = nullptr;
     int* label = nullptr;
     float* evol = nullptr;
+    unsigned* loc_start = nullptr;  // bounding-box grid (HostMesh::grid) on the device
+    unsigned* loc_items = nullptr;
     float lo[3] = {0.f, 0.f, 0.f};  // bounding box of the nodes
     float hi[3] = {0.f, 0.f, 0.f};
 };

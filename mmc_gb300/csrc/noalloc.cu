@@ -79,7 +79,8 @@ extern "C" int32_t mmcgb_simulate_noalloc(mmcgb_mesh* mesh, const mmcgb_config* 
     using namespace mmcgb;
     if (!mesh || !c || !out) return fail(MMCGB_E_ARG, "null argument");
     if (!out->field_raw || !out->energy || !out->counters) return fail(MMCGB_E_ARG, "field_raw, energy and counters are required");
-    if (c->srctype != 0) return fail(MMCGB_E_ARG, "only the pencil source (srctype 0) is implemented");
+    if (!(c->srctype == 0 || c->srctype == 1 || c->srctype == 2 || c->srctype == 7))
+        return fail(MMCGB_E_ARG, "no-alloc entry: point sources only (pencil, isotropic, cone, arcsine)");
     if (!(c->tstep > 0.f) || !(c->tend > c->tstart)) return fail(MMCGB_E_ARG, "time gates need tstep > 0 and tend > tstart");
     if (c->nmedia < 2 || !c->media) return fail(MMCGB_E_ARG, "media table needs at least 2 rows");
     if (c->nmedia > kNoAllocMaxMedia)
@@ -142,6 +143,10 @@ extern "C" int32_t mmcgb_simulate_noalloc(mmcgb_mesh* mesh, const mmcgb_config* 
         S.srcpos[k] = c->srcpos[k];
         S.srcdir[k] = c->srcdir[k];
     }
+    S.srctype = c->srctype;
+    S.srcp1 = make_float4(c->srcparam1[0], c->srcparam1[1], c->srcparam1[2], c->srcparam1[3]);
+    S.srcp2 = make_float4(c->srcparam2[0], c->srcparam2[1], c->srcparam2[2], c->srcparam2[3]);
+    S.focus = c->focus;
     S.tstart = c->tstart;
     S.tend = c->tstart + c->tstep * (float)maxgate;
     S.Rtstep = 1.f / c->tstep;
@@ -169,6 +174,7 @@ extern "C" int32_t mmcgb_simulate_noalloc(mmcgb_mesh* mesh, const mmcgb_config* 
     S.maxdet = c->issavedet ? c->maxdetphoton : 0;
     S.energy = out->energy;
     S.counters = reinterpret_cast<unsigned long long*>(out->counters);
+    S.ncounters = 2;
 
     LaunchShape shape = default_shape(mesh->device, false);
     if (c->threads > 0) shape.threads = std::max(32, std::min(c->threads, 128) / 32 * 32);

@@ -19,7 +19,7 @@ from typing import Optional
 
 import numpy as np
 
-from .core import SimConfig
+from .core import SOURCE_TYPES, SimConfig
 
 MCH_HEADER = struct.Struct("<4sIIIIIIIfIfIiI2i")  # 64 bytes
 OUTPUT_LETTERS = {"x": "flux", "f": "fluence", "e": "energy", "j": "jacobian", "l": "wl", "p": "wp", "n": "wn"}
@@ -98,11 +98,17 @@ def load_input(path: str):
     detpos = None
     if dets:
         detpos = np.array([[*d["Pos"][:3], d.get("R", 1.0)] for d in dets], np.float32)
-    srcdir = np.asarray(src.get("Dir", [0.0, 0.0, 1.0]), np.float64)[:3]
+    dir4 = [float(x) for x in src.get("Dir", [0.0, 0.0, 1.0])]
+    srcdir = np.asarray(dir4[:3], np.float64)
     srcdir = srcdir / np.linalg.norm(srcdir)
-    stype = str(src.get("Type", "pencil")).lower()
-    if stype not in ("pencil", ""):
-        raise ValueError(f"source type '{stype}' is not implemented (pencil only)")
+    focus = dir4[3] if len(dir4) > 3 else 0.0
+    stype = str(src.get("Type", "pencil")).lower() or "pencil"
+    if stype not in SOURCE_TYPES:
+        raise ValueError(f"unknown source type '{stype}'")
+    pattern = src.get("Pattern")
+    if isinstance(pattern, dict):
+        pattern = pattern.get("Data")
+    pattern = None if pattern is None else np.asarray(pattern, np.float32).ravel()
     t0 = float(fwd.get("T0", 0.0))
     t1 = float(fwd.get("T1", 5e-9))
     dt = float(fwd.get("Dt", t1 - t0))
@@ -111,6 +117,9 @@ def load_input(path: str):
     cfg = SimConfig(
         media=media, nphoton=int(float(ses.get("Photons", 1e6))), seed=int(ses.get("RNGSeed", 0x623F9A9E)),
         srcpos=tuple(float(x) for x in src.get("Pos", [0, 0, 0])[:3]), srcdir=tuple(float(x) for x in srcdir),
+        srctype=stype, srcparam1=tuple(float(x) for x in (list(src.get("Param1", [])) + [0.0] * 4)[:4]),
+        srcparam2=tuple(float(x) for x in (list(src.get("Param2", [])) + [0.0] * 4)[:4]), focus=focus,
+        srcpattern=pattern,
         e0=int(msh.get("InitElem", 0)), tstart=t0, tend=t1, tstep=dt,
         isreflect=int(ses.get("DoMismatch", 1)), isspecular=int(ses.get("DoSpecular", 0)),
         issavedet=int(ses.get("DoPartialPath", 1 if dets else 0)), issaveseed=int(ses.get("DoSaveSeed", 0)),

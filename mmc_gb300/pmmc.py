@@ -15,7 +15,7 @@ import time
 import numpy as np
 
 from . import _native
-from .core import Mesh, SimConfig, simulate
+from .core import SOURCE_TYPES, Mesh, SimConfig, simulate
 
 _SCALARS_INT = ["nphoton", "isreflect", "isspecular", "ismomentum", "issaveexit", "issavedet", "issaveseed",
                 "basisorder", "isnormalized", "maxdetphoton", "voidtime", "e0"]
@@ -54,12 +54,22 @@ def _parse(cfg: dict):
     if _METHODS[method] is None:
         raise ValueError(f"method '{method}' is not implemented (use 'elem': branchless Badouel, element deposit)")
     srctype = str(cfg.get("srctype", "pencil")).lower()
-    if srctype != "pencil":
-        raise ValueError(f"srctype '{srctype}' is not implemented (pencil only)")
-    kw = dict(media=prop, srcpos=tuple(np.asarray(cfg["srcpos"], np.float64).ravel()[:3]))
+    if srctype not in SOURCE_TYPES:
+        raise ValueError(f"unknown srctype '{srctype}'")
+    kw = dict(media=prop, srcpos=tuple(np.asarray(cfg["srcpos"], np.float64).ravel()[:3]), srctype=srctype)
     if "srcdir" in cfg:
-        d = np.asarray(cfg["srcdir"], np.float64).ravel()[:3]
+        d4 = np.asarray(cfg["srcdir"], np.float64).ravel()
+        d = d4[:3]
         kw["srcdir"] = tuple(d / np.linalg.norm(d))
+        if d4.size > 3:
+            kw["focus"] = float(d4[3])
+    for k in ("srcparam1", "srcparam2"):
+        if k in cfg:
+            v = list(np.asarray(cfg[k], np.float64).ravel()) + [0.0] * 4
+            kw[k] = tuple(float(x) for x in v[:4])
+    if "srcpattern" in cfg:
+        # pmmc passes patterns as [Nx, Ny(, Nz)] arrays in Fortran order: x runs fastest
+        kw["srcpattern"] = np.asarray(cfg["srcpattern"], np.float32).ravel(order="F")
     for k in _SCALARS_INT:
         if k in cfg:
             kw[k] = int(cfg[k])

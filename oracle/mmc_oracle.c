@@ -20,6 +20,7 @@
 
 /* ---- constants (src/mmc_core.cl:330-360, src/mmc_mesh.h:66-74) ---- */
 #define O_EPS        1e-6f              /* EPS seen by the CUDA build: src/mmc_mesh.h:70 */
+#define O_PI         3.14159265358979323846f
 #define O_R_C0       3.335640951981520e-12f
 #define O_MAX_ACCUM  1000.f
 #define O_R_MIN_MUS  1e9f
@@ -292,11 +293,22 @@ int oracle_initelem(int nn, const float* node, int ne, const int* elem, const fl
 /* ======================================================================
  * photon engine
  * ====================================================================== */
+/* bounding-box grid over the mesh: cell (x,y,z) lists the elements whose
+ * bounding boxes overlap it, in index order (the CUDA library builds the same
+ * grid in its mesh preparation; the per-photon source search reads it) */
+typedef struct {
+    int res;
+    float lo[3], inv[3];
+    uint32_t* start;
+    uint32_t* items;
+} locgrid;
+
 typedef struct {
     int ne, nn, M;
     const float* node;
     const int* elem;
     const int* type;
+    const locgrid* grid;
     const int* facenb;
     const float* nrm;
     const oracle_cfg* cfg;
@@ -471,7 +483,7 @@ static void reflectray(engine* g, ray* r, int oldeid, int* eid, int faceid, uint
     r->vx *= inv; r->vy *= inv; r->vz *= inv;
 }
 
-/* direction update: src/mmc_core.cl:1307-1332 */
+/* direction update: src/mmc_core.cl:1345-1377 */
 static void rotatevector(ray* r, float stheta, float ctheta, float sphi, float cphi) {
     float px, py, pz;
     if (r->vz > -1.f + O_EPS && r->vz < 1.f - O_EPS) {
@@ -538,10 +550,326 @@ static int finddetector(const engine* g, const ray* r) {
     return 0;
 }
 
+static void grid_range(const float* node, const int* e, const locgrid* g, int b0[3], int b1[3]) {
+    float mn[3] = {1e30f, 1e30f, 1e30f}, mx[3] = {-1e30f, -1e30f, -1e30f};
+    for (int j = 0; j < 4; j++)
+        for (int d = 0; d < 3; d++) {
+            float v = node[3 * (size_t)(e[j] - 1) + d];
+            if (v < mn[d]) mn[d] = v;
+            if (v > mx[d]) mx[d] = v;
+        }
+    for (int d = 0; d < 3; d++) {
+        int a = (int)floorf((mn[d] - g->lo[d]) * g->inv[d]);
+        int b = (int)floorf((mx[d] - g->lo[d]) * g->inv[d]);
+        b0[d] = a < 0 ? 0 : (a > g->res - 1 ? g->res - 1 : a);
+        b1[d] = b < 0 ? 0 : (b > g->res - 1 ? g->res - 1 : b);
+    }
+}
+
+static void grid_build(int nn, const float* node, int ne, const int* elem, locgrid* g) {
+    float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+    for (int i = 0; i < nn; i++)
+        for (int d = 0; d < 3; d++) {
+            if (node[3 * (size_t)i + d] < lo[d]) lo[d] = node[3 * (size_t)i + d];
+            if (node[3 * (size_t)i + d] > hi[d]) hi[d] = node[3 * (size_t)i + d];
+        }
+    int res = (int)cbrt((double)ne / 4.0);
+    if (res < 1) res = 1;
+    if (res > 256) res = 256;
+    g->res = res;
+    for (int d = 0; d < 3; d++) {
+        float span = hi[d] - lo[d];
+        g->lo[d] = lo[d];
+        g->inv[d] = span > 0 ? res / span : 0.f;
+    }
+    size_t nbin = (size_t)res * res * res;
+    g->start = (uint32_t*)calloc(nbin + 1, sizeof(uint32_t));
+    int b0[3], b1[3];
+    for (int e = 0; e < ne; e++) {
+        grid_range(node, elem + 4 * (size_t)e, g, b0, b1);
+        for (int z = b0[2]; z <= b1[2]; z++)
+            for (int y = b0[1]; y <= b1[1]; y++)
+                for (int x = b0[0]; x <= b1[0]; x++) g->start[((size_t)z * res + y) * res + x + 1]++;
+    }
+    for (size_t i = 0; i < nbin; i++) g->start[i + 1] += g->start[i];
+    g->items = (uint32_t*)malloc(sizeof(uint32_t) * (g->start[nbin] ? g->start[nbin] : 1));
+    uint32_t* fill = (uint32_t*)malloc(sizeof(uint32_t) * nbin);
+    memcpy(fill, g->start, sizeof(uint32_t) * nbin);
+    for (int e = 0; e < ne; e++) {
+        grid_range(node, elem + 4 * (size_t)e, g, b0, b1);
+        for (int z = b0[2]; z <= b1[2]; z++)
+            for (int y = b0[1]; y <= b1[1]; y++)
+                for (int x = b0[0]; x <= b1[0]; x++) g->items[fill[((size_t)z * res + y) * res + x]++] = (uint32_t)e;
+    }
+    free(fill);
+}
+
+/* barycentric test of the reference's source-element search
+ * (src/mmc_raytrace.c:2599-2652): unnormalized face normals, tolerance -1e-4 */
+static float face_bary(const float* a, const float* b, const float* c, float px, float py, float pz) {
+    float abx = b[0] - a[0], aby = b[1] - a[1], abz = b[2] - a[2];
+    float acx = c[0] - a[0], acy = c[1] - a[1], acz = c[2] - a[2];
+    float sx = px - a[0], sy = py - a[1], sz = pz - a[2];
+    float nx = aby * acz - abz * acy, ny = abz * acx - abx * acz, nz = abx * acy - aby * acx;
+    return -((sx * nx + sy * ny) + sz * nz);
+}
+
+static int src_encloses(const engine* g, int e, float px, float py, float pz) {
+    const int* el = g->elem + 4 * (size_t)e;
+    const float* n0 = g->node + 3 * (size_t)(el[0] - 1);
+    const float* n1 = g->node + 3 * (size_t)(el[1] - 1);
+    const float* n2 = g->node + 3 * (size_t)(el[2] - 1);
+    const float* n3 = g->node + 3 * (size_t)(el[3] - 1);
+    float b2 = face_bary(n0, n3, n1, px, py, pz);
+    float b0 = face_bary(n3, n2, n1, px, py, pz);
+    float b1 = face_bary(n0, n2, n3, px, py, pz);
+    float b3 = face_bary(n0, n1, n2, px, py, pz);
+    return !(b0 < -1e-4f || b1 < -1e-4f || b2 < -1e-4f || b3 < -1e-4f);
+}
+
+/* lowest-index enclosing element in p's grid cell, else in the 26 neighbours */
+static int src_locate(const engine* g, float px, float py, float pz) {
+    const locgrid* G = g->grid;
+    int res = G->res;
+    float fx = (px - G->lo[0]) * G->inv[0], fy = (py - G->lo[1]) * G->inv[1], fz = (pz - G->lo[2]) * G->inv[2];
+    float lo = -1e-3f * res, hi = res * (1.f + 1e-3f);
+    if (!(fx >= lo) || !(fx <= hi) || !(fy >= lo) || !(fy <= hi) || !(fz >= lo) || !(fz <= hi)) return 0;
+    int b[3] = {(int)floorf(fx), (int)floorf(fy), (int)floorf(fz)};
+    for (int d = 0; d < 3; d++) b[d] = b[d] < 0 ? 0 : (b[d] > res - 1 ? res - 1 : b[d]);
+    for (int pass = 0; pass < 2; pass++) {
+        int best = 0x7FFFFFFF;
+        for (int z = b[2] - pass; z <= b[2] + pass; z++)
+            for (int y = b[1] - pass; y <= b[1] + pass; y++)
+                for (int x = b[0] - pass; x <= b[0] + pass; x++) {
+                    if (x < 0 || y < 0 || z < 0 || x >= res || y >= res || z >= res) continue;
+                    size_t cell = ((size_t)z * res + y) * res + x;
+                    for (uint32_t k = G->start[cell]; k < G->start[cell + 1]; k++) {
+                        int e = (int)G->items[k];
+                        if (e < best && src_encloses(g, e, px, py, pz)) best = e;
+                    }
+                }
+        if (best != 0x7FFFFFFF) return best + 1;
+    }
+    return 0;
+}
+
+/* photon launch for every source type, src/mmc_raytrace.c:2346-2671 (the CPU
+ * launch; the GPU version src/mmc_core.cl:1416-1834 differs in leaving
+ * cone/arcsine/zgaussian directions unrotated and the disk radius without an
+ * inner bound).  Restated with these changes, which the CUDA engine shares:
+ * the cone's polar angle is sampled by inversion instead of rejection; acos
+ * is replaced by the identities cos(acos x) = x, sin(acos x) = sqrt(1-x^2);
+ * the Gaussian radius and angle add EPS inside the log; a photon is located
+ * in the initial element first, then through the bounding-box grid (the
+ * reference searches a user-labelled candidate list).  Returns 0 when no
+ * element encloses the launch position. */
+static int launch_photon(const engine* g, ray* r, uint64_t* ran) {
+    const oracle_cfg* cfg = g->cfg;
+    const float* p1 = cfg->srcparam1;
+    const float* p2 = cfg->srcparam2;
+    const int st = cfg->srctype;
+    float ox = r->px, oy = r->py, oz = r->pz;
+    int canfocus = 1;
+    r->slen = -oracle_logf(oracle_rng_next(ran) + O_EPS);
+    if (st == 0) {
+        if (r->eid > 0) return 1;
+    } else if (st == 4 || st == 5 || st == 15 || st == 6 || st == 14) {
+        float rx = oracle_rng_next(ran);
+        float ry = oracle_rng_next(ran);
+        if (st == 15) {
+            float rz = oracle_rng_next(ran);
+            r->px = cfg->srcpos[0] + rx * p1[0];
+            r->py = cfg->srcpos[1] + ry * p1[1];
+            r->pz = cfg->srcpos[2] + rz * p1[2];
+            int nx = (int)p1[0], ny = (int)p1[1], nz = (int)p1[2];
+            int ix = (int)(rx * nx), iy = (int)(ry * ny), iz = (int)(rz * nz);
+            if (ix > nx - 1) ix = nx - 1;
+            if (iy > ny - 1) iy = ny - 1;
+            if (iz > nz - 1) iz = nz - 1;
+            r->weight = cfg->srcpattern[((size_t)iz * ny + iy) * nx + ix];
+            ox += p1[0] * 0.5f; oy += p1[1] * 0.5f; oz += p1[2] * 0.5f;
+        } else if (st == 14) {
+            float fx = floorf(rx * p1[3]), fy = floorf(ry * p2[3]);
+            r->px = cfg->srcpos[0] + fx * p1[0] / (p1[3] - 1.f) + fy * p2[0] / (p2[3] - 1.f);
+            r->py = cfg->srcpos[1] + fx * p1[1] / (p1[3] - 1.f) + fy * p2[1] / (p2[3] - 1.f);
+            r->pz = cfg->srcpos[2] + fx * p1[2] / (p1[3] - 1.f) + fy * p2[2] / (p2[3] - 1.f);
+            ox += (p1[0] + p2[0]) * 0.5f; oy += (p1[1] + p2[1]) * 0.5f; oz += (p1[2] + p2[2]) * 0.5f;
+        } else {
+            r->px = cfg->srcpos[0] + rx * p1[0] + ry * p2[0];
+            r->py = cfg->srcpos[1] + rx * p1[1] + ry * p2[1];
+            r->pz = cfg->srcpos[2] + rx * p1[2] + ry * p2[2];
+            if (st == 5) {
+                int nx = (int)p1[3], ny = (int)p2[3];
+                int iy = (int)(ry * ny), ix = (int)(rx * nx);
+                if (iy > ny - 1) iy = ny - 1;
+                if (ix > nx - 1) ix = nx - 1;
+                r->weight = cfg->srcpattern[iy * nx + ix];
+            } else if (st == 6) {
+                float sv, cv;
+                oracle_sincos2pi(floorf(p1[3]) * rx + floorf(p2[3]) * ry + p1[3] - floorf(p1[3]), &sv, &cv);
+                r->weight = (cv * (1.f - p2[3] + floorf(p2[3])) + 1.f) * 0.5f;
+            }
+            ox += (p1[0] + p2[0]) * 0.5f; oy += (p1[1] + p2[1]) * 0.5f; oz += (p1[2] + p2[2]) * 0.5f;
+        }
+    } else if (st == 9 || st == 10) {
+        float rx = oracle_rng_next(ran);
+        float ry = oracle_rng_next(ran);
+        float w = p1[3] * (1.f / sqrtf(p1[0] * p1[0] + p1[1] * p1[1] + p1[2] * p1[2]));
+        float v2x = w * (cfg->srcdir[1] * p1[2] - cfg->srcdir[2] * p1[1]);
+        float v2y = w * (cfg->srcdir[2] * p1[0] - cfg->srcdir[0] * p1[2]);
+        float v2z = w * (cfg->srcdir[0] * p1[1] - cfg->srcdir[1] * p1[0]);
+        r->px = cfg->srcpos[0] + rx * p1[0] + ry * v2x;
+        r->py = cfg->srcpos[1] + rx * p1[1] + ry * v2y;
+        r->pz = cfg->srcpos[2] + rx * p1[2] + ry * v2z;
+        float s1, c1, s2, c2;
+        if (st == 10) {
+            oracle_sincos2pi(p2[0] * rx + p2[2], &s1, &c1);
+            oracle_sincos2pi(p2[1] * ry + p2[3], &s2, &c2);
+            r->weight = (s1 * s2 + 1.f) * 0.5f;
+        } else {
+            oracle_sincos2pi(p2[0] * rx + p2[1] * ry + p2[2], &s1, &c1);
+            r->weight = (c1 * (1.f - p2[3]) + 1.f) * 0.5f;
+        }
+        ox += (p1[0] + v2x) * 0.5f; oy += (p1[1] + v2y) * 0.5f; oz += (p1[2] + v2z) * 0.5f;
+    } else if (st == 8 || st == 17 || st == 3) {
+        float sphi, cphi, r0;
+        if (st == 17 && (p1[2] > 0.f || p1[3] > 0.f)) {
+            float phi = fabsf(p1[2] - p1[3]) * oracle_rng_next(ran) + fminf(p1[2], p1[3]);
+            oracle_sincos2pi(phi * (0.5f / O_PI), &sphi, &cphi);
+        } else {
+            oracle_sincos2pi(oracle_rng_next(ran), &sphi, &cphi);
+        }
+        if (st == 8 || st == 17) {
+            r0 = sqrtf(oracle_rng_next(ran) * fabsf(p1[0] * p1[0] - p1[1] * p1[1]) + p1[1] * p1[1]);
+        } else if (fabsf(cfg->focus) < 1e-5f || fabsf(p1[1]) < 1e-5f) {
+            r0 = sqrtf(-oracle_logf(oracle_rng_next(ran) + O_EPS)) * p1[0];
+        } else {
+            float z0 = p1[0] * p1[0] * O_PI / p1[1];
+            r0 = sqrtf(-oracle_logf(oracle_rng_next(ran) + O_EPS) * (1.f + (cfg->focus * cfg->focus / (z0 * z0)))) * p1[0];
+        }
+        float dx = cfg->srcdir[0], dy = cfg->srcdir[1], dz = cfg->srcdir[2];
+        if (dz > -1.f + O_EPS && dz < 1.f - O_EPS) {
+            float tmp0 = 1.f - dz * dz;
+            float tmp1 = r0 / sqrtf(tmp0);
+            r->px = cfg->srcpos[0] + tmp1 * (dx * dz * cphi - dy * sphi);
+            r->py = cfg->srcpos[1] + tmp1 * (dy * dz * cphi + dx * sphi);
+            r->pz = cfg->srcpos[2] - tmp1 * tmp0 * cphi;
+        } else {
+            r->px += r0 * cphi;
+            r->py += r0 * sphi;
+        }
+    } else if (st == 2 || st == 1 || st == 7) {
+        float sphi, cphi, stheta, ctheta;
+        oracle_sincos2pi(oracle_rng_next(ran), &sphi, &cphi);
+        if (st == 2) {
+            float u = oracle_rng_next(ran);
+            if (p1[1] > 0.f) {
+                oracle_sincos2pi(u * p1[0] * (0.5f / O_PI), &stheta, &ctheta);
+            } else {
+                float sa, ca;
+                oracle_sincos2pi(p1[0] * (0.5f / O_PI), &sa, &ca);
+                ctheta = 1.f - u * (1.f - ca);
+                stheta = sqrtf(fmaxf(0.f, 1.f - ctheta * ctheta));
+            }
+        } else if (st == 1) {
+            ctheta = 2.f * oracle_rng_next(ran) - 1.f;
+            stheta = sqrtf(fmaxf(0.f, 1.f - ctheta * ctheta));
+        } else {
+            oracle_sincos2pi(0.5f * oracle_rng_next(ran), &stheta, &ctheta);
+        }
+        rotatevector(r, stheta, ctheta, sphi, cphi);
+        canfocus = 0;
+        if (r->eid > 0) return 1;
+    } else if (st == 11) {
+        float sphi, cphi, stheta, ctheta;
+        oracle_sincos2pi(oracle_rng_next(ran), &sphi, &cphi);
+        float u1 = oracle_rng_next(ran);
+        float u2 = oracle_rng_next(ran);
+        float ang = sqrtf(-2.f * oracle_logf(u1 + O_EPS)) * (1.f - 2.f * u2) * p1[0];
+        oracle_sincos2pi(ang * (0.5f / O_PI), &stheta, &ctheta);
+        rotatevector(r, stheta, ctheta, sphi, cphi);
+        canfocus = 0;
+    } else if (st == 16) {
+        float sphi, cphi;
+        oracle_sincos2pi(oracle_rng_next(ran), &sphi, &cphi);
+        float r0 = sqrtf(0.5f * -oracle_logf(oracle_rng_next(ran) + O_EPS)) * p1[0];
+        float tilt = (p1[2] > 0.f) ? (-p1[1] / p1[2]) : 0.f;
+        float bx = -r0 * sphi, by = r0 * cphi, bz = p1[2];
+        float nb = 1.f / sqrtf(bx * bx + by * by + bz * bz);
+        bx *= nb; by *= nb; bz *= nb;
+        float qx = r0 * (cphi - tilt * sphi), qy = r0 * (sphi + tilt * cphi);
+        float dx = cfg->srcdir[0], dy = cfg->srcdir[1], dz = cfg->srcdir[2];
+        if (dz > -1.f + O_EPS && dz < 1.f - O_EPS) {
+            float sint = sqrtf(1.f - dz * dz);
+            float isint = 1.f / sint;
+            float cb = dx * isint, sb = dy * isint;
+            r->px = cfg->srcpos[0] + qx * cb * dz - qy * sb;
+            r->py = cfg->srcpos[1] + qx * sb * dz + qy * cb;
+            r->pz = cfg->srcpos[2] - qx * sint;
+            r->vx = bx * cb * dz - by * sb + bz * cb * sint;
+            r->vy = bx * sb * dz + by * cb + bz * sb * sint;
+            r->vz = -bx * sint + bz * dz;
+        } else {
+            r->px = cfg->srcpos[0] + qx;
+            r->py = cfg->srcpos[1] + qy;
+            r->pz = cfg->srcpos[2];
+            r->vx = bx; r->vy = by;
+            r->vz = (dz > 0.f) ? bz : -bz;
+        }
+        float nv = 1.f / sqrtf(r->vx * r->vx + r->vy * r->vy + r->vz * r->vz);
+        r->vx *= nv; r->vy *= nv; r->vz *= nv;
+        canfocus = 0;
+    } else if (st == 12 || st == 13) {
+        float t = oracle_rng_next(ran);
+        r->px += t * p1[0]; r->py += t * p1[1]; r->pz += t * p1[2];
+        if (st == 12) {
+            t = 1.f - 2.f * oracle_rng_next(ran);
+            float s = 1.f - 2.f * oracle_rng_next(ran);
+            float sign = (oracle_rng_next(ran) > 0.5f) ? 1.f : -1.f;
+            float p = sqrtf(1.f - r->vx * r->vx - r->vy * r->vy) * sign;
+            float vx = r->vy * p - r->vz * s, vy = r->vz * t - r->vx * p, vz = r->vx * s - r->vy * t;
+            r->vx = vx; r->vy = vy; r->vz = vz;
+        }
+        ox += p1[0] * 0.5f; oy += p1[1] * 0.5f; oz += p1[2] * 0.5f;
+        canfocus = (st == 13);
+    }
+    if (canfocus) {
+        float f = cfg->focus;
+        if (f != f) {
+            float sphi, cphi;
+            oracle_sincos2pi(oracle_rng_next(ran), &sphi, &cphi);
+            float ctheta = 2.f * oracle_rng_next(ran) - 1.f;
+            rotatevector(r, sqrtf(fmaxf(0.f, 1.f - ctheta * ctheta)), ctheta, sphi, cphi);
+        } else if (f < 0.f && isinf(f)) {
+            float sphi, cphi;
+            oracle_sincos2pi(oracle_rng_next(ran), &sphi, &cphi);
+            float stheta = sqrtf(oracle_rng_next(ran));
+            rotatevector(r, stheta, sqrtf(1.f - stheta * stheta), sphi, cphi);
+        } else if (f != 0.f) {
+            ox += f * r->vx; oy += f * r->vy; oz += f * r->vz;
+            float vx, vy, vz;
+            if (f < 0.f) { vx = r->px - ox; vy = r->py - oy; vz = r->pz - oz; }
+            else { vx = ox - r->px; vy = oy - r->py; vz = oz - r->pz; }
+            float rn = 1.f / sqrtf(vx * vx + vy * vy + vz * vz);
+            r->vx = vx * rn; r->vy = vy * rn; r->vz = vz * rn;
+        }
+    }
+    r->px = r->px + r->vx * O_EPS;
+    r->py = r->py + r->vy * O_EPS;
+    r->pz = r->pz + r->vz * O_EPS;
+    int e = 0;
+    if (r->eid > 0 && src_encloses(g, r->eid - 1, r->px, r->py, r->pz)) e = r->eid;
+    else if (g->grid) e = src_locate(g, r->px, r->py, r->pz);
+    if (e <= 0) return 0;
+    r->eid = e;
+    return 1;
+}
+
 typedef struct {
     double etot, eesc;
     uint64_t raytet;
     uint64_t aborted;
+    uint64_t outside;
 } tallies;
 
 /* the photon life: src/mmc_core.cl:1851-2161 */
@@ -572,10 +900,18 @@ static void onephoton(engine* g, uint64_t pidx, float* ppath, oracle_out* out, t
     int fixcount = 0, oldeid = 0, detid = 0;
     uint64_t steps = 0;
     int aborted = 0;
-    /* pencil launch: src/mmc_core.cl:1521-1526 */
-    r->slen = -oracle_logf(oracle_rng_next(ran) + O_EPS);
+    /* launch: src/mmc_raytrace.c:2346-2671 */
+    const int placed = launch_photon(g, r, ran);
     if (cfg->issavedet) ppath[reclen - 1] = r->weight;
     tl->etot += r->weight;
+    if (!placed) {
+        tl->outside++;
+        tl->eesc += r->weight;
+        if (out->photon_weight) out->photon_weight[pidx] = r->weight;
+        if (out->photon_steps) out->photon_steps[pidx] = 0;
+        if (out->photon_det) out->photon_det[pidx] = 0;
+        return;
+    }
 
 #define STEP()                                                         \
     do {                                                               \
@@ -711,6 +1047,12 @@ int oracle_run(int nn, const float* node, int ne, const int* elem, const int* la
     memset(&g, 0, sizeof(g));
     g.ne = ne; g.nn = nn; g.M = cfg->nmedia - 1;
     g.node = node; g.elem = ee; g.type = label; g.facenb = fnb; g.nrm = nrm; g.cfg = cfg;
+    locgrid grid;
+    memset(&grid, 0, sizeof(grid));
+    if (!(cfg->srctype == 0 && cfg->e0 > 0)) {
+        grid_build(nn, node, ne, ee, &grid);
+        g.grid = &grid;
+    }
     g.Rtstep = 1.f / cfg->tstep;
     g.maxgate = cfg->maxgate;
     g.reclen = (2 + (cfg->ismomentum > 0)) * g.M + (cfg->issaveexit > 0) * 6 + 1;
@@ -725,25 +1067,28 @@ int oracle_run(int nn, const float* node, int ne, const int* elem, const int* la
     }
     out->detected = 0;
     double etot = 0, eesc = 0;
-    uint64_t raytet = 0, aborted = 0;
+    uint64_t raytet = 0, aborted = 0, outside = 0;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
     (void)nthreads;
 #endif
-#pragma omp parallel reduction(+:etot, eesc, raytet, aborted)
+#pragma omp parallel reduction(+:etot, eesc, raytet, aborted, outside)
     {
         float* ppath = (float*)calloc((size_t)g.reclen + 1, sizeof(float));
-        tallies tl = {0, 0, 0, 0};
+        tallies tl = {0, 0, 0, 0, 0};
 #pragma omp for schedule(dynamic, 64)
         for (long long i = 0; i < (long long)cfg->nphoton; i++) onephoton(&g, (uint64_t)i, ppath, out, &tl);
-        etot += tl.etot; eesc += tl.eesc; raytet += tl.raytet; aborted += tl.aborted;
+        etot += tl.etot; eesc += tl.eesc; raytet += tl.raytet; aborted += tl.aborted; outside += tl.outside;
         free(ppath);
     }
     out->energytot = etot;
     out->energyesc = eesc;
     out->raytet = raytet;
     out->aborted = aborted;
+    out->outside = outside;
+    free(grid.start);
+    free(grid.items);
     if (!cfg->accum_f64) {
         for (size_t i = 0; i < flen; i++) out->field_raw[i] = (double)g.f32a[i] + (double)g.f32b[i];
         free(g.f32a);

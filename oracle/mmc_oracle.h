@@ -52,6 +52,10 @@ typedef struct oracle_cfg {
     const float* replaytime;
     int accum_f64;          /* 1: double fluence sums; 0: float + 1000 overflow split */
     uint64_t step_budget;   /* max ray-tet tests per photon */
+    int srctype;            /* the reference's source types, src/mmc_utils.h:101-105 */
+    float srcparam1[4], srcparam2[4];
+    float focus;            /* srcdir.w of the reference */
+    const float* srcpattern;
 } oracle_cfg;
 
 typedef struct oracle_out {
@@ -66,6 +70,7 @@ typedef struct oracle_out {
     double energytot, energyesc;
     uint64_t raytet;
     uint64_t aborted;
+    uint64_t outside;       /* photons launched at a position no element encloses */
 } oracle_out;
 
 /* Mesh preparation (volumes with orientation fix, face neighbours, normals,

@@ -16,6 +16,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 OUTPUT_TYPES = {"flux": 0, "fluence": 1, "energy": 2, "jacobian": 3, "wl": 4, "wp": 5, "wn": 16}
+SOURCE_TYPES = {"pencil": 0, "isotropic": 1, "cone": 2, "gaussian": 3, "planar": 4, "pattern": 5, "fourier": 6,
+                "arcsine": 7, "disk": 8, "fourierx": 9, "fourierx2d": 10, "zgaussian": 11, "line": 12, "slit": 13,
+                "pencilarray": 14, "pattern3d": 15, "hyperboloid": 16, "ring": 17}
 _lib = None
 
 
@@ -32,6 +35,8 @@ class OCfg(C.Structure):
         ("detnum", C.c_int), ("detpos", C.c_void_p),
         ("replayseed", C.c_void_p), ("replayweight", C.c_void_p), ("replaytime", C.c_void_p),
         ("accum_f64", C.c_int), ("step_budget", C.c_uint64),
+        ("srctype", C.c_int), ("srcparam1", C.c_float * 4), ("srcparam2", C.c_float * 4), ("focus", C.c_float),
+        ("srcpattern", C.c_void_p),
     ]
 
 
@@ -40,7 +45,7 @@ class OOut(C.Structure):
         ("field_raw", C.c_void_p), ("detp", C.c_void_p), ("seeds", C.c_void_p),
         ("photon_weight", C.c_void_p), ("photon_steps", C.c_void_p), ("photon_det", C.c_void_p),
         ("detected", C.c_uint32), ("reclen", C.c_int), ("energytot", C.c_double),
-        ("energyesc", C.c_double), ("raytet", C.c_uint64), ("aborted", C.c_uint64),
+        ("energyesc", C.c_double), ("raytet", C.c_uint64), ("aborted", C.c_uint64), ("outside", C.c_uint64),
     ]
 
 
@@ -152,6 +157,16 @@ def _ocfg(cfg, maxgate, e0, keep):
         c.replayseed, c.replayweight, c.replaytime = _p(rs), _p(rw), _p(rt)
     c.accum_f64 = int(cfg.accum_f64)
     c.step_budget = int(cfg.step_budget) if cfg.step_budget else 100000000
+    st = getattr(cfg, "srctype", 0)
+    c.srctype = SOURCE_TYPES[st] if isinstance(st, str) else int(st)
+    c.srcparam1 = (C.c_float * 4)(*[float(x) for x in getattr(cfg, "srcparam1", (0, 0, 0, 0))])
+    c.srcparam2 = (C.c_float * 4)(*[float(x) for x in getattr(cfg, "srcparam2", (0, 0, 0, 0))])
+    c.focus = float(getattr(cfg, "focus", 0.0))
+    pat = getattr(cfg, "srcpattern", None)
+    if pat is not None:
+        pat = np.ascontiguousarray(pat, np.float32).ravel()
+        keep.append(pat)
+        c.srcpattern = _p(pat)
     return c
 
 
@@ -162,8 +177,11 @@ def run(node, elem, label, cfg, nthreads=1, trace=False, normalize=True):
     nn, ne = node.shape[0], elem.shape[0]
     maxgate = cfg.maxgate
     e0 = cfg.e0 if cfg.e0 else initelem(node, elem, label, cfg.srcpos)
-    if e0 <= 0:
+    st = getattr(cfg, "srctype", 0)
+    st = SOURCE_TYPES[st] if isinstance(st, str) else int(st)
+    if e0 <= 0 and st in (0, 1, 2, 7):  # point sources start in the initial element
         raise ValueError("oracle: source outside the mesh")
+    e0 = max(int(e0), 0)
     keep = []
     c = _ocfg(cfg, maxgate, e0, keep)
     raw = np.zeros((maxgate, ne), np.float64)
@@ -181,7 +199,7 @@ def run(node, elem, label, cfg, nthreads=1, trace=False, normalize=True):
     if rc:
         raise ValueError("oracle run failed")
     res = dict(raw=raw, detected=int(out.detected), energytot=out.energytot, energyesc=out.energyesc,
-               raytet=int(out.raytet), aborted=int(out.aborted), reclen=int(out.reclen), e0=e0,
+               raytet=int(out.raytet), aborted=int(out.aborted), outside=int(out.outside), reclen=int(out.reclen), e0=e0,
                photon_weight=pw, photon_steps=ps, photon_det=pd)
     saved = min(int(out.detected), int(cfg.maxdetphoton)) if cfg.issavedet else 0
     res["detp"] = detp[:saved] if detp is not None else None

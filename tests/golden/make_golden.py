@@ -12,6 +12,12 @@ Badouel tracer and element-based output (-M s -C 0), unnormalized (-U 0):
   incl48k  20^3 voxels x 6 tets at 3 mm, +/-0.6 mm jitter, r=10 mm inclusion
            (mua=0.05 mus=5 g=0.9), 10 gates of 0.5 ns, 4 detectors R=2 mm on
            z=0 at x=40..55, detected photons saved, 1e5 photons
+  src_*    source types on the cube6k mesh, one 5 ns gate, 1e5 photons:
+           isotropic and cone (half angle 0.6 rad about (0.6,0,0.8)) at the
+           centre; disk (R=10 mm), gaussian (waist 5 mm) and planar (20x20 mm)
+           on the z=0 face over a 6 mm void layer (voxel layer z<6 mm; the
+           reference needs the layer's tets labelled -1, its source-element
+           candidates, which it then treats as void, label 0)
 
 Six more runs with fresh seeds calibrate the null: their coverage of the
 10-run statistics (fraction of cells within 3 sigma, mean z) is stored, and a
@@ -33,6 +39,7 @@ import struct
 import subprocess
 import sys
 import tempfile
+import zlib
 from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
@@ -48,18 +55,46 @@ NNULL = 6
 SEED0 = 20260101
 
 
+SOURCE_CASES = {
+    "src_isotropic": dict(Type="isotropic", Pos=[30.0, 30.0, 30.0], Dir=[0.0, 0.0, 1.0], void=False),
+    "src_cone": dict(Type="cone", Pos=[30.0, 30.0, 30.0], Dir=[0.6, 0.0, 0.8], Param1=[0.6, 0, 0, 0], void=False),
+    "src_disk": dict(Type="disk", Pos=[30.0, 30.0, 0.0], Dir=[0.0, 0.0, 1.0], Param1=[10.0, 0, 0, 0], void=True),
+    "src_gaussian": dict(Type="gaussian", Pos=[30.0, 30.0, 0.0], Dir=[0.0, 0.0, 1.0], Param1=[5.0, 0, 0, 0],
+                         void=True),
+    "src_planar": dict(Type="planar", Pos=[20.0, 20.0, 0.0], Dir=[0.0, 0.0, 1.0], Param1=[20.0, 0, 0, 0],
+                       Param2=[0, 20.0, 0, 0], void=True),
+}
+
+
+def void_layer_labels(m):
+    """Labels of the cube6k mesh with the voxel layer z < 6 mm made void (0)."""
+    label = m.label.copy()
+    label[meshgen.centroids(m.node, m.elem)[:, 2] < 6.0] = 0
+    return label
+
+
 def case_defs():
     cube = meshgen.homogeneous_cube(n=10)
     incl = meshgen.inclusion_cube(n=20, jitter=0.6, seed=7)
-    return {
+    cases = {
         "cube6k": dict(mesh=cube, photons=100000, t1=5e-9, dt=5e-9, det=None),
         "incl48k": dict(mesh=incl, photons=100000, t1=5e-9, dt=0.5e-9, det=meshgen.c1_detectors()),
     }
+    for name, src in SOURCE_CASES.items():
+        c = dict(mesh=cube, photons=100000, t1=5e-9, dt=5e-9, det=None, src=src)
+        if src["void"]:
+            lab = void_layer_labels(cube)
+            c["mesh"] = meshgen.Mesh(cube.node, cube.elem, lab, cube.media, "cube6k-void")
+            c["reflabel"] = np.where(lab == 0, -1, lab)  # the reference's source candidates
+        cases[name] = c
+    return cases
 
 
 def write_json(path, name, c):
     m = c["mesh"]
-    elem = np.c_[m.elem, m.label].tolist()
+    elem = np.c_[m.elem, c.get("reflabel", m.label)].tolist()
+    src = c.get("src") or dict(Pos=[30.0, 30.0, 0.0], Dir=[0.0, 0.0, 1.0])
+    source = {k: v for k, v in src.items() if k in ("Type", "Pos", "Dir", "Param1", "Param2")}
     cfg = {
         "Session": {"ID": name, "Photons": c["photons"], "RNGSeed": SEED0, "OutputFormat": "bin",
                     "DoMismatch": 1},
@@ -67,7 +102,7 @@ def write_json(path, name, c):
                              for r in m.media]},
         "Mesh": {"MeshNode": m.node.astype(np.float64).tolist(), "MeshElem": elem, "InitElem": int(c["e0"])},
         "Forward": {"T0": 0.0, "T1": c["t1"], "Dt": c["dt"]},
-        "Optode": {"Source": {"Pos": [30.0, 30.0, 0.0], "Dir": [0.0, 0.0, 1.0]}},
+        "Optode": {"Source": source},
     }
     if c["det"] is not None:
         cfg["Optode"]["Detector"] = [{"Pos": [float(d[0]), float(d[1]), float(d[2])], "R": float(d[3])}
@@ -182,15 +217,20 @@ def run_ref(workdir, name, seed, photons, normalized=False, savedet=False):
     return out
 
 
-def main():
+def main(only=()):
+    """Regenerates every case, or only the named ones (each case draws its
+    random cell subset from its own generator, so cases are independent)."""
     if not os.path.exists(REF):
         subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
-    rng = np.random.default_rng(5)
     with tempfile.TemporaryDirectory() as wd:
         for name, c in case_defs().items():
+            if only and name not in only:
+                continue
+            rng = np.random.default_rng(zlib.crc32(name.encode()))
             sys.path.insert(0, os.path.join(ROOT, "oracle"))
             import oracle
-            c["e0"] = oracle.initelem(c["mesh"].node, c["mesh"].elem, c["mesh"].label, (30.0, 30.0, 0.0))
+            srcpos = tuple((c.get("src") or {}).get("Pos", (30.0, 30.0, 0.0)))
+            c["e0"] = oracle.initelem(c["mesh"].node, c["mesh"].elem, c["mesh"].label, srcpos)
             write_json(os.path.join(wd, name + ".json"), name, c)
             m = c["mesh"]
             ne = m.ne
@@ -245,6 +285,9 @@ def main():
                 fx.update(det_count=np.array(counts, np.float64), det_wsum=np.array(wsum),
                           det_plen=np.array(plen), det_nscat=np.array(nscat))
             np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **fx)
+            if name.startswith("src_"):  # the source cases reuse the cube6k mesh: no pins of their own
+                print(name, "absorbed", fx["absorbed"].mean(), "tests/photon", fx["tests_per_photon"].mean())
+                continue
             # pins of the host stages: prepared mesh and output normalization
             md = run_ref_mesh(wd, name)
             sub = np.sort(rng.choice(ne, size=min(ne, 3000), replace=False)).astype(np.int32)
@@ -265,4 +308,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

@@ -39,6 +39,27 @@ def case_mesh_and_config(name, nphoton=None, seed=4242):
         cfg = SimConfig(media=m.media, nphoton=nphoton or int(fx["photons"]), seed=seed, srcpos=(30.0, 30.0, 0.0),
                         srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=0.5e-9, basisorder=0, isnormalized=0, issavedet=1,
                         detpos=meshgen.c1_detectors(), maxdetphoton=200000)
+    elif name.startswith("src_"):
+        # source types (tests/golden/make_golden.py SOURCE_CASES): the cube6k mesh, with the
+        # voxel layer z < 6 mm void for the sources on the z=0 face
+        m = meshgen.homogeneous_cube(n=10)
+        src = {
+            "src_isotropic": dict(srctype="isotropic", srcpos=(30.0, 30.0, 30.0), srcdir=(0.0, 0.0, 1.0)),
+            "src_cone": dict(srctype="cone", srcpos=(30.0, 30.0, 30.0), srcdir=(0.6, 0.0, 0.8),
+                             srcparam1=(0.6, 0, 0, 0)),
+            "src_disk": dict(srctype="disk", srcpos=(30.0, 30.0, 0.0), srcdir=(0.0, 0.0, 1.0),
+                             srcparam1=(10.0, 0, 0, 0)),
+            "src_gaussian": dict(srctype="gaussian", srcpos=(30.0, 30.0, 0.0), srcdir=(0.0, 0.0, 1.0),
+                                 srcparam1=(5.0, 0, 0, 0)),
+            "src_planar": dict(srctype="planar", srcpos=(20.0, 20.0, 0.0), srcdir=(0.0, 0.0, 1.0),
+                               srcparam1=(20.0, 0, 0, 0), srcparam2=(0, 20.0, 0, 0)),
+        }[name]
+        if src["srcpos"][2] == 0.0:
+            label = m.label.copy()
+            label[meshgen.centroids(m.node, m.elem)[:, 2] < 6.0] = 0
+            m = meshgen.Mesh(m.node, m.elem, label, m.media, "cube6k-void")
+        cfg = SimConfig(media=m.media, nphoton=nphoton or int(fx["photons"]), seed=seed, tend=5e-9, tstep=5e-9,
+                        basisorder=0, isnormalized=0, **src)
     else:
         raise KeyError(name)
     return m, cfg, fx

@@ -68,7 +68,14 @@ def test_pmmc_dict_parsing():
     with pytest.raises(ValueError):
         pmmc._parse(dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[1, 1, 1], method="plucker"))
     with pytest.raises(ValueError):
-        pmmc._parse(dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[1, 1, 1], srctype="disk"))
+        pmmc._parse(dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[1, 1, 1], srctype="laser"))
+    # source types, parameters, focus (the 4th srcdir entry) and patterns (Fortran order, x fastest)
+    pat = np.arange(6, dtype=np.float32).reshape(3, 2, order="F")
+    *_, sc, _ = pmmc._parse(dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[1, 1, 1], srctype="pattern",
+                                srcdir=[0, 0, 1, -5], srcparam1=[10, 0, 0, 3], srcparam2=[0, 10, 0, 2],
+                                srcpattern=pat))
+    assert sc.srctype == "pattern" and sc.focus == -5 and sc.srcparam1 == (10, 0, 0, 3)
+    assert sc.srcpattern.tolist() == [0, 1, 2, 3, 4, 5]
     # a uint8 [16, N] seed matrix selects replay
     *_, s2 = pmmc._parse(dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[30, 30, 0],
                               seed=np.zeros((16, 5), np.uint8)))

@@ -10,7 +10,10 @@ import golden_checks as gc
 NTHREADS = os.cpu_count() or 4
 
 
-@pytest.mark.parametrize("name", ["cube6k", "incl48k"])
+SOURCE_CASES = ["src_isotropic", "src_cone", "src_disk", "src_gaussian", "src_planar"]
+
+
+@pytest.mark.parametrize("name", ["cube6k", "incl48k"] + SOURCE_CASES)
 def test_oracle_matches_reference_runs(oracle_mod, name):
     m, cfg, fx = gc.case_mesh_and_config(name)
     r = oracle_mod.run(m.node, m.elem, m.label, cfg, nthreads=NTHREADS, normalize=False)
