@@ -3,7 +3,7 @@
 * Every source type of the reference (src/mmc_raytrace.c:2346-2671), with the
   beam-focus variants, against the CPU oracle photon by photon (IEEE
   arithmetic): final weights, ray-tet counts, detectors, launched weight and
-  fluence.  Sources on the z=0 face sit over a void voxel layer (z < 6 mm),
+  fluence.  Sources on the z=0 face sit over a void voxel layer (z < 5 mm),
   where each photon is located per launch.
 * The sources with reference golden data (tests/golden/src_*.npz) against the
   reference runs, statistically, with both arithmetic policies.
