@@ -123,6 +123,9 @@ typedef struct mmcgb_config {
                                 < 0 diverging; NaN random direction, -inf Lambertian */
     const float* srcpattern; /* pattern source weights: srcparam1.w x srcparam2.w values (type 5)
                                 or srcparam1.x x .y x .z (type 15), row-major, else NULL */
+    int32_t issaveref;       /* 1: accumulate the weight of photons leaving through each exterior
+                                face per gate (diffuse reflectance/transmittance, -X) into
+                                mmcgb_result.dref */
 } mmcgb_config;
 
 /* Outputs.  Pointers may be NULL to skip an output; counts are always set. */
@@ -143,6 +146,9 @@ typedef struct mmcgb_result {
     uint64_t raytet;         /* ray-tetrahedron tests */
     uint64_t aborted;        /* photons stopped by the step budget */
     uint64_t outside;        /* photons whose launch position lies in no element (an error) */
+    double* dref;            /* issaveref: maxgate*nf exiting weight per exterior face (faces
+                                numbered as mmcgb_mesh_info's nf), divided by the launched weight
+                                when isnormalized, else NULL */
     float kernel_ms;         /* device time of the photon kernel */
 } mmcgb_result;
 

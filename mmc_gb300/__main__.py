@@ -47,6 +47,7 @@ def main(argv=None):
     ap.add_argument("-G", "--gpu", type=int, default=1)
     ap.add_argument("-D", "--debug", default="")
     ap.add_argument("-M", "--method", default="s")
+    ap.add_argument("-X", "--saveref", type=int)
     ap.add_argument("-r", "--root", default="")
     args = ap.parse_args(argv)
 
@@ -68,7 +69,7 @@ def main(argv=None):
         upd["outputtype"] = OUTPUT_LETTERS[args.outputtype.lower()]
     for k, a in (("issavedet", args.savedet), ("issaveexit", args.saveexit), ("issaveseed", args.saveseed),
                  ("ismomentum", args.momentum), ("isreflect", args.reflect), ("minenergy", args.minenergy),
-                 ("maxdetphoton", args.maxdetphoton)):
+                 ("maxdetphoton", args.maxdetphoton), ("issaveref", args.saveref)):
         if a is not None:
             upd[k] = a
     replay_file = None
@@ -110,6 +111,8 @@ def main(argv=None):
             io.write_dat(base + ".dat", res.field)
         else:
             io.write_bin(base + ".bin", res.field)
+    if res.dref is not None:  # exiting weight per exterior face: <session>_dref.dat (src/mmc_mesh.c:1726-1800)
+        io.write_dat(base + "_dref.dat", res.dref)
     if res.detp is not None and cfg.issavedet:
         io.write_mch(base + ".mch", res.detp, res.seeds if cfg.issaveseed else None,
                      maxmedia=np.asarray(cfg.media).shape[0] - 1,

@@ -175,6 +175,7 @@ class SimConfig:
     srcparam2: Sequence[float] = (0.0, 0.0, 0.0, 0.0)
     focus: float = 0.0                          # the reference's srcdir.w
     srcpattern: Optional[np.ndarray] = None     # pattern / pattern3d weights
+    issaveref: int = 0                          # exiting weight per exterior face (result.dref)
     save_field: bool = True
 
     @property
@@ -198,6 +199,7 @@ class SimConfig:
             pat = np.ascontiguousarray(self.srcpattern, dtype=np.float32).reshape(-1)
             keep["pattern"] = pat
             c.srcpattern = _ptr(pat)
+        c.issaveref = int(self.issaveref)
         c.e0 = int(self.e0)
         c.tstart, c.tend, c.tstep = float(self.tstart), float(self.tend), float(self.tstep)
         c.isreflect, c.isspecular, c.voidtime = int(self.isreflect), int(self.isspecular), int(self.voidtime)
@@ -249,6 +251,7 @@ class SimResult:
     photon_weight: Optional[np.ndarray] = None
     photon_steps: Optional[np.ndarray] = None
     photon_det: Optional[np.ndarray] = None
+    dref: Optional[np.ndarray] = None   # (maxgate, nf) exiting weight per exterior face (issaveref)
 
     @property
     def absorbed_fraction(self) -> float:
@@ -279,8 +282,9 @@ def _alloc_result(mesh: Mesh, cfg: SimConfig, trace: bool, out: Optional[np.ndar
         arrs["photon_det"] = np.zeros(n, np.int32)
     else:
         arrs["photon_weight"] = arrs["photon_steps"] = arrs["photon_det"] = None
+    arrs["dref"] = np.zeros((G, mesh.nf), np.float64) if cfg.issaveref else None
     r = N.Result()
-    for k in ("field", "detp", "seeds", "photon_weight", "photon_steps", "photon_det"):
+    for k in ("field", "detp", "seeds", "photon_weight", "photon_steps", "photon_det", "dref"):
         setattr(r, k, _ptr(arrs[k]))
     return r, arrs
 
@@ -293,7 +297,7 @@ def _make_result(r: N.Result, arrs) -> SimResult:
                      energytot=r.energytot, energyesc=r.energyesc, normalizer=r.normalizer,
                      raytet=int(r.raytet), aborted=int(r.aborted), kernel_ms=float(r.kernel_ms),
                      maxgate=int(r.maxgate), reclen=int(r.reclen), photon_weight=arrs["photon_weight"],
-                     photon_steps=arrs["photon_steps"], photon_det=arrs["photon_det"])
+                     photon_steps=arrs["photon_steps"], photon_det=arrs["photon_det"], dref=arrs["dref"])
 
 
 def simulate(mesh: Mesh, cfg: SimConfig, trace: bool = False, out: Optional[np.ndarray] = None) -> SimResult:

@@ -99,6 +99,7 @@ struct SimBuffers {
     double* energy = nullptr;
     unsigned long long* counters = nullptr;
     float* pattern = nullptr;
+    double* dref = nullptr;
     unsigned long long* rseed = nullptr;
     float* rweight = nullptr;
     float* rtime = nullptr;
@@ -180,6 +181,10 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     CK(B.alloc(&B.detcount, 1));
     CK(B.alloc(&B.energy, 2));
     CK(B.alloc(&B.counters, 3));
+    if (c.issaveref) {
+        CK(B.alloc(&B.dref, (size_t)m.nf * P.maxgate));
+        CK(cudaMemsetAsync(B.dref, 0, sizeof(double) * (size_t)m.nf * P.maxgate, stream));
+    }
     const size_t plen = pattern_len(c);
     if (plen) {
         CK(B.alloc(&B.pattern, plen));
@@ -274,6 +279,8 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     S.photon_weight = B.pw;
     S.photon_steps = B.ps;
     S.photon_det = B.pd;
+    S.dref = B.dref;
+    S.nf = m.nf;
     return MMCGB_OK;
 }
 
@@ -328,6 +335,8 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
     if (res->photon_weight) CK(cudaMemcpyAsync(res->photon_weight, B.pw, sizeof(float) * c.nphoton, cudaMemcpyDeviceToHost, stream));
     if (res->photon_steps) CK(cudaMemcpyAsync(res->photon_steps, B.ps, sizeof(unsigned) * c.nphoton, cudaMemcpyDeviceToHost, stream));
     if (res->photon_det) CK(cudaMemcpyAsync(res->photon_det, B.pd, sizeof(int) * c.nphoton, cudaMemcpyDeviceToHost, stream));
+    const size_t nref = (size_t)mesh->host.nf * P.maxgate;
+    if (res->dref && B.dref) CK(cudaMemcpyAsync(res->dref, B.dref, sizeof(double) * nref, cudaMemcpyDeviceToHost, stream));
     B.release();
     CK(cudaStreamSynchronize(stream));
     res->detected = detected;
@@ -341,6 +350,11 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
     res->aborted = counters[1];
     res->outside = counters[2];
     res->normalizer = normalizer;
+    if (res->dref && B.dref == nullptr && nref) std::memset(res->dref, 0, sizeof(double) * nref);
+    if (res->dref && c.isnormalized && energy[0] > 0) {  // src/mmc_mesh.c:2160-2167
+        const float normalizor = 1.f / (float)energy[0];
+        for (size_t i = 0; i < nref; i++) res->dref[i] *= normalizor;
+    }
     if (res->outside)
         return fail(MMCGB_E_SOURCE, std::to_string(res->outside) + " photons were launched at positions no element encloses");
     if (res->aborted) return fail(MMCGB_E_BUDGET, "some photons exceeded the per-photon step budget");

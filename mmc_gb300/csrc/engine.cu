@@ -1079,6 +1079,13 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                         PP(S.reclen - 3) = L.vy;
                         PP(S.reclen - 2) = L.vz;
                     }
+                    // diffuse reflectance/transmittance per exterior face, src/mmc_raytrace.c:2000-2003
+                    if (S.dref && L.eid < 0 && -L.eid <= S.nf) {
+                        const float gf = (L.ptime - S.tstart) * S.Rtstep;
+                        int gate = (gf < (float)(S.maxgate - 1)) ? (int)gf : S.maxgate - 1;
+                        gate = max(gate, 0);
+                        atomicAdd(S.dref + ((-L.eid) - 1) + (size_t)gate * S.nf, (double)L.weight);
+                    }
                     int detid = 0;
                     if (S.issavedet && L.eid <= 0) {
                         detid = finddetector(L, S);

@@ -95,6 +95,8 @@ struct SimDev {
     double* energy;        // [0] launched weight, [1] escaped weight
     unsigned long long* counters;  // [0] ray-tet tests, [1] aborted photons, [2] photons launched outside
     int ncounters;         // entries of `counters` (2 for callers that give two)
+    double* dref;          // issaveref: exiting weight per exterior face and gate, [gate][face]
+    int nf;                // exterior faces
     // optional per-photon trace (parity tests)
     float* photon_weight;
     unsigned int* photon_steps;

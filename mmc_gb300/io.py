@@ -98,7 +98,9 @@ def load_input(path: str):
     detpos = None
     if dets:
         detpos = np.array([[*d["Pos"][:3], d.get("R", 1.0)] for d in dets], np.float32)
-    dir4 = [float(x) for x in src.get("Dir", [0.0, 0.0, 1.0])]
+    # a 4th Dir entry is the focal length; the reference writes NaN/+-inf as strings
+    special = {"_NaN_": float("nan"), "_Inf_": float("inf"), "-_Inf_": float("-inf")}
+    dir4 = [special[x] if isinstance(x, str) else float(x) for x in src.get("Dir", [0.0, 0.0, 1.0])]
     srcdir = np.asarray(dir4[:3], np.float64)
     srcdir = srcdir / np.linalg.norm(srcdir)
     focus = dir4[3] if len(dir4) > 3 else 0.0
@@ -121,7 +123,7 @@ def load_input(path: str):
         srcparam2=tuple(float(x) for x in (list(src.get("Param2", [])) + [0.0] * 4)[:4]), focus=focus,
         srcpattern=pattern,
         e0=int(msh.get("InitElem", 0)), tstart=t0, tend=t1, tstep=dt,
-        isreflect=int(ses.get("DoMismatch", 1)), isspecular=int(ses.get("DoSpecular", 0)),
+        isreflect=int(ses.get("DoMismatch", 1)), issaveref=int(ses.get("DoSaveRef", 0)), isspecular=int(ses.get("DoSpecular", 0)),
         issavedet=int(ses.get("DoPartialPath", 1 if dets else 0)), issaveseed=int(ses.get("DoSaveSeed", 0)),
         issaveexit=int(ses.get("DoSaveExit", 0)), isnormalized=int(ses.get("DoNormalize", 1)),
         basisorder=int(ses.get("BasisOrder", 1)), outputtype=otype, nout=float(fwd.get("N0", 1.0)),

@@ -18,7 +18,7 @@ from . import _native
 from .core import SOURCE_TYPES, Mesh, SimConfig, simulate
 
 _SCALARS_INT = ["nphoton", "isreflect", "isspecular", "ismomentum", "issaveexit", "issavedet", "issaveseed",
-                "basisorder", "isnormalized", "maxdetphoton", "voidtime", "e0"]
+                "basisorder", "isnormalized", "maxdetphoton", "voidtime", "e0", "issaveref"]
 _SCALARS_FLOAT = ["tstart", "tstep", "tend", "roulettesize", "minenergy", "unitinmm", "nout"]
 _METHODS = {"plucker": None, "havel": None, "badouel": None, "elem": "elem", "grid": None}
 _OUTPUTS = {"flux", "fluence", "energy", "jacobian", "wl", "wp", "wn"}
@@ -124,6 +124,8 @@ def run(cfg: dict) -> dict:
                                              energytot=res.energytot, energyabs=res.energytot - res.energyesc,
                                              normalizer=res.normalizer, raytet=res.raytet,
                                              kernel_ms=res.kernel_ms)}
+    if sc.issaveref and res.dref is not None:
+        out["dref"] = res.dref.T  # [nf, maxgate], as pmmc (src/pmmc.cpp:1226-1234)
     if sc.issavedet and res.detp is not None and len(res.detp):
         out["detp"] = res.detp.T
         if sc.issaveseed and res.seeds is not None:

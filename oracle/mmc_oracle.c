@@ -977,6 +977,14 @@ static void onephoton(engine* g, uint64_t pidx, float* ppath, oracle_out* out, t
                 ppath[reclen - 7] = r->px; ppath[reclen - 6] = r->py; ppath[reclen - 5] = r->pz;
                 ppath[reclen - 4] = r->vx; ppath[reclen - 3] = r->vy; ppath[reclen - 2] = r->vz;
             }
+            /* diffuse reflectance per exterior face: src/mmc_raytrace.c:2000-2003 */
+            if (cfg->issaveref && out->dref && r->eid < 0 && -r->eid <= out->nf) {
+                float gf = (r->photontimer - cfg->tstart) * g->Rtstep;
+                int gate = (gf < (float)(g->maxgate - 1)) ? (int)gf : g->maxgate - 1;
+                if (gate < 0) gate = 0;
+#pragma omp atomic
+                out->dref[((-r->eid) - 1) + (size_t)gate * out->nf] += (double)r->weight;
+            }
             if (cfg->issavedet && r->eid <= 0) {
                 /* savedetphoton: src/mmc_core.cl:624-682 */
                 detid = finddetector(g, r);
@@ -1057,6 +1065,8 @@ int oracle_run(int nn, const float* node, int ne, const int* elem, const int* la
     g.maxgate = cfg->maxgate;
     g.reclen = (2 + (cfg->ismomentum > 0)) * g.M + (cfg->issaveexit > 0) * 6 + 1;
     out->reclen = g.reclen + 1;
+    out->nf = nf;
+    if (out->dref) memset(out->dref, 0, sizeof(double) * (size_t)nf * cfg->maxgate);
     size_t flen = (size_t)ne * cfg->maxgate;
     if (cfg->accum_f64) {
         g.f64 = out->field_raw;

@@ -56,6 +56,7 @@ typedef struct oracle_cfg {
     float srcparam1[4], srcparam2[4];
     float focus;            /* srcdir.w of the reference */
     const float* srcpattern;
+    int issaveref;          /* exiting weight per exterior face and gate into oracle_out.dref */
 } oracle_cfg;
 
 typedef struct oracle_out {
@@ -71,6 +72,8 @@ typedef struct oracle_out {
     uint64_t raytet;
     uint64_t aborted;
     uint64_t outside;       /* photons launched at a position no element encloses */
+    double* dref;           /* issaveref: maxgate*nf (raw, unnormalized), may be NULL */
+    int nf;                 /* exterior faces of the prepared mesh */
 } oracle_out;
 
 /* Mesh preparation (volumes with orientation fix, face neighbours, normals,

@@ -36,7 +36,7 @@ class OCfg(C.Structure):
         ("replayseed", C.c_void_p), ("replayweight", C.c_void_p), ("replaytime", C.c_void_p),
         ("accum_f64", C.c_int), ("step_budget", C.c_uint64),
         ("srctype", C.c_int), ("srcparam1", C.c_float * 4), ("srcparam2", C.c_float * 4), ("focus", C.c_float),
-        ("srcpattern", C.c_void_p),
+        ("srcpattern", C.c_void_p), ("issaveref", C.c_int),
     ]
 
 
@@ -46,6 +46,7 @@ class OOut(C.Structure):
         ("photon_weight", C.c_void_p), ("photon_steps", C.c_void_p), ("photon_det", C.c_void_p),
         ("detected", C.c_uint32), ("reclen", C.c_int), ("energytot", C.c_double),
         ("energyesc", C.c_double), ("raytet", C.c_uint64), ("aborted", C.c_uint64), ("outside", C.c_uint64),
+        ("dref", C.c_void_p), ("nf", C.c_int),
     ]
 
 
@@ -162,6 +163,7 @@ def _ocfg(cfg, maxgate, e0, keep):
     c.srcparam1 = (C.c_float * 4)(*[float(x) for x in getattr(cfg, "srcparam1", (0, 0, 0, 0))])
     c.srcparam2 = (C.c_float * 4)(*[float(x) for x in getattr(cfg, "srcparam2", (0, 0, 0, 0))])
     c.focus = float(getattr(cfg, "focus", 0.0))
+    c.issaveref = int(getattr(cfg, "issaveref", 0))
     pat = getattr(cfg, "srcpattern", None)
     if pat is not None:
         pat = np.ascontiguousarray(pat, np.float32).ravel()
@@ -195,6 +197,8 @@ def run(node, elem, label, cfg, nthreads=1, trace=False, normalize=True):
     pd = np.zeros(int(cfg.nphoton), np.int32) if trace else None
     out.field_raw, out.detp, out.seeds = _p(raw), _p(detp), _p(seeds)
     out.photon_weight, out.photon_steps, out.photon_det = _p(pw), _p(ps), _p(pd)
+    dref = np.zeros(maxgate * 4 * ne, np.float64) if getattr(cfg, "issaveref", 0) else None  # nf <= 4 ne
+    out.dref = _p(dref)
     rc = lib.oracle_run(nn, _p(node), ne, _p(elem), _p(label), C.byref(c), C.byref(out), int(nthreads))
     if rc:
         raise ValueError("oracle run failed")
@@ -204,6 +208,8 @@ def run(node, elem, label, cfg, nthreads=1, trace=False, normalize=True):
     saved = min(int(out.detected), int(cfg.maxdetphoton)) if cfg.issavedet else 0
     res["detp"] = detp[:saved] if detp is not None else None
     res["seeds"] = seeds[:saved] if seeds is not None else None
+    res["nf"] = int(out.nf)
+    res["dref"] = dref[:maxgate * out.nf].reshape(maxgate, out.nf) if dref is not None else None
     if normalize:
         datalen = nn if cfg.basisorder else ne
         field = np.zeros((maxgate, datalen), np.float64)

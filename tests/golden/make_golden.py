@@ -217,12 +217,58 @@ def run_ref(workdir, name, seed, photons, normalized=False, savedet=False):
     return out
 
 
+def run_ref_dref(workdir, name, seed, photons, nf, gates):
+    """Exiting weight per exterior face and gate of one reference run (-X 1),
+    read from its text output <session>_dref.dat (the binary writer of the
+    reference stores the fluence array under that name instead)."""
+    sess = f"{name}_{seed}_ref"
+    cmd = [REF, "-f", os.path.join(workdir, name + ".json"), "-c", "sse", "-M", "s", "-C", "0", "-b", "1",
+           "-U", "0", "-F", "ascii", "-s", sess, "-E", str(seed), "-n", str(photons), "-X", "1", "-D", "T"]
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    p = subprocess.run(cmd, cwd=workdir, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(p.stdout[-2000:])
+    vals = np.loadtxt(os.path.join(workdir, sess + "_dref.dat"))[:, 1]
+    return vals.reshape(gates, nf)
+
+
+def make_dref_case(wd):
+    """dref_cube6k: exiting weight per exterior face of the cube6k mesh, pencil
+    (30,30,0) +z, 5 gates of 1 ns, 1e5 photons; 10 runs + 6 null runs."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    name = "dref_cube6k"
+    m = meshgen.homogeneous_cube(n=10)
+    c = dict(mesh=m, photons=100000, t1=5e-9, dt=1e-9, det=None)
+    c["e0"] = oracle.initelem(m.node, m.elem, m.label, (30.0, 30.0, 0.0))
+    write_json(os.path.join(wd, name + ".json"), name, c)
+    nf = oracle.prep_mesh(m.node, m.elem, m.label)["nf"]
+    G = 5
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        runs = list(ex.map(lambda s: run_ref_dref(wd, name, s, c["photons"], nf, G), [SEED0 + k for k in range(NRUNS)]))
+        nulls = list(ex.map(lambda s: run_ref_dref(wd, name, s, c["photons"], nf, G),
+                            [SEED0 + 1000 + k for k in range(NNULL)]))
+    runs = np.stack(runs)              # (runs, G, nf)
+    per_face = runs.sum(1)
+    per_gate = runs.sum(2)
+    sys.path.insert(0, os.path.dirname(HERE))
+    import golden_checks as gc
+    fx = dict(nf=nf, gates=G, photons=c["photons"], face_mean=per_face.mean(0), face_std=per_face.std(0, ddof=1),
+              gate_mean=per_gate.mean(0), gate_std=per_gate.std(0, ddof=1))
+    st = [gc.zstats(x.sum(0), fx["face_mean"], fx["face_std"]) for x in nulls]
+    fx.update(null_face_frac=np.array([t[0] for t in st]), null_face_meanz=np.array([t[1] for t in st]))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **fx)
+    print(name, "nf", nf, "escaped per photon", per_gate.sum(1).mean() / c["photons"])
+
+
 def main(only=()):
     """Regenerates every case, or only the named ones (each case draws its
     random cell subset from its own generator, so cases are independent)."""
     if not os.path.exists(REF):
         subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
     with tempfile.TemporaryDirectory() as wd:
+        if not only or "dref_cube6k" in only:
+            make_dref_case(wd)
         for name, c in case_defs().items():
             if only and name not in only:
                 continue

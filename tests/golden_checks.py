@@ -39,6 +39,10 @@ def case_mesh_and_config(name, nphoton=None, seed=4242):
         cfg = SimConfig(media=m.media, nphoton=nphoton or int(fx["photons"]), seed=seed, srcpos=(30.0, 30.0, 0.0),
                         srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=0.5e-9, basisorder=0, isnormalized=0, issavedet=1,
                         detpos=meshgen.c1_detectors(), maxdetphoton=200000)
+    elif name == "dref_cube6k":
+        m = meshgen.homogeneous_cube(n=10)
+        cfg = SimConfig(media=m.media, nphoton=nphoton or int(fx["photons"]), seed=seed, srcpos=(30.0, 30.0, 0.0),
+                        srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=1e-9, basisorder=0, isnormalized=0, issaveref=1)
     elif name.startswith("src_"):
         # source types (tests/golden/make_golden.py SOURCE_CASES): the cube6k mesh, with the
         # voxel layer z < 6 mm void for the sources on the z=0 face
@@ -100,6 +104,17 @@ def check_field(raw, fx, media, label, photons):
     a = fx["absorbed"]
     if abs(absorbed - a.mean()) > 3 * a.std(ddof=1) * INFLATE:
         msgs.append(f"absorbed fraction {absorbed:.5f} vs reference {a.mean():.5f} +- {a.std(ddof=1):.5f}")
+    return msgs
+
+
+def check_dref(dref, fx):
+    """dref: (gates, nf) raw exiting weight per exterior face of one run."""
+    msgs = _zcheck("per-face exiting weight", dref.sum(0), fx["face_mean"], fx["face_std"], 100,
+                   fx["null_face_frac"], fx["null_face_meanz"])
+    gm, gs = fx["gate_mean"], fx["gate_std"]
+    gz = np.abs(dref.sum(1) - gm) / (gs * INFLATE)
+    if np.any(gz[gm > 0] > 4.0):
+        msgs.append(f"per-gate exiting totals z = {np.round(gz, 2)}")
     return msgs
 
 

@@ -101,3 +101,22 @@ def test_launch_outside_the_mesh_is_an_error(oracle_mod, void_layer_cube):
         simulate(mesh, cfg)
     assert e.value.code == 4
     assert oracle_mod.run(m.node, m.elem, m.label, cfg, nthreads=4)["outside"] > 0
+
+
+def test_exiting_weight_per_face(oracle_mod, gpu_ready):
+    """issaveref (-X): the exiting weight per exterior face and gate equals the
+    oracle's (IEEE arithmetic, to summation order) and matches the reference
+    runs statistically (fast arithmetic); normalized output divides by the
+    launched weight (src/mmc_mesh.c:2160-2167)."""
+    m, cfg, fx = gc.case_mesh_and_config("dref_cube6k")
+    mesh = Mesh(m.node, m.elem, m.label)
+    assert mesh.nf == int(fx["nf"])
+    small = dataclasses.replace(cfg, nphoton=20000, fast_math=0)
+    g = simulate(mesh, small)
+    o = oracle_mod.run(m.node, m.elem, m.label, small, nthreads=4, normalize=False)
+    np.testing.assert_allclose(g.dref, o["dref"], rtol=1e-9, atol=1e-12)
+    r = simulate(mesh, dataclasses.replace(cfg, fast_math=1))
+    msgs = gc.check_dref(r.dref, fx)
+    assert not msgs, "\n".join(msgs)
+    n = simulate(mesh, dataclasses.replace(small, isnormalized=1))
+    np.testing.assert_allclose(n.dref, g.dref / np.float32(g.energytot), rtol=1e-6)

@@ -25,6 +25,17 @@ def test_oracle_matches_reference_runs(oracle_mod, name):
     assert not msgs, "\n".join(msgs)
 
 
+def test_oracle_exiting_weight_matches_reference_runs(oracle_mod):
+    """Exiting weight per exterior face and gate (-X) against the reference."""
+    m, cfg, fx = gc.case_mesh_and_config("dref_cube6k")
+    r = oracle_mod.run(m.node, m.elem, m.label, cfg, nthreads=NTHREADS, normalize=False)
+    assert r["nf"] == int(fx["nf"])
+    msgs = gc.check_dref(r["dref"], fx)
+    assert not msgs, "\n".join(msgs)
+    # escaped weight = weight out through exterior faces + weight of photons stopped at the time limit
+    assert 0.99 * r["energyesc"] < r["dref"].sum() <= r["energyesc"]
+
+
 def test_oracle_detects_a_planted_error(oracle_mod):
     """The statistical check has power: a 5% change of the absorption
     coefficient, planted in the oracle's input, must fail it."""
