@@ -126,6 +126,11 @@ typedef struct mmcgb_config {
     int32_t issaveref;       /* 1: accumulate the weight of photons leaving through each exterior
                                 face per gate (diffuse reflectance/transmittance, -X) into
                                 mmcgb_result.dref */
+    int32_t method;          /* 0: element output (branchless Badouel, -M S); 1: dual-grid output
+                                (DMMC, -M G): fluence on a voxel grid over the mesh's bounding
+                                box, datalen = dim.x*dim.y*dim.z (mmcgb_grid_info), x fastest */
+    float gridstep;          /* voxel edge of the grid output in mm (the reference's Domain.Step);
+                                0 = 1 mm */
 } mmcgb_config;
 
 /* Outputs.  Pointers may be NULL to skip an output; counts are always set. */
@@ -171,6 +176,10 @@ int32_t mmcgb_mesh_export(const mmcgb_mesh* mesh, int32_t* elem, int32_t* facenb
                           float* evol, float* nvol);
 /* First element (1-based, by index) enclosing p, 0 if none
  * (src/mmc_mesh.c:1060-1090). */
+/* Dimensions and origin of the dual-grid output of `m` for voxel edge `step`
+ * (mesh_createdualmesh, src/mmc_mesh.c:349-381): origin = node minimum - 1e-6,
+ * dim = (int)((max - min + 2e-6) / step) + 1 per axis. */
+int32_t mmcgb_grid_info(const mmcgb_mesh* m, float step, int32_t dim[3], float origin[3]);
 int32_t mmcgb_mesh_locate(const mmcgb_mesh* mesh, const float p[3]);
 
 /* One simulation on a resident mesh (src/mmc_cu_host.cu:204-1528). */

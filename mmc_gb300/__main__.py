@@ -55,8 +55,8 @@ def main(argv=None):
     from .core import Mesh, simulate
     from .io import OUTPUT_LETTERS
 
-    if args.method not in ("s", "elem", "b"):
-        ap.error("only the branchless Badouel tracer (-M s) with element deposition is implemented")
+    if args.method.lower() not in ("s", "elem", "b", "g", "grid"):
+        ap.error("only the branchless Badouel tracer is implemented: -M s (element output) or -M G (dual grid)")
     mesh_d, cfg, meta = io.load_input(args.input)
     upd = {}
     if args.photon is not None:
@@ -78,6 +78,8 @@ def main(argv=None):
             replay_file = args.seed
         else:
             upd["seed"] = int(args.seed)
+    if args.method.lower() in ("g", "grid"):
+        upd["method"] = "grid"
     cfg = dataclasses.replace(cfg, **upd)
     session = args.session or meta["session"]
     fmt = (args.outputformat or meta["outputformat"]).lower()

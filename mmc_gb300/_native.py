@@ -55,7 +55,7 @@ class Config(C.Structure):
         ("accum_f64", C.c_int32), ("step_budget", C.c_uint64),
         ("threads", C.c_int32), ("blocks", C.c_int32), ("fast_math", C.c_int32), ("phased", C.c_int32),
         ("srcparam1", C.c_float * 4), ("srcparam2", C.c_float * 4), ("focus", C.c_float), ("srcpattern", C.c_void_p),
-        ("issaveref", C.c_int32),
+        ("issaveref", C.c_int32), ("method", C.c_int32), ("gridstep", C.c_float),
     ]
 
 
@@ -76,7 +76,7 @@ EXPORTS = [
     "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run", "mmcgb_session_begin", "mmcgb_session_launch",
     "mmcgb_session_sync", "mmcgb_session_end", "mmcgb_prepare_host", "mmcgb_normalize_host",
     "mmcgb_session_launch_batch", "mmcgb_session_stream", "mmcgb_session_launch_batch_on",
-    "mmcgb_session_launch_repeat",
+    "mmcgb_session_launch_repeat", "mmcgb_grid_info",
 ]
 
 
@@ -120,7 +120,9 @@ def load():
         lib.mmcgb_session_launch_batch_on.argtypes = [C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
                                                       C.POINTER(C.c_uint64), C.c_void_p]
         lib.mmcgb_session_launch_repeat.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32]
-        for name in ("mmcgb_session_launch_batch", "mmcgb_session_launch_batch_on", "mmcgb_session_launch_repeat", "mmcgb_prepare_host", "mmcgb_normalize_host", "mmcgb_session_begin", "mmcgb_session_launch", "mmcgb_session_sync", "mmcgb_session_end",
+        lib.mmcgb_grid_info.argtypes = [C.c_void_p, C.c_float, C.POINTER(C.c_int32), C.POINTER(C.c_float)]
+        for name in ("mmcgb_session_launch_batch", "mmcgb_session_launch_batch_on", "mmcgb_session_launch_repeat",
+                     "mmcgb_grid_info", "mmcgb_prepare_host", "mmcgb_normalize_host", "mmcgb_session_begin", "mmcgb_session_launch", "mmcgb_session_sync", "mmcgb_session_end",
                      "mmcgb_mesh_create", "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export",
                      "mmcgb_mesh_locate", "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run"):
             getattr(lib, name).restype = C.c_int32

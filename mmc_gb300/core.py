@@ -120,6 +120,14 @@ class Mesh:
         arr = (C.c_float * 3)(*[float(x) for x in p])
         return int(N.load().mmcgb_mesh_locate(self.handle, C.byref(arr)))
 
+    def grid_dims(self, step: float = 1.0):
+        """(dim.x, dim.y, dim.z) of the dual-grid output for voxel edge `step`
+        (mmcgb_grid_info); the grid field is (maxgate, dim.z, dim.y, dim.x)."""
+        dim = (C.c_int32 * 3)()
+        org = (C.c_float * 3)()
+        N.check(N.load().mmcgb_grid_info(self._h, float(step), dim, org))
+        return tuple(int(x) for x in dim)
+
     def close(self):
         if getattr(self, "_h", None) is not None:
             N.load().mmcgb_mesh_destroy(self._h)
@@ -176,6 +184,8 @@ class SimConfig:
     focus: float = 0.0                          # the reference's srcdir.w
     srcpattern: Optional[np.ndarray] = None     # pattern / pattern3d weights
     issaveref: int = 0                          # exiting weight per exterior face (result.dref)
+    method: object = "elem"                     # "elem" (element output) or "grid" (dual-grid, DMMC)
+    gridstep: float = 1.0                       # voxel edge of the grid output (mm)
     save_field: bool = True
 
     @property
@@ -200,6 +210,9 @@ class SimConfig:
             keep["pattern"] = pat
             c.srcpattern = _ptr(pat)
         c.issaveref = int(self.issaveref)
+        m = self.method
+        c.method = {"elem": 0, "grid": 1}[m] if isinstance(m, str) else int(m)
+        c.gridstep = float(self.gridstep)
         c.e0 = int(self.e0)
         c.tstart, c.tend, c.tstep = float(self.tstart), float(self.tend), float(self.tstep)
         c.isreflect, c.isspecular, c.voidtime = int(self.isreflect), int(self.isspecular), int(self.voidtime)
@@ -260,7 +273,10 @@ class SimResult:
 
 def _alloc_result(mesh: Mesh, cfg: SimConfig, trace: bool, out: Optional[np.ndarray] = None):
     G = cfg.maxgate
-    datalen = mesh.nn if cfg.basisorder else mesh.ne
+    if cfg.method in ("grid", 1):
+        datalen = int(np.prod(mesh.grid_dims(cfg.gridstep)))
+    else:
+        datalen = mesh.nn if cfg.basisorder else mesh.ne
     nmed = np.asarray(cfg.media).reshape(-1, 4).shape[0]
     reclen = 1 + (2 + (1 if cfg.ismomentum else 0)) * (nmed - 1) + (6 if cfg.issaveexit else 0) + 1
     arrs = {}

@@ -46,6 +46,34 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 int gates_of(const mmcgb_config& c) { return (int)((c.tend - c.tstart) / c.tstep + 0.5f); }
 
+// Dual-grid geometry (mesh_createdualmesh, src/mmc_mesh.c:349-381): float
+// arithmetic, bounding box padded by EPS, dim = (int)(span / step) + 1.
+void grid_geometry(const HostMesh& m, float step, unsigned dim[3], float nmin[3]) {
+    float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+    for (int i = 0; i < m.nn; i++)
+        for (int k = 0; k < 3; k++) {
+            lo[k] = std::min(m.node[3 * (size_t)i + k], lo[k]);
+            hi[k] = std::max(m.node[3 * (size_t)i + k], hi[k]);
+        }
+    for (int k = 0; k < 3; k++) {
+        lo[k] -= 1e-6f;
+        hi[k] += 1e-6f;
+        nmin[k] = lo[k];
+        dim[k] = (unsigned)(int)((hi[k] - lo[k]) / step) + 1u;
+    }
+}
+
+float grid_step(const mmcgb_config& c) { return c.gridstep > 0.f ? c.gridstep : 1.f; }
+
+// Fluence entries per gate: elements, or grid voxels for the dual-grid output.
+size_t frame_len(const HostMesh& m, const mmcgb_config& c) {
+    if (c.method != 1) return (size_t)m.ne;
+    unsigned dim[3];
+    float nmin[3];
+    grid_geometry(m, grid_step(c), dim, nmin);
+    return (size_t)dim[0] * dim[1] * dim[2];
+}
+
 // Source types whose photons all start at srcpos in the initial element (the
 // reference returns early from the launch for them, src/mmc_raytrace.c:2353-2357,
 // :2483-2485); the others are located per photon.
@@ -61,6 +89,13 @@ size_t pattern_len(const mmcgb_config& c) {
 
 int validate(const HostMesh& m, const mmcgb_config& c, std::string& err) {
     if (c.srctype < 0 || c.srctype > 17) { err = "srctype must be 0..17"; return MMCGB_E_ARG; }
+    if (c.method != 0 && c.method != 1) { err = "method must be 0 (element output) or 1 (dual grid)"; return MMCGB_E_ARG; }
+    if (c.method == 1 && c.replayseed) { err = "replay runs deposit on the elements (method 0)"; return MMCGB_E_ARG; }
+    if (c.method == 1 && !(c.gridstep >= 0.f && std::isfinite(c.gridstep))) { err = "gridstep must be >= 0"; return MMCGB_E_ARG; }
+    if (c.method == 1 && frame_len(m, c) * (size_t)gates_of(c) > 0xFFFFFFFFull) {
+        err = "grid output exceeds 2^32 entries: use a larger gridstep";
+        return MMCGB_E_ARG;
+    }
     if ((c.srctype == 5 || c.srctype == 15) && (!c.srcpattern || pattern_len(c) == 0)) {
         err = "pattern sources need srcpattern and a positive pattern size in srcparam1/srcparam2";
         return MMCGB_E_ARG;
@@ -164,7 +199,7 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     const int M = c.nmedia - 1;
     const int reclen_dev = (2 + (c.ismomentum > 0)) * M + (c.issaveexit > 0) * 6 + 1;
     P.reclen = reclen_dev + 1;
-    P.flen = (size_t)m.ne * P.maxgate;
+    P.flen = frame_len(m, c) * P.maxgate;
     SimBuffers& B = P.buf;
     B.stream = stream;
     const bool f64 = c.accum_f64 != 0;
@@ -281,6 +316,12 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     S.photon_det = B.pd;
     S.dref = B.dref;
     S.nf = m.nf;
+    S.grid = (c.method == 1) ? 1 : 0;
+    S.framelen = (unsigned)frame_len(m, c);
+    if (S.grid) {
+        grid_geometry(m, grid_step(c), S.gdim, S.gmin);
+        S.gstep_inv = 1.f / grid_step(c);
+    }
     return MMCGB_OK;
 }
 
@@ -298,13 +339,14 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
     double normalizer = 1.0;
     if (res->field) {
         // output stage on the device, then one copy of the final field
-        const size_t datalen = c.basisorder ? (size_t)mesh->host.nn : (size_t)mesh->host.ne;
+        const size_t datalen = c.method == 1 ? frame_len(mesh->host, c)
+                                             : (c.basisorder ? (size_t)mesh->host.nn : (size_t)mesh->host.ne);
         const size_t nout = datalen * P.maxgate;
         double* dout = nullptr;
         float* dnvol = nullptr;
         CK(cudaStreamSynchronize(stream));  // energies are needed by the normalization
         CK(cudaMallocAsync((void**)&dout, sizeof(double) * nout, stream));
-        if (c.basisorder) {
+        if (c.basisorder && c.method != 1) {
             const std::vector<float> nv = surface_fixed_nvol(mesh->host, c);
             CK(cudaMallocAsync((void**)&dnvol, sizeof(float) * nv.size(), stream));
             CK(cudaMemcpyAsync(dnvol, nv.data(), sizeof(float) * nv.size(), cudaMemcpyHostToDevice, stream));
@@ -325,6 +367,7 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
         A.nvol = dnvol;
         A.media = B.media;
         A.out = dout;
+        A.gridlen = c.method == 1 ? datalen : 0;
         CK(device_output(A, stream, &normalizer));
         CK(cudaMemcpyAsync(res->field, dout, sizeof(double) * nout, cudaMemcpyDeviceToHost, stream));
         CK(cudaFreeAsync(dout, stream));
@@ -565,7 +608,7 @@ int phased_setup(mmcgb_session* s, uint64_t nphoton, bool* use) {
     const bool sorted = nphoton <= 0xFFFFFFFFull;
     const size_t per = phase_bytes_per_photon(s->P.sim) + (sorted ? sizeof(unsigned) : 0);
     const size_t need = per * nphoton + sizeof(unsigned) * 2 * kBuckets + 4096;
-    const size_t plane = (size_t)s->mesh->host.ne * (c.accum_f64 ? 8 : 4);
+    const size_t plane = s->P.flen / (size_t)s->P.maxgate * (c.accum_f64 ? 8 : 4);
     if (c.phased > 0) {
         s->pq_span = c.phased;
     } else {
@@ -574,7 +617,7 @@ int phased_setup(mmcgb_session* s, uint64_t nphoton, bool* use) {
         s->pq_span = std::max(1, (int)(0.9 * (double)l2 / (double)plane) - 1);
     }
     if (c.phased == 0) {
-        const size_t fluence = (size_t)s->mesh->host.ne * s->P.maxgate * 8;
+        const size_t fluence = s->P.flen * 8;
         if (s->P.maxgate < 8 || fluence < ((size_t)64 << 20) || nphoton < 4000000ull ||
             s->pq_span >= s->P.maxgate)
             return MMCGB_OK;
@@ -954,8 +997,37 @@ int32_t mmcgb_normalize_host(const mmcgb_mesh_desc* desc, const mmcgb_config* cf
     if (rc) return fail(rc, err);
     if (cfg->nmedia < 2 || !cfg->media || h.maxlabel > cfg->nmedia - 1) return fail(MMCGB_E_ARG, "media table does not cover the mesh labels");
     if (!(cfg->tstep > 0.f)) return fail(MMCGB_E_ARG, "tstep must be positive");
+    if (cfg->method == 1) {  // dual-grid output: one scale factor, src/mmc_mesh.c:2204-2206
+        const size_t n = frame_len(h, *cfg) * gates_of(*cfg);
+        double norm = 1.0;
+        const float Et = (float)energytot;
+        if (cfg->isnormalized) {
+            if (cfg->outputtype == MMCGB_OUT_ENERGY) {
+                norm = 1.f / Et;
+            } else {
+                norm = 1.0 / (Et * cfg->unitinmm * cfg->unitinmm * cfg->unitinmm);
+                if (cfg->outputtype == MMCGB_OUT_FLUX) norm /= cfg->tstep;
+            }
+        }
+        for (size_t i = 0; i < n; i++) field[i] = raw[i] * norm;
+        if (normalizer) *normalizer = norm;
+        return MMCGB_OK;
+    }
     const double n = normalize_output(h, *cfg, gates_of(*cfg), raw, energytot, energyesc, field);
     if (normalizer) *normalizer = n;
+    return MMCGB_OK;
+}
+
+int32_t mmcgb_grid_info(const mmcgb_mesh* m, float step, int32_t dim[3], float origin[3]) {
+    if (!m || !dim) return fail(MMCGB_E_ARG, "null argument");
+    if (!(step > 0.f)) return fail(MMCGB_E_ARG, "step must be positive");
+    unsigned d[3];
+    float o[3];
+    grid_geometry(m->host, step, d, o);
+    for (int k = 0; k < 3; k++) {
+        dim[k] = (int32_t)d[k];
+        if (origin) origin[k] = o[k];
+    }
     return MMCGB_OK;
 }
 

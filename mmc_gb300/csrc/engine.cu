@@ -155,7 +155,9 @@ __device__ __forceinline__ void deposit(const SimDev& S, unsigned idx, float val
 // One branchless Badouel step with fused deposit.  Requires 1 <= L.eid <= ne.
 // REPLAY: the kernel may run replay simulations (output types wl, wp, wn and
 // the Jacobian); kernels for forward runs are compiled without those branches.
-template <class MP, bool REPLAY>
+// GEN: the kernel may deposit into a voxel grid (DMMC output) instead of the
+// elements.
+template <class MP, bool REPLAY, bool GEN>
 __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const float4* med) {
     const TetRec* R = S.rec + (L.eid - 1);
     const float4 nx = __ldg(&R->nx);
@@ -233,6 +235,51 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
         gate = max(gate, 0);
         if (ot != OT_ENERGY && !(REPLAY && (ot == OT_WP || ot == OT_WL)))
             ww = (prop.x < kEps) ? (currweight * Lmove) : MP::div(ww, prop.x);
+        if (GEN && S.grid) {
+            // DMMC: the step's loss is spread over 2(floor(Lmove/step)+1) equal segments,
+            // each deposited in the grid voxel of its midpoint (src/mmc_core.cl:1019-1218)
+            const int nseg = ((int)(Lmove * S.gstep_inv) + 1) << 1;
+            const float seg = MP::div(Lmove, (float)nseg);
+            const float segloss = MP::exp(-prop.x * seg);
+            const float tx = L.vx * seg, ty = L.vy * seg, tz = L.vz * seg;
+            float sx = (L.px - S.gmin[0]) + tx * 0.5f;
+            float sy = (L.py - S.gmin[1]) + ty * 0.5f;
+            float sz = (L.pz - S.gmin[2]) + tz * 0.5f;
+            const float loss = 1.f - att;
+            const float frac = (loss == 0.f) ? 0.f : MP::div(1.f - segloss, loss);
+            const unsigned tshift = (unsigned)gate * S.framelen;
+            float w0 = ww;
+            const bool flush = (L.faceid == -2 || !L.isend);
+            for (int k = 0; k < nseg; k++) {
+                const unsigned ix = (sx > 0.f) ? (unsigned)floorf(sx * S.gstep_inv) : 0u;
+                const unsigned iy = (sy > 0.f) ? (unsigned)floorf(sy * S.gstep_inv) : 0u;
+                const unsigned iz = (sz > 0.f) ? (unsigned)floorf(sz * S.gstep_inv) : 0u;
+                const unsigned newidx = min(iz, S.gdim[2] - 1) * (S.gdim[0] * S.gdim[1]) +
+                                        min(iy, S.gdim[1] - 1) * S.gdim[0] + min(ix, S.gdim[0] - 1) + tshift;
+                const float dw = w0 * frac;
+                if (L.oldidx == (unsigned)kIdUndef) L.oldidx = newidx;
+                if (newidx != L.oldidx) {
+                    if (L.oldw > 0.f) deposit(S, L.oldidx, L.oldw);
+                    L.oldidx = newidx;
+                    L.oldw = dw;
+                } else {
+                    L.oldw += dw;
+                }
+                if (flush) {
+                    deposit(S, newidx, L.oldw);
+                    L.oldw = 0.f;
+                }
+                w0 *= segloss;
+                sx += tx;
+                sy += ty;
+                sz += tz;
+            }
+            L.px = MP::mad(Lmove, L.vx, L.px);
+            L.py = MP::mad(Lmove, L.vy, L.py);
+            L.pz = MP::mad(Lmove, L.vz, L.pz);
+            L.slen = (L.faceid == -2) ? 0.f : L.slen;
+            return;
+        }
         const unsigned newidx = (unsigned)(L.eid - 1) + (unsigned)(gate * S.ne);
         if (L.oldidx == (unsigned)kIdUndef) L.oldidx = newidx;
         if (newidx != L.oldidx) {
@@ -979,7 +1026,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
 
         // ---- (2) one ray-tet step ----
         const bool bad_elem = (L.eid < 1 || L.eid > S.ne);  // defensive: never expected
-        if (!bad_elem) raytet_step<MP, REPLAY>(L, S, med);
+        if (!bad_elem) raytet_step<MP, REPLAY, SRC>(L, S, med);
         L.steps++;
         tally.raytet++;
         bool ended = false;
@@ -1176,10 +1223,11 @@ size_t smem_bytes(int nmed_rows, int reclen_max, int threads, int want_seed) {
     return b;
 }
 
-// Kernels compiled with the general source launch (SRC) serve simulations
-// whose source is not a pencil beam starting in a known element; the others
-// carry only the pencil launch, which keeps the step loop's registers free.
-bool general_source(const SimDev& s) { return s.srctype != ST_PENCIL || s.e0 <= 0; }
+// Kernels compiled with the general launch and deposit (SRC) serve
+// simulations whose source is not a pencil beam starting in a known element,
+// or that deposit into a voxel grid; the others carry only the pencil launch
+// and the element deposit, which keeps the step loop's registers free.
+bool general_source(const SimDev& s) { return s.srctype != ST_PENCIL || s.e0 <= 0 || s.grid; }
 
 }  // namespace
 

@@ -95,6 +95,12 @@ struct SimDev {
     double* energy;        // [0] launched weight, [1] escaped weight
     unsigned long long* counters;  // [0] ray-tet tests, [1] aborted photons, [2] photons launched outside
     int ncounters;         // entries of `counters` (2 for callers that give two)
+    // DMMC grid output (method 1): voxel (x,y,z) of gate g at g*framelen + (z*dim.y + y)*dim.x + x
+    int grid;
+    float gstep_inv;       // 1 / voxel edge
+    float gmin[3];         // grid origin (node minimum - EPS)
+    unsigned gdim[3];
+    unsigned framelen;     // fluence entries per gate: ne, or dim.x*dim.y*dim.z
     double* dref;          // issaveref: exiting weight per exterior face and gate, [gate][face]
     int nf;                // exterior faces
     // optional per-photon trace (parity tests)

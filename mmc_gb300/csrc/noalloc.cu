@@ -90,6 +90,7 @@ extern "C" int32_t mmcgb_simulate_noalloc(mmcgb_mesh* mesh, const mmcgb_config* 
         return fail(MMCGB_E_ARG, "no-alloc entry: detnum must be 0.." + std::to_string(kNoAllocMaxDet));
     if (!c->accum_f64) return fail(MMCGB_E_ARG, "no-alloc entry accumulates in float64 only");
     if (c->replayseed) return fail(MMCGB_E_ARG, "no-alloc entry does not replay");
+    if (c->method != 0) return fail(MMCGB_E_ARG, "no-alloc entry deposits on the elements (method 0)");
     if (mesh->host.maxlabel > c->nmedia - 1) return fail(MMCGB_E_ARG, "mesh label exceeds the number of media");
     if (c->issavedet && (!out->detp || !out->detcount || c->maxdetphoton == 0))
         return fail(MMCGB_E_ARG, "issavedet needs detp, detcount and maxdetphoton");

@@ -104,6 +104,23 @@ cudaError_t device_output(const DeviceOutputArgs& A, cudaStream_t st, double* no
     const size_t nraw = (size_t)ne * G;
     const size_t nout = (size_t)(cfg.basisorder ? nn : ne) * G;
     cudaError_t e;
+    if (A.gridlen) {
+        // dual-grid output: one scale factor, src/mmc_mesh.c:2204-2206 (no volume division)
+        const size_t n = A.gridlen * G;
+        double norm = 1.0;
+        const float Et = (float)A.energytot;
+        if (cfg.isnormalized) {
+            if (cfg.outputtype == OT_ENERGY) {
+                norm = 1.f / Et;
+            } else {
+                norm = 1.0 / (Et * cfg.unitinmm * cfg.unitinmm * cfg.unitinmm);
+                if (cfg.outputtype == OT_FLUX) norm /= cfg.tstep;
+            }
+        }
+        k_elem<<<grid_for(n), 256, 0, st>>>(A.f64, A.f32a, A.f32b, A.evol, A.label, A.media, ne, n, 0, norm, A.out);
+        *normalizer = norm;
+        return cudaGetLastError();
+    }
     double* scratch = nullptr;  // [0] sum
     if ((e = cudaMallocAsync((void**)&scratch, sizeof(double) * 2, st)) != cudaSuccess) return e;
     cudaMemsetAsync(scratch, 0, sizeof(double) * 2, st);

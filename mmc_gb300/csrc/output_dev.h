@@ -24,6 +24,7 @@ struct DeviceOutputArgs {
     const float* nvol;      // nodal volumes after the surface fix (basisorder 1)
     const float4* media;
     double* out;            // maxgate * datalen
+    size_t gridlen;         // dual-grid output (cfg->method 1): voxels per gate, else 0
 };
 
 cudaError_t device_output(const DeviceOutputArgs& args, cudaStream_t stream, double* normalizer);

@@ -123,7 +123,8 @@ def load_input(path: str):
         srcparam2=tuple(float(x) for x in (list(src.get("Param2", [])) + [0.0] * 4)[:4]), focus=focus,
         srcpattern=pattern,
         e0=int(msh.get("InitElem", 0)), tstart=t0, tend=t1, tstep=dt,
-        isreflect=int(ses.get("DoMismatch", 1)), issaveref=int(ses.get("DoSaveRef", 0)), isspecular=int(ses.get("DoSpecular", 0)),
+        isreflect=int(ses.get("DoMismatch", 1)), issaveref=int(ses.get("DoSaveRef", 0)),
+        gridstep=float(np.ravel(dom.get("Step", [1.0]))[0]), isspecular=int(ses.get("DoSpecular", 0)),
         issavedet=int(ses.get("DoPartialPath", 1 if dets else 0)), issaveseed=int(ses.get("DoSaveSeed", 0)),
         issaveexit=int(ses.get("DoSaveExit", 0)), isnormalized=int(ses.get("DoNormalize", 1)),
         basisorder=int(ses.get("BasisOrder", 1)), outputtype=otype, nout=float(fwd.get("N0", 1.0)),

@@ -20,7 +20,7 @@ from .core import SOURCE_TYPES, Mesh, SimConfig, simulate
 _SCALARS_INT = ["nphoton", "isreflect", "isspecular", "ismomentum", "issaveexit", "issavedet", "issaveseed",
                 "basisorder", "isnormalized", "maxdetphoton", "voidtime", "e0", "issaveref"]
 _SCALARS_FLOAT = ["tstart", "tstep", "tend", "roulettesize", "minenergy", "unitinmm", "nout"]
-_METHODS = {"plucker": None, "havel": None, "badouel": None, "elem": "elem", "grid": None}
+_METHODS = {"plucker": None, "havel": None, "badouel": None, "elem": "elem", "grid": "grid"}
 _OUTPUTS = {"flux", "fluence", "energy", "jacobian", "wl", "wp", "wn"}
 
 
@@ -56,7 +56,10 @@ def _parse(cfg: dict):
     srctype = str(cfg.get("srctype", "pencil")).lower()
     if srctype not in SOURCE_TYPES:
         raise ValueError(f"unknown srctype '{srctype}'")
-    kw = dict(media=prop, srcpos=tuple(np.asarray(cfg["srcpos"], np.float64).ravel()[:3]), srctype=srctype)
+    kw = dict(media=prop, srcpos=tuple(np.asarray(cfg["srcpos"], np.float64).ravel()[:3]), srctype=srctype,
+              method=_METHODS[method])
+    if "steps" in cfg:  # dual-grid voxel edge (the reference takes steps[0] for all axes)
+        kw["gridstep"] = float(np.asarray(cfg["steps"], np.float64).ravel()[0])
     if "srcdir" in cfg:
         d4 = np.asarray(cfg["srcdir"], np.float64).ravel()
         d = d4[:3]
@@ -115,12 +118,17 @@ def run(cfg: dict) -> dict:
         else:
             res = simulate(mesh, sc)
             nph = sc.nphoton
+        mesh_dims = mesh.grid_dims(sc.gridstep) if sc.method == "grid" else None
         mesh.close()
     except _native.MmcgbError as e:
         if e.code == 1:
             raise ValueError(str(e)) from e
         raise RuntimeError(str(e)) from e
-    out = {"flux": res.field.T, "stat": dict(runtime=(time.perf_counter() - t0) * 1e3, nphoton=nph,
+    field = res.field.T
+    if sc.method == "grid":  # [dim.x, dim.y, dim.z, maxgate], x fastest as the reference
+        dx, dy, dz = mesh_dims
+        field = res.field.reshape(-1, dz, dy, dx).transpose(3, 2, 1, 0)
+    out = {"flux": field, "stat": dict(runtime=(time.perf_counter() - t0) * 1e3, nphoton=nph,
                                              energytot=res.energytot, energyabs=res.energytot - res.energyesc,
                                              normalizer=res.normalizer, raytet=res.raytet,
                                              kernel_ms=res.kernel_ms)}

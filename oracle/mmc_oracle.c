@@ -309,6 +309,11 @@ typedef struct {
     const int* elem;
     const int* type;
     const locgrid* grid;
+    int dgrid;         /* dual-grid output (method 1) */
+    float gstep_inv;
+    float gmin[3];
+    uint32_t gdim[3];
+    uint32_t framelen; /* fluence entries per gate */
     const int* facenb;
     const float* nrm;
     const oracle_cfg* cfg;
@@ -422,6 +427,50 @@ static float raytet_step(engine* g, ray* r) {
         uint32_t tshift = (uint32_t)(gate * g->ne);
         if (cfg->outputtype != OT_ENERGY && cfg->outputtype != OT_WP && cfg->outputtype != OT_WL)
             ww = (mua < O_EPS) ? (currweight * r->Lmove) : (ww / mua);
+        if (g->dgrid) {
+            /* dual-grid (DMMC) deposit: src/mmc_core.cl:1019-1218, src/mmc_raytrace.c:1614-1666;
+             * voxel indices clamped to the grid */
+            int nseg = ((int)(r->Lmove * g->gstep_inv) + 1) << 1;
+            float seg = r->Lmove / (float)nseg;
+            float segloss = oracle_expf(-mua * seg);
+            float tx = r->vx * seg, ty = r->vy * seg, tz = r->vz * seg;
+            float sx = (r->px - g->gmin[0]) + tx * 0.5f;
+            float sy = (r->py - g->gmin[1]) + ty * 0.5f;
+            float sz = (r->pz - g->gmin[2]) + tz * 0.5f;
+            float loss = 1.f - totalloss;
+            float frac = (loss == 0.f) ? 0.f : (1.f - segloss) / loss;
+            uint32_t gshift = (uint32_t)gate * g->framelen;
+            float w0 = ww;
+            int flush = (r->faceid == -2 || !r->isend);
+            for (int k = 0; k < nseg; k++) {
+                uint32_t ix = (sx > 0.f) ? (uint32_t)floorf(sx * g->gstep_inv) : 0u;
+                uint32_t iy = (sy > 0.f) ? (uint32_t)floorf(sy * g->gstep_inv) : 0u;
+                uint32_t iz = (sz > 0.f) ? (uint32_t)floorf(sz * g->gstep_inv) : 0u;
+                if (ix > g->gdim[0] - 1) ix = g->gdim[0] - 1;
+                if (iy > g->gdim[1] - 1) iy = g->gdim[1] - 1;
+                if (iz > g->gdim[2] - 1) iz = g->gdim[2] - 1;
+                uint32_t nidx = iz * (g->gdim[0] * g->gdim[1]) + iy * g->gdim[0] + ix + gshift;
+                float dw = w0 * frac;
+                if (r->oldidx == (uint32_t)O_ID_UNDEF) r->oldidx = nidx;
+                if (nidx != r->oldidx) {
+                    if (r->oldweight > 0.f) deposit(g, r->oldidx, r->oldweight);
+                    r->oldidx = nidx;
+                    r->oldweight = dw;
+                } else {
+                    r->oldweight += dw;
+                }
+                if (flush) {
+                    deposit(g, nidx, r->oldweight);
+                    r->oldweight = 0.f;
+                }
+                w0 *= segloss;
+                sx += tx; sy += ty; sz += tz;
+            }
+            r->px = r->px + r->Lmove * r->vx;
+            r->py = r->py + r->Lmove * r->vy;
+            r->pz = r->pz + r->Lmove * r->vz;
+            return (r->faceid == -2) ? 0.f : r->slen;
+        }
         uint32_t newidx = (uint32_t)(r->eid - 1) + tshift;
         if (r->oldidx == (uint32_t)O_ID_UNDEF) r->oldidx = newidx;
         if (newidx != r->oldidx) {
@@ -548,6 +597,21 @@ static int finddetector(const engine* g, const ray* r) {
             return i + 1;
     }
     return 0;
+}
+
+void oracle_grid_dims(int nn, const float* node, float step, int dim[3], float nmin[3]) {
+    float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+    for (int i = 0; i < nn; i++)
+        for (int k = 0; k < 3; k++) {
+            if (node[3 * (size_t)i + k] < lo[k]) lo[k] = node[3 * (size_t)i + k];
+            if (node[3 * (size_t)i + k] > hi[k]) hi[k] = node[3 * (size_t)i + k];
+        }
+    for (int k = 0; k < 3; k++) {
+        lo[k] -= O_EPS;
+        hi[k] += O_EPS;
+        nmin[k] = lo[k];
+        dim[k] = (int)((hi[k] - lo[k]) / step) + 1;
+    }
 }
 
 static void grid_range(const float* node, const int* e, const locgrid* g, int b0[3], int b1[3]) {
@@ -1067,7 +1131,17 @@ int oracle_run(int nn, const float* node, int ne, const int* elem, const int* la
     out->reclen = g.reclen + 1;
     out->nf = nf;
     if (out->dref) memset(out->dref, 0, sizeof(double) * (size_t)nf * cfg->maxgate);
-    size_t flen = (size_t)ne * cfg->maxgate;
+    g.framelen = (uint32_t)ne;
+    if (cfg->method == 1) {
+        int d[3];
+        float step = cfg->gridstep > 0.f ? cfg->gridstep : 1.f;
+        oracle_grid_dims(nn, node, step, d, g.gmin);
+        g.dgrid = 1;
+        g.gstep_inv = 1.f / step;
+        for (int k = 0; k < 3; k++) g.gdim[k] = (uint32_t)d[k];
+        g.framelen = (uint32_t)d[0] * (uint32_t)d[1] * (uint32_t)d[2];
+    }
+    size_t flen = (size_t)g.framelen * cfg->maxgate;
     if (cfg->accum_f64) {
         g.f64 = out->field_raw;
         memset(g.f64, 0, sizeof(double) * flen);

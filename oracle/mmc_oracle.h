@@ -57,6 +57,8 @@ typedef struct oracle_cfg {
     float focus;            /* srcdir.w of the reference */
     const float* srcpattern;
     int issaveref;          /* exiting weight per exterior face and gate into oracle_out.dref */
+    int method;             /* 0 element output, 1 dual-grid (DMMC) output */
+    float gridstep;         /* voxel edge of the grid output (mm), 0 = 1 */
 } oracle_cfg;
 
 typedef struct oracle_out {
@@ -82,6 +84,10 @@ typedef struct oracle_out {
 int oracle_prep_mesh(int nn, const float* node, int ne, const int* elem, const int* label,
                      const int* facenb_in, int* elem_out, int* facenb_out, float* normals,
                      float* evol, float* nvol, int* nf);
+
+/* Dual-grid dimensions for voxel edge `step`: mesh_createdualmesh,
+ * src/mmc_mesh.c:349-381 (bounding box padded by 1e-6, dim = (int)(span/step)+1). */
+void oracle_grid_dims(int nn, const float* node, float step, int dim[3], float nmin[3]);
 
 /* First element (by index) whose bounding box and barycentric test enclose p. */
 int oracle_initelem(int nn, const float* node, int ne, const int* elem, const float* p);

@@ -36,7 +36,7 @@ class OCfg(C.Structure):
         ("replayseed", C.c_void_p), ("replayweight", C.c_void_p), ("replaytime", C.c_void_p),
         ("accum_f64", C.c_int), ("step_budget", C.c_uint64),
         ("srctype", C.c_int), ("srcparam1", C.c_float * 4), ("srcparam2", C.c_float * 4), ("focus", C.c_float),
-        ("srcpattern", C.c_void_p), ("issaveref", C.c_int),
+        ("srcpattern", C.c_void_p), ("issaveref", C.c_int), ("method", C.c_int), ("gridstep", C.c_float),
     ]
 
 
@@ -115,6 +115,16 @@ def prep_mesh(node, elem, label):
     return dict(elem=ee, facenb=fnb, normals=nrm, evol=evol, nvol=nvol, nf=nf.value)
 
 
+def grid_dims(node, step):
+    """(dim.x, dim.y, dim.z) of the dual-grid output (oracle_grid_dims)."""
+    lib = load()
+    node = np.ascontiguousarray(node, np.float32).reshape(-1, 3)
+    dim = (C.c_int * 3)()
+    org = (C.c_float * 3)()
+    lib.oracle_grid_dims(node.shape[0], _p(node), C.c_float(float(step)), dim, org)
+    return tuple(int(x) for x in dim)
+
+
 def initelem(node, elem, label, p):
     lib = load()
     node, elem, label = _arr(node, elem, label)
@@ -164,6 +174,9 @@ def _ocfg(cfg, maxgate, e0, keep):
     c.srcparam2 = (C.c_float * 4)(*[float(x) for x in getattr(cfg, "srcparam2", (0, 0, 0, 0))])
     c.focus = float(getattr(cfg, "focus", 0.0))
     c.issaveref = int(getattr(cfg, "issaveref", 0))
+    m = getattr(cfg, "method", 0)
+    c.method = {"elem": 0, "grid": 1}[m] if isinstance(m, str) else int(m)
+    c.gridstep = float(getattr(cfg, "gridstep", 1.0))
     pat = getattr(cfg, "srcpattern", None)
     if pat is not None:
         pat = np.ascontiguousarray(pat, np.float32).ravel()
@@ -186,7 +199,10 @@ def run(node, elem, label, cfg, nthreads=1, trace=False, normalize=True):
     e0 = max(int(e0), 0)
     keep = []
     c = _ocfg(cfg, maxgate, e0, keep)
-    raw = np.zeros((maxgate, ne), np.float64)
+    framelen = ne
+    if c.method == 1:
+        framelen = int(np.prod(grid_dims(node, cfg.gridstep if cfg.gridstep > 0 else 1.0)))
+    raw = np.zeros((maxgate, framelen), np.float64)
     nmed = c.nmedia
     reclen = 1 + (2 + (1 if cfg.ismomentum else 0)) * (nmed - 1) + (6 if cfg.issaveexit else 0) + 1
     out = OOut()
@@ -210,7 +226,18 @@ def run(node, elem, label, cfg, nthreads=1, trace=False, normalize=True):
     res["seeds"] = seeds[:saved] if seeds is not None else None
     res["nf"] = int(out.nf)
     res["dref"] = dref[:maxgate * out.nf].reshape(maxgate, out.nf) if dref is not None else None
-    if normalize:
+    if normalize and c.method == 1:  # dual grid: one scale factor (src/mmc_mesh.c:2204-2206)
+        norm = 1.0
+        if cfg.isnormalized:
+            et = float(np.float32(out.energytot))
+            if c.outputtype == OUTPUT_TYPES["energy"]:
+                norm = float(np.float32(1.0) / np.float32(et))
+            else:
+                norm = 1.0 / (et * cfg.unitinmm ** 3)
+                if c.outputtype == OUTPUT_TYPES["flux"]:
+                    norm /= float(np.float32(cfg.tstep))
+        res["normalizer"], res["field"] = norm, raw * norm
+    elif normalize:
         datalen = nn if cfg.basisorder else ne
         field = np.zeros((maxgate, datalen), np.float64)
         res["normalizer"] = lib.oracle_normalize(nn, _p(node), ne, _p(elem), _p(label), C.byref(c), _p(raw),

@@ -261,6 +261,50 @@ def make_dref_case(wd):
     print(name, "nf", nf, "escaped per photon", per_gate.sum(1).mean() / c["photons"])
 
 
+def run_ref_grid(workdir, name, seed, photons, nvox):
+    """Dual-grid (DMMC, -M G) fluence of one reference run, unnormalized."""
+    sess = f"{name}_{seed}_grid"
+    cmd = [REF, "-f", os.path.join(workdir, name + ".json"), "-c", "sse", "-M", "G", "-C", "0", "-b", "1",
+           "-U", "0", "-F", "bin", "-s", sess, "-E", str(seed), "-n", str(photons), "-D", "T"]
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    p = subprocess.run(cmd, cwd=workdir, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(p.stdout[-2000:])
+    raw = np.fromfile(os.path.join(workdir, sess + ".bin"), np.float64)
+    return raw.reshape(-1, nvox)
+
+
+def make_grid_case(wd):
+    """grid_cube6k: the cube6k run (pencil (30,30,0) +z, one 5 ns gate, 1e5
+    photons) with dual-grid output on 2 mm voxels; 10 runs + 6 null runs."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    name = "grid_cube6k"
+    m = meshgen.homogeneous_cube(n=10)
+    c = dict(mesh=m, photons=100000, t1=5e-9, dt=5e-9, det=None)
+    c["e0"] = oracle.initelem(m.node, m.elem, m.label, (30.0, 30.0, 0.0))
+    path = os.path.join(wd, name + ".json")
+    write_json(path, name, c)
+    cfgj = json.load(open(path))
+    cfgj["Domain"]["Step"] = [2.0, 2.0, 2.0]
+    json.dump(cfgj, open(path, "w"))
+    dim = oracle.grid_dims(m.node, 2.0)
+    nvox = int(np.prod(dim))
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        runs = list(ex.map(lambda s: run_ref_grid(wd, name, s, c["photons"], nvox), [SEED0 + k for k in range(NRUNS)]))
+        nulls = list(ex.map(lambda s: run_ref_grid(wd, name, s, c["photons"], nvox),
+                            [SEED0 + 1000 + k for k in range(NNULL)]))
+    vox = np.stack([r.sum(0) for r in runs])
+    sys.path.insert(0, os.path.dirname(HERE))
+    import golden_checks as gc
+    fx = dict(dim=np.array(dim), photons=c["photons"], step=2.0, vox_mean=vox.mean(0), vox_std=vox.std(0, ddof=1),
+              total=np.array([r.sum() for r in runs]))
+    st = [gc.zstats(x.sum(0), fx["vox_mean"], fx["vox_std"]) for x in nulls]
+    fx.update(null_vox_frac=np.array([t[0] for t in st]), null_vox_meanz=np.array([t[1] for t in st]))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **fx)
+    print(name, "dim", dim, "absorbed per photon", fx["total"].mean() * 0.005 / c["photons"])
+
+
 def main(only=()):
     """Regenerates every case, or only the named ones (each case draws its
     random cell subset from its own generator, so cases are independent)."""
@@ -269,6 +313,8 @@ def main(only=()):
     with tempfile.TemporaryDirectory() as wd:
         if not only or "dref_cube6k" in only:
             make_dref_case(wd)
+        if not only or "grid_cube6k" in only:
+            make_grid_case(wd)
         for name, c in case_defs().items():
             if only and name not in only:
                 continue

@@ -39,6 +39,11 @@ def case_mesh_and_config(name, nphoton=None, seed=4242):
         cfg = SimConfig(media=m.media, nphoton=nphoton or int(fx["photons"]), seed=seed, srcpos=(30.0, 30.0, 0.0),
                         srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=0.5e-9, basisorder=0, isnormalized=0, issavedet=1,
                         detpos=meshgen.c1_detectors(), maxdetphoton=200000)
+    elif name == "grid_cube6k":
+        m = meshgen.homogeneous_cube(n=10)
+        cfg = SimConfig(media=m.media, nphoton=nphoton or int(fx["photons"]), seed=seed, srcpos=(30.0, 30.0, 0.0),
+                        srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=5e-9, basisorder=0, isnormalized=0, method="grid",
+                        gridstep=float(fx["step"]))
     elif name == "dref_cube6k":
         m = meshgen.homogeneous_cube(n=10)
         cfg = SimConfig(media=m.media, nphoton=nphoton or int(fx["photons"]), seed=seed, srcpos=(30.0, 30.0, 0.0),
@@ -115,6 +120,16 @@ def check_dref(dref, fx):
     gz = np.abs(dref.sum(1) - gm) / (gs * INFLATE)
     if np.any(gz[gm > 0] > 4.0):
         msgs.append(f"per-gate exiting totals z = {np.round(gz, 2)}")
+    return msgs
+
+
+def check_grid(raw, fx):
+    """raw: (gates, voxels) dual-grid deposits of one run."""
+    msgs = _zcheck("per-voxel", raw.sum(0), fx["vox_mean"], fx["vox_std"], 100,
+                   fx["null_vox_frac"], fx["null_vox_meanz"])
+    t = fx["total"]
+    if abs(raw.sum() - t.mean()) > 3 * t.std(ddof=1) * INFLATE:
+        msgs.append(f"grid total {raw.sum():.1f} vs reference {t.mean():.1f} +- {t.std(ddof=1):.1f}")
     return msgs
 
 

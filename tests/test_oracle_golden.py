@@ -36,6 +36,17 @@ def test_oracle_exiting_weight_matches_reference_runs(oracle_mod):
     assert 0.99 * r["energyesc"] < r["dref"].sum() <= r["energyesc"]
 
 
+def test_oracle_dual_grid_matches_reference_runs(oracle_mod):
+    """Dual-grid (DMMC, -M G) fluence on 2 mm voxels against the reference."""
+    m, cfg, fx = gc.case_mesh_and_config("grid_cube6k")
+    assert oracle_mod.grid_dims(m.node, cfg.gridstep) == tuple(int(x) for x in fx["dim"])
+    r = oracle_mod.run(m.node, m.elem, m.label, cfg, nthreads=NTHREADS, normalize=False)
+    msgs = gc.check_grid(r["raw"], fx)
+    assert not msgs, "\n".join(msgs)
+    # every deposit is the lost weight divided by mua: the grid holds the absorbed energy
+    assert r["raw"].sum() * m.media[1, 0] == pytest.approx(r["energytot"] - r["energyesc"], rel=1e-5)
+
+
 def test_oracle_detects_a_planted_error(oracle_mod):
     """The statistical check has power: a 5% change of the absorption
     coefficient, planted in the oracle's input, must fail it."""
