@@ -29,7 +29,7 @@ from typing import Optional
 
 import numpy as np
 
-from .core import Mesh, SimConfig, simulate
+from .core import Mesh, SimConfig, simulate, simulate_batch
 
 R_C0 = np.float32(3.335640951981520e-12)
 
@@ -87,8 +87,12 @@ def jacobians(mesh: Mesh, cfg: SimConfig, detp: np.ndarray, seeds: np.ndarray, r
     w = detected_weight(detp, np.asarray(cfg.media), cfg.unitinmm).astype(np.float64)
     if coef is not None:
         w = w * np.asarray(coef, np.float64)
-    wl, _ = replay(mesh, cfg, detp, seeds, "wl", replaydet, weight=w.astype(np.float32))
-    wn, _ = replay(mesh, cfg, detp, seeds, "wn", replaydet, weight=w.astype(np.float32))
+    # both replays (path lengths and scatter counts) share one batched launch
+    s, _, t, idx = replay_inputs(detp, seeds, np.asarray(cfg.media), replaydet, cfg.tstart, cfg.tend, cfg.unitinmm)
+    base = dataclasses.replace(cfg, nphoton=len(idx), replayseed=s, replayweight=w[idx].astype(np.float32),
+                               replaytime=t, isnormalized=0, basisorder=0, photon_offset=0)
+    wl, wn = simulate_batch([mesh, mesh], [dataclasses.replace(base, outputtype="wl"),
+                                           dataclasses.replace(base, outputtype="wn")])
     mus = np.asarray(cfg.media, np.float64)[mesh.label, 1]
     with np.errstate(divide="ignore", invalid="ignore"):
         jmus = np.where(mus > 0, wn.field / mus, 0.0) - wl.field
@@ -105,7 +109,10 @@ def loss_and_grads(mesh: Mesh, cfg: SimConfig, detp: np.ndarray, seeds: np.ndarr
     ndet = len(c)
     W = np.array([w[ids == d + 1].sum() for d in range(ndet)])
     L = float(np.sum(np.asarray(c) * np.log(W)))
-    coef = np.array([c[i - 1] / W[i - 1] if 1 <= i <= ndet else 0.0 for i in ids])
+    c = np.asarray(c, np.float64)
+    ok = (ids >= 1) & (ids <= ndet)
+    coef = np.zeros(len(ids))
+    coef[ok] = c[ids[ok] - 1] / W[ids[ok] - 1]
     jmua, jmus = jacobians(mesh, cfg, detp, seeds, 0, coef)
     return L, W, jmua.sum(0), jmus.sum(0)
 
