@@ -65,3 +65,37 @@ def test_pmmc_run_matches_api(gpu_ready):
     assert rep["flux"].sum() > 0
     with pytest.raises(ValueError):
         pmmc.run(dict(cfg, prop=m.media[:1]))
+
+
+def test_cli_sources_grid_and_exiting_weight(gpu_ready, tmp_path):
+    """The command line with a wide-field source (Optode.Source Type/Param1), the
+    dual-grid method (-M G, Domain.Step) and the exiting weight (-X 1)."""
+    m = meshgen.homogeneous_cube(n=10)
+    label = m.label.copy()
+    label[meshgen.centroids(m.node, m.elem)[:, 2] < 6.0] = -1  # the reference's source candidates
+    cfg = {"Session": {"ID": "g", "Photons": 20000, "RNGSeed": 5, "DoSaveRef": 1},
+           "Domain": {"Media": m.media.tolist(), "Step": [2.0, 2.0, 2.0]},
+           "Mesh": {"MeshNode": m.node.tolist(), "MeshElem": np.c_[m.elem, label].tolist()},
+           "Forward": {"T0": 0.0, "T1": 5e-9, "Dt": 5e-9},
+           "Optode": {"Source": {"Type": "disk", "Pos": [30, 30, 0], "Dir": [0, 0, 1], "Param1": [10, 0, 0, 0]}}}
+    (tmp_path / "in.json").write_text(json.dumps(cfg))
+    env = dict(os.environ, PYTHONPATH=ROOT)
+    r = subprocess.run([sys.executable, "-m", "mmc_gb300", "-f", "in.json", "-M", "G", "-U", "0"], cwd=tmp_path,
+                       env=env, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    grid = io.read_bin(str(tmp_path / "g.bin"), 1)
+    assert grid.shape == (1, 31 * 31 * 31) and grid.sum() > 0
+    dref = np.loadtxt(tmp_path / "g_dref.dat")
+    assert dref.shape[0] > 0 and dref[:, 1].sum() > 0
+
+
+def test_pmmc_sources_grid_and_exiting_weight(gpu_ready):
+    m = meshgen.homogeneous_cube(n=10)
+    label = m.label.copy()
+    label[meshgen.centroids(m.node, m.elem)[:, 2] < 6.0] = 0
+    out = pmmc.run(dict(node=m.node, elem=m.elem, elemprop=label, prop=m.media, srcpos=[20, 20, 0],
+                        srcdir=[0, 0, 1], srctype="planar", srcparam1=[20, 0, 0, 0], srcparam2=[0, 20, 0, 0],
+                        nphoton=20000, seed=3, tstart=0.0, tend=5e-9, tstep=1e-9, method="grid", steps=[3, 3, 3],
+                        issaveref=1, isnormalized=1))
+    assert out["flux"].shape == (21, 21, 21, 5)   # [dim.x, dim.y, dim.z, maxgate]
+    assert out["dref"].shape[1] == 5 and out["dref"].sum() > 0
