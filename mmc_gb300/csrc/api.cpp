@@ -46,6 +46,24 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 int gates_of(const mmcgb_config& c) { return (int)((c.tend - c.tstart) / c.tstep + 0.5f); }
 
+// Free device memory for new stream-ordered allocations: what the driver
+// reports plus what the default pool holds without using.
+size_t free_device_memory(int device) {
+    size_t freeb = 0, totalb = 0;
+    if (cudaMemGetInfo(&freeb, &totalb) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 0;
+    }
+    cudaMemPool_t pool;
+    uint64_t reserved = 0, used = 0;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess &&
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess &&
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess && reserved > used)
+        freeb += (size_t)(reserved - used);
+    (void)cudaGetLastError();
+    return freeb;
+}
+
 // Dual-grid geometry (mesh_createdualmesh, src/mmc_mesh.c:349-381): float
 // arithmetic, bounding box padded by EPS, dim = (int)(span / step) + 1.
 void grid_geometry(const HostMesh& m, float step, unsigned dim[3], float nmin[3]) {
@@ -205,8 +223,7 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     const bool f64 = c.accum_f64 != 0;
     const size_t maxdet = c.issavedet ? c.maxdetphoton : 0;
     size_t need = P.flen * (f64 ? 8 : 8) + maxdet * (P.reclen * 4 + (c.issaveseed ? 16 : 0));
-    size_t freeb = 0, totalb = 0;
-    CK(cudaMemGetInfo(&freeb, &totalb));
+    const size_t freeb = free_device_memory(mesh->device);
     if (need + (64ull << 20) > freeb) return fail(MMCGB_E_NOMEM, "not enough free device memory for fluence and detector buffers");
     CK(B.alloc(&B.media, c.nmedia));
     CK(B.alloc(&B.det, c.detnum));
@@ -485,6 +502,18 @@ int32_t mmcgb_mesh_create(const mmcgb_mesh_desc* desc, int32_t device, mmcgb_mes
     if (rc) return fail(rc, err);
     m->device = device;
     CK(cudaSetDevice(device));
+    {
+        // Simulations allocate their buffers stream-ordered from the device's default pool
+        // (fluence, records, gate-phase queues of tens of GB); keep up to 32 GB of freed blocks
+        // in the pool instead of returning them at every synchronization, so repeated
+        // simulate() calls reuse them.  A setting of this process's pool only.
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t keep = 32ull << 30;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        (void)cudaGetLastError();
+    }
     std::vector<TetRec> rec;
     pack_records(m->host, rec);
     std::vector<float4> node(m->host.nn);
@@ -621,13 +650,8 @@ int phased_setup(mmcgb_session* s, uint64_t nphoton, bool* use) {
         if (s->P.maxgate < 8 || fluence < ((size_t)64 << 20) || nphoton < 4000000ull ||
             s->pq_span >= s->P.maxgate)
             return MMCGB_OK;
-        if (nphoton > s->pq_cap) {
-            size_t free_b = 0, total_b = 0;
-            if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || need > free_b / 2) {
-                (void)cudaGetLastError();
-                return MMCGB_OK;  // not enough room for the queues: trace in one launch
-            }
-        }
+        if (nphoton > s->pq_cap && need > free_device_memory(s->mesh->device) / 2)
+            return MMCGB_OK;  // not enough room for the queues: trace in one launch
     }
     if (nphoton > s->pq_cap) {
         if (s->pq_mem) CK(cudaFreeAsync(s->pq_mem, s->stream));
