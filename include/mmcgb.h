@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define MMCGB_ABI_VERSION 2
+#define MMCGB_ABI_VERSION 3
 
 typedef enum mmcgb_status {
     MMCGB_OK = 0,
@@ -131,6 +131,9 @@ typedef struct mmcgb_config {
                                 box, datalen = dim.x*dim.y*dim.z (mmcgb_grid_info), x fastest */
     float gridstep;          /* voxel edge of the grid output in mm (the reference's Domain.Step);
                                 0 = 1 mm */
+    uint32_t maxjumpdebug;   /* > 0: save photon trajectories (the reference's -D M): a record at
+                                each launch, scattering event and photon end, at most this many,
+                                into mmcgb_result.traj */
 } mmcgb_config;
 
 /* Outputs.  Pointers may be NULL to skip an output; counts are always set. */
@@ -151,6 +154,9 @@ typedef struct mmcgb_result {
     uint64_t raytet;         /* ray-tetrahedron tests */
     uint64_t aborted;        /* photons stopped by the step budget */
     uint64_t outside;        /* photons whose launch position lies in no element (an error) */
+    float* traj;             /* maxjumpdebug*6 trajectory records: photon id (uint32 bits), x, y, z,
+                                weight, element id (int32 bits); src/mmc_core.cl:692-704 */
+    uint32_t ntraj;          /* trajectory records produced (may exceed maxjumpdebug) */
     double* dref;            /* issaveref: maxgate*nf exiting weight per exterior face (faces
                                 numbered as mmcgb_mesh_info's nf), divided by the launched weight
                                 when isnormalized, else NULL */

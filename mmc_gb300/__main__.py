@@ -4,12 +4,15 @@ photon path (src/mmc.c:58-112 and the option table of src/mmc_utils.c:103-128):
     python -m mmc_gb300 -f input.json [-n photons] [-E seed|file.mch] [-s session]
         [-C basisorder] [-U normalize] [-O x|f|e|j|l|p] [-d savedet] [-x saveexit]
         [-q saveseed] [-m momentum] [-b reflect] [-e minenergy] [-P replaydet]
-        [-H maxdetphoton] [-F bin|dat|mch] [-G gpu] [-D T] [-M s] [--bench]
+        [-H maxdetphoton] [-F bin|dat|mch] [-G gpu] [-D T|M] [--maxjumpdebug n] [-M s|G] [-X 0|1]
 
 Writes <session>.bin (or .dat) with the normalized output and, when detected
 photons are saved, <session>.mch -- as the reference does in standalone mode
 (src/mmc_cu_host.cu:1397-1440).  `-E file.mch` replays the photons saved in a
-previous run (src/mmc_mesh.c:815-898).
+previous run (src/mmc_mesh.c:815-898).  `-D M` saves photon trajectories (a
+record per launch, scattering event and photon end, at most --maxjumpdebug of
+them) into <session>.mch with 6 columns and `detected` 0, written after (and so
+in place of) the detected photons, as src/mmc_host.c:434-459 does.
 """
 from __future__ import annotations
 
@@ -46,6 +49,7 @@ def main(argv=None):
     ap.add_argument("-F", "--outputformat")
     ap.add_argument("-G", "--gpu", type=int, default=1)
     ap.add_argument("-D", "--debug", default="")
+    ap.add_argument("--maxjumpdebug", type=_intflag, default=10000000)  # src/mmc_utils.c:342
     ap.add_argument("-M", "--method", default="s")
     ap.add_argument("-X", "--saveref", type=int)
     ap.add_argument("-r", "--root", default="")
@@ -80,6 +84,9 @@ def main(argv=None):
             upd["seed"] = int(args.seed)
     if args.method.lower() in ("g", "grid"):
         upd["method"] = "grid"
+    debug = (args.debug + meta.get("debugflag", "")).upper()
+    if "M" in debug:
+        upd["maxjumpdebug"] = args.maxjumpdebug
     cfg = dataclasses.replace(cfg, **upd)
     session = args.session or meta["session"]
     fmt = (args.outputformat or meta["outputformat"]).lower()
@@ -105,7 +112,7 @@ def main(argv=None):
     if res.energytot > 0 and not replay_file:
         print(f"total simulated energy: {res.energytot:.0f}\tabsorbed: {100 * res.absorbed_fraction:.5f}%\t"
               f"normalizor={res.normalizer:g}")
-    if "T" in args.debug.upper():
+    if "T" in debug:
         print(f"detected {res.detected} photons")
     base = os.path.join(outdir, session)
     if res.field is not None:
@@ -120,6 +127,13 @@ def main(argv=None):
                      maxmedia=np.asarray(cfg.media).shape[0] - 1,
                      detnum=0 if cfg.detpos is None else len(cfg.detpos), totalphoton=nphoton,
                      detected=res.detected, unitinmm=cfg.unitinmm, normalizer=res.normalizer)
+    if res.traj is not None:
+        if res.ntraj > len(res.traj):
+            print(f"WARNING: the saved trajectory positions ({res.ntraj}) are more than what you have specified "
+                  f"({len(res.traj)}), please use the --maxjumpdebug option to specify a greater number")
+        io.write_mch(base + ".mch", res.traj, None, maxmedia=np.asarray(cfg.media).shape[0] - 1,
+                     detnum=0 if cfg.detpos is None else len(cfg.detpos), totalphoton=nphoton, detected=0,
+                     unitinmm=cfg.unitinmm, normalizer=res.normalizer)
     mesh.close()
     return 0
 

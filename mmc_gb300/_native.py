@@ -55,7 +55,7 @@ class Config(C.Structure):
         ("accum_f64", C.c_int32), ("step_budget", C.c_uint64),
         ("threads", C.c_int32), ("blocks", C.c_int32), ("fast_math", C.c_int32), ("phased", C.c_int32),
         ("srcparam1", C.c_float * 4), ("srcparam2", C.c_float * 4), ("focus", C.c_float), ("srcpattern", C.c_void_p),
-        ("issaveref", C.c_int32), ("method", C.c_int32), ("gridstep", C.c_float),
+        ("issaveref", C.c_int32), ("method", C.c_int32), ("gridstep", C.c_float), ("maxjumpdebug", C.c_uint32),
     ]
 
 
@@ -65,7 +65,8 @@ class Result(C.Structure):
         ("photon_weight", C.c_void_p), ("photon_steps", C.c_void_p), ("photon_det", C.c_void_p),
         ("detected", C.c_uint32), ("saved", C.c_uint32), ("reclen", C.c_int32), ("maxgate", C.c_int32),
         ("energytot", C.c_double), ("energyesc", C.c_double), ("normalizer", C.c_double),
-        ("raytet", C.c_uint64), ("aborted", C.c_uint64), ("outside", C.c_uint64), ("dref", C.c_void_p),
+        ("raytet", C.c_uint64), ("aborted", C.c_uint64), ("outside", C.c_uint64), ("traj", C.c_void_p),
+        ("ntraj", C.c_uint32), ("dref", C.c_void_p),
         ("kernel_ms", C.c_float),
     ]
 
@@ -126,7 +127,7 @@ def load():
                      "mmcgb_mesh_create", "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export",
                      "mmcgb_mesh_locate", "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run"):
             getattr(lib, name).restype = C.c_int32
-        if lib.mmcgb_abi_version() != 2:
+        if lib.mmcgb_abi_version() != 3:
             raise NativeLibraryError("libmmcgb ABI version mismatch")
         _lib = lib
         return lib

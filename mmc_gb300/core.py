@@ -184,6 +184,7 @@ class SimConfig:
     focus: float = 0.0                          # the reference's srcdir.w
     srcpattern: Optional[np.ndarray] = None     # pattern / pattern3d weights
     issaveref: int = 0                          # exiting weight per exterior face (result.dref)
+    maxjumpdebug: int = 0                       # > 0: save up to this many trajectory records
     method: object = "elem"                     # "elem" (element output) or "grid" (dual-grid, DMMC)
     gridstep: float = 1.0                       # voxel edge of the grid output (mm)
     save_field: bool = True
@@ -210,6 +211,7 @@ class SimConfig:
             keep["pattern"] = pat
             c.srcpattern = _ptr(pat)
         c.issaveref = int(self.issaveref)
+        c.maxjumpdebug = int(self.maxjumpdebug)
         m = self.method
         c.method = {"elem": 0, "grid": 1}[m] if isinstance(m, str) else int(m)
         c.gridstep = float(self.gridstep)
@@ -265,6 +267,8 @@ class SimResult:
     photon_steps: Optional[np.ndarray] = None
     photon_det: Optional[np.ndarray] = None
     dref: Optional[np.ndarray] = None   # (maxgate, nf) exiting weight per exterior face (issaveref)
+    traj: Optional[np.ndarray] = None   # (records, 6) trajectory: id bits, x, y, z, weight, eid bits
+    ntraj: int = 0                      # trajectory records produced (more than kept when truncated)
 
     @property
     def absorbed_fraction(self) -> float:
@@ -299,8 +303,9 @@ def _alloc_result(mesh: Mesh, cfg: SimConfig, trace: bool, out: Optional[np.ndar
     else:
         arrs["photon_weight"] = arrs["photon_steps"] = arrs["photon_det"] = None
     arrs["dref"] = np.zeros((G, mesh.nf), np.float64) if cfg.issaveref else None
+    arrs["traj"] = np.zeros((int(cfg.maxjumpdebug), 6), np.float32) if cfg.maxjumpdebug else None
     r = N.Result()
-    for k in ("field", "detp", "seeds", "photon_weight", "photon_steps", "photon_det", "dref"):
+    for k in ("field", "detp", "seeds", "photon_weight", "photon_steps", "photon_det", "dref", "traj"):
         setattr(r, k, _ptr(arrs[k]))
     return r, arrs
 
@@ -313,7 +318,9 @@ def _make_result(r: N.Result, arrs) -> SimResult:
                      energytot=r.energytot, energyesc=r.energyesc, normalizer=r.normalizer,
                      raytet=int(r.raytet), aborted=int(r.aborted), kernel_ms=float(r.kernel_ms),
                      maxgate=int(r.maxgate), reclen=int(r.reclen), photon_weight=arrs["photon_weight"],
-                     photon_steps=arrs["photon_steps"], photon_det=arrs["photon_det"], dref=arrs["dref"])
+                     photon_steps=arrs["photon_steps"], photon_det=arrs["photon_det"], dref=arrs["dref"],
+                     traj=None if arrs["traj"] is None else arrs["traj"][:min(int(r.ntraj), len(arrs["traj"]))].copy(),
+                     ntraj=int(r.ntraj))
 
 
 def simulate(mesh: Mesh, cfg: SimConfig, trace: bool = False, out: Optional[np.ndarray] = None) -> SimResult:

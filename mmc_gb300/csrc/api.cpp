@@ -153,6 +153,8 @@ struct SimBuffers {
     unsigned long long* counters = nullptr;
     float* pattern = nullptr;
     double* dref = nullptr;
+    float* traj = nullptr;
+    unsigned* trajcount = nullptr;
     unsigned long long* rseed = nullptr;
     float* rweight = nullptr;
     float* rtime = nullptr;
@@ -233,6 +235,11 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     CK(B.alloc(&B.detcount, 1));
     CK(B.alloc(&B.energy, 2));
     CK(B.alloc(&B.counters, 3));
+    if (c.maxjumpdebug) {
+        CK(B.alloc(&B.traj, (size_t)c.maxjumpdebug * 6));
+        CK(B.alloc(&B.trajcount, 1));
+        CK(cudaMemsetAsync(B.trajcount, 0, sizeof(unsigned), stream));
+    }
     if (c.issaveref) {
         CK(B.alloc(&B.dref, (size_t)m.nf * P.maxgate));
         CK(cudaMemsetAsync(B.dref, 0, sizeof(double) * (size_t)m.nf * P.maxgate, stream));
@@ -333,6 +340,9 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     S.photon_det = B.pd;
     S.dref = B.dref;
     S.nf = m.nf;
+    S.traj = B.traj;
+    S.trajcount = B.trajcount;
+    S.maxtraj = c.maxjumpdebug;
     S.grid = (c.method == 1) ? 1 : 0;
     S.framelen = (unsigned)frame_len(m, c);
     if (S.grid) {
@@ -395,6 +405,15 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
     if (res->photon_weight) CK(cudaMemcpyAsync(res->photon_weight, B.pw, sizeof(float) * c.nphoton, cudaMemcpyDeviceToHost, stream));
     if (res->photon_steps) CK(cudaMemcpyAsync(res->photon_steps, B.ps, sizeof(unsigned) * c.nphoton, cudaMemcpyDeviceToHost, stream));
     if (res->photon_det) CK(cudaMemcpyAsync(res->photon_det, B.pd, sizeof(int) * c.nphoton, cudaMemcpyDeviceToHost, stream));
+    unsigned ntraj = 0;
+    if (B.trajcount) {
+        CK(cudaMemcpyAsync(&ntraj, B.trajcount, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        if (res->traj && ntraj)
+            CK(cudaMemcpyAsync(res->traj, B.traj, sizeof(float) * 6 * std::min(ntraj, c.maxjumpdebug),
+                               cudaMemcpyDeviceToHost, stream));
+    }
+    res->ntraj = ntraj;
     const size_t nref = (size_t)mesh->host.nf * P.maxgate;
     if (res->dref && B.dref) CK(cudaMemcpyAsync(res->dref, B.dref, sizeof(double) * nref, cudaMemcpyDeviceToHost, stream));
     B.release();

@@ -743,6 +743,21 @@ __device__ __forceinline__ bool launch_photon(Lane& L, const SimDev& S) {
     return true;
 }
 
+// One trajectory record (src/mmc_core.cl:692-704): photon id (within the whole simulation),
+// position, weight, element.
+__device__ __forceinline__ void save_traj(const SimDev& S, const Lane& L) {
+    const unsigned pos = atomicAdd(S.trajcount, 1u);
+    if (pos < S.maxtraj) {
+        float* r = S.traj + (size_t)pos * 6;
+        r[0] = __uint_as_float((unsigned)(S.photon_offset + L.pid));
+        r[1] = L.px;
+        r[2] = L.py;
+        r[3] = L.pz;
+        r[4] = L.weight;
+        r[5] = __int_as_float(L.eid);
+    }
+}
+
 struct Tally {
     float eesc;
     float etot;
@@ -924,6 +939,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                     }
                     if (placed) {
                         L.mode = M_OUTER;
+                        if (S.traj) save_traj(S, L);
                     } else {  // launch position in no element: counted, reported as an error
                         tally.outside++;
                         tally.eesc += L.weight;
@@ -992,6 +1008,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                             killed = true;
                     }
                     if (killed) {
+                        if (S.traj) save_traj(S, L);
                         if (S.photon_det) S.photon_det[L.pid] = 0;
                         tally.eesc += L.weight;
                         if (S.photon_weight) S.photon_weight[L.pid] = L.weight;
@@ -1008,6 +1025,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                         const int tp = L.label;
                         L.slen0 = next_scatter<MP>(L, med[tp].z, ctheta);
                         L.slen = L.slen0;
+                        if (S.traj) save_traj(S, L);
                         if (S.issavedet && tp > 0) {
                             const int M = S.nmedia - 1;
                             if (S.ismomentum) PP(2 * M + tp - 1) += (1.f - ctheta);
@@ -1171,6 +1189,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
             if (S.photon_det) S.photon_det[L.pid] = 0;
         }
         if (ended) {
+            if (S.traj) save_traj(S, L);
             tally.eesc += L.weight;
             if (S.photon_weight) S.photon_weight[L.pid] = L.weight;
             if (S.photon_steps) S.photon_steps[L.pid] = L.steps;

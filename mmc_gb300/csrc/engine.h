@@ -101,6 +101,9 @@ struct SimDev {
     float gmin[3];         // grid origin (node minimum - EPS)
     unsigned gdim[3];
     unsigned framelen;     // fluence entries per gate: ne, or dim.x*dim.y*dim.z
+    float* traj;           // trajectory records (6 words) at launch, scattering and photon end
+    unsigned* trajcount;
+    unsigned maxtraj;
     double* dref;          // issaveref: exiting weight per exterior face and gate, [gate][face]
     int nf;                // exterior faces
     // optional per-photon trace (parity tests)

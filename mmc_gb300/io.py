@@ -130,8 +130,18 @@ def load_input(path: str):
         basisorder=int(ses.get("BasisOrder", 1)), outputtype=otype, nout=float(fwd.get("N0", 1.0)),
         detpos=detpos, unitinmm=unit)
     meta = dict(session=str(ses.get("ID", "default")), outputformat=str(ses.get("OutputFormat", "bin")),
-                saveweight=int(ses.get("DoSaveVolume", 1)), root=root)
+                saveweight=int(ses.get("DoSaveVolume", 1)), root=root,
+                debugflag=str(ses.get("DebugFlag", "")) if not isinstance(ses.get("DebugFlag"), int) else
+                _debug_letters(ses["DebugFlag"]))
     return mesh, cfg, meta
+
+
+# debug flag letters by bit, src/mmc_utils.c:139 (T = detected count, M = trajectories)
+DEBUG_LETTERS = "SCBWDIOXATRPEM"
+
+
+def _debug_letters(level: int) -> str:
+    return "".join(c for i, c in enumerate(DEBUG_LETTERS) if int(level) >> i & 1)
 
 
 # ---------------------------------------------------------------------------

@@ -86,6 +86,14 @@ def _parse(cfg: dict):
         kw["outputtype"] = ot
     if "detpos" in cfg:
         kw["detpos"] = np.asarray(cfg["detpos"], np.float32).reshape(-1, 4)
+    if "debuglevel" in cfg:  # letters R, M, P (src/pmmc.cpp:692-710); M saves photon trajectories
+        dl = str(cfg["debuglevel"]).upper()
+        if not dl:
+            raise ValueError("the 'debuglevel' field must be a non-empty string")
+        if not any(c in "RMP" for c in dl):
+            raise ValueError("the specified debuglevel is not supported")
+        if "M" in dl:
+            kw["maxjumpdebug"] = int(cfg.get("maxjumpdebug", 10000000))
     seeds = None
     if "seed" in cfg:
         s = cfg["seed"]
@@ -134,6 +142,8 @@ def run(cfg: dict) -> dict:
                                              kernel_ms=res.kernel_ms)}
     if sc.issaveref and res.dref is not None:
         out["dref"] = res.dref.T  # [nf, maxgate], as pmmc (src/pmmc.cpp:1226-1234)
+    if res.traj is not None:
+        out["traj"] = res.traj.T  # [6, records]: id, x, y, z, weight, element (src/pmmc.cpp:1092-1108)
     if sc.issavedet and res.detp is not None and len(res.detp):
         out["detp"] = res.detp.T
         if sc.issaveseed and res.seeds is not None:

@@ -937,6 +937,23 @@ typedef struct {
 } tallies;
 
 /* the photon life: src/mmc_core.cl:1851-2161 */
+/* One trajectory record, savedebugdata in src/mmc_raytrace.c:1739-1756:
+ * photon id, position, weight and element (the ids as raw 32-bit words). */
+static void save_traj(const engine* g, const ray* r, uint64_t pidx, oracle_out* out) {
+    uint32_t pos;
+#pragma omp atomic capture
+    pos = out->ntraj++;
+    if (pos < out->maxtraj) {
+        float* rec = out->traj + (size_t)pos * 6;
+        uint32_t id = (uint32_t)(g->cfg->photon_offset + pidx);
+        int32_t eid = r->eid;
+        memcpy(rec, &id, 4);
+        rec[1] = r->px; rec[2] = r->py; rec[3] = r->pz;
+        rec[4] = r->weight;
+        memcpy(rec + 5, &eid, 4);
+    }
+}
+
 static void onephoton(engine* g, uint64_t pidx, float* ppath, oracle_out* out, tallies* tl) {
     const oracle_cfg* cfg = g->cfg;
     const int M = g->M;
@@ -976,6 +993,7 @@ static void onephoton(engine* g, uint64_t pidx, float* ppath, oracle_out* out, t
         if (out->photon_det) out->photon_det[pidx] = 0;
         return;
     }
+    if (out->traj) save_traj(g, r, pidx, out);   /* src/mmc_raytrace.c:1804-1806 */
 
 #define STEP()                                                         \
     do {                                                               \
@@ -1087,6 +1105,7 @@ static void onephoton(engine* g, uint64_t pidx, float* ppath, oracle_out* out, t
         int tp = g->type[r->eid - 1];
         r->slen0 = next_scatter(medium(g, tp, 2), r, ran, &mom);
         r->slen = r->slen0;
+        if (out->traj) save_traj(g, r, pidx, out);   /* src/mmc_raytrace.c:2065-2067 */
         if (cfg->issavedet) {
             if (cfg->ismomentum && tp > 0) ppath[2 * M + tp - 1] += mom;
             if (tp > 0) ppath[tp - 1] += 1.f;
@@ -1095,6 +1114,7 @@ static void onephoton(engine* g, uint64_t pidx, float* ppath, oracle_out* out, t
 done:
 #undef STEP
 #undef PPATH
+    if (out->traj) save_traj(g, r, pidx, out);   /* src/mmc_raytrace.c:2109-2111 */
     tl->eesc += r->weight;
     tl->raytet += steps;
     tl->aborted += aborted;

@@ -76,6 +76,9 @@ typedef struct oracle_out {
     uint64_t outside;       /* photons launched at a position no element encloses */
     double* dref;           /* issaveref: maxgate*nf (raw, unnormalized), may be NULL */
     int nf;                 /* exterior faces of the prepared mesh */
+    float* traj;            /* maxtraj*6 trajectory records (id, x, y, z, w, eid), may be NULL */
+    uint32_t maxtraj;
+    uint32_t ntraj;         /* records written or attempted (may exceed maxtraj) */
 } oracle_out;
 
 /* Mesh preparation (volumes with orientation fix, face neighbours, normals,

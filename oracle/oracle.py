@@ -47,6 +47,7 @@ class OOut(C.Structure):
         ("detected", C.c_uint32), ("reclen", C.c_int), ("energytot", C.c_double),
         ("energyesc", C.c_double), ("raytet", C.c_uint64), ("aborted", C.c_uint64), ("outside", C.c_uint64),
         ("dref", C.c_void_p), ("nf", C.c_int),
+        ("traj", C.c_void_p), ("maxtraj", C.c_uint32), ("ntraj", C.c_uint32),
     ]
 
 
@@ -215,6 +216,9 @@ def run(node, elem, label, cfg, nthreads=1, trace=False, normalize=True):
     out.photon_weight, out.photon_steps, out.photon_det = _p(pw), _p(ps), _p(pd)
     dref = np.zeros(maxgate * 4 * ne, np.float64) if getattr(cfg, "issaveref", 0) else None  # nf <= 4 ne
     out.dref = _p(dref)
+    maxtraj = int(getattr(cfg, "maxjumpdebug", 0))
+    traj = np.zeros((maxtraj, 6), np.float32) if maxtraj else None
+    out.traj, out.maxtraj = _p(traj), maxtraj
     rc = lib.oracle_run(nn, _p(node), ne, _p(elem), _p(label), C.byref(c), C.byref(out), int(nthreads))
     if rc:
         raise ValueError("oracle run failed")
@@ -226,6 +230,8 @@ def run(node, elem, label, cfg, nthreads=1, trace=False, normalize=True):
     res["seeds"] = seeds[:saved] if seeds is not None else None
     res["nf"] = int(out.nf)
     res["dref"] = dref[:maxgate * out.nf].reshape(maxgate, out.nf) if dref is not None else None
+    res["ntraj"] = int(out.ntraj)
+    res["traj"] = traj[:min(int(out.ntraj), maxtraj)] if traj is not None else None
     if normalize and c.method == 1:  # dual grid: one scale factor (src/mmc_mesh.c:2204-2206)
         norm = 1.0
         if cfg.isnormalized:

@@ -18,6 +18,10 @@ Badouel tracer and element-based output (-M s -C 0), unnormalized (-U 0):
            on the z=0 face over a 6 mm void layer (voxel layer z<6 mm; the
            reference needs the layer's tets labelled -1, its source-element
            candidates, which it then treats as void, label 0)
+  dref_cube6k / grid_cube6k / traj_cube6k
+           the cube6k mesh with exiting weight per face (-X 1, 5 gates of
+           1 ns), dual-grid output on 2 mm voxels (-M G), trajectory records
+           (-D M, 5 gates of 1 ns, 2e4 photons: statistics per run)
 
 Six more runs with fresh seeds calibrate the null: their coverage of the
 10-run statistics (fraction of cells within 3 sigma, mean z) is stored, and a
@@ -305,6 +309,45 @@ def make_grid_case(wd):
     print(name, "dim", dim, "absorbed per photon", fx["total"].mean() * 0.005 / c["photons"])
 
 
+def run_ref_traj(workdir, name, seed, photons, maxjump):
+    """Trajectory records of one reference run (-D M): <session>.mch with six
+    columns (src/mmc_host.c:452-459)."""
+    sess = f"{name}_{seed}_traj"
+    cmd = [REF, "-f", os.path.join(workdir, name + ".json"), "-c", "sse", "-M", "s", "-C", "0", "-b", "1",
+           "-U", "0", "-F", "bin", "-s", sess, "-E", str(seed), "-n", str(photons), "-D", "M",
+           "--maxjumpdebug", str(maxjump)]
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    p = subprocess.run(cmd, cwd=workdir, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(p.stdout[-2000:])
+    data, hdr = read_mch(os.path.join(workdir, sess + ".mch"))
+    assert hdr["colcount"] == 6 and hdr["detected"] == 0 and len(data) < maxjump
+    return data
+
+
+def make_traj_case(wd):
+    """traj_cube6k: trajectory records (-D M) of the cube6k mesh, pencil
+    (30,30,0) +z, 5 gates of 1 ns, 2e4 photons; statistics of 10 runs."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    name = "traj_cube6k"
+    m = meshgen.homogeneous_cube(n=10)
+    c = dict(mesh=m, photons=20000, t1=5e-9, dt=1e-9, det=None)
+    c["e0"] = oracle.initelem(m.node, m.elem, m.label, (30.0, 30.0, 0.0))
+    write_json(os.path.join(wd, name + ".json"), name, c)
+    maxjump = 6000000
+    sys.path.insert(0, os.path.dirname(HERE))
+    import golden_checks as gc
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        stats = list(ex.map(lambda s: gc.traj_stats(run_ref_traj(wd, name, s, c["photons"], maxjump), c["photons"]),
+                            [SEED0 + k for k in range(NRUNS)]))
+    fx = dict(photons=c["photons"], maxjumpdebug=maxjump, edges=gc.TRAJ_EDGES)
+    for k in gc.TRAJ_KEYS + ("launch_pos", "launch_weight"):
+        fx["traj_" + k] = np.array([s[k] for s in stats], np.float64)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **fx)
+    print(name, "records/photon", fx["traj_records_per_photon"].mean(), "+-", fx["traj_records_per_photon"].std())
+
+
 def main(only=()):
     """Regenerates every case, or only the named ones (each case draws its
     random cell subset from its own generator, so cases are independent)."""
@@ -315,6 +358,8 @@ def main(only=()):
             make_dref_case(wd)
         if not only or "grid_cube6k" in only:
             make_grid_case(wd)
+        if not only or "traj_cube6k" in only:
+            make_traj_case(wd)
         for name, c in case_defs().items():
             if only and name not in only:
                 continue

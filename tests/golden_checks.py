@@ -48,6 +48,11 @@ def case_mesh_and_config(name, nphoton=None, seed=4242):
         m = meshgen.homogeneous_cube(n=10)
         cfg = SimConfig(media=m.media, nphoton=nphoton or int(fx["photons"]), seed=seed, srcpos=(30.0, 30.0, 0.0),
                         srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=1e-9, basisorder=0, isnormalized=0, issaveref=1)
+    elif name == "traj_cube6k":
+        m = meshgen.homogeneous_cube(n=10)
+        cfg = SimConfig(media=m.media, nphoton=nphoton or int(fx["photons"]), seed=seed, srcpos=(30.0, 30.0, 0.0),
+                        srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=1e-9, basisorder=0, isnormalized=0,
+                        maxjumpdebug=int(fx["maxjumpdebug"]))
     elif name.startswith("src_"):
         # source types (tests/golden/make_golden.py SOURCE_CASES): the cube6k mesh, with the
         # voxel layer z < 6 mm void for the sources on the z=0 face
@@ -130,6 +135,58 @@ def check_grid(raw, fx):
     t = fx["total"]
     if abs(raw.sum() - t.mean()) > 3 * t.std(ddof=1) * INFLATE:
         msgs.append(f"grid total {raw.sum():.1f} vs reference {t.mean():.1f} +- {t.std(ddof=1):.1f}")
+    return msgs
+
+
+# records-per-photon histogram edges of the trajectory statistics
+TRAJ_EDGES = np.array([0, 3, 4, 6, 10, 20, 50, 100, 200, 400, 800, 1 << 30])
+
+
+def traj_stats(traj, nphoton):
+    """Statistics of one run's trajectory records (id bits, x, y, z, w, eid
+    bits), with every record of the run kept.  A photon's records are in
+    order in the buffer (one thread writes them), so a stable sort by photon
+    id gives each photon's launch record first and its end record last."""
+    ids = traj[:, 0].view(np.uint32)
+    order = np.argsort(ids, kind="stable")
+    t, ids = traj[order], ids[order]
+    cnt = np.bincount(ids, minlength=nphoton).astype(np.float64)
+    first = np.r_[0, np.nonzero(np.diff(ids))[0] + 1]
+    last = np.r_[first[1:] - 1, len(ids) - 1]
+    return dict(
+        records_per_photon=cnt.mean(),
+        hist=np.histogram(cnt, TRAJ_EDGES)[0] / float(nphoton),
+        final_weight=float(t[last, 4].astype(np.float64).mean()),
+        escaped=float((t[last, 5].view(np.int32) <= 0).mean()),
+        mean_pos=t[:, 1:4].astype(np.float64).mean(0),
+        mean_weight=float(t[:, 4].astype(np.float64).mean()),
+        launch_pos=t[first, 1:4].astype(np.float64).mean(0),
+        launch_weight=float(t[first, 4].astype(np.float64).mean()),
+    )
+
+
+TRAJ_KEYS = ("records_per_photon", "hist", "final_weight", "escaped", "mean_pos", "mean_weight")
+
+
+def check_traj(traj, nphoton, fx, nsigma=4.0):
+    """Trajectory statistics of one run against the reference runs: each
+    within nsigma run-to-run deviations, the launch records exact."""
+    st = traj_stats(traj, nphoton)
+    msgs = []
+    for k in TRAJ_KEYS:
+        x = np.atleast_1d(st[k])
+        runs = fx["traj_" + k].reshape(len(fx["traj_" + k]), -1)   # (runs, values)
+        m, s = runs.mean(0), runs.std(0, ddof=1)
+        if k == "hist":  # multinomial bin fractions: the binomial sigma, steadier than 10 runs' spread
+            s = np.sqrt(m * (1.0 - m) / nphoton)
+        ok = s > 0
+        z = np.abs(x[ok] - m[ok]) / (s[ok] * INFLATE)
+        if np.any(z > nsigma):
+            msgs.append(f"trajectory {k}: {np.round(x, 4)} vs reference {np.round(m, 4)} +- {np.round(s, 4)}")
+        if np.any(~ok & (x != m)):
+            msgs.append(f"trajectory {k}: {np.round(x, 4)} vs constant reference {np.round(m, 4)}")
+    if not np.allclose(st["launch_pos"], fx["traj_launch_pos"][0]) or st["launch_weight"] != 1.0:
+        msgs.append(f"launch records at {st['launch_pos']} w {st['launch_weight']}")
     return msgs
 
 

@@ -1,6 +1,7 @@
 """The CPU oracle against the reference golden fixtures (statistical parity),
 at the fixtures' own photon counts: this pins the oracle, which in turn checks
 the CUDA engine photon by photon."""
+import dataclasses
 import os
 
 import pytest
@@ -45,6 +46,27 @@ def test_oracle_dual_grid_matches_reference_runs(oracle_mod):
     assert not msgs, "\n".join(msgs)
     # every deposit is the lost weight divided by mua: the grid holds the absorbed energy
     assert r["raw"].sum() * m.media[1, 0] == pytest.approx(r["energytot"] - r["energyesc"], rel=1e-5)
+
+
+def test_oracle_trajectories_match_reference_runs(oracle_mod):
+    """Trajectory records (-D M: launch, every scattering event, photon end)
+    against the reference's records: records per photon and their histogram,
+    end weights, escaped fraction, mean record position and weight."""
+    import numpy as np
+    m, cfg, fx = gc.case_mesh_and_config("traj_cube6k")
+    r = oracle_mod.run(m.node, m.elem, m.label, cfg, nthreads=NTHREADS, normalize=False, trace=True)
+    assert r["ntraj"] == len(r["traj"]) < cfg.maxjumpdebug
+    msgs = gc.check_traj(r["traj"], cfg.nphoton, fx)
+    assert not msgs, "\n".join(msgs)
+    # each photon's last record carries its final weight; a small buffer keeps the first records
+    t = r["traj"]
+    ids = t[:, 0].view(np.uint32)
+    order = np.argsort(ids, kind="stable")
+    last = np.r_[np.nonzero(np.diff(ids[order]))[0], len(ids) - 1]
+    assert np.array_equal(t[order][last, 4], r["photon_weight"])
+    small = oracle_mod.run(m.node, m.elem, m.label, dataclasses.replace(cfg, nphoton=200, maxjumpdebug=500),
+                           nthreads=1, normalize=False)
+    assert small["ntraj"] > 500 and len(small["traj"]) == 500
 
 
 def test_oracle_detects_a_planted_error(oracle_mod):
