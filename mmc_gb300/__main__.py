@@ -5,6 +5,8 @@ photon path (src/mmc.c:58-112 and the option table of src/mmc_utils.c:103-128):
         [-C basisorder] [-U normalize] [-O x|f|e|j|l|p] [-d savedet] [-x saveexit]
         [-q saveseed] [-m momentum] [-b reflect] [-e minenergy] [-P replaydet]
         [-H maxdetphoton] [-F bin|dat|mch] [-G gpu] [-D T|M] [--maxjumpdebug n] [-M s|G] [-X 0|1]
+        [-S 0|1]
+    python -m mmc_gb300 -Q [dmmc-cube60|dmmc-cube60b] [options]   (built-in benchmarks)
 
 Writes <session>.bin (or .dat) with the normalized output and, when detected
 photons are saved, <session>.mch -- as the reference does in standalone mode
@@ -31,7 +33,8 @@ def _intflag(v):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="mmc_gb300", description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
-    ap.add_argument("-f", "--input", required=True)
+    ap.add_argument("-f", "--input")
+    ap.add_argument("-Q", "--bench", nargs="?", const="")   # built-in benchmark; alone: list them
     ap.add_argument("-n", "--photon", type=_intflag)
     ap.add_argument("-E", "--seed")
     ap.add_argument("-s", "--session")
@@ -50,7 +53,8 @@ def main(argv=None):
     ap.add_argument("-G", "--gpu", type=int, default=1)
     ap.add_argument("-D", "--debug", default="")
     ap.add_argument("--maxjumpdebug", type=_intflag, default=10000000)  # src/mmc_utils.c:342
-    ap.add_argument("-M", "--method", default="s")
+    ap.add_argument("-M", "--method")
+    ap.add_argument("-S", "--save2pt", type=int)
     ap.add_argument("-X", "--saveref", type=int)
     ap.add_argument("-r", "--root", default="")
     args = ap.parse_args(argv)
@@ -59,9 +63,22 @@ def main(argv=None):
     from .core import Mesh, simulate
     from .io import OUTPUT_LETTERS
 
-    if args.method.lower() not in ("s", "elem", "b", "g", "grid"):
+    if args.bench == "":
+        print("Built-in benchmarks:\n" + "".join(f"\t{n}\n" for n in io.BENCHMARKS), end="")
+        return 0
+    if args.bench is not None:
+        try:
+            source = io.builtin_benchmark(args.bench)
+        except ValueError as e:
+            ap.error(str(e))
+    elif args.input:
+        source = args.input
+    else:
+        ap.error("an input file (-f) or a built-in benchmark (-Q) is required")
+    mesh_d, cfg, meta = io.load_input(source)
+    method = (args.method or meta.get("raytracer") or "s").lower()
+    if method not in ("s", "elem", "b", "g", "grid"):
         ap.error("only the branchless Badouel tracer is implemented: -M s (element output) or -M G (dual grid)")
-    mesh_d, cfg, meta = io.load_input(args.input)
     upd = {}
     if args.photon is not None:
         upd["nphoton"] = args.photon
@@ -82,8 +99,9 @@ def main(argv=None):
             replay_file = args.seed
         else:
             upd["seed"] = int(args.seed)
-    if args.method.lower() in ("g", "grid"):
+    if method in ("g", "grid"):
         upd["method"] = "grid"
+        upd["basisorder"] = 0  # the dual grid has no nodal form (src/mmc_utils.c:2300-2302)
     debug = (args.debug + meta.get("debugflag", "")).upper()
     if "M" in debug:
         upd["maxjumpdebug"] = args.maxjumpdebug
@@ -115,7 +133,8 @@ def main(argv=None):
     if "T" in debug:
         print(f"detected {res.detected} photons")
     base = os.path.join(outdir, session)
-    if res.field is not None:
+    save2pt = args.save2pt if args.save2pt is not None else meta.get("saveweight", 1)
+    if res.field is not None and save2pt:
         if fmt == "dat":
             io.write_dat(base + ".dat", res.field)
         else:

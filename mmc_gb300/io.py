@@ -64,11 +64,43 @@ def _media_from_json(media):
     return np.asarray(rows, np.float32)
 
 
-def load_input(path: str):
-    """Reads a reference JSON input; returns (mesh dict, SimConfig, meta)."""
-    with open(path) as f:
-        cfgj = json.load(f)
-    root = os.path.dirname(os.path.abspath(path))
+def builtin_benchmark(name: str) -> dict:
+    """The reference's built-in benchmark inputs (src/mmc_bench.c:44-190) in
+    the photon path's scope, as JSON dicts: dmmc-cube60 (no refractive
+    mismatch) and dmmc-cube60b (mismatch on), a 60 mm cube of 6 tets (the
+    Kuhn split along the main diagonal), mua 0.005 mus 1 g 0.01 n 1.37, 1e6
+    photons, pencil at (30.1, 30.2, 0) +z, one 5 ns gate, 4 detectors R=1 mm
+    on z=0 at 10 mm from the axis.  The implicit-MMC benchmarks (edgeimmc,
+    nodeimmc, faceimmc) need the iMMC tracer, which is not built."""
+    if name not in BENCHMARKS:
+        raise ValueError(f"unsupported benchmark '{name}' (built in: {', '.join(BENCHMARKS)})")
+    from . import meshgen
+    m = meshgen.homogeneous_cube(n=1)
+    return {
+        "Session": {"ID": name, "Photons": 1e6, "RNGSeed": 1648335518, "OutputFormat": "bin",
+                    "DoMismatch": BENCHMARKS[name]},
+        "Domain": {"Media": [dict(mua=float(r[0]), mus=float(r[1]), g=float(r[2]), n=float(r[3])) for r in m.media]},
+        "Mesh": {"MeshNode": m.node.tolist(), "MeshElem": np.c_[m.elem, m.label].tolist(), "InitElem": 2},
+        "Forward": {"T0": 0.0, "T1": 5e-9, "Dt": 5e-9},
+        "Optode": {"Source": {"Pos": [30.1, 30.2, 0.0], "Dir": [0.0, 0.0, 1.0]},
+                   "Detector": [{"Pos": p, "R": 1.0} for p in
+                                ([30.0, 20.0, 0.0], [30.0, 40.0, 0.0], [20.0, 30.0, 0.0], [40.0, 30.0, 0.0])]},
+    }
+
+
+# built-in benchmarks of the photon path -> Session.DoMismatch
+BENCHMARKS = {"dmmc-cube60": 0, "dmmc-cube60b": 1}
+
+
+def load_input(path):
+    """Reads a reference JSON input (a path, or the parsed dict); returns
+    (mesh dict, SimConfig, meta)."""
+    if isinstance(path, dict):
+        cfgj, root = path, os.getcwd()
+    else:
+        with open(path) as f:
+            cfgj = json.load(f)
+        root = os.path.dirname(os.path.abspath(path))
     ses = cfgj.get("Session", {})
     dom = cfgj.get("Domain", {})
     msh = cfgj.get("Mesh", {})
@@ -131,6 +163,7 @@ def load_input(path: str):
         detpos=detpos, unitinmm=unit)
     meta = dict(session=str(ses.get("ID", "default")), outputformat=str(ses.get("OutputFormat", "bin")),
                 saveweight=int(ses.get("DoSaveVolume", 1)), root=root,
+                raytracer=str(ses.get("RayTracer", "")).lower()[:1],
                 debugflag=str(ses.get("DebugFlag", "")) if not isinstance(ses.get("DebugFlag"), int) else
                 _debug_letters(ses["DebugFlag"]))
     return mesh, cfg, meta

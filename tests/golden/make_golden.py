@@ -22,6 +22,9 @@ Badouel tracer and element-based output (-M s -C 0), unnormalized (-U 0):
            the cube6k mesh with exiting weight per face (-X 1, 5 gates of
            1 ns), dual-grid output on 2 mm voxels (-M G), trajectory records
            (-D M, 5 gates of 1 ns, 2e4 photons: statistics per run)
+  bench_dmmc-cube60, bench_dmmc-cube60b
+           the reference's built-in benchmarks (-Q), dual-grid output on
+           1 mm voxels, 1e5 photons
 
 Six more runs with fresh seeds calibrate the null: their coverage of the
 10-run statistics (fraction of cells within 3 sigma, mean z) is stored, and a
@@ -348,6 +351,53 @@ def make_traj_case(wd):
     print(name, "records/photon", fx["traj_records_per_photon"].mean(), "+-", fx["traj_records_per_photon"].std())
 
 
+def run_ref_bench(workdir, name, seed, photons):
+    """One run of a built-in benchmark of the reference (-Q name, src/mmc_bench.c)
+    with dual-grid output, unnormalized: (grid deposits, absorbed fraction,
+    ray-tet tests per photon).  With -Q the reference prints no energy line
+    (its debug flags come from the benchmark's JSON), so the absorbed fraction
+    is taken from the deposits."""
+    sess = f"{name}_{seed}_bench"
+    cmd = [REF, "-Q", name, "-c", "sse", "-M", "g", "-U", "0", "-F", "bin", "-s", sess, "-E", str(seed),
+           "-n", str(photons), "-D", "T"]
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    p = subprocess.run(cmd, cwd=workdir, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(p.stdout[-2000:])
+    tests = None
+    for line in p.stdout.splitlines():
+        if "ray-tetrahedron tests" in line:
+            tests = float(line.split("photon/ms")[1].split()[1].strip(","))
+    raw = np.fromfile(os.path.join(workdir, sess + ".bin"), np.float64)
+    # grid deposits are the lost weight over mua (0.005 throughout): absorbed fraction from their sum
+    return raw, raw.sum() * 0.005 / photons, tests / photons
+
+
+def make_bench_cases(wd):
+    """bench_dmmc-cube60(b): the reference's built-in benchmarks (6-tet 60 mm
+    cube, pencil (30.1,30.2,0) +z, one 5 ns gate) with dual-grid output on
+    1 mm voxels, 1e5 photons per run; 10 runs + 6 null runs each."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import golden_checks as gc
+    for bench in ("dmmc-cube60", "dmmc-cube60b"):
+        photons = 100000
+        with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+            runs = list(ex.map(lambda s: run_ref_bench(wd, bench, s, photons), [SEED0 + k for k in range(NRUNS)]))
+            nulls = list(ex.map(lambda s: run_ref_bench(wd, bench, s, photons),
+                                [SEED0 + 1000 + k for k in range(NNULL)]))
+        vox = np.stack([r[0] for r in runs])
+        # a random subset of the visited voxels keeps the fixture small
+        rng = np.random.default_rng(zlib.crc32(bench.encode()))
+        sub = np.sort(rng.choice(np.flatnonzero(vox.mean(0) > 0), size=20000, replace=False)).astype(np.int32)
+        fx = dict(photons=photons, nvox=vox.shape[1], sub=sub, vox_mean=vox[:, sub].mean(0).astype(np.float32),
+                  vox_std=vox[:, sub].std(0, ddof=1).astype(np.float32), total=vox.sum(1), absorbed=np.array([r[1] for r in runs]),
+                  tests_per_photon=np.array([r[2] for r in runs]))
+        st = [gc.zstats(x[0][sub], fx["vox_mean"], fx["vox_std"]) for x in nulls]
+        fx.update(null_vox_frac=np.array([t[0] for t in st]), null_vox_meanz=np.array([t[1] for t in st]))
+        np.savez_compressed(os.path.join(HERE, f"bench_{bench}.npz"), **fx)
+        print(bench, "absorbed", fx["absorbed"].mean(), "tests/photon", fx["tests_per_photon"].mean())
+
+
 def main(only=()):
     """Regenerates every case, or only the named ones (each case draws its
     random cell subset from its own generator, so cases are independent)."""
@@ -360,6 +410,8 @@ def main(only=()):
             make_grid_case(wd)
         if not only or "traj_cube6k" in only:
             make_traj_case(wd)
+        if not only or "bench" in only:
+            make_bench_cases(wd)
         for name, c in case_defs().items():
             if only and name not in only:
                 continue

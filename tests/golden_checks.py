@@ -14,6 +14,7 @@ the coverage and mean z of six fresh reference runs scored the same way, and a
 candidate run passes when it scores like them (see _zcheck); aggregate
 quantities must lie within 3 sigma.
 """
+import dataclasses
 import os
 
 import numpy as np
@@ -53,6 +54,13 @@ def case_mesh_and_config(name, nphoton=None, seed=4242):
         cfg = SimConfig(media=m.media, nphoton=nphoton or int(fx["photons"]), seed=seed, srcpos=(30.0, 30.0, 0.0),
                         srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=1e-9, basisorder=0, isnormalized=0,
                         maxjumpdebug=int(fx["maxjumpdebug"]))
+    elif name.startswith("bench_"):
+        # the reference's built-in benchmarks (-Q), dual-grid output on 1 mm voxels
+        from mmc_gb300 import io
+        d, cfg, _ = io.load_input(io.builtin_benchmark(name[len("bench_"):]))
+        m = meshgen.Mesh(d["node"], d["elem"], d["label"], cfg.media, name)
+        cfg = dataclasses.replace(cfg, nphoton=nphoton or int(fx["photons"]), seed=seed, isnormalized=0,
+                                  method="grid", gridstep=1.0, basisorder=0, issavedet=0)
     elif name.startswith("src_"):
         # source types (tests/golden/make_golden.py SOURCE_CASES): the cube6k mesh, with the
         # voxel layer z < 6 mm void for the sources on the z=0 face
@@ -187,6 +195,20 @@ def check_traj(traj, nphoton, fx, nsigma=4.0):
             msgs.append(f"trajectory {k}: {np.round(x, 4)} vs constant reference {np.round(m, 4)}")
     if not np.allclose(st["launch_pos"], fx["traj_launch_pos"][0]) or st["launch_weight"] != 1.0:
         msgs.append(f"launch records at {st['launch_pos']} w {st['launch_weight']}")
+    return msgs
+
+
+def check_bench(raw, fx):
+    """raw: (gates, voxels) dual-grid deposits of one run of a built-in benchmark."""
+    x = raw.sum(0)
+    msgs = [] if x.size == int(fx["nvox"]) else [f"grid of {x.size} voxels vs the reference's {int(fx['nvox'])}"]
+    if msgs:
+        return msgs
+    msgs = _zcheck("per-voxel", x[fx["sub"]], fx["vox_mean"], fx["vox_std"], 100,
+                   fx["null_vox_frac"], fx["null_vox_meanz"])
+    t = fx["total"]
+    if abs(x.sum() - t.mean()) > 3 * t.std(ddof=1) * INFLATE:
+        msgs.append(f"grid total {x.sum():.1f} vs reference {t.mean():.1f} +- {t.std(ddof=1):.1f}")
     return msgs
 
 

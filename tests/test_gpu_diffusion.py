@@ -1,0 +1,60 @@
+"""Physics check against diffusion theory, the reference's own validation
+(examples/meshtest/README.txt, plotmmcsph.m): a 60 mm cube (mua 0.002,
+mus 1, g 0.01, n 1.37) with a 10 mm sphere (mua 0.05, mus 5, g 0.9) at its
+centre, pencil source at the centre of the z=0 face, no refractive mismatch at
+the boundary (-b 0), 50 gates of 0.1 ns.  The time-integrated fluence on the
+plane through the source and the sphere centre must follow the analytic
+sphere-in-slab solution (oracle/sphdiffusion.py, pinned to the reference's
+sphdiffsemiinf.mat) where diffusion theory holds: at least 10 mm from the
+source, away from the sphere surface and from the cube's side faces (the
+analytic slab is laterally infinite)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from mmc_gb300 import meshgen
+from mmc_gb300.core import Mesh, SimConfig, simulate
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(os.path.dirname(HERE), "oracle"))
+import sphdiffusion as sd  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+MEDIA = np.array([[0.0, 0.0, 1.0, 1.0], [0.002, 1.0, 0.01, 1.37], [0.05, 5.0, 0.9, 1.37]], np.float32)
+
+
+def mc_plane_fluence(xs, zs, photons, seed=7):
+    """Time-integrated fluence of the MC engine at the points (x, 0, z) about
+    the sphere centre: the mean over the tets whose centroids lie within
+    1 mm of the point (all tets have the same volume)."""
+    from scipy.spatial import cKDTree
+    m = meshgen.inclusion_cube(n=60, jitter=0.0, media=MEDIA)
+    cfg = SimConfig(media=MEDIA, nphoton=photons, seed=seed, srcpos=(30.0, 30.0, 0.0), srcdir=(0.0, 0.0, 1.0),
+                    tend=5e-9, tstep=1e-10, basisorder=0, isreflect=0, outputtype="flux", isnormalized=1)
+    r = simulate(Mesh(m.node, m.elem, m.label), cfg)
+    cw = r.field.sum(0) * cfg.tstep
+    tree = cKDTree(meshgen.centroids(m.node, m.elem))
+    pts = np.c_[xs + 30.0, np.full_like(xs, 30.0), zs + 30.0]
+    return np.array([cw[idx].mean() for idx in tree.query_ball_point(pts, 1.0)])
+
+
+def test_fluence_follows_the_sphere_in_slab_diffusion_solution(gpu_ready):
+    f = np.load(os.path.join(HERE, "golden", "sphdiffsemiinf.npz"))
+    x, z = np.meshgrid(f["x"], f["z"], indexing="ij")
+    phi = f["phi"]
+    rs = np.hypot(x, z)
+    keep = (np.abs(x) <= 12.0) & (np.hypot(x, z + 30.0) >= 10.0) & (np.abs(rs - 10.0) >= 1.5)
+    xs, zs, ana = x[keep], z[keep], phi[keep]
+    mc = mc_plane_fluence(xs, zs, 30_000_000)
+    lr = np.log10(mc / ana)
+    inside = rs[keep] < 10.0
+    for name, sel in (("outside", ~inside), ("inside", inside)):
+        q = np.percentile(np.abs(lr[sel]), [50, 95])
+        print(f"{name}: {sel.sum()} points, median log10(mc/ana) {np.median(lr[sel]):+.4f}, "
+              f"|log10| p50 {q[0]:.4f} p95 {q[1]:.4f} max {np.abs(lr[sel]).max():.4f}")
+    assert np.all(np.isfinite(lr))
+    assert abs(np.median(lr)) < 0.1
+    assert np.percentile(np.abs(lr), 95) < 0.2

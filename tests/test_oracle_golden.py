@@ -48,6 +48,16 @@ def test_oracle_dual_grid_matches_reference_runs(oracle_mod):
     assert r["raw"].sum() * m.media[1, 0] == pytest.approx(r["energytot"] - r["energyesc"], rel=1e-5)
 
 
+@pytest.mark.parametrize("name", ["bench_dmmc-cube60", "bench_dmmc-cube60b"])
+def test_oracle_builtin_benchmarks_match_reference_runs(oracle_mod, name):
+    """The reference's built-in benchmarks (-Q dmmc-cube60, dmmc-cube60b: a
+    6-tet cube, so photons cross few, large elements) with dual-grid output."""
+    m, cfg, fx = gc.case_mesh_and_config(name)
+    r = oracle_mod.run(m.node, m.elem, m.label, cfg, nthreads=NTHREADS, normalize=False)
+    msgs = gc.check_bench(r["raw"], fx) + gc.check_tests_per_photon(r["raytet"] / cfg.nphoton, fx)
+    assert not msgs, "\n".join(msgs)
+
+
 def test_oracle_trajectories_match_reference_runs(oracle_mod):
     """Trajectory records (-D M: launch, every scattering event, photon end)
     against the reference's records: records per photon and their histogram,
