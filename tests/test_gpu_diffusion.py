@@ -27,16 +27,18 @@ MEDIA = np.array([[0.0, 0.0, 1.0, 1.0], [0.002, 1.0, 0.01, 1.37], [0.05, 5.0, 0.
 
 
 def mc_plane_fluence(xs, zs, photons, seed=7):
-    """Time-integrated fluence of the MC engine at the points (x, 0, z) about
-    the sphere centre: the mean over the tets whose centroids lie within
-    1 mm of the point (all tets have the same volume)."""
+    """Time-integrated nodal fluence of the MC engine at the points (x, 0, z)
+    about the sphere centre: the mean over the nodes within 1 mm of the point.
+    Nodal output, as the reference's validation uses: its element output
+    divides the mua-scaled deposits by mua once more (src/mmc_mesh.c:2244-2256),
+    which is exact only where mua is uniform."""
     from scipy.spatial import cKDTree
     m = meshgen.inclusion_cube(n=60, jitter=0.0, media=MEDIA)
     cfg = SimConfig(media=MEDIA, nphoton=photons, seed=seed, srcpos=(30.0, 30.0, 0.0), srcdir=(0.0, 0.0, 1.0),
-                    tend=5e-9, tstep=1e-10, basisorder=0, isreflect=0, outputtype="flux", isnormalized=1)
+                    tend=5e-9, tstep=1e-10, basisorder=1, isreflect=0, outputtype="flux", isnormalized=1)
     r = simulate(Mesh(m.node, m.elem, m.label), cfg)
     cw = r.field.sum(0) * cfg.tstep
-    tree = cKDTree(meshgen.centroids(m.node, m.elem))
+    tree = cKDTree(m.node)
     pts = np.c_[xs + 30.0, np.full_like(xs, 30.0), zs + 30.0]
     return np.array([cw[idx].mean() for idx in tree.query_ball_point(pts, 1.0)])
 
@@ -51,10 +53,11 @@ def test_fluence_follows_the_sphere_in_slab_diffusion_solution(gpu_ready):
     mc = mc_plane_fluence(xs, zs, 30_000_000)
     lr = np.log10(mc / ana)
     inside = rs[keep] < 10.0
-    for name, sel in (("outside", ~inside), ("inside", inside)):
+    assert np.all(np.isfinite(lr))
+    # measured on a GB300 (3e7 photons): outside median +0.007, p95 0.087; inside median -0.022, p95 0.060
+    for name, sel, med_tol, p95_tol in (("outside", ~inside, 0.03, 0.12), ("inside", inside, 0.05, 0.1)):
         q = np.percentile(np.abs(lr[sel]), [50, 95])
         print(f"{name}: {sel.sum()} points, median log10(mc/ana) {np.median(lr[sel]):+.4f}, "
               f"|log10| p50 {q[0]:.4f} p95 {q[1]:.4f} max {np.abs(lr[sel]).max():.4f}")
-    assert np.all(np.isfinite(lr))
-    assert abs(np.median(lr)) < 0.1
-    assert np.percentile(np.abs(lr), 95) < 0.2
+        assert abs(np.median(lr[sel])) < med_tol, name
+        assert q[1] < p95_tol, name
