@@ -67,10 +67,15 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
         return out
     jobs = []
     objs = []
-    for f in cu:
-        o = os.path.join(BUILDDIR, f + ".o")
+    # the engine is compiled once per arithmetic policy: the exact kernels without
+    # multiply-add contraction (the oracle's float sequence), the fast ones with it
+    units = [("engine.cu", "engine_exact", ["-DMMCGB_ENGINE_FAST=0", "-fmad=false"]),
+             ("engine.cu", "engine_fast", ["-DMMCGB_ENGINE_FAST=1", "-fmad=true"])]
+    units += [(f, f, ["-fmad=false"]) for f in cu if f != "engine.cu"]
+    for f, name, flags in units:
+        o = os.path.join(BUILDDIR, name + ".o")
         objs.append(o)
-        jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+        jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", *flags, "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xptxas", "-v", "-c", os.path.join(CSRC, f), "-o", o])
     for f in cpp:
         o = os.path.join(BUILDDIR, f + ".o")

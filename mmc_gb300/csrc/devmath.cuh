@@ -89,6 +89,19 @@ __device__ __forceinline__ float rng_next(unsigned long long& t0, unsigned long 
     return __uint_as_float(0x3F800000u | (lo >> 9)) - 1.0f;
 }
 
+// One xorshift128+ step giving two floats in [0,1): the return value from the
+// low 32 bits of the output (as rng_next) and `hi` from its high 32 bits.
+__device__ __forceinline__ float rng_next_pair(unsigned long long& t0, unsigned long long& t1, float& hi) {
+    unsigned long long s1 = t0;
+    const unsigned long long s0 = t1;
+    t0 = s0;
+    s1 ^= s1 << 23;
+    t1 = s1 ^ s0 ^ (s1 >> 18) ^ (s0 >> 5);
+    const unsigned long long r = t1 + s0;
+    hi = __uint_as_float(0x3F800000u | ((uint32_t)(r >> 32) >> 9)) - 1.0f;
+    return __uint_as_float(0x3F800000u | ((uint32_t)r >> 9)) - 1.0f;
+}
+
 __host__ __device__ __forceinline__ unsigned long long splitmix64(unsigned long long z) {
     z += 0x9E3779B97F4A7C15ull;
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;

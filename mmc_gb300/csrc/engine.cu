@@ -9,8 +9,15 @@
 //             the deposit fused in, (3) the lane applies the reference's
 //             post-step control flow (fix/cross/reflect/exit/detect/roulette/
 //             scatter) as a state transition.
-// Compile with -fmad=false: the float sequence is the contract shared with the
-// CPU oracle, and explicit fmaf() appears only in devmath.cuh.
+// The file is compiled twice.  MMCGB_ENGINE_FAST=0 with -fmad=false builds the
+// ExactMath kernels, whose float sequence is the contract shared with the CPU
+// oracle (no contraction; the polynomial exp/log/sincos of devmath.cuh).
+// MMCGB_ENGINE_FAST=1 with -fmad=true builds the FastMath kernels, where the
+// compiler may fuse any multiply-add; that unit also holds the dispatchers
+// that pick a policy per simulation.
+#if !defined(MMCGB_ENGINE_FAST) || (MMCGB_ENGINE_FAST != 0 && MMCGB_ENGINE_FAST != 1)
+#error "compile engine.cu with -DMMCGB_ENGINE_FAST=0 (exact kernels) or =1 (fast kernels)"
+#endif
 #include <cooperative_groups.h>
 #include <algorithm>
 #include <cstdio>
@@ -67,6 +74,8 @@ struct ExactMath {
     static __device__ __forceinline__ void sincos2pi(float u, float& s, float& c) { mmc_sincos2pi(u, s, c); }
     static __device__ __forceinline__ float rsqrt(float x) { return 1.f / sqrtf(x); }
     static __device__ __forceinline__ float mad(float a, float b, float c) { return a * b + c; }
+    static __device__ __forceinline__ float sqrt(float x) { return sqrtf(x); }
+    static constexpr bool kPairedDraw = false;
 };
 struct FastMath {
     static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
@@ -77,6 +86,14 @@ struct FastMath {
     }
     static __device__ __forceinline__ float rsqrt(float x) { return rsqrtf(x); }
     static __device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
+    static __device__ __forceinline__ float sqrt(float x) {
+        float r;
+        asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+        return r;
+    }
+    // One xorshift128+ output gives both scattering angles: its low 32 bits
+    // (the reference's float recipe) and its high 32 bits.
+    static constexpr bool kPairedDraw = true;
 };
 
 __device__ __forceinline__ int decode_nb(int w) { return (w << 8) >> 8; }
@@ -336,7 +353,7 @@ __device__ __forceinline__ int reflectray(Lane& L, const SimDev& S, const float4
     float tmp2 = 1.f - MP::div(tmp0, tmp1) * (1.f - Icos * Icos);
     if (tmp2 > 0.f && !((eid <= 0) && (S.isreflect == BC_MIRROR))) {
         float Re = tmp0 * Icos * Icos + tmp1 * tmp2;
-        tmp2 = sqrtf(tmp2);
+        tmp2 = MP::sqrt(tmp2);
         float Im = 2.f * n1 * n2 * Icos * tmp2;
         float Rtotal = MP::div(Re - Im, Re + Im);
         Re = tmp1 * Icos * Icos + tmp0 * tmp2 * tmp2;
@@ -400,17 +417,24 @@ template <class MP>
 __device__ __forceinline__ float next_scatter(Lane& L, float g, float& ctheta_out) {
     const float nextslen = -MP::log(rng_next(L.t0, L.t1) + kEps);
     float sphi, cphi, stheta, ctheta;
-    MP::sincos2pi(rng_next(L.t0, L.t1), sphi, cphi);
+    float utheta = 0.f;
+    if (MP::kPairedDraw) {
+        MP::sincos2pi(rng_next_pair(L.t0, L.t1, utheta), sphi, cphi);
+    } else {
+        MP::sincos2pi(rng_next(L.t0, L.t1), sphi, cphi);
+    }
     if (g > kEps) {
-        float tmp0 = MP::div(1.f - g * g, 1.f - g + 2.f * g * rng_next(L.t0, L.t1));
+        if (!MP::kPairedDraw) utheta = rng_next(L.t0, L.t1);
+        float tmp0 = MP::div(1.f - g * g, 1.f - g + 2.f * g * utheta);
         tmp0 *= tmp0;
         tmp0 = MP::div(1.f + g * g - tmp0, 2.f * g);
         tmp0 = fmaxf(-1.f, fminf(tmp0, 1.f));
-        stheta = sqrtf(1.f - tmp0 * tmp0);
+        stheta = MP::sqrt(1.f - tmp0 * tmp0);
         ctheta = tmp0;
     } else {
-        ctheta = 2.f * rng_next(L.t0, L.t1) - 1.f;
-        stheta = sqrtf(1.f - ctheta * ctheta);
+        if (!MP::kPairedDraw) utheta = rng_next(L.t0, L.t1);
+        ctheta = 2.f * utheta - 1.f;
+        stheta = MP::sqrt(1.f - ctheta * ctheta);
     }
     rotate_dir<MP>(L, stheta, ctheta, sphi, cphi);
     ctheta_out = ctheta;
@@ -1250,19 +1274,13 @@ bool general_source(const SimDev& s) { return s.srctype != ST_PENCIL || s.e0 <= 
 
 }  // namespace
 
-LaunchShape default_shape(int device, bool batched) {
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    int per_sm = 0;
-    const int threads = 128;
-    if (batched)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_batched<FastMath, false>, threads, 4096);
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_plain<FastMath, false, false>, threads,
-                                                      1024);
-    if (per_sm < 1) per_sm = 1;
-    return LaunchShape{sms * per_sm, threads};
-}
+#if MMCGB_ENGINE_FAST
+#define MMCGB_POLICY_NS fast
+using Policy = FastMath;
+#else
+#define MMCGB_POLICY_NS exact
+using Policy = ExactMath;
+#endif
 
 template <class MP, bool REPLAY, bool SRC>
 static cudaError_t launch_plain_t(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
@@ -1281,29 +1299,6 @@ static cudaError_t launch_plain_t(const SimDev& sim, unsigned long long* work_co
     photon_engine_plain<MP, REPLAY, SRC><<<shape.blocks, shape.threads, smem, stream>>>(sim, work_counter,
                                                                                        reclen_max, want_seed);
     return cudaGetLastError();
-}
-
-cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
-                         cudaStream_t stream) {
-    const bool src = general_source(sim);
-    if (sim.replay) {
-        if (src)
-            return sim.fast_math ? launch_plain_t<FastMath, true, true>(sim, work_counter, shape, stream)
-                                 : launch_plain_t<ExactMath, true, true>(sim, work_counter, shape, stream);
-        return sim.fast_math ? launch_plain_t<FastMath, true, false>(sim, work_counter, shape, stream)
-                             : launch_plain_t<ExactMath, true, false>(sim, work_counter, shape, stream);
-    }
-    if (src)
-        return sim.fast_math ? launch_plain_t<FastMath, false, true>(sim, work_counter, shape, stream)
-                             : launch_plain_t<ExactMath, false, true>(sim, work_counter, shape, stream);
-    return sim.fast_math ? launch_plain_t<FastMath, false, false>(sim, work_counter, shape, stream)
-                         : launch_plain_t<ExactMath, false, false>(sim, work_counter, shape, stream);
-}
-
-size_t phase_bytes_per_photon(const SimDev& sim) {
-    const int want_seed = (sim.issavedet && sim.seeds) ? 1 : 0;
-    return 2 * (sizeof(PState) + (sim.issavedet ? (size_t)sim.reclen * sizeof(float) : 0) +
-                (want_seed ? 2 * sizeof(unsigned long long) : 0));
 }
 
 template <class MP, bool SRC>
@@ -1351,18 +1346,6 @@ static cudaError_t launch_phased_t(const SimDev& sim, unsigned long long* work_c
     return cudaSuccess;
 }
 
-cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
-                          cudaStream_t stream, const PhaseQueue q[2], int span, unsigned* order,
-                          unsigned* bscratch, const float lo[3], const float hi[3]) {
-    if (general_source(sim))
-        return sim.fast_math
-                   ? launch_phased_t<FastMath, true>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi)
-                   : launch_phased_t<ExactMath, true>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi);
-    return sim.fast_math
-               ? launch_phased_t<FastMath, false>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi)
-               : launch_phased_t<ExactMath, false>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi);
-}
-
 template <class MP, bool SRC>
 static cudaError_t launch_batched_t(const SimDev* sims, const unsigned long long* cum, int nsims,
                                     unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
@@ -1382,19 +1365,83 @@ static cudaError_t launch_batched_t(const SimDev* sims, const unsigned long long
     return cudaGetLastError();
 }
 
+// The launchers of this unit's arithmetic policy.
+namespace MMCGB_POLICY_NS {
+
+cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
+                         cudaStream_t stream) {
+    const bool src = general_source(sim);
+    if (sim.replay)
+        return src ? launch_plain_t<Policy, true, true>(sim, work_counter, shape, stream)
+                   : launch_plain_t<Policy, true, false>(sim, work_counter, shape, stream);
+    return src ? launch_plain_t<Policy, false, true>(sim, work_counter, shape, stream)
+               : launch_plain_t<Policy, false, false>(sim, work_counter, shape, stream);
+}
+
+cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
+                          cudaStream_t stream, const PhaseQueue q[2], int span, unsigned* order,
+                          unsigned* bscratch, const float lo[3], const float hi[3]) {
+    return general_source(sim)
+               ? launch_phased_t<Policy, true>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi)
+               : launch_phased_t<Policy, false>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi);
+}
+
+cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
+                           unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
+                           unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream,
+                           int general_src) {
+    return general_src ? launch_batched_t<Policy, true>(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
+                                                        work_counter, shape, stream)
+                       : launch_batched_t<Policy, false>(sims, cum, nsims, total, nmed_stride, reclen_max,
+                                                         want_seed, work_counter, shape, stream);
+}
+
+}  // namespace MMCGB_POLICY_NS
+
+#if MMCGB_ENGINE_FAST
+// Entry points (engine.h): one definition, in the fast unit, dispatching on the policy.
+LaunchShape default_shape(int device, bool batched) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    int per_sm = 0;
+    const int threads = 128;
+    if (batched)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_batched<FastMath, false>, threads, 4096);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_plain<FastMath, false, false>, threads,
+                                                      1024);
+    if (per_sm < 1) per_sm = 1;
+    return LaunchShape{sms * per_sm, threads};
+}
+
+size_t phase_bytes_per_photon(const SimDev& sim) {
+    const int want_seed = (sim.issavedet && sim.seeds) ? 1 : 0;
+    return 2 * (sizeof(PState) + (sim.issavedet ? (size_t)sim.reclen * sizeof(float) : 0) +
+                (want_seed ? 2 * sizeof(unsigned long long) : 0));
+}
+
+cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
+                         cudaStream_t stream) {
+    return sim.fast_math ? fast::launch_plain(sim, work_counter, shape, stream)
+                         : exact::launch_plain(sim, work_counter, shape, stream);
+}
+
+cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
+                          cudaStream_t stream, const PhaseQueue q[2], int span, unsigned* order,
+                          unsigned* bscratch, const float lo[3], const float hi[3]) {
+    return sim.fast_math ? fast::launch_phased(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi)
+                         : exact::launch_phased(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi);
+}
+
 cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
                            unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
                            unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream, int fast_math,
                            int general_src) {
-    if (general_src)
-        return fast_math ? launch_batched_t<FastMath, true>(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
-                                                            work_counter, shape, stream)
-                         : launch_batched_t<ExactMath, true>(sims, cum, nsims, total, nmed_stride, reclen_max,
-                                                             want_seed, work_counter, shape, stream);
-    return fast_math ? launch_batched_t<FastMath, false>(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
-                                                         work_counter, shape, stream)
-                     : launch_batched_t<ExactMath, false>(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
-                                                          work_counter, shape, stream);
+    return fast_math ? fast::launch_batched(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
+                                            work_counter, shape, stream, general_src)
+                     : exact::launch_batched(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
+                                             work_counter, shape, stream, general_src);
 }
+#endif
 
 }  // namespace mmcgb

@@ -183,6 +183,31 @@ cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, in
                            int fast_math, int general_src);
 LaunchShape default_shape(int device, bool batched);
 
+// The launchers of each arithmetic policy: engine.cu is compiled once per
+// policy, and the entry points above dispatch on SimDev::fast_math.
+namespace exact {
+cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
+                         cudaStream_t stream);
+cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
+                          cudaStream_t stream, const PhaseQueue q[2], int span, unsigned* order,
+                          unsigned* bscratch, const float lo[3], const float hi[3]);
+cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
+                           unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
+                           unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream,
+                           int general_src);
+}  // namespace exact
+namespace fast {
+cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
+                         cudaStream_t stream);
+cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
+                          cudaStream_t stream, const PhaseQueue q[2], int span, unsigned* order,
+                          unsigned* bscratch, const float lo[3], const float hi[3]);
+cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
+                           unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
+                           unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream,
+                           int general_src);
+}  // namespace fast
+
 // Records the message returned by mmcgb_last_error() on this thread.
 void set_last_error(const std::string& msg);
 

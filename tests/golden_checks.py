@@ -212,9 +212,13 @@ def check_bench(raw, fx):
     return msgs
 
 
-def check_tests_per_photon(tpp, fx, rel=0.01):
-    ref = float(fx["tests_per_photon"].mean())
-    return [] if abs(tpp - ref) <= rel * ref else [f"ray-tet tests/photon {tpp:.2f} vs reference {ref:.2f}"]
+def check_tests_per_photon(tpp, fx, rel=0.01, nsigma=4.0):
+    """Within `rel` of the reference mean, or nsigma run-to-run deviations
+    where the reference's own spread is wider (few, large elements)."""
+    t = fx["tests_per_photon"]
+    ref = float(t.mean())
+    tol = max(rel * ref, nsigma * float(t.std(ddof=1)) * INFLATE)
+    return [] if abs(tpp - ref) <= tol else [f"ray-tet tests/photon {tpp:.2f} vs reference {ref:.2f} (tolerance {tol:.2f})"]
 
 
 def check_detectors(detp, media, fx):
