@@ -9,12 +9,14 @@
 //             the deposit fused in, (3) the lane applies the reference's
 //             post-step control flow (fix/cross/reflect/exit/detect/roulette/
 //             scatter) as a state transition.
-// The file is compiled twice.  MMCGB_ENGINE_FAST=0 with -fmad=false builds the
+// The file is compiled twice, with -fmad=false: MMCGB_ENGINE_FAST=0 builds the
 // ExactMath kernels, whose float sequence is the contract shared with the CPU
-// oracle (no contraction; the polynomial exp/log/sincos of devmath.cuh).
-// MMCGB_ENGINE_FAST=1 with -fmad=true builds the FastMath kernels, where the
-// compiler may fuse any multiply-add; that unit also holds the dispatchers
-// that pick a policy per simulation.
+// oracle (no contraction; the polynomial exp/log/sincos of devmath.cuh), and
+// MMCGB_ENGINE_FAST=1 the FastMath kernels, which fuse multiply-adds only where
+// the policy says so (MP::mad, MP::msub, MP::plane), so every kernel of a policy
+// computes the same floats (a simulation gives the same result alone, batched
+// or phased).  The fast unit also holds the dispatchers that pick a policy per
+// simulation.
 #if !defined(MMCGB_ENGINE_FAST) || (MMCGB_ENGINE_FAST != 0 && MMCGB_ENGINE_FAST != 1)
 #error "compile engine.cu with -DMMCGB_ENGINE_FAST=0 (exact kernels) or =1 (fast kernels)"
 #endif
@@ -74,6 +76,12 @@ struct ExactMath {
     static __device__ __forceinline__ void sincos2pi(float u, float& s, float& c) { mmc_sincos2pi(u, s, c); }
     static __device__ __forceinline__ float rsqrt(float x) { return 1.f / sqrtf(x); }
     static __device__ __forceinline__ float mad(float a, float b, float c) { return a * b + c; }
+    static __device__ __forceinline__ float msub(float a, float b, float c) { return c - a * b; }
+    // d - p.n of a face plane, summed as the oracle does
+    static __device__ __forceinline__ float plane(float d, float px, float py, float pz, float nx, float ny,
+                                                  float nz) {
+        return d - ((px * nx + py * ny) + pz * nz);
+    }
     static __device__ __forceinline__ float sqrt(float x) { return sqrtf(x); }
     static constexpr bool kPairedDraw = false;
 };
@@ -86,6 +94,11 @@ struct FastMath {
     }
     static __device__ __forceinline__ float rsqrt(float x) { return rsqrtf(x); }
     static __device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
+    static __device__ __forceinline__ float msub(float a, float b, float c) { return fmaf(-a, b, c); }
+    static __device__ __forceinline__ float plane(float d, float px, float py, float pz, float nx, float ny,
+                                                  float nz) {
+        return fmaf(-pz, nz, fmaf(-py, ny, fmaf(-px, nx, d)));
+    }
     static __device__ __forceinline__ float sqrt(float x) {
         float r;
         asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
@@ -189,10 +202,10 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
     float S1 = MP::mad(L.vz, nz.y, MP::mad(L.vy, ny.y, L.vx * nx.y));
     float S2 = MP::mad(L.vz, nz.z, MP::mad(L.vy, ny.z, L.vx * nx.z));
     float S3 = MP::mad(L.vz, nz.w, MP::mad(L.vy, ny.w, L.vx * nx.w));
-    float T0 = nd.x - MP::mad(L.pz, nz.x, MP::mad(L.py, ny.x, L.px * nx.x));
-    float T1 = nd.y - MP::mad(L.pz, nz.y, MP::mad(L.py, ny.y, L.px * nx.y));
-    float T2 = nd.z - MP::mad(L.pz, nz.z, MP::mad(L.py, ny.z, L.px * nx.z));
-    float T3 = nd.w - MP::mad(L.pz, nz.w, MP::mad(L.py, ny.w, L.px * nx.w));
+    float T0 = MP::plane(nd.x, L.px, L.py, L.pz, nx.x, ny.x, nz.x);
+    float T1 = MP::plane(nd.y, L.px, L.py, L.pz, nx.y, ny.y, nz.y);
+    float T2 = MP::plane(nd.z, L.px, L.py, L.pz, nx.z, ny.z, nz.z);
+    float T3 = MP::plane(nd.w, L.px, L.py, L.pz, nx.w, ny.w, nz.w);
     T0 = (S0 > 0.f) ? MP::div(T0, S0) : 1e10f;
     T1 = (S1 > 0.f) ? MP::div(T1, S1) : 1e10f;
     T2 = (S2 > 0.f) ? MP::div(T2, S2) : 1e10f;
@@ -211,7 +224,7 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
         L.hit = 1;
         const float rc = prop.w * kRC0;
         // (int)x > maxgate-1, written without the float->int conversion
-        if ((L.ptime + Lmove * rc - S.tstart) * S.Rtstep >= (float)S.maxgate) {
+        if ((MP::mad(Lmove, rc, L.ptime) - S.tstart) * S.Rtstep >= (float)S.maxgate) {
             L.faceid = -2;
             L.hit = 0;
             Lmove = MP::div(S.tend - L.ptime, rc) - 1e-4f;
@@ -232,9 +245,9 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
                 currweight += L.weight;
             }
         }
-        L.slen -= Lmove * prop.y;
+        L.slen = MP::msub(Lmove, prop.y, L.slen);
         float ww = currweight - L.weight;
-        L.ptime += Lmove * rc;
+        L.ptime = MP::mad(Lmove, rc, L.ptime);
         if (REPLAY && ot == OT_WN) {  // scatter counts are deposited at the scattering events only
             L.px = MP::mad(Lmove, L.vx, L.px);
             L.py = MP::mad(Lmove, L.vy, L.py);
@@ -395,18 +408,18 @@ template <class MP>
 __device__ __forceinline__ void rotate_dir(Lane& L, float stheta, float ctheta, float sphi, float cphi) {
     float px, py, pz;
     if (L.vz > -1.f + kEps && L.vz < 1.f - kEps) {
-        const float tmp0 = 1.f - L.vz * L.vz;
+        const float tmp0 = MP::msub(L.vz, L.vz, 1.f);
         float tmp1 = MP::rsqrt(tmp0);
         tmp1 = stheta * tmp1;
-        px = tmp1 * (L.vx * L.vz * cphi - L.vy * sphi) + L.vx * ctheta;
-        py = tmp1 * (L.vy * L.vz * cphi + L.vx * sphi) + L.vy * ctheta;
-        pz = -tmp1 * tmp0 * cphi + L.vz * ctheta;
+        px = MP::mad(tmp1, MP::msub(L.vy, sphi, L.vx * L.vz * cphi), L.vx * ctheta);
+        py = MP::mad(tmp1, MP::mad(L.vx, sphi, L.vy * L.vz * cphi), L.vy * ctheta);
+        pz = MP::mad(-tmp1 * tmp0, cphi, L.vz * ctheta);
     } else {
         px = stheta * cphi;
         py = stheta * sphi;
         pz = (L.vz > 0.f) ? ctheta : -ctheta;
     }
-    const float inv = MP::rsqrt(px * px + py * py + pz * pz);
+    const float inv = MP::rsqrt(MP::mad(pz, pz, MP::mad(py, py, px * px)));
     L.vx = px * inv;
     L.vy = py * inv;
     L.vz = pz * inv;
@@ -425,16 +438,16 @@ __device__ __forceinline__ float next_scatter(Lane& L, float g, float& ctheta_ou
     }
     if (g > kEps) {
         if (!MP::kPairedDraw) utheta = rng_next(L.t0, L.t1);
-        float tmp0 = MP::div(1.f - g * g, 1.f - g + 2.f * g * utheta);
+        float tmp0 = MP::div(MP::msub(g, g, 1.f), MP::mad(2.f * g, utheta, 1.f - g));
         tmp0 *= tmp0;
-        tmp0 = MP::div(1.f + g * g - tmp0, 2.f * g);
+        tmp0 = MP::div(MP::mad(g, g, 1.f) - tmp0, 2.f * g);
         tmp0 = fmaxf(-1.f, fminf(tmp0, 1.f));
-        stheta = MP::sqrt(1.f - tmp0 * tmp0);
+        stheta = MP::sqrt(MP::msub(tmp0, tmp0, 1.f));
         ctheta = tmp0;
     } else {
         if (!MP::kPairedDraw) utheta = rng_next(L.t0, L.t1);
         ctheta = 2.f * utheta - 1.f;
-        stheta = MP::sqrt(1.f - ctheta * ctheta);
+        stheta = MP::sqrt(MP::msub(ctheta, ctheta, 1.f));
     }
     rotate_dir<MP>(L, stheta, ctheta, sphi, cphi);
     ctheta_out = ctheta;
@@ -963,7 +976,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                     }
                     if (placed) {
                         L.mode = M_OUTER;
-                        if (S.traj) save_traj(S, L);
+                        if (SRC && S.traj) save_traj(S, L);
                     } else {  // launch position in no element: counted, reported as an error
                         tally.outside++;
                         tally.eesc += L.weight;
@@ -1032,7 +1045,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                             killed = true;
                     }
                     if (killed) {
-                        if (S.traj) save_traj(S, L);
+                        if (SRC && S.traj) save_traj(S, L);
                         if (S.photon_det) S.photon_det[L.pid] = 0;
                         tally.eesc += L.weight;
                         if (S.photon_weight) S.photon_weight[L.pid] = L.weight;
@@ -1049,7 +1062,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                         const int tp = L.label;
                         L.slen0 = next_scatter<MP>(L, med[tp].z, ctheta);
                         L.slen = L.slen0;
-                        if (S.traj) save_traj(S, L);
+                        if (SRC && S.traj) save_traj(S, L);
                         if (S.issavedet && tp > 0) {
                             const int M = S.nmedia - 1;
                             if (S.ismomentum) PP(2 * M + tp - 1) += (1.f - ctheta);
@@ -1213,7 +1226,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
             if (S.photon_det) S.photon_det[L.pid] = 0;
         }
         if (ended) {
-            if (S.traj) save_traj(S, L);
+            if (SRC && S.traj) save_traj(S, L);
             tally.eesc += L.weight;
             if (S.photon_weight) S.photon_weight[L.pid] = L.weight;
             if (S.photon_steps) S.photon_steps[L.pid] = L.steps;
@@ -1266,13 +1279,16 @@ size_t smem_bytes(int nmed_rows, int reclen_max, int threads, int want_seed) {
     return b;
 }
 
+}  // namespace
+
 // Kernels compiled with the general launch and deposit (SRC) serve
 // simulations whose source is not a pencil beam starting in a known element,
-// or that deposit into a voxel grid; the others carry only the pencil launch
-// and the element deposit, which keeps the step loop's registers free.
-bool general_source(const SimDev& s) { return s.srctype != ST_PENCIL || s.e0 <= 0 || s.grid; }
-
-}  // namespace
+// that deposit into a voxel grid or that record trajectories; the others
+// carry only the pencil launch and the element deposit, which keeps the step
+// loop's registers free.
+#if MMCGB_ENGINE_FAST
+bool general_source(const SimDev& s) { return s.srctype != ST_PENCIL || s.e0 <= 0 || s.grid || s.traj; }
+#endif
 
 #if MMCGB_ENGINE_FAST
 #define MMCGB_POLICY_NS fast

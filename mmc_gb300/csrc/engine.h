@@ -182,6 +182,9 @@ cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, in
                            unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream,
                            int fast_math, int general_src);
 LaunchShape default_shape(int device, bool batched);
+// Whether `s` needs the general kernels (a non-pencil source, a pencil without
+// a known initial element, dual-grid output or trajectory records).
+bool general_source(const SimDev& s);
 
 // The launchers of each arithmetic policy: engine.cu is compiled once per
 // policy, and the entry points above dispatch on SimDev::fast_math.

@@ -103,3 +103,25 @@ def test_respin_graph_equals_one_launch(gpu_ready):
     r = s.end()
     np.testing.assert_allclose(r.field, alone.field, rtol=1e-9, atol=1e-12)
     assert r.raytet == alone.raytet and _rows(r) == _rows(alone)
+
+
+def test_batch_mixing_grid_output_and_trajectories(gpu_ready):
+    """A pencil-beam simulation with dual-grid output or trajectory records
+    runs in the general kernels; a batch holding one next to a plain element
+    simulation must run them there too, each equal to its solo run."""
+    a = meshgen.inclusion_cube(n=16, jitter=0.5, seed=4)
+    m = Mesh(a.node, a.elem, a.label)
+    base = SimConfig(media=a.media, nphoton=20000, seed=9, srcpos=(30, 30, 0), tend=5e-9, tstep=1e-9,
+                     basisorder=0, isnormalized=0)
+    cfgs = [base, dataclasses.replace(base, seed=10, method="grid", gridstep=2.0),
+            dataclasses.replace(base, seed=11, maxjumpdebug=4_000_000)]
+    alone = [simulate(m, c) for c in cfgs]
+    mixed = simulate_batch([m, m, m], cfgs)
+    for a_, b_ in zip(alone, mixed):
+        assert b_.field.shape == a_.field.shape
+        np.testing.assert_allclose(b_.field, a_.field, rtol=1e-9, atol=1e-12)
+        assert a_.raytet == b_.raytet
+    t_a, t_b = alone[2].traj, mixed[2].traj
+    assert alone[2].ntraj == mixed[2].ntraj == len(t_b)
+    order = lambda t: t[np.argsort(t[:, 0].view(np.uint32), kind="stable")].view(np.uint32)  # noqa: E731
+    assert np.array_equal(order(t_a), order(t_b))
