@@ -751,7 +751,7 @@ int batch_launch(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets, c
     std::vector<SimDev> sims(n);
     std::vector<unsigned long long> cum(n);
     unsigned long long total = 0;
-    int nmed_stride = 0, reclen_max = 0, want_seed = 0, want_io = 0;
+    int nmed_stride = 0, reclen_max = 0, want_seed = 0, want_io = 0, want_replay = 0;
     for (int i = 0; i < n; i++) {
         mmcgb_session* s = ss[i];
         if (!s || s->mesh->device != device) return fail(MMCGB_E_ARG, "batched sessions must live on one device");
@@ -767,6 +767,7 @@ int batch_launch(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets, c
         if (s->cfg.issavedet) reclen_max = std::max(reclen_max, s->P.sim.reclen);
         if (s->cfg.issavedet && s->P.sim.seeds) want_seed = 1;
         if (general_source(s->P.sim)) want_io = 1;
+        if (s->P.sim.replay) want_replay = 1;
         total += counts[i];
         cum[i] = total;
     }
@@ -801,7 +802,8 @@ int batch_launch(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets, c
     if (n == 1)  // a single simulation takes the plain kernel (its parameter block in constant memory)
         CK(launch_plain(sims[0], work, s0->shape, st));
     else
-        CK(launch_batched(dsims, dcum, n, total, nmed_stride, reclen_max, want_seed, work, shape, st, fast, want_io));
+        CK(launch_batched(dsims, dcum, n, total, nmed_stride, reclen_max, want_seed, work, shape, st, fast, want_io,
+                          want_replay));
     if (ordered) CK(cudaEventRecord(s0->ev1, st));
     CK(cudaFreeAsync(dsims, st));
     CK(cudaFreeAsync(dcum, st));
@@ -951,7 +953,7 @@ int32_t mmcgb_simulate_batch(int32_t n, mmcgb_mesh* const* meshes, const mmcgb_c
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     std::vector<Prepared> P(n);
     int rc = MMCGB_OK;
-    int nmed_stride = 0, reclen_max = 0, want_seed = 0, want_io = 0;
+    int nmed_stride = 0, reclen_max = 0, want_seed = 0, want_io = 0, want_replay = 0;
     std::vector<unsigned long long> cum(n);
     unsigned long long total = 0;
     for (int i = 0; i < n && rc == MMCGB_OK; i++) {
@@ -961,6 +963,7 @@ int32_t mmcgb_simulate_batch(int32_t n, mmcgb_mesh* const* meshes, const mmcgb_c
         if (cfgs[i].issavedet) reclen_max = std::max(reclen_max, P[i].sim.reclen);
         if (cfgs[i].issavedet && cfgs[i].issaveseed) want_seed = 1;
         if (general_source(P[i].sim)) want_io = 1;
+        if (P[i].sim.replay) want_replay = 1;
         if ((cfgs[i].fast_math != 0) != (cfgs[0].fast_math != 0)) {
             rc = fail(MMCGB_E_ARG, "batched simulations must share fast_math");
             break;
@@ -989,7 +992,7 @@ int32_t mmcgb_simulate_batch(int32_t n, mmcgb_mesh* const* meshes, const mmcgb_c
         if (e == cudaSuccess) e = cudaEventRecord(ev0, stream);
         if (e == cudaSuccess)
             e = launch_batched(dsims, dcum, n, total, nmed_stride, reclen_max, want_seed, work, shape, stream,
-                               cfgs[0].fast_math ? 1 : 0, want_io);
+                               cfgs[0].fast_math ? 1 : 0, want_io, want_replay);
         if (e == cudaSuccess) e = cudaEventRecord(ev1, stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) rc = cuda_fail(e, "batched photon engine");

@@ -1278,7 +1278,7 @@ __global__ void __launch_bounds__(128, 8) photon_engine_phased(const __grid_cons
                                                         work_counter, pa);
 }
 
-template <class MP, bool SRC>
+template <class MP, bool REPLAY, bool SRC>
 __global__ void __launch_bounds__(128, 8) photon_engine_batched(const SimDev* __restrict__ sims,
                                                                 const unsigned long long* __restrict__ cum,
                                                                 int nsims, unsigned long long total,
@@ -1286,7 +1286,7 @@ __global__ void __launch_bounds__(128, 8) photon_engine_batched(const SimDev* __
                                                                 int reclen_max, int want_seed) {
     ManySims acc{sims};
     const PhaseArgs none{};
-    engine_body<MP, ManySims, true, false, true, SRC>(acc, cum, nsims, total, nmed_stride, reclen_max, want_seed,
+    engine_body<MP, ManySims, true, false, REPLAY, SRC>(acc, cum, nsims, total, nmed_stride, reclen_max, want_seed,
                                                       work_counter, none);
 }
 
@@ -1380,21 +1380,21 @@ static cudaError_t launch_phased_t(const SimDev& sim, unsigned long long* work_c
     return cudaSuccess;
 }
 
-template <class MP, bool SRC>
+template <class MP, bool REPLAY, bool SRC>
 static cudaError_t launch_batched_t(const SimDev* sims, const unsigned long long* cum, int nsims,
                                     unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
                                     unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream) {
     const size_t smem = smem_bytes(nsims * nmed_stride, reclen_max, shape.threads, want_seed);
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(photon_engine_batched<MP, SRC>,
+        cudaError_t e = cudaFuncSetAttribute(photon_engine_batched<MP, REPLAY, SRC>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     (void)cudaGetLastError();  // the launch check below must see this launch's status only
-    // batches may mix forward and replay simulations: the batched kernel keeps the replay branches
-    photon_engine_batched<MP, SRC><<<shape.blocks, shape.threads, smem, stream>>>(
+    // a batch holding a replay simulation runs the kernel with the replay branches
+    photon_engine_batched<MP, REPLAY, SRC><<<shape.blocks, shape.threads, smem, stream>>>(
         sims, cum, nsims, total, nmed_stride, work_counter, reclen_max, want_seed);
     return cudaGetLastError();
 }
@@ -1423,11 +1423,12 @@ cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, L
 cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
                            unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
                            unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream,
-                           int general_src) {
-    return general_src ? launch_batched_t<Policy, true>(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
-                                                        work_counter, shape, stream)
-                       : launch_batched_t<Policy, false>(sims, cum, nsims, total, nmed_stride, reclen_max,
-                                                         want_seed, work_counter, shape, stream);
+                           int general_src, int replay) {
+#define MMCGB_BATCHED(R, G) \
+    launch_batched_t<Policy, R, G>(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed, work_counter, shape, stream)
+    if (replay) return general_src ? MMCGB_BATCHED(true, true) : MMCGB_BATCHED(true, false);
+    return general_src ? MMCGB_BATCHED(false, true) : MMCGB_BATCHED(false, false);
+#undef MMCGB_BATCHED
 }
 
 }  // namespace MMCGB_POLICY_NS
@@ -1440,7 +1441,8 @@ LaunchShape default_shape(int device, bool batched) {
     int per_sm = 0;
     const int threads = 128;
     if (batched)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_batched<FastMath, false>, threads, 4096);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_batched<FastMath, true, false>, threads,
+                                                      4096);
     else
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_plain<FastMath, false, false>, threads,
                                                       1024);
@@ -1470,11 +1472,11 @@ cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, L
 cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
                            unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
                            unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream, int fast_math,
-                           int general_src) {
+                           int general_src, int replay) {
     return fast_math ? fast::launch_batched(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
-                                            work_counter, shape, stream, general_src)
+                                            work_counter, shape, stream, general_src, replay)
                      : exact::launch_batched(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed,
-                                             work_counter, shape, stream, general_src);
+                                             work_counter, shape, stream, general_src, replay);
 }
 #endif
 

@@ -176,11 +176,13 @@ cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, L
 cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
                          cudaStream_t stream);
 // Launches the batched engine over `nsims` simulations (`sims` in device memory,
-// `cum` = inclusive prefix sums of photon counts, length nsims).
+// `cum` = inclusive prefix sums of photon counts, length nsims).  `general_src`:
+// some simulation needs the general kernels (general_source); `replay`: some
+// simulation is a replay.
 cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
                            unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
                            unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream,
-                           int fast_math, int general_src);
+                           int fast_math, int general_src, int replay);
 LaunchShape default_shape(int device, bool batched);
 // Whether `s` needs the general kernels (a non-pencil source, a pencil without
 // a known initial element, dual-grid output or trajectory records).
@@ -197,7 +199,7 @@ cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, L
 cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
                            unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
                            unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream,
-                           int general_src);
+                           int general_src, int replay);
 }  // namespace exact
 namespace fast {
 cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
@@ -208,7 +210,7 @@ cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, L
 cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
                            unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
                            unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream,
-                           int general_src);
+                           int general_src, int replay);
 }  // namespace fast
 
 // Records the message returned by mmcgb_last_error() on this thread.
