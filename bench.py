@@ -125,12 +125,12 @@ def cpu_baseline(m, cfg, target_s=12.0):
     n = 20000
     while True:
         c = dataclasses.replace(cfg, nphoton=n, maxdetphoton=max(1000, n))
-        t0 = time.perf_counter()
-        oracle.run(m.node, m.elem, m.label, c, nthreads=cores, normalize=False)
-        dt = time.perf_counter() - t0
+        dt = oracle.run(m.node, m.elem, m.label, c, nthreads=cores, normalize=False)["sim_seconds"]
         if dt >= target_s * 0.5 or n >= 5_000_000:
             return {"value": n / (dt * 1e3), "unit": "photons/ms", "cores": cores, "kind": "port",
-                    "sample": f"{n} photons of the {JOB_PHOTONS:.0e}-photon job, {dt:.1f} s on {cores} threads"}
+                    "sample": f"{n} photons of the {JOB_PHOTONS:.0e}-photon job, {dt:.1f} s of photon loop "
+                              f"on {cores} threads (mesh preparation excluded, as the reference times "
+                              f"its speed)"}
         n = int(n * min(10.0, max(1.5, target_s / max(dt, 1e-3))))
 
 
@@ -142,12 +142,11 @@ def run_reference(args, rank, world):
     import oracle
     import dataclasses
     cores = os.cpu_count() or 1
-    # size one step to a few seconds of CPU work
+    # size one step to a few seconds of photon loop; each step times the photon loop alone, as the
+    # reference times the speed it reports (mesh preparation and output stage excluded)
     n = 20000
     c = dataclasses.replace(cfg, nphoton=n, maxdetphoton=n)
-    t0 = time.perf_counter()
-    oracle.run(m.node, m.elem, m.label, c, nthreads=cores, normalize=False)
-    dt = time.perf_counter() - t0
+    dt = oracle.run(m.node, m.elem, m.label, c, nthreads=cores, normalize=False)["sim_seconds"]
     n = max(20000, int(n * 4.0 / max(dt, 1e-3)))
     c = dataclasses.replace(cfg, nphoton=n, maxdetphoton=n)
     for _ in range(args.warmup):
@@ -156,18 +155,18 @@ def run_reference(args, rank, world):
     times = []
     for k in range(args.steps):
         ck = dataclasses.replace(c, photon_offset=k * n)
-        t0 = time.perf_counter()
-        oracle.run(m.node, m.elem, m.label, ck, nthreads=cores, normalize=True)
-        times.append(time.perf_counter() - t0)
+        times.append(oracle.run(m.node, m.elem, m.label, ck, nthreads=cores, normalize=False)["sim_seconds"])
     total = sum(times)
     value = n * args.steps / (total * 1e3)
     line = {"impl": "reference", "metric": "photons/ms", "value": value, "unit": "photons/ms", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "photons_per_step": n, "gates": 50, "detectors": 4,
-                       "note": "CPU restatement of the reference algorithm (reference C sources are not on the box)"},
+                       "note": "CPU restatement of the reference algorithm (reference C sources are not on the box); "
+                               "photon loop timed, as the reference times its reported speed"},
             "cpu_baseline": {"value": value, "unit": "photons/ms", "cores": cores, "kind": "port",
-                             "sample": f"{n} photons per step x {args.steps} steps on {cores} threads"},
+                             "sample": f"{n} photons per step x {args.steps} steps on {cores} threads, "
+                                       f"photon loop only"},
             "e2e": {"value": value, "unit": "photons/ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

@@ -14,6 +14,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <float.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -1177,6 +1178,9 @@ int oracle_run(int nn, const float* node, int ne, const int* elem, const int* la
 #else
     (void)nthreads;
 #endif
+    /* the photon loop alone is timed, as the reference times its speed report (src/mmc_host.c:194, :359-362) */
+    struct timespec t_start, t_end;
+    clock_gettime(CLOCK_MONOTONIC, &t_start);
 #pragma omp parallel reduction(+:etot, eesc, raytet, aborted, outside)
     {
         float* ppath = (float*)calloc((size_t)g.reclen + 1, sizeof(float));
@@ -1186,6 +1190,8 @@ int oracle_run(int nn, const float* node, int ne, const int* elem, const int* la
         etot += tl.etot; eesc += tl.eesc; raytet += tl.raytet; aborted += tl.aborted; outside += tl.outside;
         free(ppath);
     }
+    clock_gettime(CLOCK_MONOTONIC, &t_end);
+    out->sim_seconds = (double)(t_end.tv_sec - t_start.tv_sec) + 1e-9 * (double)(t_end.tv_nsec - t_start.tv_nsec);
     out->energytot = etot;
     out->energyesc = eesc;
     out->raytet = raytet;

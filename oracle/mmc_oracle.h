@@ -79,6 +79,7 @@ typedef struct oracle_out {
     float* traj;            /* maxtraj*6 trajectory records (id, x, y, z, w, eid), may be NULL */
     uint32_t maxtraj;
     uint32_t ntraj;         /* records written or attempted (may exceed maxtraj) */
+    double sim_seconds;     /* wall time of the photon loop (mesh preparation excluded) */
 } oracle_out;
 
 /* Mesh preparation (volumes with orientation fix, face neighbours, normals,

@@ -48,6 +48,7 @@ class OOut(C.Structure):
         ("energyesc", C.c_double), ("raytet", C.c_uint64), ("aborted", C.c_uint64), ("outside", C.c_uint64),
         ("dref", C.c_void_p), ("nf", C.c_int),
         ("traj", C.c_void_p), ("maxtraj", C.c_uint32), ("ntraj", C.c_uint32),
+        ("sim_seconds", C.c_double),
     ]
 
 
@@ -231,6 +232,7 @@ def run(node, elem, label, cfg, nthreads=1, trace=False, normalize=True):
     res["nf"] = int(out.nf)
     res["dref"] = dref[:maxgate * out.nf].reshape(maxgate, out.nf) if dref is not None else None
     res["ntraj"] = int(out.ntraj)
+    res["sim_seconds"] = float(out.sim_seconds)
     res["traj"] = traj[:min(int(out.ntraj), maxtraj)] if traj is not None else None
     if normalize and c.method == 1:  # dual grid: one scale factor (src/mmc_mesh.c:2204-2206)
         norm = 1.0
