@@ -89,3 +89,45 @@ def test_bin_and_dat_writers(tmp_path):
     io.write_dat(str(tmp_path / "a.dat"), f)
     lines = open(tmp_path / "a.dat").read().split("\n")
     assert lines[0].split("\t")[0] == "1" and len([x for x in lines if x]) == 12
+
+
+def test_builtin_benchmarks_and_session_flags():
+    """-Q inputs (src/mmc_bench.c:44-190): the 6-tet 60 mm cube with the benchmark's
+    source, detectors and mismatch flag; Session.DebugFlag letters or bit mask
+    and Session.RayTracer reach the front end."""
+    for name, mismatch in (("dmmc-cube60", 0), ("dmmc-cube60b", 1)):
+        mesh, cfg, meta = io.load_input(io.builtin_benchmark(name))
+        assert mesh["elem"].shape == (6, 4) and mesh["node"].shape == (8, 3)
+        assert cfg.isreflect == mismatch and cfg.e0 == 2 and cfg.nphoton == 1_000_000
+        assert cfg.srcpos == (30.1, 30.2, 0.0) and cfg.detpos.shape == (4, 4)
+        assert meta["session"] == name
+    with pytest.raises(ValueError):
+        io.builtin_benchmark("edgeimmc")
+    d = io.builtin_benchmark("dmmc-cube60")
+    d["Session"].update(DebugFlag="TM", RayTracer="g")
+    _, _, meta = io.load_input(d)
+    assert meta["debugflag"] == "TM" and meta["raytracer"] == "g"
+    d["Session"]["DebugFlag"] = (1 << 9) | (1 << 13)   # T and M as a bit mask (src/mmc_utils.c:139)
+    assert io.load_input(d)[2]["debugflag"] == "TM"
+
+
+def test_cli_lists_builtin_benchmarks():
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-m", "mmc_gb300", "-Q"], env=dict(os.environ, PYTHONPATH=root),
+                       capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.split() == ["Built-in", "benchmarks:", "dmmc-cube60", "dmmc-cube60b"]
+
+
+def test_pmmc_debuglevel_parsing():
+    """debuglevel letters of pmmc (src/pmmc.cpp:692-710): M asks for trajectories."""
+    m = meshgen.homogeneous_cube(n=2)
+    base = dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[30, 30, 0])
+    sc = pmmc._parse(dict(base, debuglevel="M", maxjumpdebug=500))[4]
+    assert sc.maxjumpdebug == 500
+    assert pmmc._parse(dict(base, debuglevel="m"))[4].maxjumpdebug == 10_000_000
+    assert pmmc._parse(dict(base, debuglevel="R"))[4].maxjumpdebug == 0
+    for bad in ("", "Q"):
+        with pytest.raises(ValueError):
+            pmmc._parse(dict(base, debuglevel=bad))
