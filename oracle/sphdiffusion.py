@@ -20,7 +20,10 @@ add image sources (extrapolated boundary z_b = 2D(1+R)/(1-R), source depth
 z_0 = 1/mu_s') and the first-order images of the sphere.
 
 Pinned by tests/golden/sphdiffsemiinf.npz (the reference's
-examples/meshtest/sphdiffsemiinf.mat).
+examples/meshtest/sphdiffsemiinf.mat).  `point_semi_infinite` is the
+homogeneous semi-infinite medium in closed form (the same image sources with
+no sphere), equal to `semi_infinite` with a sphere of the background's
+properties.
 """
 from __future__ import annotations
 
@@ -186,3 +189,20 @@ def slab(reff1, reff2, h, x, y, z, cfg=SphereCfg()):
     res[out] -= scatter_only(x, y, zs, replace(cfg, src=(s0[0] - z0, np.pi - s0[1], s0[2])))[out]
     res[out] += scatter_only(x, y, zs, replace(cfg, src=(s0[0] + 2 * zb + z0, np.pi - s0[1], s0[2])))[out]
     return res
+
+
+def point_semi_infinite(reff, mua, musp, x, y, depth, v=299792458000.0):
+    """Continuous-wave fluence of a unit pencil source entering a homogeneous
+    semi-infinite medium at the origin, at points (x, y) and `depth` below the
+    surface: the source moved to depth z0 = 1/(mua + mus') and its image at
+    -(z0 + 2 z_b), z_b = 2D(1+R)/(1-R), D = 1/(3(mua + mus')), as
+    matlab/sphdiffusionsemi.m builds them, each with the Green's function of
+    matlab/sphdiffincident.m (v/(4 pi D' d) exp(-mu_eff d), D' = v/(3 mus'))."""
+    D = 1.0 / (3.0 * (mua + musp))
+    zb = (1.0 + reff) / (1.0 - reff) * 2.0 * D
+    z0 = 1.0 / (musp + mua)
+    dout = v / (3.0 * musp)
+    mueff = np.sqrt(v * mua / dout)
+    r1 = np.sqrt(x * x + y * y + (depth - z0) ** 2)
+    r2 = np.sqrt(x * x + y * y + (depth + z0 + 2.0 * zb) ** 2)
+    return v / (4.0 * np.pi * dout) * (np.exp(-mueff * r1) / r1 - np.exp(-mueff * r2) / r2)

@@ -1,13 +1,19 @@
-"""Physics check against diffusion theory, the reference's own validation
-(examples/meshtest/README.txt, plotmmcsph.m): a 60 mm cube (mua 0.002,
-mus 1, g 0.01, n 1.37) with a 10 mm sphere (mua 0.05, mus 5, g 0.9) at its
-centre, pencil source at the centre of the z=0 face, no refractive mismatch at
+"""Physics checks against diffusion theory.
+
+The reference's own validation (examples/meshtest/README.txt, plotmmcsph.m):
+a 60 mm cube (mua 0.002, mus 1, g 0.01, n 1.37) with a 10 mm sphere (mua
+0.05, mus 5, g 0.9) at its centre, pencil source at the centre of the z=0 face, no refractive mismatch at
 the boundary (-b 0), 50 gates of 0.1 ns.  The time-integrated fluence on the
 plane through the source and the sphere centre must follow the analytic
 sphere-in-slab solution (oracle/sphdiffusion.py, pinned to the reference's
 sphdiffsemiinf.mat) where diffusion theory holds: at least 10 mm from the
 source, away from the sphere surface and from the cube's side faces (the
-analytic slab is laterally infinite)."""
+analytic slab is laterally infinite).
+
+A homogeneous semi-infinite medium: the benchmark's background medium (mua
+0.005, mus 1, g 0.01) in the same cube, against the closed-form pair of image
+sources (oracle/sphdiffusion.py point_semi_infinite) in the upper half of
+the cube, where its bottom face is far."""
 import os
 import sys
 
@@ -26,15 +32,15 @@ pytestmark = pytest.mark.gpu
 MEDIA = np.array([[0.0, 0.0, 1.0, 1.0], [0.002, 1.0, 0.01, 1.37], [0.05, 5.0, 0.9, 1.37]], np.float32)
 
 
-def mc_plane_fluence(xs, zs, photons, seed=7):
+def mc_plane_fluence(xs, zs, photons, seed=7, media=MEDIA):
     """Time-integrated nodal fluence of the MC engine at the points (x, 0, z)
     about the sphere centre: the mean over the nodes within 1 mm of the point.
     Nodal output, as the reference's validation uses: its element output
     divides the mua-scaled deposits by mua once more (src/mmc_mesh.c:2244-2256),
     which is exact only where mua is uniform."""
     from scipy.spatial import cKDTree
-    m = meshgen.inclusion_cube(n=60, jitter=0.0, media=MEDIA)
-    cfg = SimConfig(media=MEDIA, nphoton=photons, seed=seed, srcpos=(30.0, 30.0, 0.0), srcdir=(0.0, 0.0, 1.0),
+    m = meshgen.inclusion_cube(n=60, jitter=0.0, media=media)
+    cfg = SimConfig(media=media, nphoton=photons, seed=seed, srcpos=(30.0, 30.0, 0.0), srcdir=(0.0, 0.0, 1.0),
                     tend=5e-9, tstep=1e-10, basisorder=1, isreflect=0, outputtype="flux", isnormalized=1)
     r = simulate(Mesh(m.node, m.elem, m.label), cfg)
     cw = r.field.sum(0) * cfg.tstep
@@ -61,3 +67,21 @@ def test_fluence_follows_the_sphere_in_slab_diffusion_solution(gpu_ready):
               f"|log10| p50 {q[0]:.4f} p95 {q[1]:.4f} max {np.abs(lr[sel]).max():.4f}")
         assert abs(np.median(lr[sel])) < med_tol, name
         assert q[1] < p95_tol, name
+
+
+def test_fluence_follows_the_semi_infinite_diffusion_solution(gpu_ready):
+    homogeneous = MEDIA.copy()
+    homogeneous[2] = homogeneous[1] = [0.005, 1.0, 0.01, 1.37]
+    x, z = np.meshgrid(np.arange(-12.0, 12.1, 1.5), np.arange(-25.0, 0.1, 1.5), indexing="ij")
+    keep = np.hypot(x, z + 30.0) >= 10.0
+    xs, zs = x[keep], z[keep]
+    ana = sd.point_semi_infinite(0.0, 0.005, 0.99, xs, 0.0, zs + 30.0)
+    mc = mc_plane_fluence(xs, zs, 30_000_000, media=homogeneous)
+    lr = np.log10(mc / ana)
+    q = np.percentile(np.abs(lr), [50, 95])
+    print(f"semi-infinite: {lr.size} points, median log10(mc/ana) {np.median(lr):+.4f}, "
+          f"|log10| p50 {q[0]:.4f} p95 {q[1]:.4f} max {np.abs(lr).max():.4f}")
+    assert np.all(np.isfinite(lr))
+    # measured on a GB300 (3e7 photons): median +0.016, p95 0.026, max 0.039
+    assert abs(np.median(lr)) < 0.04
+    assert q[1] < 0.06

@@ -29,3 +29,15 @@ def test_homogeneous_sphere_reduces_to_the_point_source():
     y = np.zeros_like(x)
     phi = sd.infinite(x, y, z, cfg)
     np.testing.assert_allclose(phi, sd.incident(x, y, z, cfg), rtol=1e-8)
+
+
+def test_homogeneous_semi_infinite_closed_form():
+    """With a sphere of the background's properties the semi-infinite
+    solution is the closed-form pair of image sources."""
+    cfg = sd.SphereCfg(omua=0.005, omusp=0.99, imua=0.005, imusp=0.99)
+    x = np.array([0.0, 5.0, 10.0, 0.0, 8.0, 3.0])
+    z = np.array([-20.0, -15.0, -10.0, 0.0, -5.0, 12.0])
+    phi = sd.semi_infinite(0.0, x, np.zeros_like(x), z, cfg)
+    np.testing.assert_allclose(phi.real, sd.point_semi_infinite(0.0, 0.005, 0.99, x, 0.0, z + 30.0), rtol=1e-8)
+    # an index-mismatched boundary (R > 0) moves the image source away and raises the fluence
+    assert np.all(sd.point_semi_infinite(0.4, 0.005, 0.99, x, 0.0, z + 30.0) > phi.real)
