@@ -189,3 +189,26 @@ def test_mus_gradient_agrees_with_central_differences(scattering_groups):
     assert np.all(np.abs(an.mean(0) - fd.mean(0)) < 4 * se + 1e-3 * np.abs(fd.mean(0)))
     assert np.median(se) < 0.5 * np.abs(fd.mean(0)).max()
     assert np.corrcoef(an.mean(0), fd.mean(0))[0, 1] > 0.8
+
+
+@pytest.mark.parametrize("outputtype", ["wl", "wp", "jacobian", "wn"])
+def test_replay_outputs_match_oracle(oracle_mod, gpu_ready, outputtype):
+    """The replay deposits (the reference's -O L / P / J and the scatter-count
+    replay) against the oracle's replay of the same seeds, weights and times
+    (IEEE arithmetic): equal up to the order of the atomic additions."""
+    m = meshgen.inclusion_cube(n=12, jitter=0.4, seed=3)
+    mesh = Mesh(m.node, m.elem, m.label)
+    det = np.array([[40, 30, 0, 3], [45, 30, 0, 3]], np.float32)
+    cfg = SimConfig(media=m.media, nphoton=40000, seed=8, srcpos=(30.0, 30.0, 0.0), tend=5e-9, tstep=1e-9,
+                    issavedet=1, issaveseed=1, detpos=det, maxdetphoton=100000, basisorder=0, isnormalized=0,
+                    fast_math=0)
+    fwd = simulate(mesh, cfg)
+    assert fwd.detected > 50
+    s, w, t, idx = rp.replay_inputs(fwd.detp, fwd.seeds, np.asarray(cfg.media), 1, cfg.tstart, cfg.tend)
+    rcfg = dataclasses.replace(cfg, nphoton=len(idx), replayseed=s, replayweight=w, replaytime=t,
+                               outputtype=outputtype, photon_offset=0)
+    g = simulate(mesh, rcfg)
+    o = oracle_mod.run(m.node, m.elem, m.label, rcfg, nthreads=4, normalize=False)
+    assert g.field.sum() > 0
+    np.testing.assert_allclose(g.field, o["raw"], rtol=1e-8, atol=1e-12 * np.abs(o["raw"]).max())
+    assert g.raytet == o["raytet"]
