@@ -1009,7 +1009,9 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
         if (PHASED && !pa.last) {
             const SimDev& S = sims(0);
             const bool live = (L.mode == M_OUTER || L.mode == M_INNER || L.mode == M_FIXIN || L.mode == M_SCAT);
-            if (live && (L.ptime - S.tstart) * S.Rtstep >= (float)(pa.phase + pa.span)) {
+            // the window's end as a time, precomputed on the host: where a photon is parked
+            // changes only which launch continues it, not what it computes
+            if (live && L.ptime >= pa.tpark) {
                 cg::coalesced_group grp = cg::coalesced_threads();
                 unsigned long long base = 0;
                 if (grp.thread_rank() == 0) base = atomicAdd(pa.out.count, (unsigned long long)grp.size());
@@ -1360,6 +1362,7 @@ static cudaError_t launch_phased_t(const SimDev& sim, unsigned long long* work_c
         PhaseArgs pa;
         pa.phase = g;
         pa.span = span;
+        pa.tpark = sim.tstart + (float)(g + span) / sim.Rtstep;
         pa.last = (g + span >= sim.maxgate) ? 1 : 0;
         pa.in = q[(k + 1) & 1];  // written by the previous launch
         pa.out = q[k & 1];

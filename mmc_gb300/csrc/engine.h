@@ -159,6 +159,7 @@ struct PhaseArgs {
     unsigned* bcount;        // kBuckets photon counts of `out` by spatial key
     float lo[3];             // bounding box origin of the mesh
     float scale[3];          // grid cells per mm along each axis
+    float tpark;             // photons whose time reaches this (s) are parked for the next launch
 };
 
 // Bytes of queue storage per photon of a phased launch (both queues).
