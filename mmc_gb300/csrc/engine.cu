@@ -48,20 +48,16 @@ constexpr unsigned kLiveModes = (1u << M_OUTER) | (1u << M_INNER) | (1u << M_FIX
 constexpr unsigned kIdleModes = (1u << M_NEED) | (1u << M_DONE) | (1u << M_SCAT);
 
 // Scattering runs at the top of the trip after the step that ends inside an
-// element (roulette, then the scatter), ahead of that lane's next step.  The
-// scatter may be batched across lanes: a lane parks until kScatBatch lanes of
-// its warp are parked or one has waited kMaxWait trips.  Measured on GB300,
-// batching (8 lanes / 4 trips) was 4% slower than scattering at once, so the
-// batch size is 1.  Each photon performs the same operations in either case.
-constexpr int kScatBatch = 1;
-constexpr int kMaxWait = 4;
+// element (roulette, then the scatter), ahead of that lane's next step.
+// Batching it across lanes (a lane waiting until 8 lanes of its warp need a
+// scatter, or for 4 trips) measured 4% slower on GB300 than scattering at once.
 
 struct Lane {
     float px, py, pz, vx, vy, vz;
     float weight, ptime, slen, Lmove, slen0, oldw;
     unsigned oldidx;
     int eid, faceid, isend, hit, label, nbword;
-    int fixcount, mode, wait;
+    int fixcount, mode;
     unsigned steps;
     unsigned long long t0, t1;
     unsigned long long pid;  // photon index inside its simulation
@@ -947,7 +943,6 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                         L.faceid = 0;
                         L.isend = 0;
                         L.hit = 0;
-                        L.wait = 0;
                         if (S.issavedet)
                             for (int i = 0; i < S.reclen; i++) PP(i) = __ldcs(pa.in.ppath + qi * S.reclen + i);
                         if (want_seed) {
@@ -1055,50 +1050,43 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
         }
 
         // ---- (1b) deferred roulette + scatter, src/mmc_core.cl:2101-2134 ----
-        const unsigned parked = __ballot_sync(kFull, L.mode == M_SCAT);
-        if (parked) {
-            const bool fire = (__popc(parked) >= kScatBatch) ||
-                              __any_sync(kFull, L.mode == M_SCAT && L.wait >= kMaxWait);
+        if (__any_sync(kFull, L.mode == M_SCAT)) {
             if (L.mode == M_SCAT) {
-                if (!fire) {
-                    L.wait++;
+                const SimDev& S = sims(L.sim);
+                const float4* med = smed + (BATCHED ? L.sim * nmed_stride : 0);
+                bool killed = false;
+                if (S.roulette_on && (S.minenergy > 0.f) && (L.weight < S.minenergy)) {
+                    if (rng_next(L.t0, L.t1) * S.roulettesize <= 1.f)
+                        L.weight *= S.roulettesize;
+                    else
+                        killed = true;
+                }
+                if (killed) {
+                    if (SRC && S.traj) save_traj(S, L);
+                    if (S.photon_det) S.photon_det[L.pid] = 0;
+                    tally.eesc += L.weight;
+                    if (BATCHED) tally.raytet += L.steps; else atomicAdd(&s_cnt[0], (unsigned long long)L.steps);
+                    if (S.photon_weight) S.photon_weight[L.pid] = L.weight;
+                    if (S.photon_steps) S.photon_steps[L.pid] = L.steps;
+                    L.mode = M_NEED;
                 } else {
-                    const SimDev& S = sims(L.sim);
-                    const float4* med = smed + (BATCHED ? L.sim * nmed_stride : 0);
-                    bool killed = false;
-                    if (S.roulette_on && (S.minenergy > 0.f) && (L.weight < S.minenergy)) {
-                        if (rng_next(L.t0, L.t1) * S.roulettesize <= 1.f)
-                            L.weight *= S.roulettesize;
-                        else
-                            killed = true;
+                    if (REPLAY && S.replay && S.outputtype == OT_WN) {
+                        const float gf = __ldg(S.replaytime + L.pid) * S.Rtstep;
+                        int gate = (gf < (float)(S.maxgate - 1)) ? (int)gf : S.maxgate - 1;
+                        gate = max(gate, 0);
+                        deposit(S, (unsigned)(L.eid - 1) + (unsigned)(gate * S.ne), __ldg(S.replayweight + L.pid));
                     }
-                    if (killed) {
-                        if (SRC && S.traj) save_traj(S, L);
-                        if (S.photon_det) S.photon_det[L.pid] = 0;
-                        tally.eesc += L.weight;
-                        if (BATCHED) tally.raytet += L.steps; else atomicAdd(&s_cnt[0], (unsigned long long)L.steps);
-                        if (S.photon_weight) S.photon_weight[L.pid] = L.weight;
-                        if (S.photon_steps) S.photon_steps[L.pid] = L.steps;
-                        L.mode = M_NEED;
-                    } else {
-                        if (REPLAY && S.replay && S.outputtype == OT_WN) {
-                            const float gf = __ldg(S.replaytime + L.pid) * S.Rtstep;
-                            int gate = (gf < (float)(S.maxgate - 1)) ? (int)gf : S.maxgate - 1;
-                            gate = max(gate, 0);
-                            deposit(S, (unsigned)(L.eid - 1) + (unsigned)(gate * S.ne), __ldg(S.replayweight + L.pid));
-                        }
-                        float ctheta;
-                        const int tp = L.label;
-                        L.slen0 = next_scatter<MP>(L, med[tp].z, ctheta);
-                        L.slen = L.slen0;
-                        if (SRC && S.traj) save_traj(S, L);
-                        if (S.issavedet && tp > 0) {
-                            const int M = S.nmedia - 1;
-                            if (S.ismomentum) PP(2 * M + tp - 1) += (1.f - ctheta);
-                            PP(tp - 1) += 1.f;
-                        }
-                        L.mode = M_OUTER;
+                    float ctheta;
+                    const int tp = L.label;
+                    L.slen0 = next_scatter<MP>(L, med[tp].z, ctheta);
+                    L.slen = L.slen0;
+                    if (SRC && S.traj) save_traj(S, L);
+                    if (S.issavedet && tp > 0) {
+                        const int M = S.nmedia - 1;
+                        if (S.ismomentum) PP(2 * M + tp - 1) += (1.f - ctheta);
+                        PP(tp - 1) += 1.f;
                     }
+                    L.mode = M_OUTER;
                 }
             }
         }
@@ -1243,7 +1231,6 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                     ended = true;
                 } else {
                     L.mode = M_SCAT;  // roulette + scatter run batched at the top of a later trip
-                    L.wait = 0;
                 }
             } else if (ended) {
                 if (S.photon_det) S.photon_det[L.pid] = 0;
