@@ -998,9 +998,9 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                     } else {  // launch position in no element: counted, reported as an error
                         if (BATCHED) tally.outside++; else atomicAdd(&s_cnt[2], 1ull);
                         tally.eesc += L.weight;
-                        if (S.photon_det) S.photon_det[L.pid] = 0;
-                        if (S.photon_weight) S.photon_weight[L.pid] = L.weight;
-                        if (S.photon_steps) S.photon_steps[L.pid] = 0;
+                        if (SRC && S.photon_det) S.photon_det[L.pid] = 0;
+                        if (SRC && S.photon_weight) S.photon_weight[L.pid] = L.weight;
+                        if (SRC && S.photon_steps) S.photon_steps[L.pid] = 0;
                         L.mode = M_NEED;
                     }
                     }
@@ -1063,11 +1063,11 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                 }
                 if (killed) {
                     if (SRC && S.traj) save_traj(S, L);
-                    if (S.photon_det) S.photon_det[L.pid] = 0;
+                    if (SRC && S.photon_det) S.photon_det[L.pid] = 0;
                     tally.eesc += L.weight;
                     if (BATCHED) tally.raytet += L.steps; else atomicAdd(&s_cnt[0], (unsigned long long)L.steps);
-                    if (S.photon_weight) S.photon_weight[L.pid] = L.weight;
-                    if (S.photon_steps) S.photon_steps[L.pid] = L.steps;
+                    if (SRC && S.photon_weight) S.photon_weight[L.pid] = L.weight;
+                    if (SRC && S.photon_steps) S.photon_steps[L.pid] = L.steps;
                     L.mode = M_NEED;
                 } else {
                     if (REPLAY && S.replay && S.outputtype == OT_WN) {
@@ -1227,25 +1227,25 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                             }
                         }
                     }
-                    if (S.photon_det) S.photon_det[L.pid] = detid;
+                    if (SRC && S.photon_det) S.photon_det[L.pid] = detid;
                     ended = true;
                 } else {
                     L.mode = M_SCAT;  // roulette + scatter run batched at the top of a later trip
                 }
             } else if (ended) {
-                if (S.photon_det) S.photon_det[L.pid] = 0;
+                if (SRC && S.photon_det) S.photon_det[L.pid] = 0;
             }
         } else {
             ended = true;
             if (BATCHED) tally.aborted++; else atomicAdd(&s_cnt[1], 1ull);
-            if (S.photon_det) S.photon_det[L.pid] = 0;
+            if (SRC && S.photon_det) S.photon_det[L.pid] = 0;
         }
         if (ended) {
             if (SRC && S.traj) save_traj(S, L);
             tally.eesc += L.weight;
             if (BATCHED) tally.raytet += L.steps; else atomicAdd(&s_cnt[0], (unsigned long long)L.steps);
-            if (S.photon_weight) S.photon_weight[L.pid] = L.weight;
-            if (S.photon_steps) S.photon_steps[L.pid] = L.steps;
+            if (SRC && S.photon_weight) S.photon_weight[L.pid] = L.weight;
+            if (SRC && S.photon_steps) S.photon_steps[L.pid] = L.steps;
             L.mode = M_NEED;
         }
     }
@@ -1308,11 +1308,15 @@ size_t smem_bytes(int nmed_rows, int reclen_max, int threads, int want_seed) {
 
 // Kernels compiled with the general launch and deposit (SRC) serve
 // simulations whose source is not a pencil beam starting in a known element,
-// that deposit into a voxel grid or that record trajectories; the others
-// carry only the pencil launch and the element deposit, which keeps the step
-// loop's registers free.
+// that deposit into a voxel grid, record trajectories or write the per-photon
+// trace outputs; the others carry only the pencil launch and the element
+// deposit, which keeps the step loop's registers free (the trace outputs'
+// eleven null tests alone cost the pencil kernels 4.9%).
 #if MMCGB_ENGINE_FAST
-bool general_source(const SimDev& s) { return s.srctype != ST_PENCIL || s.e0 <= 0 || s.grid || s.traj; }
+bool general_source(const SimDev& s) {
+    return s.srctype != ST_PENCIL || s.e0 <= 0 || s.grid || s.traj || s.photon_weight || s.photon_steps ||
+           s.photon_det;
+}
 #endif
 
 #if MMCGB_ENGINE_FAST

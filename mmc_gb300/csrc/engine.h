@@ -186,7 +186,8 @@ cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, in
                            int fast_math, int general_src, int replay);
 LaunchShape default_shape(int device, bool batched);
 // Whether `s` needs the general kernels (a non-pencil source, a pencil without
-// a known initial element, dual-grid output or trajectory records).
+// a known initial element, dual-grid output, trajectory records or per-photon
+// trace outputs).
 bool general_source(const SimDev& s);
 
 // The launchers of each arithmetic policy: engine.cu is compiled once per

@@ -73,6 +73,30 @@ def test_detected_records_bitexact(gpu_ready, oracle_mod, small_inclusion, phase
         return sorted(map(bytes, np.concatenate([detp.view(np.uint8).reshape(len(detp), -1), seeds], 1)))
     assert rows(g.detp, g.seeds) == rows(o["detp"], o["seeds"])
     np.testing.assert_allclose(g.field, o["field"], rtol=1e-8)
+    # without the per-photon trace outputs the run takes the pencil-only kernels (the benchmark's):
+    # the same records, bit for bit
+    p = simulate(mesh, cfg)
+    assert p.raytet == o["raytet"] and rows(p.detp, p.seeds) == rows(o["detp"], o["seeds"])
+    np.testing.assert_allclose(p.field, o["field"], rtol=1e-8)
+
+
+@pytest.mark.parametrize("fast_math", [0, 1])
+@pytest.mark.parametrize("phased", [-1, 3])
+def test_pencil_kernels_equal_general_kernels(gpu_ready, small_inclusion, fast_math, phased):
+    """A pencil-beam run takes the pencil-only kernels unless it asks for the
+    per-photon trace outputs (or trajectories, grid output, other sources),
+    which the general kernels serve; both compute every photon the same way."""
+    m = small_inclusion
+    cfg = _cfg(m, nphoton=20000, tend=5e-9, tstep=0.5e-9, issavedet=1, issaveseed=1, detpos=meshgen.c1_detectors(),
+               maxdetphoton=100000, phased=phased, fast_math=fast_math, isnormalized=0)
+    mesh = Mesh(m.node, m.elem, m.label)
+    general = simulate(mesh, cfg, trace=True)
+    pencil = simulate(mesh, cfg)
+    rows = lambda r: sorted(map(bytes, np.concatenate([r.detp.view(np.uint8).reshape(len(r.detp), -1), r.seeds], 1)))  # noqa: E731
+    assert pencil.raytet == general.raytet and pencil.detected == general.detected > 0
+    assert rows(pencil) == rows(general)
+    np.testing.assert_allclose(pencil.field, general.field, rtol=1e-9, atol=1e-12)
+    assert pencil.energyesc == pytest.approx(general.energyesc, rel=1e-9)
 
 
 def test_node_output_and_normalization(gpu_ready, oracle_mod, small_cube):
