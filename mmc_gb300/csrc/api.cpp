@@ -305,7 +305,7 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     S.tend = c.tstart + c.tstep * (float)P.maxgate;
     S.Rtstep = 1.f / c.tstep;
     S.maxgate = P.maxgate;
-    S.roulette_on = ((S.tend - S.tstart) * S.Rtstep <= 1.f) ? 1 : 0;
+    S.roulette_on = ((S.tend - S.tstart) * S.Rtstep <= 1.f && c.minenergy > 0.f) ? 1 : 0;
     S.minenergy = c.minenergy;
     S.roulettesize = c.roulettesize;
     S.nout = c.nout;

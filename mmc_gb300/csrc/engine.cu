@@ -1055,7 +1055,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                 const SimDev& S = sims(L.sim);
                 const float4* med = smed + (BATCHED ? L.sim * nmed_stride : 0);
                 bool killed = false;
-                if (S.roulette_on && (S.minenergy > 0.f) && (L.weight < S.minenergy)) {
+                if (SRC && S.roulette_on && (L.weight < S.minenergy)) {
                     if (rng_next(L.t0, L.t1) * S.roulettesize <= 1.f)
                         L.weight *= S.roulettesize;
                     else
@@ -1083,7 +1083,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                     if (SRC && S.traj) save_traj(S, L);
                     if (S.issavedet && tp > 0) {
                         const int M = S.nmedia - 1;
-                        if (S.ismomentum) PP(2 * M + tp - 1) += (1.f - ctheta);
+                        if (SRC && S.ismomentum) PP(2 * M + tp - 1) += (1.f - ctheta);
                         PP(tp - 1) += 1.f;
                     }
                     L.mode = M_OUTER;
@@ -1308,14 +1308,15 @@ size_t smem_bytes(int nmed_rows, int reclen_max, int threads, int want_seed) {
 
 // Kernels compiled with the general launch and deposit (SRC) serve
 // simulations whose source is not a pencil beam starting in a known element,
-// that deposit into a voxel grid, record trajectories or write the per-photon
-// trace outputs; the others carry only the pencil launch and the element
-// deposit, which keeps the step loop's registers free (the trace outputs'
-// eleven null tests alone cost the pencil kernels 4.9%).
+// that deposit into a voxel grid, record trajectories, write the per-photon
+// trace outputs, play Russian roulette or save momentum transfer; the others
+// carry only the pencil launch and the element deposit, which keeps the step
+// loop lean (the trace outputs' eleven null tests alone cost the pencil
+// kernels 4.9%, the roulette and momentum tests 2%).
 #if MMCGB_ENGINE_FAST
 bool general_source(const SimDev& s) {
     return s.srctype != ST_PENCIL || s.e0 <= 0 || s.grid || s.traj || s.photon_weight || s.photon_steps ||
-           s.photon_det;
+           s.photon_det || s.roulette_on || s.ismomentum;
 }
 #endif
 

@@ -69,7 +69,7 @@ struct SimDev {
     // time gates
     float tstart, tend, Rtstep;
     int maxgate;
-    int roulette_on;       // (tend-tstart)*Rtstep <= 1, precomputed as the reference does
+    int roulette_on;       // minenergy > 0 and (tend-tstart)*Rtstep <= 1, as the reference tests it
     float minenergy, roulettesize, nout;
     // switches
     int isreflect, isspecular, voidtime;
@@ -186,8 +186,8 @@ cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, in
                            int fast_math, int general_src, int replay);
 LaunchShape default_shape(int device, bool batched);
 // Whether `s` needs the general kernels (a non-pencil source, a pencil without
-// a known initial element, dual-grid output, trajectory records or per-photon
-// trace outputs).
+// a known initial element, dual-grid output, trajectory records, per-photon
+// trace outputs, Russian roulette or momentum transfer).
 bool general_source(const SimDev& s);
 
 // The launchers of each arithmetic policy: engine.cu is compiled once per

@@ -152,7 +152,7 @@ extern "C" int32_t mmcgb_simulate_noalloc(mmcgb_mesh* mesh, const mmcgb_config* 
     S.tend = c->tstart + c->tstep * (float)maxgate;
     S.Rtstep = 1.f / c->tstep;
     S.maxgate = maxgate;
-    S.roulette_on = ((S.tend - S.tstart) * S.Rtstep <= 1.f) ? 1 : 0;
+    S.roulette_on = ((S.tend - S.tstart) * S.Rtstep <= 1.f && c->minenergy > 0.f) ? 1 : 0;
     S.minenergy = c->minenergy;
     S.roulettesize = c->roulettesize;
     S.nout = c->nout;
