@@ -766,7 +766,7 @@ int batch_launch(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets, c
         nmed_stride = std::max(nmed_stride, s->cfg.nmedia);
         if (s->cfg.issavedet) reclen_max = std::max(reclen_max, s->P.sim.reclen);
         if (s->cfg.issavedet && s->P.sim.seeds) want_seed = 1;
-        if (general_source(s->P.sim)) want_io = 1;
+        if (general_source(s->P.sim) || s->P.sim.roulette_on) want_io = 1;  // batched kernels: lean or general
         if (s->P.sim.replay) want_replay = 1;
         total += counts[i];
         cum[i] = total;
@@ -962,7 +962,7 @@ int32_t mmcgb_simulate_batch(int32_t n, mmcgb_mesh* const* meshes, const mmcgb_c
         nmed_stride = std::max(nmed_stride, cfgs[i].nmedia);
         if (cfgs[i].issavedet) reclen_max = std::max(reclen_max, P[i].sim.reclen);
         if (cfgs[i].issavedet && cfgs[i].issaveseed) want_seed = 1;
-        if (general_source(P[i].sim)) want_io = 1;
+        if (general_source(P[i].sim) || P[i].sim.roulette_on) want_io = 1;
         if (P[i].sim.replay) want_replay = 1;
         if ((cfgs[i].fast_math != 0) != (cfgs[0].fast_math != 0)) {
             rc = fail(MMCGB_E_ARG, "batched simulations must share fast_math");

@@ -47,6 +47,11 @@ constexpr unsigned kLiveModes = (1u << M_OUTER) | (1u << M_INNER) | (1u << M_FIX
 // modes that take no ray-tet step in the current trip
 constexpr unsigned kIdleModes = (1u << M_NEED) | (1u << M_DONE) | (1u << M_SCAT);
 
+// Kernel kinds: the lean pencil kernels, the pencil kernel with Russian roulette
+// (single-window runs with minenergy > 0), and the general kernels (every
+// source type, dual-grid output, trajectories, trace outputs, momentum).
+enum KernelKind : int { KIND_LEAN = 0, KIND_ROULETTE = 1, KIND_GENERAL = 2 };
+
 // Scattering runs at the top of the trip after the step that ends inside an
 // element (roulette, then the scatter), ahead of that lane's next step.
 // Batching it across lanes (a lane waiting until 8 lanes of its warp need a
@@ -841,10 +846,12 @@ struct ManySims {
 
 // Shared-memory layout: media[nsims_local * nmed_stride] | ppath[reclen_max][blockDim] |
 // seed0[2][blockDim] (u64)
-template <class MP, class Sims, bool BATCHED, bool PHASED, bool REPLAY, bool SRC>
+template <class MP, class Sims, bool BATCHED, bool PHASED, bool REPLAY, int KIND>
 __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned long long* cum, int nsims,
                                             unsigned long long total, int nmed_stride, int reclen_max,
                                             int want_seed, unsigned long long* work_counter, const PhaseArgs& pa) {
+    constexpr bool SRC = (KIND == KIND_GENERAL);  // general launch, grid deposits, trace/trajectory outputs
+    constexpr bool ROUL = (KIND != KIND_LEAN);    // Russian roulette
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float4* smed = reinterpret_cast<float4*>(smem_raw);
     const int nmed_rows = nsims * nmed_stride;
@@ -1055,7 +1062,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                 const SimDev& S = sims(L.sim);
                 const float4* med = smed + (BATCHED ? L.sim * nmed_stride : 0);
                 bool killed = false;
-                if (SRC && S.roulette_on && (L.weight < S.minenergy)) {
+                if (ROUL && S.roulette_on && (L.weight < S.minenergy)) {
                     if (rng_next(L.t0, L.t1) * S.roulettesize <= 1.f)
                         L.weight *= S.roulettesize;
                     else
@@ -1262,17 +1269,17 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
     }
 }
 
-template <class MP, bool REPLAY, bool SRC>
+template <class MP, bool REPLAY, int KIND>
 __global__ void __launch_bounds__(128, 8) photon_engine_plain(const __grid_constant__ SimDev sim,
                                                               unsigned long long* work_counter, int reclen_max,
                                                               int want_seed) {
     SingleSim acc{sim};
     const PhaseArgs none{};
-    engine_body<MP, SingleSim, false, false, REPLAY, SRC>(acc, nullptr, 1, sim.nphoton, sim.nmedia, reclen_max,
+    engine_body<MP, SingleSim, false, false, REPLAY, KIND>(acc, nullptr, 1, sim.nphoton, sim.nmedia, reclen_max,
                                                           want_seed, work_counter, none);
 }
 
-template <class MP, bool SRC>
+template <class MP, int KIND>
 __global__ void __launch_bounds__(128, 8) photon_engine_phased(const __grid_constant__ SimDev sim,
                                                                const __grid_constant__ PhaseArgs pa,
                                                                unsigned long long* work_counter, int reclen_max,
@@ -1281,11 +1288,11 @@ __global__ void __launch_bounds__(128, 8) photon_engine_phased(const __grid_cons
     // gate 0 launches the run's photons; later gates resume the ones parked by the previous launch
     unsigned long long total = sim.nphoton;
     if (pa.phase > 0) total = min(*pa.in.count, pa.cap);
-    engine_body<MP, SingleSim, false, true, false, SRC>(acc, nullptr, 1, total, sim.nmedia, reclen_max, want_seed,
+    engine_body<MP, SingleSim, false, true, false, KIND>(acc, nullptr, 1, total, sim.nmedia, reclen_max, want_seed,
                                                         work_counter, pa);
 }
 
-template <class MP, bool REPLAY, bool SRC>
+template <class MP, bool REPLAY, int KIND>
 __global__ void __launch_bounds__(128, 8) photon_engine_batched(const SimDev* __restrict__ sims,
                                                                 const unsigned long long* __restrict__ cum,
                                                                 int nsims, unsigned long long total,
@@ -1293,7 +1300,7 @@ __global__ void __launch_bounds__(128, 8) photon_engine_batched(const SimDev* __
                                                                 int reclen_max, int want_seed) {
     ManySims acc{sims};
     const PhaseArgs none{};
-    engine_body<MP, ManySims, true, false, REPLAY, SRC>(acc, cum, nsims, total, nmed_stride, reclen_max, want_seed,
+    engine_body<MP, ManySims, true, false, REPLAY, KIND>(acc, cum, nsims, total, nmed_stride, reclen_max, want_seed,
                                                       work_counter, none);
 }
 
@@ -1309,14 +1316,15 @@ size_t smem_bytes(int nmed_rows, int reclen_max, int threads, int want_seed) {
 // Kernels compiled with the general launch and deposit (SRC) serve
 // simulations whose source is not a pencil beam starting in a known element,
 // that deposit into a voxel grid, record trajectories, write the per-photon
-// trace outputs, play Russian roulette or save momentum transfer; the others
-// carry only the pencil launch and the element deposit, which keeps the step
-// loop lean (the trace outputs' eleven null tests alone cost the pencil
-// kernels 4.9%, the roulette and momentum tests 2%).
+// trace outputs or save momentum transfer; the others carry only the pencil
+// launch and the element deposit, which keeps the step loop lean (the trace
+// outputs' eleven null tests alone cost the pencil kernels 4.9%, the roulette
+// and momentum tests 2%).  Forward single-simulation runs with Russian
+// roulette have a pencil kernel of their own (KIND_ROULETTE).
 #if MMCGB_ENGINE_FAST
 bool general_source(const SimDev& s) {
     return s.srctype != ST_PENCIL || s.e0 <= 0 || s.grid || s.traj || s.photon_weight || s.photon_steps ||
-           s.photon_det || s.roulette_on || s.ismomentum;
+           s.photon_det || s.ismomentum;
 }
 #endif
 
@@ -1328,26 +1336,26 @@ using Policy = FastMath;
 using Policy = ExactMath;
 #endif
 
-template <class MP, bool REPLAY, bool SRC>
+template <class MP, bool REPLAY, int KIND>
 static cudaError_t launch_plain_t(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
                                   cudaStream_t stream) {
     const int want_seed = (sim.issavedet && sim.seeds) ? 1 : 0;
     const int reclen_max = sim.issavedet ? sim.reclen : 0;
     const size_t smem = smem_bytes(sim.nmedia, reclen_max, shape.threads, want_seed);
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(photon_engine_plain<MP, REPLAY, SRC>,
+        cudaError_t e = cudaFuncSetAttribute(photon_engine_plain<MP, REPLAY, KIND>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     (void)cudaGetLastError();  // the launch check below must see this launch's status only
-    photon_engine_plain<MP, REPLAY, SRC><<<shape.blocks, shape.threads, smem, stream>>>(sim, work_counter,
+    photon_engine_plain<MP, REPLAY, KIND><<<shape.blocks, shape.threads, smem, stream>>>(sim, work_counter,
                                                                                        reclen_max, want_seed);
     return cudaGetLastError();
 }
 
-template <class MP, bool SRC>
+template <class MP, int KIND>
 static cudaError_t launch_phased_t(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
                                    cudaStream_t stream, const PhaseQueue q[2], int span, unsigned* order,
                                    unsigned* bscratch, const float lo[3], const float hi[3]) {
@@ -1355,7 +1363,7 @@ static cudaError_t launch_phased_t(const SimDev& sim, unsigned long long* work_c
     const int reclen_max = sim.issavedet ? sim.reclen : 0;
     const size_t smem = smem_bytes(sim.nmedia, reclen_max, shape.threads, want_seed);
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(photon_engine_phased<MP, SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(photon_engine_phased<MP, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
     }
@@ -1380,7 +1388,7 @@ static cudaError_t launch_phased_t(const SimDev& sim, unsigned long long* work_c
         if (e == cudaSuccess) e = cudaMemsetAsync(bscratch, 0, sizeof(unsigned) * kBuckets, stream);
         if (e != cudaSuccess) return e;
         (void)cudaGetLastError();
-        photon_engine_phased<MP, SRC><<<shape.blocks, shape.threads, smem, stream>>>(sim, pa, work_counter,
+        photon_engine_phased<MP, KIND><<<shape.blocks, shape.threads, smem, stream>>>(sim, pa, work_counter,
                                                                                     reclen_max, want_seed);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if (!pa.last && order) {  // resume order of the photons just parked
@@ -1393,13 +1401,13 @@ static cudaError_t launch_phased_t(const SimDev& sim, unsigned long long* work_c
     return cudaSuccess;
 }
 
-template <class MP, bool REPLAY, bool SRC>
+template <class MP, bool REPLAY, int KIND>
 static cudaError_t launch_batched_t(const SimDev* sims, const unsigned long long* cum, int nsims,
                                     unsigned long long total, int nmed_stride, int reclen_max, int want_seed,
                                     unsigned long long* work_counter, LaunchShape shape, cudaStream_t stream) {
     const size_t smem = smem_bytes(nsims * nmed_stride, reclen_max, shape.threads, want_seed);
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(photon_engine_batched<MP, REPLAY, SRC>,
+        cudaError_t e = cudaFuncSetAttribute(photon_engine_batched<MP, REPLAY, KIND>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
@@ -1407,7 +1415,7 @@ static cudaError_t launch_batched_t(const SimDev* sims, const unsigned long long
     if (e != cudaSuccess) return e;
     (void)cudaGetLastError();  // the launch check below must see this launch's status only
     // a batch holding a replay simulation runs the kernel with the replay branches
-    photon_engine_batched<MP, REPLAY, SRC><<<shape.blocks, shape.threads, smem, stream>>>(
+    photon_engine_batched<MP, REPLAY, KIND><<<shape.blocks, shape.threads, smem, stream>>>(
         sims, cum, nsims, total, nmed_stride, work_counter, reclen_max, want_seed);
     return cudaGetLastError();
 }
@@ -1417,20 +1425,23 @@ namespace MMCGB_POLICY_NS {
 
 cudaError_t launch_plain(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
                          cudaStream_t stream) {
-    const bool src = general_source(sim);
+    // replays with roulette run in the general kernel (the roulette pencil kernel is forward-only)
+    const bool src = general_source(sim) || (sim.replay && sim.roulette_on);
     if (sim.replay)
-        return src ? launch_plain_t<Policy, true, true>(sim, work_counter, shape, stream)
-                   : launch_plain_t<Policy, true, false>(sim, work_counter, shape, stream);
-    return src ? launch_plain_t<Policy, false, true>(sim, work_counter, shape, stream)
-               : launch_plain_t<Policy, false, false>(sim, work_counter, shape, stream);
+        return src ? launch_plain_t<Policy, true, KIND_GENERAL>(sim, work_counter, shape, stream)
+                   : launch_plain_t<Policy, true, KIND_LEAN>(sim, work_counter, shape, stream);
+    if (src) return launch_plain_t<Policy, false, KIND_GENERAL>(sim, work_counter, shape, stream);
+    return sim.roulette_on ? launch_plain_t<Policy, false, KIND_ROULETTE>(sim, work_counter, shape, stream)
+                           : launch_plain_t<Policy, false, KIND_LEAN>(sim, work_counter, shape, stream);
 }
 
 cudaError_t launch_phased(const SimDev& sim, unsigned long long* work_counter, LaunchShape shape,
                           cudaStream_t stream, const PhaseQueue q[2], int span, unsigned* order,
                           unsigned* bscratch, const float lo[3], const float hi[3]) {
-    return general_source(sim)
-               ? launch_phased_t<Policy, true>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi)
-               : launch_phased_t<Policy, false>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi);
+    // roulette needs a single gate window, so phased runs never play it; checked all the same
+    return (general_source(sim) || sim.roulette_on)
+               ? launch_phased_t<Policy, KIND_GENERAL>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi)
+               : launch_phased_t<Policy, KIND_LEAN>(sim, work_counter, shape, stream, q, span, order, bscratch, lo, hi);
 }
 
 cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, int nsims,
@@ -1439,8 +1450,8 @@ cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, in
                            int general_src, int replay) {
 #define MMCGB_BATCHED(R, G) \
     launch_batched_t<Policy, R, G>(sims, cum, nsims, total, nmed_stride, reclen_max, want_seed, work_counter, shape, stream)
-    if (replay) return general_src ? MMCGB_BATCHED(true, true) : MMCGB_BATCHED(true, false);
-    return general_src ? MMCGB_BATCHED(false, true) : MMCGB_BATCHED(false, false);
+    if (replay) return general_src ? MMCGB_BATCHED(true, KIND_GENERAL) : MMCGB_BATCHED(true, KIND_LEAN);
+    return general_src ? MMCGB_BATCHED(false, KIND_GENERAL) : MMCGB_BATCHED(false, KIND_LEAN);
 #undef MMCGB_BATCHED
 }
 
@@ -1454,10 +1465,10 @@ LaunchShape default_shape(int device, bool batched) {
     int per_sm = 0;
     const int threads = 128;
     if (batched)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_batched<FastMath, true, false>, threads,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_batched<FastMath, true, KIND_LEAN>, threads,
                                                       4096);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_plain<FastMath, false, false>, threads,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, photon_engine_plain<FastMath, false, KIND_LEAN>, threads,
                                                       1024);
     if (per_sm < 1) per_sm = 1;
     return LaunchShape{sms * per_sm, threads};

@@ -187,7 +187,9 @@ cudaError_t launch_batched(const SimDev* sims, const unsigned long long* cum, in
 LaunchShape default_shape(int device, bool batched);
 // Whether `s` needs the general kernels (a non-pencil source, a pencil without
 // a known initial element, dual-grid output, trajectory records, per-photon
-// trace outputs, Russian roulette or momentum transfer).
+// trace outputs or momentum transfer).  Russian roulette (SimDev::roulette_on)
+// runs in a pencil kernel of its own for forward single-simulation launches and
+// in the general kernels otherwise.
 bool general_source(const SimDev& s);
 
 // The launchers of each arithmetic policy: engine.cu is compiled once per

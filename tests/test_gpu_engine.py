@@ -84,14 +84,18 @@ def test_detected_records_bitexact(gpu_ready, oracle_mod, small_inclusion, phase
 
 
 @pytest.mark.parametrize("fast_math", [0, 1])
-@pytest.mark.parametrize("phased", [-1, 3])
-def test_pencil_kernels_equal_general_kernels(gpu_ready, small_inclusion, fast_math, phased):
-    """A pencil-beam run takes the pencil-only kernels unless it asks for the
-    per-photon trace outputs (or trajectories, grid output, other sources),
-    which the general kernels serve; both compute every photon the same way."""
+@pytest.mark.parametrize("phased", [-1, 3, "roulette"])
+def test_pencil_kernels_equal_general_kernels(gpu_ready, oracle_mod, small_inclusion, fast_math, phased):
+    """A pencil-beam run takes the pencil-only kernels (with Russian roulette:
+    a single time window and minenergy > 0) unless it asks for the per-photon
+    trace outputs (or trajectories, grid output, other sources), which the
+    general kernels serve; both compute every photon the same way."""
     m = small_inclusion
-    cfg = _cfg(m, nphoton=20000, tend=5e-9, tstep=0.5e-9, issavedet=1, issaveseed=1, detpos=meshgen.c1_detectors(),
-               maxdetphoton=100000, phased=phased, fast_math=fast_math, isnormalized=0)
+    extra = dict(tstep=0.5e-9, phased=phased)
+    if phased == "roulette":  # one 5 ns window; photons below weight 0.3 play roulette
+        extra = dict(tstep=5e-9, minenergy=0.3, roulettesize=10.0, phased=-1)
+    cfg = _cfg(m, nphoton=20000, tend=5e-9, issavedet=1, issaveseed=1, detpos=meshgen.c1_detectors(),
+               maxdetphoton=100000, fast_math=fast_math, isnormalized=0, **extra)
     mesh = Mesh(m.node, m.elem, m.label)
     general = simulate(mesh, cfg, trace=True)
     pencil = simulate(mesh, cfg)
@@ -100,6 +104,10 @@ def test_pencil_kernels_equal_general_kernels(gpu_ready, small_inclusion, fast_m
     assert rows(pencil) == rows(general)
     np.testing.assert_allclose(pencil.field, general.field, rtol=1e-9, atol=1e-12)
     assert pencil.energyesc == pytest.approx(general.energyesc, rel=1e-9)
+    if phased == "roulette" and not fast_math:  # and the oracle's roulette, photon by photon
+        o = oracle_mod.run(m.node, m.elem, m.label, cfg, nthreads=4, trace=True)
+        assert np.array_equal(general.photon_weight.view(np.uint32), o["photon_weight"].view(np.uint32))
+        assert np.any(o["photon_weight"] == 0.0) or np.any(o["photon_weight"] < 0.3)
 
 
 def test_node_output_and_normalization(gpu_ready, oracle_mod, small_cube):
