@@ -141,7 +141,8 @@ typedef struct mmcgb_result {
     double* field;           /* maxgate*datalen, datalen = ne (basisorder 0) or nn */
     float* detp;             /* maxdetphoton*reclen detected-photon records */
     uint8_t* seeds;          /* maxdetphoton*16 */
-    float* photon_weight;    /* nphoton final weights (parity tracing), or NULL */
+    float* photon_weight;    /* nphoton final weights (parity tracing), or NULL; any of the three
+                                per-photon outputs selects the general kernels (same results) */
     uint32_t* photon_steps;  /* nphoton ray-tet tests per photon, or NULL */
     int32_t* photon_det;     /* nphoton detector ids (0 = none), or NULL */
     uint32_t detected;       /* detected photons (may exceed maxdetphoton) */

@@ -326,7 +326,9 @@ def _make_result(r: N.Result, arrs) -> SimResult:
 def simulate(mesh: Mesh, cfg: SimConfig, trace: bool = False, out: Optional[np.ndarray] = None) -> SimResult:
     """Runs one simulation on a resident mesh (mmcgb_simulate).  `out`: an
     optional preallocated (maxgate, datalen) float64 array for the field (for
-    example pinned host memory reused across calls)."""
+    example pinned host memory reused across calls).  `trace`: also return
+    each photon's final weight, ray-tet test count and detector; such runs
+    take the general kernels (the same results, a few percent slower)."""
     lib = N.load()
     c, keep = cfg.to_c()
     r, arrs = _alloc_result(mesh, cfg, trace, out)
