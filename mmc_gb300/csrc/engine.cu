@@ -1013,8 +1013,10 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                     }
                 }
             }
+            // a lane becomes M_DONE only here, so the warp can only have finished in a trip that
+            // handed out photons: testing here instead of every trip is 0.3% faster
+            if (__all_sync(kFull, L.mode == M_DONE)) break;
         }
-        if (__all_sync(kFull, L.mode == M_DONE)) break;
 
         // ---- (1a) gate-phased runs: park photons whose time reached the next gate ----
         if (PHASED && !pa.last) {
