@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define MMCGB_ABI_VERSION 3
+#define MMCGB_ABI_VERSION 4
 
 typedef enum mmcgb_status {
     MMCGB_OK = 0,
@@ -53,6 +53,7 @@ typedef enum mmcgb_output {
 } mmcgb_output;
 
 typedef struct mmcgb_mesh mmcgb_mesh; /* opaque, device-resident mesh */
+typedef struct mmcgb_device_out mmcgb_device_out; /* device buffers, defined below */
 
 /* Mesh input (tetmesh subset, src/mmc_mesh.h:87-122). */
 typedef struct mmcgb_mesh_desc {
@@ -134,6 +135,12 @@ typedef struct mmcgb_config {
     uint32_t maxjumpdebug;   /* > 0: save photon trajectories (the reference's -D M): a record at
                                 each launch, scattering event and photon end, at most this many,
                                 into mmcgb_result.traj */
+    int32_t accumulate;      /* 0: mmcgb_result.field and .dref are overwritten; 1: this run's
+                                deposits (scattered to the nodes for basisorder 1) are added to
+                                what the caller's arrays hold, and with isnormalized the sum is
+                                then normalized in place with this run's energies -- what
+                                mmc_run_cu does to cfg->exportfield / mesh->dref
+                                (src/mmc_cu_host.cu:916-976, normalization :984-1061) */
 } mmcgb_config;
 
 /* Outputs.  Pointers may be NULL to skip an output; counts are always set. */
@@ -233,6 +240,19 @@ int32_t mmcgb_session_sync(mmcgb_session* s, float* last_kernel_ms);
  * has finished.  Valid until mmcgb_session_end. */
 void* mmcgb_session_stream(mmcgb_session* s);
 int32_t mmcgb_session_end(mmcgb_session* s, mmcgb_result* res);
+/* Device addresses of a session's raw buffers (valid until
+ * mmcgb_session_end), for a caller that combines sessions on several GPUs
+ * before the output stage -- the reference's multi-device sum of fields,
+ * energies and counters and concatenation of detected records
+ * (src/mmc_cu_host.cu:772-783, :916-921), done here with device collectives:
+ *   field_raw  maxgate*datalen doubles (NULL for float32 accumulation)
+ *   energy     2 doubles: launched, escaped weight
+ *   counters   3 uint64: ray-tet tests, photons stopped by the step budget,
+ *              photons launched outside the mesh
+ *   detcount   1 uint32; detp maxdetphoton*reclen floats; seeds 16 bytes each
+ * Synchronize the session (mmcgb_session_sync) before touching them; what a
+ * caller leaves in them is what mmcgb_session_end reads back and normalizes. */
+int32_t mmcgb_session_device_buffers(mmcgb_session* s, mmcgb_device_out* out);
 
 /* `n` simulations sharing one persistent launch; meshes may differ.  Each
  * simulation's results land in its own mmcgb_result. */
@@ -258,10 +278,19 @@ int32_t mmcgb_run(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, int32_t 
  *     deposits, maxgate*ne doubles, gate-major (the layout of mmcgb_result.field
  *     for basisorder 0, isnormalized 0); energy[0] = launched weight, energy[1] =
  *     escaped weight; counters[0] = ray-tet tests,
- *     counters[1] = photons stopped by the step budget; detp/detcount/seeds as
- *     in mmcgb_result when issavedet (maxdetphoton*reclen floats, 16-byte seeds)
- *   - limits: nmedia <= MMCGB_NOALLOC_MAX_MEDIA, detnum <= MMCGB_NOALLOC_MAX_DET,
- *     accum_f64 = 1, no replay; anything else returns MMCGB_E_ARG
+ *     counters[1] = photons stopped by the step budget
+ *   - issavedet: detp holds maxdetphoton records of
+ *     reclen = (2 + ismomentum)*(nmedia - 1) + 6*issaveexit + 2 floats each
+ *     (detector id, scatter counts, partial paths, exit position/direction,
+ *     launch weight), seeds maxdetphoton*16 bytes when issaveseed.  *detcount
+ *     counts every detected photon and can exceed maxdetphoton; only the first
+ *     min(*detcount, maxdetphoton) records are written, so clamp before reading
+ *   - the configuration passes the checks of mmcgb_simulate first (a given e0
+ *     is used only if it encloses srcpos, otherwise the source is located);
+ *     then limits: point sources, element output, nmedia <=
+ *     MMCGB_NOALLOC_MAX_MEDIA, detnum <= MMCGB_NOALLOC_MAX_DET, accum_f64 = 1,
+ *     no replay, exiting weight or trajectories; anything else returns
+ *     MMCGB_E_ARG
  *   - the first call on a device looks up the array's device address; make it
  *     before any stream capture
  *   - all calls share the array and keep its last contents; the call clears the
@@ -269,14 +298,14 @@ int32_t mmcgb_run(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, int32_t 
  * The call returns after enqueueing; synchronize `stream` before reading. */
 #define MMCGB_NOALLOC_MAX_MEDIA 64
 #define MMCGB_NOALLOC_MAX_DET 256
-typedef struct mmcgb_device_out {
+struct mmcgb_device_out {
     double* field_raw;       /* device, maxgate*ne */
     float* detp;             /* device, maxdetphoton*reclen (issavedet) */
     uint8_t* seeds;          /* device, maxdetphoton*16 (issaveseed) */
     uint32_t* detcount;      /* device, 1 (issavedet) */
     double* energy;          /* device, 2 */
     uint64_t* counters;      /* device, 2 */
-} mmcgb_device_out;
+};
 int32_t mmcgb_simulate_noalloc(mmcgb_mesh* mesh, const mmcgb_config* cfg, const mmcgb_device_out* out,
                                void* stream);
 
@@ -294,6 +323,13 @@ int32_t mmcgb_prepare_host(const mmcgb_mesh_desc* desc, int32_t* elem, int32_t* 
  * raw: maxgate*ne; field: maxgate*datalen (datalen = nn if basisorder). */
 int32_t mmcgb_normalize_host(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, const double* raw,
                              double energytot, double energyesc, double* field, double* normalizer);
+
+/* Checks a configuration against a mesh on the host, with no GPU: the tests
+ * mmcgb_simulate makes before it allocates (the reference's mcx_validatecfg,
+ * src/mmc_utils.c:3500, plus the engine's own limits such as at most 2^31-1
+ * fluence cells of gates x elements, or voxels).  Writes the initial element
+ * the run would start in to *e0 when e0 is not NULL. */
+int32_t mmcgb_check_config(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, int32_t* e0);
 
 /* Fills `cfg` with the reference defaults (src/mmc_utils.c:207-363). */
 void mmcgb_config_defaults(mmcgb_config* cfg);

@@ -56,6 +56,7 @@ class Config(C.Structure):
         ("threads", C.c_int32), ("blocks", C.c_int32), ("fast_math", C.c_int32), ("phased", C.c_int32),
         ("srcparam1", C.c_float * 4), ("srcparam2", C.c_float * 4), ("focus", C.c_float), ("srcpattern", C.c_void_p),
         ("issaveref", C.c_int32), ("method", C.c_int32), ("gridstep", C.c_float), ("maxjumpdebug", C.c_uint32),
+        ("accumulate", C.c_int32),
     ]
 
 
@@ -71,13 +72,19 @@ class Result(C.Structure):
     ]
 
 
+class DeviceOut(C.Structure):
+    _fields_ = [("field_raw", C.c_void_p), ("detp", C.c_void_p), ("seeds", C.c_void_p),
+                ("detcount", C.c_void_p), ("energy", C.c_void_p), ("counters", C.c_void_p)]
+
+
 EXPORTS = [
     "mmcgb_abi_version", "mmcgb_last_error", "mmcgb_config_defaults", "mmcgb_mesh_create",
     "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export", "mmcgb_mesh_locate",
     "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run", "mmcgb_session_begin", "mmcgb_session_launch",
     "mmcgb_session_sync", "mmcgb_session_end", "mmcgb_prepare_host", "mmcgb_normalize_host",
     "mmcgb_session_launch_batch", "mmcgb_session_stream", "mmcgb_session_launch_batch_on",
-    "mmcgb_session_launch_repeat", "mmcgb_grid_info",
+    "mmcgb_session_launch_repeat", "mmcgb_grid_info", "mmcgb_check_config",
+    "mmcgb_session_device_buffers",
 ]
 
 
@@ -121,13 +128,15 @@ def load():
         lib.mmcgb_session_launch_batch_on.argtypes = [C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
                                                       C.POINTER(C.c_uint64), C.c_void_p]
         lib.mmcgb_session_launch_repeat.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32]
+        lib.mmcgb_session_device_buffers.argtypes = [C.c_void_p, C.POINTER(DeviceOut)]
+        lib.mmcgb_check_config.argtypes = [C.POINTER(MeshDesc), C.POINTER(Config), C.POINTER(C.c_int32)]
         lib.mmcgb_grid_info.argtypes = [C.c_void_p, C.c_float, C.POINTER(C.c_int32), C.POINTER(C.c_float)]
         for name in ("mmcgb_session_launch_batch", "mmcgb_session_launch_batch_on", "mmcgb_session_launch_repeat",
-                     "mmcgb_grid_info", "mmcgb_prepare_host", "mmcgb_normalize_host", "mmcgb_session_begin", "mmcgb_session_launch", "mmcgb_session_sync", "mmcgb_session_end",
+                     "mmcgb_grid_info", "mmcgb_check_config", "mmcgb_session_device_buffers", "mmcgb_prepare_host", "mmcgb_normalize_host", "mmcgb_session_begin", "mmcgb_session_launch", "mmcgb_session_sync", "mmcgb_session_end",
                      "mmcgb_mesh_create", "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export",
                      "mmcgb_mesh_locate", "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run"):
             getattr(lib, name).restype = C.c_int32
-        if lib.mmcgb_abi_version() != 3:
+        if lib.mmcgb_abi_version() != 4:
             raise NativeLibraryError("libmmcgb ABI version mismatch")
         _lib = lib
         return lib

@@ -105,15 +105,15 @@ size_t pattern_len(const mmcgb_config& c) {
     return 0;
 }
 
-int validate(const HostMesh& m, const mmcgb_config& c, std::string& err) {
+}  // namespace
+
+// The checks every simulation entry makes before it allocates anything
+// (declared in mesh.h; mmcgb_simulate_noalloc runs them too).
+int mmcgb::validate_config(const HostMesh& m, const mmcgb_config& c, std::string& err) {
     if (c.srctype < 0 || c.srctype > 17) { err = "srctype must be 0..17"; return MMCGB_E_ARG; }
     if (c.method != 0 && c.method != 1) { err = "method must be 0 (element output) or 1 (dual grid)"; return MMCGB_E_ARG; }
     if (c.method == 1 && c.replayseed) { err = "replay runs deposit on the elements (method 0)"; return MMCGB_E_ARG; }
     if (c.method == 1 && !(c.gridstep >= 0.f && std::isfinite(c.gridstep))) { err = "gridstep must be >= 0"; return MMCGB_E_ARG; }
-    if (c.method == 1 && frame_len(m, c) * (size_t)gates_of(c) > 0xFFFFFFFFull) {
-        err = "grid output exceeds 2^32 entries: use a larger gridstep";
-        return MMCGB_E_ARG;
-    }
     if ((c.srctype == 5 || c.srctype == 15) && (!c.srcpattern || pattern_len(c) == 0)) {
         err = "pattern sources need srcpattern and a positive pattern size in srcparam1/srcparam2";
         return MMCGB_E_ARG;
@@ -126,6 +126,13 @@ int validate(const HostMesh& m, const mmcgb_config& c, std::string& err) {
         if (!std::isfinite(c.srcparam1[k]) || !std::isfinite(c.srcparam2[k])) { err = "source parameters must be finite"; return MMCGB_E_ARG; }
     if (!(c.tstep > 0.f) || !(c.tend > c.tstart)) { err = "time gates need tstep > 0 and tend > tstart"; return MMCGB_E_ARG; }
     if (gates_of(c) < 1) { err = "time window holds no gate"; return MMCGB_E_ARG; }
+    // The engine addresses a fluence cell (gate, element or voxel) with a 32-bit index and keeps
+    // 0x7FFFFFFF as its "no pending deposit" mark, so every cell index must stay below it.
+    if (frame_len(m, c) * (size_t)gates_of(c) >= (size_t)kMaxFluenceCells) {
+        err = "fluence of " + std::to_string(frame_len(m, c)) + " cells x " + std::to_string(gates_of(c)) +
+              " gates exceeds the engine's 2^31-1 cells: use fewer gates" + (c.method == 1 ? " or a larger gridstep" : "");
+        return MMCGB_E_ARG;
+    }
     if (c.nmedia < 2 || c.nmedia > kMaxMedia || !c.media) { err = "media table needs 2..64 rows (row 0 = background)"; return MMCGB_E_ARG; }
     if (m.maxlabel > c.nmedia - 1) { err = "mesh label exceeds the number of media"; return MMCGB_E_ARG; }
     if (c.detnum < 0 || (c.detnum > 0 && !c.detpos)) { err = "detnum > 0 needs detpos"; return MMCGB_E_ARG; }
@@ -139,6 +146,33 @@ int validate(const HostMesh& m, const mmcgb_config& c, std::string& err) {
     if (!(std::fabs(vn - 1.f) < 1e-3f)) { err = "srcdir must be a unit vector"; return MMCGB_E_ARG; }
     return MMCGB_OK;
 }
+
+// Initial element: a given e0 is kept only if it encloses the source
+// (src/mmc_mesh.c:1325-1329), otherwise the source is located; 0 when no
+// element encloses it.
+int mmcgb::initial_element(const HostMesh& m, const mmcgb_config& c) {
+    int e0 = c.e0;
+    if (e0 > 0 && e0 <= m.ne) {
+        const float* p = c.srcpos;
+        const int* el = &m.elem[4 * (size_t)(e0 - 1)];
+        bool inside = true;
+        for (int i = 0; i < 4; i++) {
+            const float* a = &m.node[3 * (size_t)(el[kOut[i][0]] - 1)];
+            const float* b = &m.node[3 * (size_t)(el[kOut[i][1]] - 1)];
+            const float* cc = &m.node[3 * (size_t)(el[kOut[i][2]] - 1)];
+            const float ab[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+            const float ac[3] = {cc[0] - a[0], cc[1] - a[1], cc[2] - a[2]};
+            const float s[3] = {p[0] - a[0], p[1] - a[1], p[2] - a[2]};
+            const float n[3] = {ab[1] * ac[2] - ab[2] * ac[1], ab[2] * ac[0] - ab[0] * ac[2], ab[0] * ac[1] - ab[1] * ac[0]};
+            if (-(s[0] * n[0] + s[1] * n[1] + s[2] * n[2]) < 0.f) inside = false;
+        }
+        if (inside) return e0;
+    }
+    const int e = locate(m, c.srcpos);
+    return e > 0 ? e : 0;
+}
+
+namespace {
 
 // Device buffers of one simulation (stream-ordered allocations).
 struct SimBuffers {
@@ -188,32 +222,11 @@ struct Prepared {
 int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res, cudaStream_t stream, Prepared& P) {
     const HostMesh& m = mesh->host;
     std::string err;
-    int rc = validate(m, c, err);
+    int rc = validate_config(m, c, err);
     if (rc) return fail(rc, err);
-    // initial element: keep a given one only if it encloses the source
-    // (src/mmc_mesh.c:1325-1329), otherwise locate it
-    int e0 = c.e0;
-    if (e0 > 0 && e0 <= m.ne) {
-        const float* p = c.srcpos;
-        const int* el = &m.elem[4 * (size_t)(e0 - 1)];
-        bool inside = true;
-        for (int i = 0; i < 4; i++) {
-            const float* a = &m.node[3 * (size_t)(el[kOut[i][0]] - 1)];
-            const float* b = &m.node[3 * (size_t)(el[kOut[i][1]] - 1)];
-            const float* cc = &m.node[3 * (size_t)(el[kOut[i][2]] - 1)];
-            const float ab[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
-            const float ac[3] = {cc[0] - a[0], cc[1] - a[1], cc[2] - a[2]};
-            const float s[3] = {p[0] - a[0], p[1] - a[1], p[2] - a[2]};
-            const float n[3] = {ab[1] * ac[2] - ab[2] * ac[1], ab[2] * ac[0] - ab[0] * ac[2], ab[0] * ac[1] - ab[1] * ac[0]};
-            if (-(s[0] * n[0] + s[1] * n[1] + s[2] * n[2]) < 0.f) inside = false;
-        }
-        if (!inside) e0 = locate(m, c.srcpos);
-    } else {
-        e0 = locate(m, c.srcpos);
-    }
+    int e0 = initial_element(m, c);
     // point sources start in e0; the others are located per photon and may lie outside the mesh
     if (e0 <= 0 && point_source(c.srctype)) return fail(MMCGB_E_SOURCE, "initial element does not enclose the source");
-    if (e0 < 0) e0 = 0;
 
     P.maxgate = gates_of(c);
     const int M = c.nmedia - 1;
@@ -364,7 +377,32 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
     CK(cudaMemcpyAsync(counters, B.counters, sizeof(counters), cudaMemcpyDeviceToHost, stream));
     const size_t saved = std::min<size_t>(detected, c.issavedet ? c.maxdetphoton : 0);
     double normalizer = 1.0;
-    if (res->field) {
+    if (res->field && c.accumulate) {
+        // mmc_run_cu's semantics (src/mmc_cu_host.cu:916-976, :984-1061): this run's deposits
+        // (scattered to the nodes) are added to what the caller's field holds, then the sum is
+        // normalized in place with this run's energies.  Host output stage.
+        const int G = P.maxgate;
+        std::vector<double> raw(P.flen);
+        if (B.f64) {
+            CK(cudaMemcpyAsync(raw.data(), B.f64, sizeof(double) * P.flen, cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+        } else {
+            std::vector<float> ab(2 * P.flen);
+            CK(cudaMemcpyAsync(ab.data(), B.f32, sizeof(float) * 2 * P.flen, cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+            for (size_t i = 0; i < P.flen; i++) raw[i] = (double)ab[i] + (double)ab[P.flen + i];
+        }
+        if (c.method == 1) {
+            normalizer = grid_normalizer(c, energy[0]);
+            for (size_t i = 0; i < P.flen; i++) res->field[i] = (res->field[i] + raw[i]) * normalizer;
+        } else {
+            const size_t nout = (size_t)(c.basisorder ? mesh->host.nn : mesh->host.ne) * G;
+            std::vector<double> add(nout);
+            scatter_output(mesh->host, c, G, raw.data(), add.data());
+            for (size_t i = 0; i < nout; i++) res->field[i] += add[i];
+            normalizer = normalize_in_place(mesh->host, c, G, energy[0], energy[1], res->field);
+        }
+    } else if (res->field) {
         // output stage on the device, then one copy of the final field
         const size_t datalen = c.method == 1 ? frame_len(mesh->host, c)
                                              : (c.basisorder ? (size_t)mesh->host.nn : (size_t)mesh->host.ne);
@@ -415,7 +453,15 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
     }
     res->ntraj = ntraj;
     const size_t nref = (size_t)mesh->host.nf * P.maxgate;
-    if (res->dref && B.dref) CK(cudaMemcpyAsync(res->dref, B.dref, sizeof(double) * nref, cudaMemcpyDeviceToHost, stream));
+    std::vector<double> dref_run;
+    if (res->dref && B.dref) {
+        double* dst = res->dref;
+        if (c.accumulate) {
+            dref_run.resize(nref);
+            dst = dref_run.data();
+        }
+        CK(cudaMemcpyAsync(dst, B.dref, sizeof(double) * nref, cudaMemcpyDeviceToHost, stream));
+    }
     B.release();
     CK(cudaStreamSynchronize(stream));
     res->detected = detected;
@@ -429,7 +475,9 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
     res->aborted = counters[1];
     res->outside = counters[2];
     res->normalizer = normalizer;
-    if (res->dref && B.dref == nullptr && nref) std::memset(res->dref, 0, sizeof(double) * nref);
+    if (!dref_run.empty())  // mesh->dref += dref (src/mmc_cu_host.cu:978-982)
+        for (size_t i = 0; i < nref; i++) res->dref[i] += dref_run[i];
+    if (res->dref && B.dref == nullptr && nref && !c.accumulate) std::memset(res->dref, 0, sizeof(double) * nref);
     if (res->dref && c.isnormalized && energy[0] > 0) {  // src/mmc_mesh.c:2160-2167
         const float normalizor = 1.f / (float)energy[0];
         for (size_t i = 0; i < nref; i++) res->dref[i] *= normalizor;
@@ -895,6 +943,18 @@ int32_t mmcgb_session_launch_repeat(mmcgb_session* s, uint64_t photon_offset, ui
 
 void* mmcgb_session_stream(mmcgb_session* s) { return s ? (void*)s->stream : nullptr; }
 
+int32_t mmcgb_session_device_buffers(mmcgb_session* s, mmcgb_device_out* out) {
+    if (!s || !out) return fail(MMCGB_E_ARG, "null argument");
+    const SimBuffers& B = s->P.buf;
+    out->field_raw = B.f64;
+    out->detp = B.detp;
+    out->seeds = reinterpret_cast<uint8_t*>(B.seeds);
+    out->detcount = B.detcount;
+    out->energy = B.energy;
+    out->counters = reinterpret_cast<uint64_t*>(B.counters);
+    return MMCGB_OK;
+}
+
 int32_t mmcgb_session_sync(mmcgb_session* s, float* last_kernel_ms) {
     if (!s) return fail(MMCGB_E_ARG, "null session");
     CK(cudaSetDevice(s->mesh->device));
@@ -1034,6 +1094,20 @@ int32_t mmcgb_prepare_host(const mmcgb_mesh_desc* desc, int32_t* elem, int32_t* 
     return MMCGB_OK;
 }
 
+int32_t mmcgb_check_config(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, int32_t* e0) {
+    if (!desc || !cfg) return fail(MMCGB_E_ARG, "null argument");
+    HostMesh h;
+    std::string err;
+    int rc = prepare_mesh(*desc, h, err);
+    if (rc) return fail(rc, err);
+    rc = validate_config(h, *cfg, err);
+    if (rc) return fail(rc, err);
+    const int e = initial_element(h, *cfg);
+    if (e <= 0 && point_source(cfg->srctype)) return fail(MMCGB_E_SOURCE, "initial element does not enclose the source");
+    if (e0) *e0 = e;
+    return MMCGB_OK;
+}
+
 int32_t mmcgb_normalize_host(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, const double* raw,
                              double energytot, double energyesc, double* field, double* normalizer) {
     if (!desc || !cfg || !raw || !field) return fail(MMCGB_E_ARG, "null argument");
@@ -1045,16 +1119,7 @@ int32_t mmcgb_normalize_host(const mmcgb_mesh_desc* desc, const mmcgb_config* cf
     if (!(cfg->tstep > 0.f)) return fail(MMCGB_E_ARG, "tstep must be positive");
     if (cfg->method == 1) {  // dual-grid output: one scale factor, src/mmc_mesh.c:2204-2206
         const size_t n = frame_len(h, *cfg) * gates_of(*cfg);
-        double norm = 1.0;
-        const float Et = (float)energytot;
-        if (cfg->isnormalized) {
-            if (cfg->outputtype == MMCGB_OUT_ENERGY) {
-                norm = 1.f / Et;
-            } else {
-                norm = 1.0 / (Et * cfg->unitinmm * cfg->unitinmm * cfg->unitinmm);
-                if (cfg->outputtype == MMCGB_OUT_FLUX) norm /= cfg->tstep;
-            }
-        }
+        const double norm = grid_normalizer(*cfg, energytot);
         for (size_t i = 0; i < n; i++) field[i] = raw[i] * norm;
         if (normalizer) *normalizer = norm;
         return MMCGB_OK;

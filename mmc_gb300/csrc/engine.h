@@ -19,6 +19,9 @@ constexpr int kMaxMedia = 64;        // media rows (incl. background) staged in 
 constexpr int kMaxSimsShared = 256;  // simulations whose media tables fit in one block's shared memory
 constexpr int kNbBits = 24;          // neighbour id bits in a packed face word
 constexpr int kMaxElem = (1 << (kNbBits - 1)) - 1;
+// Fluence cells (gates x elements or voxels) one simulation may hold: deposit indices are
+// 32-bit and 0x7FFFFFFF marks "no pending deposit", so every index stays below it.
+constexpr unsigned kMaxFluenceCells = 0x7FFFFFFFu;
 
 // One tetrahedron as the step kernel reads it: 80 bytes, 16-byte aligned.
 //   nx/ny/nz/nd : outward unit normals and plane offsets of the 4 faces

@@ -39,9 +39,24 @@ void pack_records(const HostMesh& m, std::vector<TetRec>& rec);
 void build_locator(HostMesh& m);
 int locate(const HostMesh& m, const float p[3]);
 
+// The configuration checks every simulation entry makes before it allocates
+// (api.cpp); MMCGB_E_* status, message in `err`.
+int validate_config(const HostMesh& m, const mmcgb_config& c, std::string& err);
+// Initial element of a simulation: a given e0 if it encloses srcpos, else the
+// located element; 0 when no element encloses the source.
+int initial_element(const HostMesh& m, const mmcgb_config& c);
+
 // Output stage (elem->node scatter, surface nodal-volume fix, normalization);
 // returns the normalization factor.  `raw` holds maxgate*ne element deposits.
 double normalize_output(const HostMesh& m, const mmcgb_config& cfg, int maxgate, const double* raw,
                         double energytot, double energyesc, double* field);
+// Its two halves: the elem->node scatter (a copy for element output) of `raw`
+// into `field`, and the normalization of a scattered field in place (returns
+// the factor; 1 when cfg.isnormalized is 0).
+void scatter_output(const HostMesh& m, const mmcgb_config& cfg, int maxgate, const double* raw, double* field);
+double normalize_in_place(const HostMesh& m, const mmcgb_config& cfg, int maxgate, double energytot,
+                          double energyesc, double* field);
+// The single scale factor of the dual-grid output.
+double grid_normalizer(const mmcgb_config& cfg, double energytot);
 
 }  // namespace mmcgb

@@ -21,8 +21,9 @@
 //    work overlaps on the GPU -- on different streams, or on one stream from
 //    several host threads without ordering -- race on the array.
 //  * Limits: at most kNoAllocMaxMedia media rows and kNoAllocMaxDet detectors;
-//    float64 accumulation only; no replay and no per-photon trace.  Larger
-//    requests are rejected with MMCGB_E_ARG.
+//    point sources, element output, float64 accumulation only; no replay, no
+//    per-photon trace, exiting weight or trajectories.  Anything else is
+//    rejected with MMCGB_E_ARG, after the checks mmcgb_simulate makes.
 //  * Nothing here calls cudaMalloc, cudaFree or an allocating library routine.
 #include <cuda_runtime.h>
 
@@ -58,6 +59,9 @@ int fail(int code, const std::string& msg) {
     return code;
 }
 
+// Source types whose photons all start at srcpos in the initial element.
+bool point_source(int t) { return t == 0 || t == 1 || t == 2 || t == 7; }
+
 // Device address of the scratch array on `device` (which must be current).
 int scratch_address(int device, unsigned char** out) {
     if (device < 0 || device >= kMaxDevices) return fail(MMCGB_E_ARG, "device index out of range");
@@ -79,35 +83,39 @@ extern "C" int32_t mmcgb_simulate_noalloc(mmcgb_mesh* mesh, const mmcgb_config* 
     using namespace mmcgb;
     if (!mesh || !c || !out) return fail(MMCGB_E_ARG, "null argument");
     if (!out->field_raw || !out->energy || !out->counters) return fail(MMCGB_E_ARG, "field_raw, energy and counters are required");
-    if (!(c->srctype == 0 || c->srctype == 1 || c->srctype == 2 || c->srctype == 7))
+    const HostMesh& m = mesh->host;
+    // the checks of the allocating entries first (time gates, media values, unit direction,
+    // fluence cell count), then the limits of this entry
+    std::string err;
+    int rc = validate_config(m, *c, err);
+    if (rc) return fail(rc, err);
+    if (!point_source(c->srctype))
         return fail(MMCGB_E_ARG, "no-alloc entry: point sources only (pencil, isotropic, cone, arcsine)");
-    if (!(c->tstep > 0.f) || !(c->tend > c->tstart)) return fail(MMCGB_E_ARG, "time gates need tstep > 0 and tend > tstart");
-    if (c->nmedia < 2 || !c->media) return fail(MMCGB_E_ARG, "media table needs at least 2 rows");
     if (c->nmedia > kNoAllocMaxMedia)
         return fail(MMCGB_E_ARG, "no-alloc entry: nmedia " + std::to_string(c->nmedia) + " exceeds the maximum " +
                                      std::to_string(kNoAllocMaxMedia));
-    if (c->detnum < 0 || c->detnum > kNoAllocMaxDet || (c->detnum > 0 && !c->detpos))
-        return fail(MMCGB_E_ARG, "no-alloc entry: detnum must be 0.." + std::to_string(kNoAllocMaxDet));
+    if (c->detnum > kNoAllocMaxDet)
+        return fail(MMCGB_E_ARG, "no-alloc entry: detnum " + std::to_string(c->detnum) + " exceeds the maximum " +
+                                     std::to_string(kNoAllocMaxDet));
     if (!c->accum_f64) return fail(MMCGB_E_ARG, "no-alloc entry accumulates in float64 only");
     if (c->replayseed) return fail(MMCGB_E_ARG, "no-alloc entry does not replay");
     if (c->method != 0) return fail(MMCGB_E_ARG, "no-alloc entry deposits on the elements (method 0)");
-    if (mesh->host.maxlabel > c->nmedia - 1) return fail(MMCGB_E_ARG, "mesh label exceeds the number of media");
-    if (c->issavedet && (!out->detp || !out->detcount || c->maxdetphoton == 0))
-        return fail(MMCGB_E_ARG, "issavedet needs detp, detcount and maxdetphoton");
+    if (c->issaveref || c->maxjumpdebug) return fail(MMCGB_E_ARG, "no-alloc entry has no exiting-weight or trajectory output");
+    if (c->issavedet && (!out->detp || !out->detcount))
+        return fail(MMCGB_E_ARG, "issavedet needs detp and detcount");
     if (c->issavedet && c->issaveseed && !out->seeds) return fail(MMCGB_E_ARG, "issaveseed needs seeds");
-    const HostMesh& m = mesh->host;
-    int e0 = (c->e0 > 0 && c->e0 <= m.ne) ? c->e0 : locate(m, c->srcpos);
-    if (e0 <= 0) return fail(MMCGB_E_SOURCE, "initial element does not enclose the source");
+    // a given e0 is used only when it encloses the source, as in mmcgb_simulate
+    const int e0 = initial_element(m, *c);
+    if (e0 <= 0) return fail(MMCGB_E_SOURCE, "no element encloses the source");
 
     cudaError_t e = cudaSetDevice(mesh->device);
     if (e != cudaSuccess) return fail(MMCGB_E_CUDA, cudaGetErrorString(e));
     unsigned char* scratch = nullptr;
-    int rc = scratch_address(mesh->device, &scratch);
+    rc = scratch_address(mesh->device, &scratch);
     if (rc) return rc;
     cudaStream_t stream = static_cast<cudaStream_t>(stream_handle);
 
     const int maxgate = (int)((c->tend - c->tstart) / c->tstep + 0.5f);
-    if (maxgate < 1) return fail(MMCGB_E_ARG, "time window holds no gate");
     const int M = c->nmedia - 1;
     const int reclen = (2 + (c->ismomentum > 0)) * M + (c->issaveexit > 0) * 6 + 1;
     const size_t flen = (size_t)m.ne * maxgate;

@@ -60,3 +60,56 @@ def test_oversized_mesh_rejected_before_any_gpu_work():
     d.ne = 9_000_000  # beyond the 24-bit neighbour field of the packed records
     rc = _native.load().mmcgb_prepare_host(d, None, None, None, None, None, None)
     assert rc == 3
+
+
+def test_fluence_beyond_the_32bit_cell_index_rejected_before_any_gpu_work():
+    """Gates x elements must stay below 2^31-1 cells (the engine's deposit index is
+    32-bit); such a run fails with MMCGB_E_ARG at the host check, before any
+    allocation, for element and dual-grid output alike."""
+    import ctypes as C
+    from mmc_gb300 import _native
+    from mmc_gb300.core import SimConfig
+    lib = _native.load()
+    m = meshgen.homogeneous_cube(n=4)  # 384 tets
+    d, keep = core._desc(m.node, m.elem, m.label)
+    ok = SimConfig(media=m.media, srcpos=(30.0, 30.0, 0.0), tend=5e-9, tstep=1e-9)
+    c, k1 = ok.to_c()
+    e0 = C.c_int32(-1)
+    assert lib.mmcgb_check_config(d, C.byref(c), C.byref(e0)) == 0, lib.mmcgb_last_error()
+    assert 1 <= e0.value <= m.ne
+    gates = (2**31 - 1) // m.ne + 1  # one gate more than the index reaches
+    big = SimConfig(media=m.media, srcpos=(30.0, 30.0, 0.0), tstart=0.0, tstep=1e-12, tend=gates * 1e-12)
+    assert big.maxgate * m.ne >= 2**31 - 1
+    c2, k2 = big.to_c()
+    assert lib.mmcgb_check_config(d, C.byref(c2), None) == 1
+    assert "2^31-1" in lib.mmcgb_last_error().decode()
+    fits = SimConfig(media=m.media, srcpos=(30.0, 30.0, 0.0), tstart=0.0, tstep=1e-12, tend=(gates - 2) * 1e-12)
+    assert fits.maxgate * m.ne < 2**31 - 1
+    c3, k3 = fits.to_c()
+    assert lib.mmcgb_check_config(d, C.byref(c3), None) == 0, lib.mmcgb_last_error()
+    grid = SimConfig(media=m.media, srcpos=(30.0, 30.0, 0.0), tstep=1e-9, tend=40e-9, method="grid", gridstep=0.05)
+    c4, k4 = grid.to_c()  # 1201^3 voxels x 40 gates
+    assert lib.mmcgb_check_config(d, C.byref(c4), None) == 1
+    assert "gridstep" in lib.mmcgb_last_error().decode()
+
+
+def test_host_check_reports_the_initial_element():
+    """A given e0 is kept only when it encloses the source; otherwise the source
+    is located (src/mmc_mesh.c:1325-1329)."""
+    import ctypes as C
+    from mmc_gb300 import _native
+    from mmc_gb300.core import SimConfig
+    lib = _native.load()
+    m = meshgen.homogeneous_cube(n=4)
+    d, keep = core._desc(m.node, m.elem, m.label)
+    cfg = SimConfig(media=m.media, srcpos=(30.0, 30.0, 0.0), tend=5e-9, tstep=1e-9)
+    c, k1 = cfg.to_c()
+    e = C.c_int32(0)
+    assert lib.mmcgb_check_config(d, C.byref(c), C.byref(e)) == 0
+    located = e.value
+    assert located >= 1
+    c.e0 = m.ne if located != m.ne else 1  # an element that does not hold the source
+    assert lib.mmcgb_check_config(d, C.byref(c), C.byref(e)) == 0
+    assert e.value == located
+    c.srcpos = (C.c_float * 3)(100.0, 30.0, 0.0)  # outside the mesh: a pencil cannot start
+    assert lib.mmcgb_check_config(d, C.byref(c), C.byref(e)) == 4
