@@ -90,3 +90,27 @@ def test_oracle_detects_a_planted_error(oracle_mod):
     r = oracle_mod.run(m.node, m.elem, m.label, dataclasses.replace(cfg, media=media), nthreads=NTHREADS,
                        normalize=False)
     assert gc.check_field(r["raw"], fx, m.media, m.label, cfg.nphoton)
+
+
+@pytest.mark.parametrize("name", ["c0_cube162k", "c1_incl1296k"])
+def test_oracle_matches_reference_runs_on_the_benchmark_workloads(oracle_mod, name):
+    """The two benchmark workloads themselves (162k-tet cube; 1.296M-tet
+    inclusion cube with 50 gates and 4 detectors), 1e6 photons, against 10
+    reference runs each; on the cube also the node output (the CUDA host's
+    scatter and the reference's mesh_normalize, pinned by the fixture)."""
+    import numpy as np
+    m, cfg, fx = gc.case_mesh_and_config(name)
+    r = oracle_mod.run(m.node, m.elem, m.label, cfg, nthreads=NTHREADS, normalize=False)
+    msgs = gc.check_field(r["raw"], fx, m.media, m.label, cfg.nphoton)
+    msgs += gc.check_tests_per_photon(r["raytet"] / cfg.nphoton, fx)
+    if cfg.issavedet:
+        msgs += gc.check_detectors(r["detp"], m.media, fx)
+    if "node_mean" in fx:
+        # node output with the absorbed weight the reference CPU engine tallies (its deposits x mua)
+        ncfg = dataclasses.replace(cfg, basisorder=1, isnormalized=1)
+        e_dep = float((r["raw"].sum(0) * m.media[m.label, 0].astype(np.float64)).sum())
+        node, _ = oracle_mod.normalize(m.node, m.elem, m.label, ncfg, r["raw"], float(cfg.nphoton),
+                                       float(cfg.nphoton) - e_dep)
+        msgs += gc.check_nodes(node[0], fx)
+    assert r["aborted"] == 0
+    assert not msgs, "\n".join(msgs)
