@@ -76,7 +76,7 @@ def replay(mesh: Mesh, cfg: SimConfig, detp: np.ndarray, seeds: np.ndarray, outp
         w = np.asarray(weight, np.float32)[idx] if len(weight) == len(detp) else np.asarray(weight, np.float32)
     rcfg = dataclasses.replace(cfg, nphoton=len(idx), replayseed=s, replayweight=w, replaytime=t,
                                outputtype=outputtype, isnormalized=1 if normalize else 0, basisorder=0,
-                               photon_offset=0)
+                               photon_offset=0, save_field=True)
     return simulate(mesh, rcfg), idx
 
 
@@ -89,8 +89,9 @@ def jacobians(mesh: Mesh, cfg: SimConfig, detp: np.ndarray, seeds: np.ndarray, r
         w = w * np.asarray(coef, np.float64)
     # both replays (path lengths and scatter counts) share one batched launch
     s, _, t, idx = replay_inputs(detp, seeds, np.asarray(cfg.media), replaydet, cfg.tstart, cfg.tend, cfg.unitinmm)
+    # the replays always return their deposits, whatever the forward configuration saved
     base = dataclasses.replace(cfg, nphoton=len(idx), replayseed=s, replayweight=w[idx].astype(np.float32),
-                               replaytime=t, isnormalized=0, basisorder=0, photon_offset=0)
+                               replaytime=t, isnormalized=0, basisorder=0, photon_offset=0, save_field=True)
     wl, wn = simulate_batch([mesh, mesh], [dataclasses.replace(base, outputtype="wl"),
                                            dataclasses.replace(base, outputtype="wn")])
     mus = np.asarray(cfg.media, np.float64)[mesh.label, 1]

@@ -11,6 +11,10 @@
  *                      the detected-photon table in cfg.exportdetected (the
  *                      reference's standalone .mch/.jdt writers take the column
  *                      count from cfg.his, which the CPU path leaves at 0)
+ *   MMCGB_SEED_OUT=f   after the run (with -q 1): int32 count, int32 seedbyte,
+ *                      then count*seedbyte bytes -- the RNG states the detected
+ *                      photons started from, cfg.exportseed (src/mmc_host.c:405-409),
+ *                      which replay (-E file.mch) reads back
  *   MMCGB_NORM_IN=f    instead of simulating: read double Eabsorb, double
  *   MMCGB_NORM_OUT=g   Etotal, double raw[maxgate*ne] element deposits; scatter
  *                      them to the nodes when basisorder=1 as the CUDA host does
@@ -75,6 +79,7 @@ int main(int argc, char** argv) {
     tetmesh mesh;
     raytracer tracer;
     const char* detp_out = getenv("MMCGB_DETP_OUT");
+    const char* seed_out = getenv("MMCGB_SEED_OUT");
     const char* mesh_out = getenv("MMCGB_MESH_OUT");
     const char* norm_in = getenv("MMCGB_NORM_IN");
     const char* norm_out = getenv("MMCGB_NORM_OUT");
@@ -95,6 +100,16 @@ int main(int argc, char** argv) {
         fwrite(&count, sizeof(int), 1, f);
         fwrite(&cols, sizeof(int), 1, f);
         if (count > 0 && cfg.exportdetected) fwrite(cfg.exportdetected, sizeof(float), (size_t)count * cols, f);
+        fclose(f);
+    }
+    if (seed_out && cfg.issavedet && cfg.issaveseed) {
+        int count = (int)cfg.detectedcount;
+        int seedbyte = (int)(sizeof(RandType) * RAND_BUF_LEN);
+        FILE* f = fopen(seed_out, "wb");
+        if (!f) return 3;
+        fwrite(&count, sizeof(int), 1, f);
+        fwrite(&seedbyte, sizeof(int), 1, f);
+        if (count > 0 && cfg.exportseed) fwrite(cfg.exportseed, 1, (size_t)count * seedbyte, f);
         fclose(f);
     }
     mmc_cleanup(&cfg, &mesh, &tracer);

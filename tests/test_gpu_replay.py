@@ -212,3 +212,79 @@ def test_replay_outputs_match_oracle(oracle_mod, gpu_ready, outputtype):
     assert g.field.sum() > 0
     np.testing.assert_allclose(g.field, o["raw"], rtol=1e-8, atol=1e-12 * np.abs(o["raw"]).max())
     assert g.raytet == o["raytet"]
+
+
+# ---- against the reference's own replay --------------------------------------------------
+
+def test_replay_jacobian_outputs_match_reference_replays(gpu_ready):
+    """The differentiation workload (4-layer shell mesh, 1.296M tets, pencil
+    (30,30,5.5) +z, 8 detectors R=1.5 mm, 1e6 photons, one 5 ns gate, no
+    roulette): a forward run and the replay of its detected photons give the
+    raw wl (replay weight x path length) and wp (x mus / slen0) deposits.  The
+    reference engine did the same 10 times (forward, then -E run.mch -O L / -O P,
+    tests/golden/replay_shell.npz); this run must score like a fresh reference
+    run on the per-element deposits, and the totals and detected counts must lie
+    within the reference's run-to-run spread."""
+    import golden_checks as gc
+    fx = gc.load("replay_shell")
+    m = meshgen.shell_mesh(n=60, jitter=0.25, seed=4321)
+    mesh = Mesh(m.node, m.elem, m.label)
+    cfg = SimConfig(media=m.media, nphoton=int(fx["photons"]), seed=20261204, srcpos=(30.0, 30.0, 5.5),
+                    srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=5e-9, issavedet=1, issaveseed=1,
+                    detpos=fx["detectors"], maxdetphoton=2_000_000, basisorder=0, isnormalized=0, minenergy=0.0)
+    fwd = simulate(mesh, cfg)
+    msgs = []
+    n, nm, ns = fwd.detected, fx["ndet"].mean(), fx["ndet"].std(ddof=1)
+    if abs(n - nm) > 3.5 * ns * gc.INFLATE:
+        msgs.append(f"detected {n} vs reference {nm:.0f} +- {ns:.0f}")
+    for key in ("wl", "wp"):
+        rep, idx = rp.replay(mesh, cfg, fwd.detp, fwd.seeds, outputtype=key)
+        assert len(idx) == fwd.detected and rep.detected == len(idx)  # every photon retraced to its detector
+        x = rep.field.sum(0)
+        msgs += gc._zcheck(f"{key} per element", x[fx[key + "_sub"]], fx[key + "_mean"], fx[key + "_std"], 100,
+                           fx["null_" + key + "_frac"], fx["null_" + key + "_meanz"])
+        t, tm, ts = x.sum(), fx[key + "_total"].mean(), fx[key + "_total"].std(ddof=1)
+        if abs(t - tm) > 3.5 * ts * gc.INFLATE:
+            msgs.append(f"{key} total {t:.5g} vs reference {tm:.5g} +- {ts:.3g}")
+    assert not msgs, "\n".join(msgs)
+
+
+def test_replay_loss_autograd_function(gpu_ready):
+    """ReplayLoss, the torch.autograd.Function of L = sum_d c_d log W_d, on the
+    differentiation workload's mesh (4-layer shells, 1.296M tets, 8 detectors):
+    its value and backward() gradients per medium equal loss_and_grads summed
+    over each medium's elements, and dL/dmua per medium agrees with central
+    differences (+-1%, common random numbers: absorption does not move any
+    photon, so the difference quotient is smooth)."""
+    import torch
+    fx_det = np.array([[*(CENTER + 25.0 * np.array([np.sin(a), 0.0, -np.cos(a)])), 1.5]
+                       for a in np.deg2rad(np.arange(10, 90, 10))], np.float32)
+    m = meshgen.shell_mesh(n=60, jitter=0.25, seed=4321)
+    mesh = Mesh(m.node, m.elem, m.label)
+    cfg = SimConfig(media=m.media, nphoton=1_000_000, seed=77, srcpos=(30.0, 30.0, 5.5), srcdir=(0.0, 0.0, 1.0),
+                    tend=5e-9, tstep=5e-9, issavedet=1, issaveseed=1, detpos=fx_det, maxdetphoton=2_000_000,
+                    basisorder=0, isnormalized=0, minenergy=0.0)
+    c = np.random.default_rng(3).normal(size=len(fx_det))
+    mua = torch.tensor(m.media[:, 0].astype(np.float64), requires_grad=True)
+    mus = torch.tensor(m.media[:, 1].astype(np.float64), requires_grad=True)
+    L = rp.ReplayLoss.apply(mesh, cfg, c, mua, mus)
+    L.backward()
+    # the same forward and replays through the plain API
+    fwd = simulate(mesh, cfg)
+    L2, W, gmua, gmus = rp.loss_and_grads(mesh, cfg, fwd.detp, fwd.seeds, c)
+    nmed = m.media.shape[0]
+    assert float(L) == pytest.approx(L2, rel=1e-9)
+    np.testing.assert_allclose(mua.grad.numpy(), np.bincount(m.label, gmua, nmed), rtol=1e-6, atol=1e-9)
+    np.testing.assert_allclose(mus.grad.numpy(), np.bincount(m.label, gmus, nmed), rtol=1e-6, atol=1e-9)
+    assert mua.grad[0] == 0 and np.all(mua.grad.numpy()[1:] != 0)
+    # dL/dmua per layer against central differences of the loss itself
+    for k in range(1, nmed):
+        d = 0.01 * float(m.media[k, 0])
+        vals = []
+        for sgn in (1.0, -1.0):
+            t = mua.detach().clone()
+            t[k] += sgn * d
+            vals.append(float(rp.ReplayLoss.apply(mesh, cfg, c, t, mus.detach())))
+        fd = (vals[0] - vals[1]) / (2 * d)
+        g = float(mua.grad[k])
+        assert g == pytest.approx(fd, rel=5e-3, abs=1e-4 * abs(float(L)) + 1e-6), (k, g, fd)
