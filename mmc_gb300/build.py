@@ -106,13 +106,15 @@ def build_oracle(force: bool = False) -> str:
 
 
 def build_reference_oracle() -> str | None:
-    """Compiles the reference CPU engine into oracle/_ref when its sources exist."""
-    ref = os.environ.get("MMC_REFERENCE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "src")):
-        return None
+    """Compiles the reference CPU engine into oracle/_ref when its sources exist
+    (oracle/build_ref.sh finds them: MMC_REFERENCE, else the development
+    checkout's location); returns None where they are absent or do not build."""
     script = os.path.join(ORACLE, "build_ref.sh")
-    p = subprocess.run(["bash", script], env={**os.environ, "REF": ref},
-                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    out = os.path.join(ORACLE, "_ref", "mmc")
+    srcs = [script, os.path.join(ORACLE, "ref_driver.c"), os.path.join(ORACLE, "ref_shim.h")]
+    if not _stale(out, srcs) and not _stale(out + "_detp", srcs):
+        return out
+    p = subprocess.run(["bash", script], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if p.returncode != 0:
         return None
     return os.path.join(ORACLE, "_ref", "mmc")

@@ -187,6 +187,7 @@ class SimConfig:
     maxjumpdebug: int = 0                       # > 0: save up to this many trajectory records
     method: object = "elem"                     # "elem" (element output) or "grid" (dual-grid, DMMC)
     gridstep: float = 1.0                       # voxel edge of the grid output (mm)
+    accumulate: int = 0                         # 1: add into the caller's field/dref (mmc_run_cu's +=)
     save_field: bool = True
 
     @property
@@ -212,6 +213,7 @@ class SimConfig:
             c.srcpattern = _ptr(pat)
         c.issaveref = int(self.issaveref)
         c.maxjumpdebug = int(self.maxjumpdebug)
+        c.accumulate = int(self.accumulate)
         m = self.method
         c.method = {"elem": 0, "grid": 1}[m] if isinstance(m, str) else int(m)
         c.gridstep = float(self.gridstep)
@@ -337,6 +339,49 @@ def simulate(mesh: Mesh, cfg: SimConfig, trace: bool = False, out: Optional[np.n
     return _make_result(r, arrs)
 
 
+class _HostMesh:
+    """Sizes of a host mesh, for laying out the outputs of a one-shot run."""
+
+    def __init__(self, node, elem, nf=0):
+        self.nn, self.ne, self.nf = int(len(node)), int(len(elem)), int(nf)
+        self._node = node
+
+    def grid_dims(self, step):
+        lo = self._node.min(0).astype(np.float32) - np.float32(1e-6)
+        hi = self._node.max(0).astype(np.float32) + np.float32(1e-6)
+        return tuple(int((hi[k] - lo[k]) / np.float32(step)) + 1 for k in range(3))
+
+
+def run(node, elem, label, cfg: SimConfig, device: int = 0, out: Optional[np.ndarray] = None,
+        dref: Optional[np.ndarray] = None) -> SimResult:
+    """One-shot simulation through mmcgb_run, the counterpart of the reference's
+    mmc_run_cu (src/mmc_cu_host.h:56): the mesh is prepared, uploaded, simulated
+    and released in one call, with host arrays in and out.  `out` (maxgate x
+    datalen float64) and `dref` (maxgate x nf) are the caller's arrays; with
+    cfg.accumulate the run adds into them as mmc_run_cu adds into
+    cfg->exportfield and mesh->dref."""
+    lib = N.load()
+    node = np.ascontiguousarray(node, np.float32)
+    elem = np.ascontiguousarray(elem, np.int32)
+    label = np.ascontiguousarray(label, np.int32)
+    d, dkeep = _desc(node, elem, label)
+    nf = dref.shape[1] if dref is not None else 0
+    if cfg.issaveref and dref is None:
+        nfo = C.c_int32()
+        N.check(lib.mmcgb_prepare_host(C.byref(d), None, None, None, None, None, C.byref(nfo)))
+        nf = nfo.value
+    c, keep = cfg.to_c()
+    r, arrs = _alloc_result(_HostMesh(node, elem, nf), cfg, False, out)
+    if dref is not None:
+        if dref.dtype != np.float64 or dref.shape != (cfg.maxgate, nf) or not dref.flags.c_contiguous:
+            raise ValueError("dref must be a C-contiguous float64 (maxgate, nf) array")
+        arrs["dref"] = dref
+        r.dref = _ptr(dref)
+    N.check(lib.mmcgb_run(C.byref(d), C.byref(c), int(device), C.byref(r)))
+    del keep, dkeep
+    return _make_result(r, arrs)
+
+
 def simulate_batch(meshes: Sequence[Mesh], cfgs: Sequence[SimConfig]) -> list:
     """Runs many simulations in one persistent launch (mmcgb_simulate_batch)."""
     lib = N.load()
@@ -390,7 +435,42 @@ class Session:
         N.check(N.load().mmcgb_session_sync(self._h, C.byref(ms)))
         return float(ms.value)
 
-    def end(self, collect: bool = True) -> Optional[SimResult]:
+    def device_buffers(self) -> dict:
+        """Torch tensors aliasing the session's raw device buffers
+        (mmcgb_session_device_buffers): ``field`` (maxgate*datalen float64, None
+        with float32 accumulation), ``energy`` (2 float64), ``counters`` (3 int64),
+        ``detcount`` (1 int32), ``detp`` (maxdetphoton*reclen float32) and
+        ``seeds`` (maxdetphoton*16 uint8) where the run saves them.  What they
+        hold when the session ends is what end() reads back and normalizes.
+        Synchronize the session before using them."""
+        import torch
+        o = N.DeviceOut()
+        N.check(N.load().mmcgb_session_device_buffers(self._h, C.byref(o)))
+        cfg, G = self.cfg, self.cfg.maxgate
+        if cfg.method in ("grid", 1):
+            datalen = int(np.prod(self.mesh.grid_dims(cfg.gridstep)))
+        else:
+            datalen = self.mesh.ne
+        nmed = np.asarray(cfg.media).reshape(-1, 4).shape[0]
+        reclen = 1 + (2 + (1 if cfg.ismomentum else 0)) * (nmed - 1) + (6 if cfg.issaveexit else 0) + 1
+        maxdet = int(cfg.maxdetphoton) if cfg.issavedet else 0
+        dev = torch.device("cuda", self.mesh.device)
+
+        def wrap(ptr, n, typestr):
+            if not ptr or n == 0:
+                return None
+            iface = {"shape": (int(n),), "typestr": typestr, "data": (int(ptr), False), "version": 3,
+                     "strides": None}
+            return torch.as_tensor(type("DevArray", (), {"__cuda_array_interface__": iface})(), device=dev)
+
+        return dict(field=wrap(o.field_raw, G * datalen, "<f8"), energy=wrap(o.energy, 2, "<f8"),
+                    counters=wrap(o.counters, 3, "<i8"), detcount=wrap(o.detcount, 1, "<i4"),
+                    detp=wrap(o.detp, maxdet * reclen, "<f4"),
+                    seeds=wrap(o.seeds, maxdet * 16, "|u1") if cfg.issaveseed else None, reclen=reclen)
+
+    def end(self, collect: bool = True, records: bool = True) -> Optional[SimResult]:
+        """Reads back, runs the output stage and releases the session.
+        `records=False` leaves the detected records (and seeds) out."""
         lib = N.load()
         h, self._h = self._h, None
         if h is None:
@@ -399,6 +479,9 @@ class Session:
             N.check(lib.mmcgb_session_end(h, None))
             return None
         r, arrs = _alloc_result(self.mesh, self.cfg, False)
+        if not records:
+            r.detp = r.seeds = None
+            arrs["detp"] = arrs["seeds"] = None
         N.check(lib.mmcgb_session_end(h, C.byref(r)))
         return _make_result(r, arrs)
 

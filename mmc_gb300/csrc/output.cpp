@@ -74,32 +74,37 @@ std::vector<float> surface_fixed_nvol(const HostMesh& m, const mmcgb_config& cfg
     return nvol;
 }
 
-double normalize_output(const HostMesh& m, const mmcgb_config& cfg, int G, const double* raw,
-                        double energytot, double energyesc, double* field) {
+void scatter_output(const HostMesh& m, const mmcgb_config& cfg, int G, const double* raw, double* field) {
+    const int nn = m.nn, ne = m.ne;
+    const size_t total = (size_t)(cfg.basisorder ? nn : ne) * G;
+    if (!cfg.basisorder) {
+        if (field != raw) std::memcpy(field, raw, sizeof(double) * total);
+        return;
+    }
+    std::memset(field, 0, sizeof(double) * total);
+    for (int i = 0; i < G; i++) {
+        const double* r = raw + (size_t)i * ne;
+        double* f = field + (size_t)i * nn;
+        for (int j = 0; j < ne; j++) {
+            const double ww = r[j] * 0.25;
+            const int* e = &m.elem[4 * (size_t)j];
+            f[e[0] - 1] += ww;
+            f[e[1] - 1] += ww;
+            f[e[2] - 1] += ww;
+            f[e[3] - 1] += ww;
+        }
+    }
+}
+
+double normalize_in_place(const HostMesh& m, const mmcgb_config& cfg, int G, double energytot, double energyesc,
+                          double* field) {
     const int nn = m.nn, ne = m.ne;
     const float* med = cfg.media;
     const int datalen = cfg.basisorder ? nn : ne;
-    const std::vector<float> nvol = surface_fixed_nvol(m, cfg);
     const size_t total = (size_t)datalen * G;
-    if (!cfg.basisorder) {
-        if (field != raw) std::memcpy(field, raw, sizeof(double) * total);
-    } else {
-        std::memset(field, 0, sizeof(double) * total);
-        for (int i = 0; i < G; i++) {
-            const double* r = raw + (size_t)i * ne;
-            double* f = field + (size_t)i * nn;
-            for (int j = 0; j < ne; j++) {
-                const double ww = r[j] * 0.25;
-                const int* e = &m.elem[4 * (size_t)j];
-                f[e[0] - 1] += ww;
-                f[e[1] - 1] += ww;
-                f[e[2] - 1] += ww;
-                f[e[3] - 1] += ww;
-            }
-        }
-    }
     double normalizor = 1.0;
     if (!cfg.isnormalized) return normalizor;
+    const std::vector<float> nvol = surface_fixed_nvol(m, cfg);
     const float Etotal = (float)energytot;
     const float Eabsorb = (float)(energytot - energyesc);
     const bool replay = cfg.replayseed != nullptr;
@@ -136,6 +141,21 @@ double normalize_output(const HostMesh& m, const mmcgb_config& cfg, int G, const
     }
     for (size_t i = 0; i < total; i++) field[i] *= normalizor;
     return normalizor;
+}
+
+double normalize_output(const HostMesh& m, const mmcgb_config& cfg, int G, const double* raw,
+                        double energytot, double energyesc, double* field) {
+    scatter_output(m, cfg, G, raw, field);
+    return normalize_in_place(m, cfg, G, energytot, energyesc, field);
+}
+
+double grid_normalizer(const mmcgb_config& cfg, double energytot) {
+    if (!cfg.isnormalized) return 1.0;
+    const float Et = (float)energytot;
+    if (cfg.outputtype == OT_ENERGY) return 1.f / Et;  // src/mmc_mesh.c:2185-2192
+    double norm = 1.0 / (Et * cfg.unitinmm * cfg.unitinmm * cfg.unitinmm);  // src/mmc_mesh.c:2204-2206
+    if (cfg.outputtype == OT_FLUX) norm /= cfg.tstep;
+    return norm;
 }
 
 }  // namespace mmcgb

@@ -11,8 +11,13 @@ counters, and an all-gather of the detected-photon records and seeds.  The
 normalization runs once on the global totals (it is not linear in the
 per-rank results).
 
-Works with any torch.distributed backend: NCCL (tensors on the rank's GPU) or
-gloo (tensors on the CPU).
+With the NCCL backend and the default runner the exchange stays on the GPUs:
+each rank traces its shard in a session, the session's raw device buffers
+(deposits, energies, counters) are summed in place with NCCL and the detected
+records gathered with NCCL, and only then does the session's output stage run
+on the device and copy the final field to the host once.  A custom runner (the
+CPU oracle in the gloo tests) goes through the host: its result is summed and
+gathered with the group's backend, then normalized on the host.
 """
 from __future__ import annotations
 
@@ -21,7 +26,7 @@ from typing import Callable, Optional
 
 import numpy as np
 
-from .core import Mesh, SimConfig, SimResult, normalize_host, simulate
+from .core import Mesh, Session, SimConfig, SimResult, normalize_host, simulate
 
 
 def shard(nphoton: int, rank: int, world: int):
@@ -84,15 +89,69 @@ def reduce_results(local: SimResult, group=None) -> SimResult:
                                raytet=int(cn[0]), aborted=int(cn[1]), detected=int(cn[2]), detp=detp, seeds=seeds)
 
 
+def _gather_rows(t, nrows, width, group):
+    """All-gathers the first nrows rows (width elements each) of the flat
+    device tensor t from every rank; returns (rows of all ranks in rank
+    order, as a host array)."""
+    import torch
+    dist = _dist()
+    world = dist.get_world_size(group)
+    n = torch.tensor([nrows], dtype=torch.int64, device=t.device)
+    sizes = [torch.zeros_like(n) for _ in range(world)]
+    dist.all_gather(sizes, n, group=group)
+    sizes = [int(x.item()) for x in sizes]
+    pad = torch.zeros((max(max(sizes), 1), width), dtype=t.dtype, device=t.device)
+    if nrows:
+        pad[:nrows] = t[:nrows * width].view(nrows, width)
+    parts = [torch.empty_like(pad) for _ in range(world)]
+    dist.all_gather(parts, pad, group=group)
+    return torch.cat([p[:k] for p, k in zip(parts, sizes)]).cpu().numpy()
+
+
+def _simulate_sharded_on_device(mesh: Mesh, cfg: SimConfig, off: int, n: int, group) -> SimResult:
+    """The rank's shard in a session; the raw device buffers are combined with
+    NCCL before the output stage (src/mmc_cu_host.cu:772-783, :916-921)."""
+    import torch
+    dist = _dist()
+    local_cfg = dataclasses.replace(cfg, photon_offset=cfg.photon_offset + off, nphoton=n, accum_f64=1)
+    sess = Session(mesh, local_cfg)
+    try:
+        if n:
+            sess.launch(0, n)
+        sess.sync()
+        b = sess.device_buffers()
+        saved = 0
+        if b["detcount"] is not None:
+            saved = min(int(b["detcount"].item()), int(cfg.maxdetphoton))
+        for key in ("field", "energy", "counters", "detcount"):
+            if b[key] is not None:
+                dist.all_reduce(b[key], op=dist.ReduceOp.SUM, group=group)
+        detp = seeds = None
+        if b["detp"] is not None:
+            reclen = b["reclen"]
+            detp = _gather_rows(b["detp"], saved, reclen, group).reshape(-1, reclen)
+            if b["seeds"] is not None:
+                seeds = _gather_rows(b["seeds"], saved, 16, group).reshape(-1, 16)
+        torch.cuda.synchronize(mesh.device)  # the collectives ran on NCCL's stream
+        res = sess.end(collect=True, records=False)
+    finally:
+        if getattr(sess, "_h", None) is not None:
+            sess.end(collect=False)
+    return dataclasses.replace(res, detp=detp, seeds=seeds)
+
+
 def simulate_sharded(mesh: Mesh, cfg: SimConfig, group=None,
                      runner: Optional[Callable[[SimConfig], SimResult]] = None) -> SimResult:
-    """One simulation split over the ranks of `group`.  `runner` simulates one
-    rank's shard and returns raw element deposits (default: the rank's GPU
-    through `simulate`); `mesh` needs node/elem/label arrays (and a device
-    handle for the default runner)."""
+    """One simulation split over the ranks of `group`.  Default: the rank's GPU
+    traces its shard and, with NCCL, the ranks combine their device buffers
+    before the output stage (`mesh` a resident Mesh).  `runner` replaces the
+    rank's simulation (it returns raw element deposits, e.g. the CPU oracle);
+    its result is combined on the host (`mesh` needs node/elem/label)."""
     dist = _dist()
     rank, world = dist.get_rank(group), dist.get_world_size(group)
     off, n = shard(cfg.nphoton, rank, world)
+    if runner is None and dist.get_backend(group) == "nccl":
+        return _simulate_sharded_on_device(mesh, cfg, off, n, group)
     local_cfg = dataclasses.replace(cfg, photon_offset=cfg.photon_offset + off, nphoton=n, isnormalized=0,
                                     basisorder=0, save_field=True)
     run = runner or (lambda c: simulate(mesh, c))

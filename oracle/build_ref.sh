@@ -4,13 +4,17 @@
 # binary produces golden fixtures (tests/golden/make_golden.py) and is never part
 # of the product.  Nothing is copied out of the reference tree.
 #
-#   REF=/path/to/mmc  oracle/build_ref.sh        (default REF=/root/reference)
+#   MMC_REFERENCE=/path/to/mmc  oracle/build_ref.sh
+#
+# Without MMC_REFERENCE the recipe reads the sources at the development
+# checkout's location below; where neither exists it exits with status 2 and
+# nothing is built (the GPU machine has no reference tree and needs none).
 #
 # Needs: gcc/g++, zlib headers, an x86-64 host (the reference's branchless
 # Badouel tracer is written with SSE4.1 intrinsics; without MMC_USE_SSE its
 # tracer_build skips the plane offsets and only the Plucker tracer works).
 set -euo pipefail
-REF=${REF:-/root/reference}
+REF=${MMC_REFERENCE:-${REF:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 SRC="$REF/src"
@@ -50,4 +54,7 @@ gcc $CFLAGS -c "$HERE/ref_driver.c" -o "$OUT/ref_driver.o"
 g++ -fopenmp -o "$OUT/mmc" "$OUT"/obj/*.o -lz -lm
 # same objects with the reference's main replaced by the table-dumping driver
 g++ -fopenmp -o "$OUT/mmc_detp" $(ls "$OUT"/obj/*.o | grep -v '/mmc\.o$') "$OUT/ref_driver.o" -lz -lm
+# where the sources were found: tests that compile against the reference's own
+# headers (tests/test_integration_shim.py) read it
+echo "$REF" > "$OUT/REF_PATH"
 echo "built $OUT/mmc and $OUT/mmc_detp"

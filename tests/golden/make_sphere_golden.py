@@ -4,9 +4,11 @@ fixture examples/meshtest/sphdiffsemiinf.mat: the diffusion solution of a
 source 30 mm below the sphere centre on its axis, on the plane y = 0 about the
 sphere centre (x = -22:0.8:22, z = -30:0.8:10 mm), made by the reference as
 sphdiffusionslab(0,0,60,-22:0.8:22,0,-30:0.8:10) (examples/meshtest/plotmmcsph.m:27-28).
-Needs the reference tree, so it runs in the development container only.
+Needs the reference tree, so it runs in the development container only; its
+location comes from the command line or the MMC_REFERENCE environment
+variable.
 
-  python tests/golden/make_sphere_golden.py [path/to/reference]
+  MMC_REFERENCE=path/to/mmc python tests/golden/make_sphere_golden.py
 """
 import os
 import sys
@@ -17,7 +19,10 @@ import scipy.io as sio
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def main(ref="/root/reference"):
+def main(ref=None):
+    ref = ref or os.environ.get("MMC_REFERENCE")
+    if not ref or not os.path.isdir(os.path.join(ref, "examples")):
+        sys.exit("set MMC_REFERENCE (or pass the path) to the reference MMC checkout")
     d = sio.loadmat(os.path.join(ref, "examples", "meshtest", "sphdiffsemiinf.mat"))
     phi = d["phi_ana"]
     assert np.abs(phi.imag).max() < 1e-12 * np.abs(phi.real).max()   # continuous wave: real
