@@ -44,6 +44,19 @@ def workload_config(nphoton):
     return m, cfg
 
 
+# Port-to-reference speed factor of the CPU baseline: the oracle's photon loop
+# ran at 0.821x the reference CPU engine's own printed speed (the reference's
+# sources built as its `make sse` target does, oracle/build_ref.sh) on the same
+# 1.296M-tet workload, 8 threads of an x86 Xeon @ 2.70 GHz, 1e6 and 2e6 photons
+# (88.9/86.7 vs 73.0/71.2 photons/ms); 0.731x on one thread (12.45 vs 9.10).
+# The reference engine is SSE4 code and does not build on the Arm host of the
+# GPU, so the factor is measured on the x86 build host and reported beside the
+# port's speed: ratio against the reference engine = ratio against the port x 0.821.
+PORT_VS_REFERENCE = {"factor": 0.821, "threads": 8, "host": "x86 Xeon @ 2.70 GHz",
+                     "measured": "oracle photon loop 73.0/71.2 vs reference mmc -G -1 -M s -C 0 88.9/86.7 photons/ms, "
+                                 "1e6/2e6 photons of this workload"}
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -53,66 +66,28 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per photon of the engine's launches (all gate windows of a
-    step) from the committed ncu summary, measured on a 5e6-photon step."""
+def profiled_traffic(key="dram_bytes_per_photon"):
+    """Bytes per photon of the engine's launches (all gate windows of a step)
+    from the committed ncu summary, measured on a 5e6-photon step: DRAM
+    (dram_bytes_per_photon) or L2 (l2_bytes_per_photon, lts__t_bytes)."""
     path = os.path.join(ROOT, "profiles", "photon_engine_phased_inclusion_cube.md")
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_photon:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":", 1)[1].split()[0])
     except OSError:
         pass
     return None
 
 
-class ClockSampler:
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
-
-    def __init__(self, device):
-        self.device = device
-        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
-        self.p = None
-
-    def start(self):
-        try:
-            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
-                                      stdout=self.f, stderr=subprocess.DEVNULL)
-        except OSError:
-            self.p = None
-
-    def stop(self):
-        if self.p is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.p.terminate()
-        try:
-            self.p.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.p.kill()
-        self.f.flush()
-        self.f.seek(0)
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.f.read().splitlines():
-            parts = [x.strip() for x in line.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
-            except ValueError:
-                continue
-            for name, v in zip(names, parts[5:9]):
-                if v.lower() == "active":
-                    reasons.add(name)
-        os.unlink(self.f.name)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
-                "samples": len(sm)}
+def l2_peak(device):
+    """This GPU's L2 read bandwidth, measured now (mmcgb_l2_read_bandwidth:
+    64 MiB resident buffer, 20 sweeps of 16-byte L1-bypassing loads)."""
+    import ctypes as C
+    from mmc_gb300 import _native
+    g = C.c_double()
+    rc = _native.load().mmcgb_l2_read_bandwidth(int(device), 64 << 20, 20, C.byref(g))
+    return g.value if rc == 0 else None
 
 
 def cpu_baseline(m, cfg, target_s=12.0):
@@ -130,7 +105,8 @@ def cpu_baseline(m, cfg, target_s=12.0):
             return {"value": n / (dt * 1e3), "unit": "photons/ms", "cores": cores, "kind": "port",
                     "sample": f"{n} photons of the {JOB_PHOTONS:.0e}-photon job, {dt:.1f} s of photon loop "
                               f"on {cores} threads (mesh preparation excluded, as the reference times "
-                              f"its speed)"}
+                              f"its speed)",
+                    "port_vs_reference": PORT_VS_REFERENCE}
         n = int(n * min(10.0, max(1.5, target_s / max(dt, 1e-3))))
 
 
@@ -166,7 +142,7 @@ def run_reference(args, rank, world):
                                "photon loop timed, as the reference times its reported speed"},
             "cpu_baseline": {"value": value, "unit": "photons/ms", "cores": cores, "kind": "port",
                              "sample": f"{n} photons per step x {args.steps} steps on {cores} threads, "
-                                       f"photon loop only"},
+                                       f"photon loop only", "port_vs_reference": PORT_VS_REFERENCE},
             "e2e": {"value": value, "unit": "photons/ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -230,6 +206,7 @@ def main():
     for w in range(args.warmup):
         sess.launch(w * nps, nps)
         sess.sync()
+    from mmc_gb300.clocks import ClockSampler
     sampler = ClockSampler(local_rank)
     barrier()
     torch.cuda.synchronize()
@@ -266,18 +243,29 @@ def main():
     tpp = profiled_traffic()
 
     # ---- end to end through the public API with host buffers ----
+    # N = 1: simulate() on the resident mesh.  N > 1: simulate_sharded(), the call a sharded job
+    # makes: each rank traces its shard, the raw device buffers are summed and the records
+    # gathered with NCCL, then one output stage and one copy of the final field to the host.
     e2e = None
+    e2e_dropin = None
     if not args.no_e2e:
         from mmc_gb300.core import pinned_empty
-        ecfg = dataclasses.replace(cfg, photon_offset=10 ** 12 + rank * 10 ** 10)
+        ecfg = dataclasses.replace(cfg, photon_offset=10 ** 12)
         out = pinned_empty((ecfg.maxgate, mesh.ne))  # the application's host buffer, reused every step
         simulate(mesh, dataclasses.replace(ecfg, nphoton=100000), out=out)  # warm the allocator
+        esteps = max(1, min(args.steps, 3))
+        if dist is not None:
+            from mmc_gb300.distributed import simulate_sharded
+            job = dataclasses.replace(ecfg, nphoton=nps * world)  # per-rank work fixed: weak scaling
+            simulate_sharded(mesh, dataclasses.replace(job, nphoton=100000 * world))
         barrier()
         t0 = time.perf_counter()
-        esteps = max(1, min(args.steps, 3))
         d2h = 0
         for k in range(esteps):
-            r = simulate(mesh, dataclasses.replace(ecfg, photon_offset=ecfg.photon_offset + k * nps), out=out)
+            if dist is None:
+                r = simulate(mesh, dataclasses.replace(ecfg, photon_offset=ecfg.photon_offset + k * nps), out=out)
+            else:
+                r = simulate_sharded(mesh, dataclasses.replace(job, photon_offset=job.photon_offset + k * nps * world))
             d2h = r.field.nbytes + (r.detp.nbytes if r.detp is not None else 0) + 64
         barrier()
         et = time.perf_counter() - t0
@@ -287,7 +275,39 @@ def main():
             et = float(t.item())
         h2d = cfg.media.nbytes + cfg.detpos.nbytes + 200
         e2e = {"value": nps * esteps * world / (et * 1e3), "unit": "photons/ms", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "steps": esteps}
+               "d2h_bytes_per_step": int(d2h), "steps": esteps,
+               "path": "simulate() on the resident mesh" if dist is None else
+                       "simulate_sharded(): per-rank shard, NCCL sum of deposits and gather of records, "
+                       "one output stage"}
+        if dist is None:
+            # the drop-in path as the reference runs it: mmcgb_run (mmc_run_cu's counterpart)
+            # prepares and uploads the mesh, simulates, normalizes and frees, every call
+            from mmc_gb300 import core
+            dsteps = 2
+            core.run(m.node, m.elem, m.label, dataclasses.replace(ecfg, nphoton=100000), out=out)
+            t0 = time.perf_counter()
+            for k in range(dsteps):
+                core.run(m.node, m.elem, m.label,
+                         dataclasses.replace(ecfg, photon_offset=ecfg.photon_offset + (esteps + k) * nps), out=out)
+            dt = time.perf_counter() - t0
+            mesh_bytes = m.node.nbytes + m.elem.nbytes + m.label.nbytes
+            e2e_dropin = {"value": nps * dsteps / (dt * 1e3), "unit": "photons/ms",
+                          "h2d_bytes_per_step": int(h2d + mesh_bytes), "d2h_bytes_per_step": int(d2h),
+                          "steps": dsteps,
+                          "path": "mmcgb_run through the C ABI: host mesh prepared, uploaded and freed per call"}
+
+    # ---- the level the gathers are served from: L2 traffic against the measured L2 bandwidth ----
+    l2 = None
+    l2pp = profiled_traffic("l2_bytes_per_photon")
+    l2bw = l2_peak(local_rank)
+    if l2bw and not l2pp:
+        l2 = {"peak": l2bw, "unit": "GB/s", "peak_kind": "measured now (mmcgb_l2_read_bandwidth)"}
+    if l2pp and l2bw:
+        l2_ach = l2pp * nps / (avg_ms * 1e-3) / 1e9
+        l2 = {"achieved": l2_ach, "peak": l2bw, "unit": "GB/s", "frac": l2_ach / l2bw,
+              "peak_kind": "measured now (mmcgb_l2_read_bandwidth)",
+              "traffic_bytes_per_photon": l2pp,
+              "note": "lts__t_bytes of the engine's launches per photon (ncu, 5e6-photon step) x photons / step time"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -313,8 +333,10 @@ def main():
                          "bytes_per_test": BYTES_PER_STEP, "tests_per_launch": raytet_per_launch,
                          "avg_launch_ms": avg_ms, "launches_per_step": launches_per_step,
                          "note": "per step: the step's phased launches together"},
+            "l2_roofline": l2,
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "e2e_dropin": e2e_dropin,
             "gpu_launches": args.steps * launches_per_step,
             "clocks": clocks,
         }

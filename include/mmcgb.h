@@ -331,6 +331,13 @@ int32_t mmcgb_normalize_host(const mmcgb_mesh_desc* desc, const mmcgb_config* cf
  * the run would start in to *e0 when e0 is not NULL. */
 int32_t mmcgb_check_config(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, int32_t* e0);
 
+/* Diagnostic, no counterpart in the reference: the L2 read bandwidth of
+ * `device` in GB/s -- a buffer of `bytes` (at most half of the L2) read once
+ * to make it resident, then `reps` sweeps with L1-bypassing 16-byte loads from
+ * every SM.  The engine's gathers are served from L2; this is the ceiling its
+ * L2 traffic is compared with.  Allocates and frees the buffer itself. */
+int32_t mmcgb_l2_read_bandwidth(int32_t device, uint64_t bytes, int32_t reps, double* gbs);
+
 /* Fills `cfg` with the reference defaults (src/mmc_utils.c:207-363). */
 void mmcgb_config_defaults(mmcgb_config* cfg);
 

@@ -60,7 +60,7 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     out = os.path.join(LIBDIR, "libmmcgb.so")
     headers = [os.path.join(CSRC, h) for h in ("engine.h", "mesh.h", "mesh_handle.h", "devmath.cuh", "output_dev.h")]
     headers.append(os.path.join(ROOT, "include", "mmcgb.h"))
-    cu = ["engine.cu", "noalloc.cu", "output.cu"]
+    cu = ["engine.cu", "noalloc.cu", "output.cu", "diag.cu"]
     cpp = ["mesh.cpp", "output.cpp", "api.cpp"]
     srcs = [os.path.join(CSRC, f) for f in cu + cpp]
     if not force and not _stale(out, srcs + headers):

@@ -78,6 +78,7 @@ class Server:
         self.completed: List[Request] = []
         self.waves = 0
         self.wave_ms: List[float] = []
+        self.enqueue_ms: List[float] = []  # host time to enqueue one wave (setup copies + launch)
         self._streams = [torch.cuda.Stream(device=dev) for _ in range(self.depth)]
         self._inflight: deque = deque()  # (event, [(entry, count)], launch time)
         self._last_done: Optional[float] = None
@@ -137,7 +138,9 @@ class Server:
             budget -= k
         live = picked
         st = self._streams[self.waves % self.depth]
+        t0 = time.perf_counter()
         launch_batch([a[1] for a in live], [a[2] for a in live], counts, stream=st.cuda_stream)
+        self.enqueue_ms.append((time.perf_counter() - t0) * 1e3)
         ev = torch.cuda.Event()
         ev.record(st)
         for a, k in zip(live, counts):
@@ -237,4 +240,5 @@ class Server:
                     p50_ms=float(np.percentile(lat, 50)) if len(lat) else None,
                     p99_ms=float(np.percentile(lat, 99)) if len(lat) else None,
                     span_s=t1 - t0, photons_per_ms=photons / max((t1 - t0) * 1e3, 1e-9),
-                    waves=self.waves, mean_wave_ms=float(np.mean(self.wave_ms)) if self.wave_ms else None)
+                    waves=self.waves, mean_wave_ms=float(np.mean(self.wave_ms)) if self.wave_ms else None,
+                    mean_enqueue_ms=float(np.mean(self.enqueue_ms)) if self.enqueue_ms else None)

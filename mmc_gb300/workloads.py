@@ -28,7 +28,8 @@ import time
 import numpy as np
 
 from mmc_gb300 import meshgen
-from mmc_gb300.autotune import autotune
+from mmc_gb300.autotune import autotune_batch
+from mmc_gb300.clocks import ClockSampler
 from mmc_gb300.core import Mesh, SimConfig, simulate, simulate_batch
 
 CENTER = np.array([30.0, 30.0, 30.0])
@@ -63,10 +64,12 @@ def run_batched(args):
         pos, d = _surface_source(rng)
         cfgs.append(SimConfig(media=_random_media(rng, m.media), nphoton=int(10 ** rng.uniform(5, 7)), seed=i + 1,
                               srcpos=pos, srcdir=d, tend=5e-9, tstep=0.5e-9, basisorder=0, isnormalized=1))
-    tune = autotune(mesh, cfgs[0])
+    tune = autotune_batch([mesh] * len(cfgs), cfgs)  # the batch is tuned as the batch it runs
     cfgs = [dataclasses.replace(c, threads=tune["threads"], blocks=tune["blocks"], accum_f64=tune["accum_f64"])
             for c in cfgs]
     total = sum(c.nphoton for c in cfgs)
+    clocks = ClockSampler(0)
+    clocks.start()
     # serial plain launches through the public API, mesh resident: one simulate() per simulation
     serial_ms, serial_wall = 0.0, 0.0
     for c in cfgs:
@@ -80,6 +83,7 @@ def run_batched(args):
     results = simulate_batch([mesh] * len(cfgs), cfgs)
     batched_wall = time.perf_counter() - t0
     batched_ms = results[0].kernel_ms
+    clk = clocks.stop()
     absorbed = float(np.mean([r.absorbed_fraction for r in results]))
     del results
     # the drop-in path as the reference runs it: every simulation prepares and uploads its mesh
@@ -94,7 +98,7 @@ def run_batched(args):
             "batched_wall_s": batched_wall, "batched_kernel_ms": batched_ms,
             "serial_wall_s": serial_wall, "serial_kernel_ms": serial_ms, "mesh_setup_s": mesh_s,
             "photons": total, "mean_absorbed_fraction": absorbed,
-            "autotune": {k: v for k, v in tune.items() if k != "trials"}, "data": "synthetic",
+            "autotune": {k: v for k, v in tune.items() if k != "trials"}, "data": "synthetic", "clocks": clk,
             "config": {"mesh": "4-layer shells 1.296M tets", "sims": 256, "gates": 10,
                        "timing": "wall clock through simulate()/simulate_batch(), host buffers included"}}
     print(json.dumps(line), flush=True)
@@ -137,6 +141,8 @@ def run_serving(args):
         reqs.append(Request(mesh=key, cfg=cfg, arrival=t))
     # continuous batching
     srv = Server({k: v[0] for k, v in meshes.items()}, wave_photons=8_000_000, min_share=100_000)
+    clocks = ClockSampler(0)
+    clocks.start()
     t0 = time.perf_counter()
     for r in reqs:
         r.arrival += t0
@@ -148,6 +154,7 @@ def run_serving(args):
         s0 = time.perf_counter()
         simulate(meshes[r.mesh][0], r.cfg)
         service.append(time.perf_counter() - s0)
+    clk = clocks.stop()
     fin, lat = 0.0, []
     arr = [r.arrival - t0 for r in reqs]
     for a, s in zip(arr, service):
@@ -158,10 +165,12 @@ def run_serving(args):
     line = {"metric": "served photons/ms (continuous batching)", "value": st["photons_per_ms"], "unit": "photons/ms",
             "n_gpus": 1, "higher_is_better": True, "workload": "serving-3-meshes",
             "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "requests": st["requests"], "waves": st["waves"],
-            "mean_wave_ms": st["mean_wave_ms"], "serial_plain_photons_per_ms": serial_rate,
+            "mean_wave_ms": st["mean_wave_ms"], "mean_wave_enqueue_ms": st["mean_enqueue_ms"],
+            "serial_plain_photons_per_ms": serial_rate,
             "speedup_vs_serial_plain": st["photons_per_ms"] / serial_rate,
             "serial_p50_ms": float(np.percentile(np.array(lat) * 1e3, 50)),
             "serial_p99_ms": float(np.percentile(np.array(lat) * 1e3, 99)), "photons": photons, "data": "synthetic",
+            "clocks": clk,
             "config": {"arrival_rate_hz": 200, "photons": "log-uniform 1e5-1e8", "gates": 10, "fluence": "float32"}}
     print(json.dumps(line), flush=True)
 
@@ -175,11 +184,14 @@ def run_replay(args):
     cfg = SimConfig(media=m.media, nphoton=10_000_000, seed=31, srcpos=(30.0, 30.0, 5.5), tend=5e-9, tstep=5e-9,
                     issavedet=1, issaveseed=1, detpos=det, maxdetphoton=5_000_000, basisorder=0, isnormalized=0)
     c = np.random.default_rng(3).normal(size=len(det))
+    clocks = ClockSampler(0)
+    clocks.start()
     t0 = time.perf_counter()
     fwd = simulate(mesh, cfg)
     t1 = time.perf_counter()
     L, W, gmua, gmus = rp.loss_and_grads(mesh, cfg, fwd.detp, fwd.seeds, c)
     t2 = time.perf_counter()
+    clk = clocks.stop()
     nrep = len(fwd.detp)
     line = {"metric": "replay (backward) photons/ms", "value": 2 * nrep / ((t2 - t1) * 1e3), "unit": "photons/ms",
             "n_gpus": 1, "higher_is_better": True, "workload": "replay-8-detectors",
@@ -187,7 +199,8 @@ def run_replay(args):
             "detected": int(fwd.detected), "replayed": nrep, "loss": L,
             "detector_weights": [float(x) for x in W], "backward_s": t2 - t1,
             "grad_mua_norm": float(np.linalg.norm(gmua)), "grad_mus_norm": float(np.linalg.norm(gmus)),
-            "data": "synthetic", "config": {"mesh": "4-layer shells 1.296M tets", "photons": 10_000_000}}
+            "data": "synthetic", "clocks": clk,
+            "config": {"mesh": "4-layer shells 1.296M tets", "photons": 10_000_000}}
     print(json.dumps(line), flush=True)
 
 

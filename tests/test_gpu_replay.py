@@ -273,7 +273,7 @@ def test_replay_loss_autograd_function(gpu_ready):
     fwd = simulate(mesh, cfg)
     L2, W, gmua, gmus = rp.loss_and_grads(mesh, cfg, fwd.detp, fwd.seeds, c)
     nmed = m.media.shape[0]
-    assert float(L) == pytest.approx(L2, rel=1e-9)
+    assert float(L.detach()) == pytest.approx(L2, rel=1e-9)
     np.testing.assert_allclose(mua.grad.numpy(), np.bincount(m.label, gmua, nmed), rtol=1e-6, atol=1e-9)
     np.testing.assert_allclose(mus.grad.numpy(), np.bincount(m.label, gmus, nmed), rtol=1e-6, atol=1e-9)
     assert mua.grad[0] == 0 and np.all(mua.grad.numpy()[1:] != 0)
