@@ -203,6 +203,7 @@ def main():
     # ---- device-resident throughput (value) ----
     # rank r simulates photons [r*K*nps, (r+1)*K*nps) of the job: no data-path collective
     sess = Session(mesh, dataclasses.replace(cfg, photon_offset=rank * (args.steps + args.warmup) * nps))
+    window = sess.phase_window(nps)
     for w in range(args.warmup):
         sess.launch(w * nps, nps)
         sess.sync()
@@ -235,9 +236,8 @@ def main():
     raytet_per_launch = steps_per_photon * nps
     avg_ms = float(np.mean(kernel_ms))
     # engine launches per step: one per window of gates (the library's automatic window)
-    l2 = getattr(torch.cuda.get_device_properties(local_rank), "L2_cache_size", 0) or (126 << 20)
-    span = max(1, int(0.9 * l2 / (mesh.ne * 8)) - 1)
-    launches_per_step = -(-cfg.maxgate // span) if (span < cfg.maxgate and nps >= 4_000_000) else 1
+    span = window
+    launches_per_step = -(-cfg.maxgate // span) if span > 0 else 1
     achieved = raytet_per_launch * BYTES_PER_STEP / (avg_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
     tpp = profiled_traffic()
@@ -323,8 +323,9 @@ def main():
             "config": {"workload": WORKLOAD, "ne": mesh.ne, "nn": mesh.nn, "photons_per_step": nps,
                        "job_photons": JOB_PHOTONS, "gates": 50, "detectors": 4, "savedet": True,
                        "l2": "flushed (256 MB write) before each timed step",
-                       "tracing": "gate-phased (automatic window: the live gate planes fill ~90% of L2; "
-                                  "parked photons resumed in spatial order)",
+                       "tracing": f"gate-phased, automatic window of {window} gates (the live gate planes "
+                                  "fill ~70% of L2; parked photons resumed in spatial order)" if window else
+                                  "one launch per step",
                        "steps_per_photon": steps_per_photon, "detected": res.detected,
                        "absorbed_fraction": res.absorbed_fraction, "wall_s": wall},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

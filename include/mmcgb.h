@@ -114,7 +114,7 @@ typedef struct mmcgb_config {
                                 the fluence take deposits at a time; same results photon for
                                 photon): 0 = auto (when >= 8 gates, fluence >= 64 MB, >= 4e6
                                 photons per launch and queue memory available; k sized so the
-                                k+1 live planes fill ~90% of the L2), k >= 1 = window of k gates
+                                k+1 live planes fill ~70% of the L2), k >= 1 = window of k gates
                                 whenever possible (not for replay), -1 = never */
     float srcparam1[4];      /* source parameters 1 and 2, as the reference's cfg->srcparam1/2
                                 (src/mmc_utils.h:219-220), e.g. disk radius, area-source edge
@@ -135,6 +135,10 @@ typedef struct mmcgb_config {
     uint32_t maxjumpdebug;   /* > 0: save photon trajectories (the reference's -D M): a record at
                                 each launch, scattering event and photon end, at most this many,
                                 into mmcgb_result.traj */
+    uint64_t phase_chunk;    /* at most this many photons per gate-phased launch (their parked
+                                states are queued on the device); 0 = as many as half of the free
+                                device memory holds.  A launch of more photons is traced as several
+                                phased launches, with the same results */
     int32_t accumulate;      /* 0: mmcgb_result.field and .dref are overwritten; 1: this run's
                                 deposits (scattered to the nodes for basisorder 1) are added to
                                 what the caller's arrays hold, and with isnormalized the sum is
@@ -240,6 +244,14 @@ int32_t mmcgb_session_sync(mmcgb_session* s, float* last_kernel_ms);
  * has finished.  Valid until mmcgb_session_end. */
 void* mmcgb_session_stream(mmcgb_session* s);
 int32_t mmcgb_session_end(mmcgb_session* s, mmcgb_result* res);
+/* How a launch of `nphoton` photons of this session would be traced:
+ * *window = 0 for one launch, k for one launch per window of k gates (the
+ * value of mmcgb_config.phased, or the automatic choice: the live gate planes
+ * fill about 70% of the L2); *chunk (may be NULL) = photons per phased launch
+ * (fewer than nphoton when the queues for all of them do not fit in half of
+ * the free device memory, or mmcgb_config.phase_chunk caps them).  No
+ * counterpart in the reference. */
+int32_t mmcgb_session_phase_window(mmcgb_session* s, uint64_t nphoton, int32_t* window, uint64_t* chunk);
 /* Device addresses of a session's raw buffers (valid until
  * mmcgb_session_end), for a caller that combines sessions on several GPUs
  * before the output stage -- the reference's multi-device sum of fields,

@@ -56,7 +56,7 @@ class Config(C.Structure):
         ("threads", C.c_int32), ("blocks", C.c_int32), ("fast_math", C.c_int32), ("phased", C.c_int32),
         ("srcparam1", C.c_float * 4), ("srcparam2", C.c_float * 4), ("focus", C.c_float), ("srcpattern", C.c_void_p),
         ("issaveref", C.c_int32), ("method", C.c_int32), ("gridstep", C.c_float), ("maxjumpdebug", C.c_uint32),
-        ("accumulate", C.c_int32),
+        ("phase_chunk", C.c_uint64), ("accumulate", C.c_int32),
     ]
 
 
@@ -84,7 +84,7 @@ EXPORTS = [
     "mmcgb_session_sync", "mmcgb_session_end", "mmcgb_prepare_host", "mmcgb_normalize_host",
     "mmcgb_session_launch_batch", "mmcgb_session_stream", "mmcgb_session_launch_batch_on",
     "mmcgb_session_launch_repeat", "mmcgb_grid_info", "mmcgb_check_config",
-    "mmcgb_session_device_buffers", "mmcgb_l2_read_bandwidth",
+    "mmcgb_session_device_buffers", "mmcgb_l2_read_bandwidth", "mmcgb_session_phase_window",
 ]
 
 
@@ -128,12 +128,15 @@ def load():
         lib.mmcgb_session_launch_batch_on.argtypes = [C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
                                                       C.POINTER(C.c_uint64), C.c_void_p]
         lib.mmcgb_session_launch_repeat.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32]
+        lib.mmcgb_session_phase_window.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(C.c_int32),
+                                                    C.POINTER(C.c_uint64)]
         lib.mmcgb_l2_read_bandwidth.argtypes = [C.c_int32, C.c_uint64, C.c_int32, C.POINTER(C.c_double)]
         lib.mmcgb_session_device_buffers.argtypes = [C.c_void_p, C.POINTER(DeviceOut)]
         lib.mmcgb_check_config.argtypes = [C.POINTER(MeshDesc), C.POINTER(Config), C.POINTER(C.c_int32)]
         lib.mmcgb_grid_info.argtypes = [C.c_void_p, C.c_float, C.POINTER(C.c_int32), C.POINTER(C.c_float)]
         for name in ("mmcgb_session_launch_batch", "mmcgb_session_launch_batch_on", "mmcgb_session_launch_repeat",
-                     "mmcgb_grid_info", "mmcgb_check_config", "mmcgb_session_device_buffers", "mmcgb_l2_read_bandwidth", "mmcgb_prepare_host", "mmcgb_normalize_host", "mmcgb_session_begin", "mmcgb_session_launch", "mmcgb_session_sync", "mmcgb_session_end",
+                     "mmcgb_grid_info", "mmcgb_check_config", "mmcgb_session_device_buffers", "mmcgb_l2_read_bandwidth", "mmcgb_session_phase_window",
+                     "mmcgb_prepare_host", "mmcgb_normalize_host", "mmcgb_session_begin", "mmcgb_session_launch", "mmcgb_session_sync", "mmcgb_session_end",
                      "mmcgb_mesh_create", "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export",
                      "mmcgb_mesh_locate", "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run"):
             getattr(lib, name).restype = C.c_int32

@@ -187,6 +187,7 @@ class SimConfig:
     maxjumpdebug: int = 0                       # > 0: save up to this many trajectory records
     method: object = "elem"                     # "elem" (element output) or "grid" (dual-grid, DMMC)
     gridstep: float = 1.0                       # voxel edge of the grid output (mm)
+    phase_chunk: int = 0                        # max photons per gate-phased launch (0: what memory holds)
     accumulate: int = 0                         # 1: add into the caller's field/dref (mmc_run_cu's +=)
     save_field: bool = True
 
@@ -213,6 +214,7 @@ class SimConfig:
             c.srcpattern = _ptr(pat)
         c.issaveref = int(self.issaveref)
         c.maxjumpdebug = int(self.maxjumpdebug)
+        c.phase_chunk = int(self.phase_chunk)
         c.accumulate = int(self.accumulate)
         m = self.method
         c.method = {"elem": 0, "grid": 1}[m] if isinstance(m, str) else int(m)
@@ -424,6 +426,18 @@ class Session:
         """`repeats` launches of `nphoton` photons as one CUDA graph
         (mmcgb_session_launch_repeat); sync() then times the whole graph."""
         N.check(N.load().mmcgb_session_launch_repeat(self._h, int(photon_offset), int(nphoton), int(repeats)))
+
+    def phase_window(self, nphoton: int) -> int:
+        """The gate window a launch of `nphoton` photons runs with (0 = one
+        launch; mmcgb_session_phase_window)."""
+        return self.phase_plan(nphoton)[0]
+
+    def phase_plan(self, nphoton: int):
+        """(gate window, photons per phased launch) of a launch of `nphoton`
+        photons (mmcgb_session_phase_window)."""
+        w, ch = C.c_int32(), C.c_uint64()
+        N.check(N.load().mmcgb_session_phase_window(self._h, int(nphoton), C.byref(w), C.byref(ch)))
+        return int(w.value), int(ch.value)
 
     @property
     def stream(self) -> int:

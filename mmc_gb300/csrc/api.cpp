@@ -688,66 +688,96 @@ int32_t mmcgb_session_begin(mmcgb_mesh* mesh, const mmcgb_config* cfg, mmcgb_res
 
 namespace {
 
-// Whether a launch of `nphoton` photons of this session runs gate-phased
-// (mmcgb_config.phased); sets up the queues and the window when it does.
-// Automatic windows keep the live gate planes (window + 1 of them) within
-// about 90% of the L2: measured on the 1.296M-tet, 50-gate benchmark
-// (10.4 MB planes, photons resumed in spatial order), windows of 6 and 10
-// gates trace 1e8 photons at 77.7k and 78.2k photons/ms against 59.4k in one
-// launch; before the spatial order, 5, 10 and 17 gates ran at 74.7k, 75.3k
-// and 71.5k, and 1 gate (parking every photon at every gate) at 59.9k.
-// Returns a status.
-int phased_setup(mmcgb_session* s, uint64_t nphoton, bool* use) {
-    *use = false;
+// The window of automatic gate phasing: the live gate planes (window + 1 of
+// them) fill about 70% of the L2, leaving the rest to the tet records.
+// Measured on the 1.296M-tet, 50-gate benchmark (10.4 MB planes, photons
+// resumed in spatial order, 1e8 photons): windows of 5, 6, 7, 8, 9, 10 and 12
+// gates ran at 103.0k, 103.8k, 104.2k, 104.4k, 104.4k, 103.4k and 95.9k
+// photons/ms (one launch: 59.4k).
+int auto_window(int device, size_t plane_bytes) {
+    int l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, device);
+    return std::max(1, (int)(0.75 * (double)l2 / (double)plane_bytes) - 1);
+}
+
+// How a launch of `nphoton` photons of this session is traced: `span` gates
+// per phased launch (0 = one unphased launch) and `chunk` photons per phased
+// launch.  Automatic phasing engages for >= 8 gates, >= 64 MB of fluence and
+// >= 4e6 photons.  The parked states of a phased launch's photons are
+// double-buffered queues (phase_bytes_per_photon each, plus a resume-order
+// index); when those for all the photons would not fit in half of the free
+// device memory the launch is split into phased launches of as many photons
+// as fit (mmcgb_config.phase_chunk caps them further).  Automatic phasing
+// needs >= 4e6 photons per such launch, else the launch runs unphased.
+struct PhasePlan {
+    int span = 0;
+    uint64_t chunk = 0;
+};
+
+PhasePlan phase_plan(const mmcgb_session* s, uint64_t nphoton) {
+    PhasePlan plan;
     const mmcgb_config& c = s->cfg;
-    if (c.phased < 0 || c.replayseed || s->P.maxgate < 2) return MMCGB_OK;
-    const bool sorted = nphoton <= 0xFFFFFFFFull;
-    const size_t per = phase_bytes_per_photon(s->P.sim) + (sorted ? sizeof(unsigned) : 0);
-    const size_t need = per * nphoton + sizeof(unsigned) * 2 * kBuckets + 4096;
-    const size_t plane = s->P.flen / (size_t)s->P.maxgate * (c.accum_f64 ? 8 : 4);
-    if (c.phased > 0) {
-        s->pq_span = c.phased;
-    } else {
-        int l2 = 0;
-        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, s->mesh->device);
-        s->pq_span = std::max(1, (int)(0.9 * (double)l2 / (double)plane) - 1);
-    }
-    if (c.phased == 0) {
+    if (nphoton == 0 || c.phased < 0 || c.replayseed || s->P.maxgate < 2) return plan;
+    int span = c.phased;
+    if (span == 0) {
+        const size_t plane = s->P.flen / (size_t)s->P.maxgate * (c.accum_f64 ? 8 : 4);
+        span = auto_window(s->mesh->device, plane);
         const size_t fluence = s->P.flen * 8;
-        if (s->P.maxgate < 8 || fluence < ((size_t)64 << 20) || nphoton < 4000000ull ||
-            s->pq_span >= s->P.maxgate)
-            return MMCGB_OK;
-        if (nphoton > s->pq_cap && need > free_device_memory(s->mesh->device) / 2)
-            return MMCGB_OK;  // not enough room for the queues: trace in one launch
+        if (s->P.maxgate < 8 || fluence < ((size_t)64 << 20) || nphoton < 4000000ull || span >= s->P.maxgate)
+            return plan;
     }
-    if (nphoton > s->pq_cap) {
-        if (s->pq_mem) CK(cudaFreeAsync(s->pq_mem, s->stream));
-        s->pq_mem = nullptr;
-        s->pq_cap = 0;
-        cudaError_t e = cudaMallocAsync(&s->pq_mem, need, s->stream);
-        if (e != cudaSuccess) {
-            (void)cudaGetLastError();
-            return fail(MMCGB_E_NOMEM, "no device memory for the gate-phased queues");
+    uint64_t chunk = std::min<uint64_t>(nphoton, 0xFFFFFFFFull);  // the resume order holds 32-bit indices
+    if (c.phase_chunk > 0) chunk = std::min<uint64_t>(chunk, c.phase_chunk);
+    if (chunk > s->pq_cap) {
+        const size_t per = phase_bytes_per_photon(s->P.sim) + sizeof(unsigned);
+        const size_t fixed = sizeof(unsigned) * 2 * kBuckets + 16 * 256;
+        const size_t avail = free_device_memory(s->mesh->device) / 2;
+        const uint64_t fit = avail > fixed ? (uint64_t)((avail - fixed) / per) : 0;
+        if (fit < chunk) {
+            // a forced window still tries a modest queue (and reports E_NOMEM if even that fails)
+            chunk = std::max<uint64_t>({fit, s->pq_cap, c.phased > 0 ? std::min<uint64_t>(nphoton, 1u << 20) : 0});
         }
-        s->pq_cap = nphoton;
-        const SimDev& sim = s->P.sim;
-        const bool want_seed = sim.issavedet && sim.seeds;
-        char* p = static_cast<char*>(s->pq_mem);
-        auto take = [&](size_t bytes) {
-            char* r = p;
-            p += (bytes + 255) & ~(size_t)255;
-            return r;
-        };
-        for (int i = 0; i < 2; i++) {
-            s->pq[i].rec = reinterpret_cast<PState*>(take(sizeof(PState) * nphoton));
-            s->pq[i].ppath = sim.issavedet ? reinterpret_cast<float*>(take(sizeof(float) * sim.reclen * nphoton)) : nullptr;
-            s->pq[i].seed0 = want_seed ? reinterpret_cast<unsigned long long*>(take(16 * nphoton)) : nullptr;
-            s->pq[i].count = reinterpret_cast<unsigned long long*>(take(sizeof(unsigned long long)));
-        }
-        s->pq_order = sorted ? reinterpret_cast<unsigned*>(take(sizeof(unsigned) * nphoton)) : nullptr;
-        s->pq_bucket = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * 2 * kBuckets));
     }
-    *use = true;
+    if (chunk == 0 || (c.phased == 0 && chunk < 4000000ull)) return plan;
+    const uint64_t parts = (nphoton + chunk - 1) / chunk;
+    plan.chunk = (nphoton + parts - 1) / parts;  // equal parts
+    plan.span = span;
+    return plan;
+}
+
+// Allocates the gate-phased queues for `chunk` photons per launch (kept for
+// later launches that need no more).  Returns a status.
+int phased_setup(mmcgb_session* s, const PhasePlan& plan) {
+    s->pq_span = plan.span;
+    const uint64_t n = plan.chunk;
+    if (n <= s->pq_cap) return MMCGB_OK;
+    const size_t per = phase_bytes_per_photon(s->P.sim) + sizeof(unsigned);
+    const size_t need = per * n + sizeof(unsigned) * 2 * kBuckets + 16 * 256;
+    if (s->pq_mem) CK(cudaFreeAsync(s->pq_mem, s->stream));
+    s->pq_mem = nullptr;
+    s->pq_cap = 0;
+    cudaError_t e = cudaMallocAsync(&s->pq_mem, need, s->stream);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return fail(MMCGB_E_NOMEM, "no device memory for the gate-phased queues");
+    }
+    s->pq_cap = n;
+    const SimDev& sim = s->P.sim;
+    const bool want_seed = sim.issavedet && sim.seeds;
+    char* p = static_cast<char*>(s->pq_mem);
+    auto take = [&](size_t bytes) {
+        char* r = p;
+        p += (bytes + 255) & ~(size_t)255;
+        return r;
+    };
+    for (int i = 0; i < 2; i++) {
+        s->pq[i].rec = reinterpret_cast<PState*>(take(sizeof(PState) * n));
+        s->pq[i].ppath = sim.issavedet ? reinterpret_cast<float*>(take(sizeof(float) * sim.reclen * n)) : nullptr;
+        s->pq[i].seed0 = want_seed ? reinterpret_cast<unsigned long long*>(take(16 * n)) : nullptr;
+        s->pq[i].count = reinterpret_cast<unsigned long long*>(take(sizeof(unsigned long long)));
+    }
+    s->pq_order = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * n));
+    s->pq_bucket = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * 2 * kBuckets));
     return MMCGB_OK;
 }
 
@@ -765,15 +795,23 @@ int32_t mmcgb_session_launch(mmcgb_session* s, uint64_t photon_offset, uint64_t 
     SimDev sim = s->P.sim;
     sim.nphoton = nphoton;
     sim.photon_offset = s->cfg.photon_offset + photon_offset;
-    bool phased = false;
-    const int rc = phased_setup(s, nphoton, &phased);
-    if (rc) return rc;
+    const PhasePlan plan = phase_plan(s, nphoton);
+    if (plan.span > 0) {
+        const int rc = phased_setup(s, plan);
+        if (rc) return rc;
+    }
     CK(cudaEventRecord(s->ev0, s->stream));
-    if (phased)
-        CK(launch_phased(sim, s->work, s->shape, s->stream, s->pq, s->pq_span, s->pq_order, s->pq_bucket,
-                         s->mesh->lo, s->mesh->hi));
-    else
+    if (plan.span > 0) {
+        for (uint64_t off = 0; off < nphoton; off += plan.chunk) {  // photon ranges whose queues fit
+            SimDev part = sim;
+            part.photon_offset = sim.photon_offset + off;
+            part.nphoton = std::min<uint64_t>(plan.chunk, nphoton - off);
+            CK(launch_phased(part, s->work, s->shape, s->stream, s->pq, s->pq_span, s->pq_order, s->pq_bucket,
+                             s->mesh->lo, s->mesh->hi));
+        }
+    } else {
         CK(launch_plain(sim, s->work, s->shape, s->stream));
+    }
     CK(cudaEventRecord(s->ev1, s->stream));
     s->launched += nphoton;
     s->launches++;
@@ -942,6 +980,15 @@ int32_t mmcgb_session_launch_repeat(mmcgb_session* s, uint64_t photon_offset, ui
 }
 
 void* mmcgb_session_stream(mmcgb_session* s) { return s ? (void*)s->stream : nullptr; }
+
+int32_t mmcgb_session_phase_window(mmcgb_session* s, uint64_t nphoton, int32_t* window, uint64_t* chunk) {
+    if (!s || !window) return fail(MMCGB_E_ARG, "null argument");
+    CK(cudaSetDevice(s->mesh->device));
+    const PhasePlan plan = phase_plan(s, nphoton);
+    *window = plan.span;
+    if (chunk) *chunk = plan.chunk;
+    return MMCGB_OK;
+}
 
 int32_t mmcgb_session_device_buffers(mmcgb_session* s, mmcgb_device_out* out) {
     if (!s || !out) return fail(MMCGB_E_ARG, "null argument");

@@ -116,7 +116,7 @@ struct FastMath {
     static constexpr bool kFast = true;
 };
 
-__device__ __forceinline__ int decode_nb(int w) { return (w << 8) >> 8; }
+__device__ __forceinline__ int decode_nb(int w) { return (w << (32 - kNbBits)) >> (32 - kNbBits); }
 
 // Morton index of the bounding-box grid cell holding p (cells clamped to the grid).
 __device__ __forceinline__ unsigned spatial_key(float px, float py, float pz, const PhaseArgs& pa) {
@@ -169,7 +169,7 @@ __global__ void k_bucket_order(const PState* rec, const unsigned long long* coun
         if (slot < n) order[slot] = (unsigned)i;
     }
 }
-__device__ __forceinline__ int decode_label(int w) { return (int)((unsigned)w >> 24); }
+__device__ __forceinline__ int decode_label(int w) { return (int)((unsigned)w >> kNbBits); }
 
 __device__ __forceinline__ void deposit(const SimDev& S, unsigned idx, float val) {
     if (S.accum_f64) {

@@ -17,7 +17,8 @@ enum Boundary { BC_NOREFLECT = 0, BC_REFLECT = 1, BC_ABSORBEXT = 2, BC_MIRROR = 
 
 constexpr int kMaxMedia = 64;        // media rows (incl. background) staged in shared memory
 constexpr int kMaxSimsShared = 256;  // simulations whose media tables fit in one block's shared memory
-constexpr int kNbBits = 24;          // neighbour id bits in a packed face word
+constexpr int kNbBits = 26;          // neighbour id bits in a packed face word (the label takes 6)
+constexpr int kMaxLabel = 63;        // medium labels a packed face word holds (kMaxMedia - 1)
 constexpr int kMaxElem = (1 << (kNbBits - 1)) - 1;
 // Fluence cells (gates x elements or voxels) one simulation may hold: deposit indices are
 // 32-bit and 0x7FFFFFFF marks "no pending deposit", so every index stays below it.
@@ -27,8 +28,8 @@ constexpr unsigned kMaxFluenceCells = 0x7FFFFFFFu;
 //   nx/ny/nz/nd : outward unit normals and plane offsets of the 4 faces
 //                 (face k of the reference normal table, src/mmc_mesh.c:1572-1601)
 //   nb          : for each face in neighbour order (src/mmc_highorder.cpp:50),
-//                 bits 0..23 = neighbour element (1-based, signed: <=0 is an
-//                 exterior face numbered -1,-2,...), bits 24..31 = the
+//                 bits 0..25 = neighbour element (1-based, signed: <=0 is an
+//                 exterior face numbered -1,-2,...), bits 26..31 = the
 //                 neighbour's medium label (0 for exterior faces).
 struct __align__(16) TetRec {
     float4 nx, ny, nz, nd;

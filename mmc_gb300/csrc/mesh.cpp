@@ -78,7 +78,7 @@ int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
         return MMCGB_E_ARG;
     }
     if (d.ne > kMaxElem) {
-        err = "mesh has more elements than the packed record format holds (8,388,607)";
+        err = "mesh has more elements than the packed record format holds (" + std::to_string(kMaxElem) + ")";
         return MMCGB_E_MESH;
     }
     m.nn = d.nn;
@@ -94,8 +94,9 @@ int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
         // void (mesh_srcdetelem, src/mmc_mesh.c:390-425); sources are located here by a
         // search over all elements, so such a tet is simply void
         if (m.label[i] == -1) m.label[i] = 0;
-        if (m.label[i] < 0 || m.label[i] > 255) {
-            err = "medium labels must be in -1..255 (-2, wide-field detector elements, is not supported)";
+        if (m.label[i] < 0 || m.label[i] > kMaxLabel) {
+            err = "medium labels must be in -1.." + std::to_string(kMaxLabel) +
+                  " (-2, wide-field detector elements, is not supported)";
             return MMCGB_E_MESH;
         }
         maxlabel = std::max(maxlabel, m.label[i]);
@@ -186,7 +187,7 @@ void pack_records(const HostMesh& m, std::vector<TetRec>& rec) {
         for (int j = 0; j < 4; j++) {
             const int nbid = m.facenb[4 * (size_t)i + j];
             const int lab = (nbid > 0) ? m.label[nbid - 1] : 0;
-            w[j] = (int)(((uint32_t)nbid & 0x00FFFFFFu) | ((uint32_t)lab << 24));
+            w[j] = (int)(((uint32_t)nbid & ((1u << kNbBits) - 1u)) | ((uint32_t)lab << kNbBits));
         }
         r.nb = make_int4(w[0], w[1], w[2], w[3]);
     }

@@ -15,18 +15,19 @@ import pytest
 
 import golden_checks as gc
 from mmc_gb300 import meshgen
-from mmc_gb300.core import Mesh, SimConfig, simulate
+from mmc_gb300.core import Mesh, Session, SimConfig, simulate
 
 pytestmark = pytest.mark.gpu
 
 
-def auto_window(ne, accum_f64=True):
-    """The gate window the automatic phased mode picks: the live planes
-    (window + 1) fill about 90% of the L2."""
-    import torch
-    l2 = torch.cuda.get_device_properties(0).L2_cache_size
-    plane = ne * (8 if accum_f64 else 4)
-    return max(1, int(0.9 * l2 / plane) - 1)
+def auto_window(mesh, cfg, nphoton=100_000_000):
+    """The gate window the automatic phased mode picks for a launch of the
+    benchmark's size (1e8 photons)."""
+    s = Session(mesh, dataclasses.replace(cfg, phased=0))
+    try:
+        return s.phase_window(nphoton)
+    finally:
+        s.end(collect=False)
 
 
 @pytest.fixture(scope="module")
@@ -35,9 +36,11 @@ def c1(gpu_ready):
     fx = gc.load("c1_incl1296k")
     cfg = SimConfig(media=m.media, nphoton=int(fx["photons"]), seed=9001, srcpos=(30.0, 30.0, 0.0),
                     srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=1e-10, issavedet=1, detpos=meshgen.c1_detectors(),
-                    maxdetphoton=2_000_000, basisorder=0, isnormalized=0, fast_math=1, accum_f64=1,
-                    phased=auto_window(m.ne))
-    return m, Mesh(m.node, m.elem, m.label), cfg, fx
+                    maxdetphoton=2_000_000, basisorder=0, isnormalized=0, fast_math=1, accum_f64=1)
+    mesh = Mesh(m.node, m.elem, m.label)
+    window = auto_window(mesh, cfg)
+    assert 1 <= window < 50
+    return m, mesh, dataclasses.replace(cfg, phased=window), fx
 
 
 def test_inclusion_cube_1296k_matches_reference_runs(c1):
@@ -57,7 +60,8 @@ def test_inclusion_cube_1296k_float32_vs_float64_accumulation(c1):
     float64 on the same photons of the benchmark workload: the per-cell error."""
     m, mesh, cfg, fx = c1
     a = simulate(mesh, cfg).field
-    b = simulate(mesh, dataclasses.replace(cfg, accum_f64=0, phased=auto_window(m.ne, False))).field
+    c32 = dataclasses.replace(cfg, accum_f64=0)
+    b = simulate(mesh, dataclasses.replace(c32, phased=auto_window(mesh, c32))).field
     nz = a > 1e-6 * a.max()
     rel = np.abs(b[nz] - a[nz]) / a[nz]
     tot = abs(b.sum() - a.sum()) / a.sum()

@@ -82,3 +82,54 @@ def test_bad_meshes_are_rejected(gpu_ready):
     with pytest.raises(_native.MmcgbError) as e:
         Mesh(m.node, m.elem, lab)
     assert e.value.code == 3
+
+
+def test_phased_launch_split_by_queue_memory(full_mesh):
+    """A gate-phased launch whose parked-photon queues would not fit is traced as
+    several phased launches over consecutive photon ranges (mmcgb_config.phase_chunk
+    forces the split here): the same photons, the same results."""
+    m, mesh = full_mesh
+    cfg = _cfg(m, nphoton=3_000_000, phased=8, issaveseed=1)
+    s = Session(mesh, cfg)
+    try:
+        assert s.phase_plan(cfg.nphoton) == (8, 3_000_000)
+    finally:
+        s.end(collect=False)
+    one = simulate(mesh, cfg)
+    split_cfg = dataclasses.replace(cfg, phase_chunk=1_100_000)
+    s = Session(mesh, split_cfg)
+    try:
+        assert s.phase_plan(cfg.nphoton) == (8, 1_000_000)  # three equal launches
+    finally:
+        s.end(collect=False)
+    split = simulate(mesh, split_cfg)
+    np.testing.assert_allclose(split.field, one.field, rtol=1e-9, atol=1e-12)
+    assert split.raytet == one.raytet and split.detected == one.detected
+    rows = lambda d, sd: sorted(map(bytes, np.concatenate([d.view(np.uint8).reshape(len(d), -1), sd], 1)))  # noqa: E731
+    assert rows(split.detp, split.seeds) == rows(one.detp, one.seeds)
+
+
+def test_automatic_phasing_plan_of_the_benchmark_job(full_mesh):
+    """The benchmark job (1e8 photons, 50 gates, float64) is traced gate-phased
+    in one set of window launches when its queues fit; automatic phasing keeps
+    at least 4e6 photons per launch and otherwise runs unphased."""
+    m, mesh = full_mesh
+    cfg = _cfg(m, nphoton=100_000_000, issaveseed=0, maxdetphoton=2_000_000)
+    s = Session(mesh, cfg)
+    try:
+        w, chunk = s.phase_plan(100_000_000)
+        assert 1 <= w < 50 and chunk == 100_000_000
+        assert s.phase_plan(3_000_000) == (0, 0)  # too few photons to phase
+        s2 = Session(mesh, dataclasses.replace(cfg, phase_chunk=30_000_000))
+        try:
+            assert s2.phase_plan(100_000_000) == (w, 25_000_000)
+            assert s2.phase_plan(10_000_000) == (w, 10_000_000)
+        finally:
+            s2.end(collect=False)
+        s3 = Session(mesh, dataclasses.replace(cfg, phase_chunk=3_000_000))
+        try:
+            assert s3.phase_plan(100_000_000) == (0, 0)  # launches below 4e6 photons run unphased
+        finally:
+            s3.end(collect=False)
+    finally:
+        s.end(collect=False)

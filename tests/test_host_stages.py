@@ -57,7 +57,7 @@ def test_oversized_mesh_rejected_before_any_gpu_work():
     elem = np.ones((4, 4), np.int32)
     lab = np.ones(4, np.int32)
     d, keep = core._desc(node, elem, lab)
-    d.ne = 9_000_000  # beyond the 24-bit neighbour field of the packed records
+    d.ne = 34_000_000  # beyond the 26-bit neighbour field of the packed records (33,554,431)
     rc = _native.load().mmcgb_prepare_host(d, None, None, None, None, None, None)
     assert rc == 3
 
