@@ -727,8 +727,10 @@ PhasePlan phase_plan(const mmcgb_session* s, uint64_t nphoton) {
             return plan;
     }
     uint64_t chunk = std::min<uint64_t>(nphoton, 0xFFFFFFFFull);  // the resume order holds 32-bit indices
-    if (c.phase_chunk > 0) chunk = std::min<uint64_t>(chunk, c.phase_chunk);
-    if (chunk > s->pq_cap) {
+    // per-photon trace outputs are indexed by the photon's place in its kernel launch: one launch
+    const bool traced = s->P.buf.pw || s->P.buf.ps || s->P.buf.pd;
+    if (c.phase_chunk > 0 && !traced) chunk = std::min<uint64_t>(chunk, c.phase_chunk);
+    if (chunk > s->pq_cap && !traced) {
         const size_t per = phase_bytes_per_photon(s->P.sim) + sizeof(unsigned);
         const size_t fixed = sizeof(unsigned) * 2 * kBuckets + 16 * 256;
         const size_t avail = free_device_memory(s->mesh->device) / 2;

@@ -287,4 +287,4 @@ def test_replay_loss_autograd_function(gpu_ready):
             vals.append(float(rp.ReplayLoss.apply(mesh, cfg, c, t, mus.detach())))
         fd = (vals[0] - vals[1]) / (2 * d)
         g = float(mua.grad[k])
-        assert g == pytest.approx(fd, rel=5e-3, abs=1e-4 * abs(float(L)) + 1e-6), (k, g, fd)
+        assert g == pytest.approx(fd, rel=5e-3, abs=1e-4 * abs(float(L.detach())) + 1e-6), (k, g, fd)
