@@ -162,6 +162,9 @@ def main():
                     help="plain: the 1.3M-tet benchmark (default); batched / serving / replay: the batched, "
                          "continuous-batching and differentiation workloads (one JSON line each)")
     ap.add_argument("--requests", type=int, default=64, help="serving: number of requests")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="plain runs: leave out the batched / serving / replay summaries (run at N=1 after the "
+                         "timed steps, under 'forms')")
     args = ap.parse_args()
     if args.workload != "plain":
         from mmc_gb300 import workloads
@@ -194,6 +197,7 @@ def main():
     m, cfg = workload_config(nps)
     cfg = dataclasses.replace(cfg, fast_math=0 if args.exact else 1)
     mesh = Mesh(m.node, m.elem, m.label, device=local_rank)
+    ne, nn = mesh.ne, mesh.nn
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local_rank}")
 
     def barrier():
@@ -313,6 +317,14 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(m, cfg)
 
+    # ---- the batched, serving and differentiation forms (N = 1, after everything timed above) ----
+    forms = None
+    if world == 1 and not args.no_forms:
+        mesh = flush = out = None  # free the benchmark's device memory first
+        torch.cuda.empty_cache()
+        from mmc_gb300 import workloads
+        forms = workloads.summaries(args)
+
     if rank == 0:
         line = {
             "metric": "photons/ms", "value": value, "unit": "photons/ms", "n_gpus": world, "steps": args.steps,
@@ -320,7 +332,7 @@ def main():
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (f64 fluence accumulation, %s)" % ("IEEE" if args.exact else "fast math"),
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "ne": mesh.ne, "nn": mesh.nn, "photons_per_step": nps,
+            "config": {"workload": WORKLOAD, "ne": ne, "nn": nn, "photons_per_step": nps,
                        "job_photons": JOB_PHOTONS, "gates": 50, "detectors": 4, "savedet": True,
                        "l2": "flushed (256 MB write) before each timed step",
                        "tracing": f"gate-phased, automatic window of {window} gates (the live gate planes "
@@ -340,6 +352,7 @@ def main():
             "e2e_dropin": e2e_dropin,
             "gpu_launches": args.steps * launches_per_step,
             "clocks": clocks,
+            "forms": forms,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

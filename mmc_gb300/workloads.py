@@ -101,7 +101,7 @@ def run_batched(args):
             "autotune": {k: v for k, v in tune.items() if k != "trials"}, "data": "synthetic", "clocks": clk,
             "config": {"mesh": "4-layer shells 1.296M tets", "sims": 256, "gates": 10,
                        "timing": "wall clock through simulate()/simulate_batch(), host buffers included"}}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_serving(args):
@@ -172,7 +172,7 @@ def run_serving(args):
             "serial_p99_ms": float(np.percentile(np.array(lat) * 1e3, 99)), "photons": photons, "data": "synthetic",
             "clocks": clk,
             "config": {"arrival_rate_hz": 200, "photons": "log-uniform 1e5-1e8", "gates": 10, "fluence": "float32"}}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_replay(args):
@@ -201,8 +201,28 @@ def run_replay(args):
             "grad_mua_norm": float(np.linalg.norm(gmua)), "grad_mus_norm": float(np.linalg.norm(gmus)),
             "data": "synthetic", "clocks": clk,
             "config": {"mesh": "4-layer shells 1.296M tets", "photons": 10_000_000}}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run(args):
-    {"batched": run_batched, "serving": run_serving, "replay": run_replay}[args.workload](args)
+    line = {"batched": run_batched, "serving": run_serving, "replay": run_replay}[args.workload](args)
+    print(json.dumps(line), flush=True)
+
+
+def summaries(args) -> dict:
+    """The three forms in brief, for the default benchmark line: each runs
+    its full workload and keeps the figures that compare it with serial
+    plain launches (a failure is reported in place of its figures)."""
+    keep = {"batched": ("value", "unit", "speedup_vs_serial_plain", "speedup_vs_serial_plain_kernel_only",
+                        "serial_plain_photons_per_ms", "photons", "autotune", "clocks"),
+            "serving": ("value", "unit", "speedup_vs_serial_plain", "serial_plain_photons_per_ms", "p50_ms", "p99_ms",
+                        "serial_p50_ms", "serial_p99_ms", "requests", "waves", "photons", "clocks"),
+            "replay": ("value", "unit", "forward_photons_per_ms", "detected", "replayed", "backward_s", "clocks")}
+    out = {}
+    for name, fn in (("batched", run_batched), ("serving", run_serving), ("replay", run_replay)):
+        try:
+            line = fn(args)
+            out[name] = {"metric": line["metric"], **{k: line[k] for k in keep[name] if k in line}}
+        except Exception as e:  # reported, so the benchmark line is still printed
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+    return out
