@@ -80,7 +80,7 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     for f in cpp:
         o = os.path.join(BUILDDIR, f + ".o")
         objs.append(o)
-        jobs.append(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-std=c++17", "-Wall",
+        jobs.append(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-std=c++17", "-pthread", "-Wall",
                      "-I" + os.path.join(cuda, "include"), "-c", os.path.join(CSRC, f), "-o", o])
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         logs = list(ex.map(_run, jobs))
@@ -88,7 +88,7 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
         for lg in logs:
             sys.stdout.write(lg)
     tmp = out + ".tmp"
-    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
+    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-Xcompiler", "-pthread"])
     os.replace(tmp, out)
     return out
 

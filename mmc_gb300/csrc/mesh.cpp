@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
 
 namespace mmcgb {
 
@@ -27,47 +28,73 @@ inline F3 node_at(const std::vector<float>& node, int i) {
     return F3{node[3 * (size_t)i], node[3 * (size_t)i + 1], node[3 * (size_t)i + 2]};
 }
 
+// Runs body(begin, end) over [0, n) split into contiguous ranges, one per
+// hardware thread (at most 16); small ranges run on the calling thread.
+template <class F>
+void parallel_ranges(size_t n, F body) {
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const size_t nt = std::min<size_t>(hw, std::max<size_t>(1, n / 65536));
+    if (nt <= 1) {
+        body((size_t)0, n);
+        return;
+    }
+    std::vector<std::thread> pool;
+    pool.reserve(nt - 1);
+    for (size_t t = 1; t < nt; t++) pool.emplace_back(body, n * t / nt, n * (t + 1) / nt);
+    body((size_t)0, n / nt);
+    for (std::thread& th : pool) th.join();
+}
+
 // Face neighbours (src/mmc_highorder.cpp:128-159): element faces are matched by
-// their sorted node triple; facenb[4e+j] is the element sharing face j.
+// their sorted node triple; facenb[4e+j] is the element sharing face j.  The
+// faces are ordered by (smallest node, middle node, largest node, face slot):
+// a counting sort on the smallest node, then each node's short list sorted on
+// its own; runs of equal triples pair up in that order (first with second,
+// third with fourth, ...).
 void compute_facenb(int nn, int ne, const std::vector<int>& elem, std::vector<int>& facenb) {
     const size_t nface = (size_t)ne * 4;
     facenb.assign(nface, 0);
-    struct Key {
-        uint64_t hi;
-        uint32_t lo;
-        uint32_t slot;
-    };
-    std::vector<Key> keys(nface);
-    const bool packed = nn < (1 << 21);
-    for (int i = 0; i < ne; i++)
-        for (int j = 0; j < 4; j++) {
-            int v[3] = {elem[4 * (size_t)i + kFaceList[j][0]], elem[4 * (size_t)i + kFaceList[j][1]],
-                        elem[4 * (size_t)i + kFaceList[j][2]]};
-            std::sort(v, v + 3);
-            Key& k = keys[4 * (size_t)i + j];
-            if (packed) {
-                k.hi = ((uint64_t)v[0] << 42) | ((uint64_t)v[1] << 21) | (uint64_t)v[2];
-                k.lo = 0;
-            } else {
-                k.hi = ((uint64_t)(uint32_t)v[0] << 32) | (uint32_t)v[1];
-                k.lo = (uint32_t)v[2];
+    std::vector<int> tri(3 * nface);
+    parallel_ranges((size_t)ne, [&](size_t b, size_t e) {
+        for (size_t i = b; i < e; i++)
+            for (int j = 0; j < 4; j++) {
+                int* v = &tri[3 * (4 * i + j)];
+                v[0] = elem[4 * i + kFaceList[j][0]];
+                v[1] = elem[4 * i + kFaceList[j][1]];
+                v[2] = elem[4 * i + kFaceList[j][2]];
+                std::sort(v, v + 3);
             }
-            k.slot = (uint32_t)(4 * (size_t)i + j);
-        }
-    std::sort(keys.begin(), keys.end(), [](const Key& a, const Key& b) {
-        if (a.hi != b.hi) return a.hi < b.hi;
-        if (a.lo != b.lo) return a.lo < b.lo;
-        return a.slot < b.slot;
     });
-    for (size_t n = 0; n + 1 < nface; n++) {
-        const Key& a = keys[n];
-        const Key& b = keys[n + 1];
-        if (a.hi == b.hi && a.lo == b.lo) {
-            facenb[a.slot] = (int)(b.slot >> 2) + 1;
-            facenb[b.slot] = (int)(a.slot >> 2) + 1;
-            n++;
-        }
+    std::vector<uint32_t> start((size_t)nn + 2, 0);
+    for (size_t f = 0; f < nface; f++) start[(size_t)tri[3 * f] + 1]++;
+    for (size_t i = 1; i < start.size(); i++) start[i] += start[i - 1];
+    std::vector<uint32_t> order(nface);
+    {
+        std::vector<uint32_t> fill(start.begin(), start.end() - 1);
+        for (size_t f = 0; f < nface; f++) order[fill[(size_t)tri[3 * f]]++] = (uint32_t)f;  // ascending slots
     }
+    parallel_ranges((size_t)nn + 1, [&](size_t b, size_t e) {
+        for (size_t v0 = b; v0 < e; v0++) {
+            uint32_t* lo = order.data() + start[v0];
+            uint32_t* hi = order.data() + start[v0 + 1];
+            std::sort(lo, hi, [&](uint32_t a, uint32_t c) {
+                const int* ta = &tri[3 * (size_t)a];
+                const int* tc = &tri[3 * (size_t)c];
+                if (ta[1] != tc[1]) return ta[1] < tc[1];
+                if (ta[2] != tc[2]) return ta[2] < tc[2];
+                return a < c;
+            });
+            for (uint32_t* q = lo; q + 1 < hi; q++) {
+                const int* ta = &tri[3 * (size_t)q[0]];
+                const int* tb = &tri[3 * (size_t)q[1]];
+                if (ta[1] == tb[1] && ta[2] == tb[2]) {
+                    facenb[q[0]] = (int)(q[1] >> 2) + 1;
+                    facenb[q[1]] = (int)(q[0] >> 2) + 1;
+                    q++;
+                }
+            }
+        }
+    });
 }
 
 }  // namespace
@@ -141,9 +168,10 @@ int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
     }
     // outward unit normals and plane offsets (src/mmc_mesh.c:1572-1601)
     m.normals.assign(16 * (size_t)d.ne, 0.f);
-    for (int i = 0; i < d.ne; i++) {
-        float* vn = &m.normals[16 * (size_t)i];
-        const int* e = &m.elem[4 * (size_t)i];
+    parallel_ranges((size_t)d.ne, [&](size_t b, size_t end) {
+    for (size_t i = b; i < end; i++) {
+        float* vn = &m.normals[16 * i];
+        const int* e = &m.elem[4 * i];
         for (int j = 0; j < 4; j++) {
             F3 a = node_at(m.node, e[kOut[j][0]] - 1);
             F3 b = node_at(m.node, e[kOut[j][1]] - 1);
@@ -161,6 +189,7 @@ int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
             vn[j + 12] = n.x * a.x + n.y * a.y + n.z * a.z;
         }
     }
+    });
     // exterior faces numbered -1,-2,... (src/mmc_mesh.c:1466-1474)
     int nf = 0;
     for (size_t i = 0; i < m.facenb.size(); i++)
@@ -176,8 +205,9 @@ int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
 
 void pack_records(const HostMesh& m, std::vector<TetRec>& rec) {
     rec.resize(m.ne);
-    for (int i = 0; i < m.ne; i++) {
-        const float* vn = &m.normals[16 * (size_t)i];
+    parallel_ranges((size_t)m.ne, [&](size_t b, size_t end) {
+    for (size_t i = b; i < end; i++) {
+        const float* vn = &m.normals[16 * i];
         TetRec& r = rec[i];
         r.nx = make_float4(vn[0], vn[1], vn[2], vn[3]);
         r.ny = make_float4(vn[4], vn[5], vn[6], vn[7]);
@@ -185,12 +215,13 @@ void pack_records(const HostMesh& m, std::vector<TetRec>& rec) {
         r.nd = make_float4(vn[12], vn[13], vn[14], vn[15]);
         int w[4];
         for (int j = 0; j < 4; j++) {
-            const int nbid = m.facenb[4 * (size_t)i + j];
+            const int nbid = m.facenb[4 * i + j];
             const int lab = (nbid > 0) ? m.label[nbid - 1] : 0;
             w[j] = (int)(((uint32_t)nbid & ((1u << kNbBits) - 1u)) | ((uint32_t)lab << kNbBits));
         }
         r.nb = make_int4(w[0], w[1], w[2], w[3]);
     }
+    });
 }
 
 // ---------------------------------------------------------------------------
@@ -216,38 +247,65 @@ void build_locator(HostMesh& m) {
         g.inv[d] = span > 0 ? res / span : 0.f;
     }
     const size_t nbin = (size_t)res * res * res;
-    std::vector<uint32_t> count(nbin + 1, 0);
-    auto bin_range = [&](int e, int b0[3], int b1[3]) {
-        float mn[3] = {1e30f, 1e30f, 1e30f}, mx[3] = {-1e30f, -1e30f, -1e30f};
-        for (int j = 0; j < 4; j++)
+    const size_t ne = (size_t)m.ne;
+    // bins spanned by each element's bounding box: x, y, z low, then x, y, z high
+    std::vector<int> br(6 * ne);
+    parallel_ranges(ne, [&](size_t b, size_t e_end) {
+        for (size_t e = b; e < e_end; e++) {
+            float mn[3] = {1e30f, 1e30f, 1e30f}, mx[3] = {-1e30f, -1e30f, -1e30f};
+            for (int j = 0; j < 4; j++)
+                for (int d = 0; d < 3; d++) {
+                    float v = m.node[3 * (size_t)(m.elem[4 * e + j] - 1) + d];
+                    mn[d] = std::min(mn[d], v);
+                    mx[d] = std::max(mx[d], v);
+                }
             for (int d = 0; d < 3; d++) {
-                float v = m.node[3 * (size_t)(m.elem[4 * (size_t)e + j] - 1) + d];
-                mn[d] = std::min(mn[d], v);
-                mx[d] = std::max(mx[d], v);
+                br[6 * e + d] = std::max(0, std::min(res - 1, (int)std::floor((mn[d] - g.lo[d]) * g.inv[d])));
+                br[6 * e + 3 + d] = std::max(0, std::min(res - 1, (int)std::floor((mx[d] - g.lo[d]) * g.inv[d])));
             }
-        for (int d = 0; d < 3; d++) {
-            b0[d] = std::max(0, std::min(res - 1, (int)std::floor((mn[d] - g.lo[d]) * g.inv[d])));
-            b1[d] = std::max(0, std::min(res - 1, (int)std::floor((mx[d] - g.lo[d]) * g.inv[d])));
         }
+    });
+    // Contiguous element chunks count and then fill their bins independently; chunk c's
+    // entries of a bin follow those of chunks < c, so every bin lists its elements in
+    // ascending order, as one pass over the elements would.  Per-chunk counts take at
+    // most 64 MB.
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    size_t nchunk = std::min<size_t>(hw, ((size_t)64 << 20) / (4 * nbin));
+    nchunk = std::max<size_t>(1, std::min<size_t>(nchunk, ne / 65536));
+    std::vector<std::vector<uint32_t>> cnt(nchunk, std::vector<uint32_t>(nbin, 0));
+    auto over_chunks = [&](auto body) {
+        std::vector<std::thread> pool;
+        for (size_t c = 1; c < nchunk; c++) pool.emplace_back(body, c);
+        body((size_t)0);
+        for (std::thread& th : pool) th.join();
     };
-    for (int e = 0; e < m.ne; e++) {
-        int b0[3], b1[3];
-        bin_range(e, b0, b1);
-        for (int z = b0[2]; z <= b1[2]; z++)
-            for (int y = b0[1]; y <= b1[1]; y++)
-                for (int x = b0[0]; x <= b1[0]; x++) count[((size_t)z * res + y) * res + x + 1]++;
+    auto for_bins = [&](size_t e, auto fn) {
+        const int* r = &br[6 * e];
+        for (int z = r[2]; z <= r[5]; z++)
+            for (int y = r[1]; y <= r[4]; y++)
+                for (int x = r[0]; x <= r[3]; x++) fn(((size_t)z * res + y) * res + x);
+    };
+    over_chunks([&](size_t c) {
+        std::vector<uint32_t>& k = cnt[c];
+        for (size_t e = ne * c / nchunk; e < ne * (c + 1) / nchunk; e++) for_bins(e, [&](size_t bin) { k[bin]++; });
+    });
+    g.start.assign(nbin + 1, 0);
+    uint32_t run = 0;
+    for (size_t bin = 0; bin < nbin; bin++) {
+        g.start[bin] = run;
+        for (size_t c = 0; c < nchunk; c++) {
+            const uint32_t k = cnt[c][bin];
+            cnt[c][bin] = run;  // this chunk's first slot in the bin
+            run += k;
+        }
     }
-    for (size_t i = 0; i < nbin; i++) count[i + 1] += count[i];
-    g.start = count;
-    g.items.assign(count[nbin], 0);
-    std::vector<uint32_t> fill(count.begin(), count.end() - 1);
-    for (int e = 0; e < m.ne; e++) {
-        int b0[3], b1[3];
-        bin_range(e, b0, b1);
-        for (int z = b0[2]; z <= b1[2]; z++)
-            for (int y = b0[1]; y <= b1[1]; y++)
-                for (int x = b0[0]; x <= b1[0]; x++) g.items[fill[((size_t)z * res + y) * res + x]++] = (uint32_t)e;
-    }
+    g.start[nbin] = run;
+    g.items.assign(run, 0);
+    over_chunks([&](size_t c) {
+        std::vector<uint32_t>& k = cnt[c];
+        for (size_t e = ne * c / nchunk; e < ne * (c + 1) / nchunk; e++)
+            for_bins(e, [&](size_t bin) { g.items[k[bin]++] = (uint32_t)e; });
+    });
 }
 
 static bool encloses(const HostMesh& m, int e, const float* p) {
