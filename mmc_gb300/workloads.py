@@ -83,9 +83,17 @@ def run_batched(args):
     results = simulate_batch([mesh] * len(cfgs), cfgs)
     batched_wall = time.perf_counter() - t0
     batched_ms = results[0].kernel_ms
-    clk = clocks.stop()
     absorbed = float(np.mean([r.absorbed_fraction for r in results]))
     del results
+    # size-aware scheduling: simulations of >= 4e6 photons on their own (gate-phased), chained on
+    # one stream; the others batched on a second stream (batching.simulate_many)
+    from mmc_gb300.batching import simulate_many
+    t0 = time.perf_counter()
+    results = simulate_many([mesh] * len(cfgs), cfgs)
+    scheduled_wall = time.perf_counter() - t0
+    n_solo = sum(1 for c in cfgs if c.nphoton >= 4_000_000)
+    del results
+    clk = clocks.stop()
     # the drop-in path as the reference runs it: every simulation prepares and uploads its mesh
     # (mmcgb_run, the counterpart of mmc_run_cu) -- serial wall time plus the measured mesh setup
     dropin_wall = serial_wall + len(cfgs) * mesh_s
@@ -95,6 +103,9 @@ def run_batched(args):
             "serial_plain_photons_per_ms": total / (serial_wall * 1e3),
             "speedup_vs_serial_plain_kernel_only": serial_ms / batched_ms,
             "speedup_vs_serial_dropin_with_mesh_setup": dropin_wall / batched_wall,
+            "scheduled_photons_per_ms": total / (scheduled_wall * 1e3),
+            "scheduled_speedup_vs_serial_plain": serial_wall / scheduled_wall,
+            "scheduled_wall_s": scheduled_wall, "scheduled_solo_simulations": n_solo,
             "batched_wall_s": batched_wall, "batched_kernel_ms": batched_ms,
             "serial_wall_s": serial_wall, "serial_kernel_ms": serial_ms, "mesh_setup_s": mesh_s,
             "photons": total, "mean_absorbed_fraction": absorbed,
@@ -214,7 +225,8 @@ def summaries(args) -> dict:
     its full workload and keeps the figures that compare it with serial
     plain launches (a failure is reported in place of its figures)."""
     keep = {"batched": ("value", "unit", "speedup_vs_serial_plain", "speedup_vs_serial_plain_kernel_only",
-                        "serial_plain_photons_per_ms", "photons", "autotune", "clocks"),
+                        "serial_plain_photons_per_ms", "scheduled_photons_per_ms", "scheduled_speedup_vs_serial_plain",
+                        "photons", "autotune", "clocks"),
             "serving": ("value", "unit", "speedup_vs_serial_plain", "serial_plain_photons_per_ms", "p50_ms", "p99_ms",
                         "serial_p50_ms", "serial_p99_ms", "requests", "waves", "photons", "clocks"),
             "replay": ("value", "unit", "forward_photons_per_ms", "detected", "replayed", "backward_s", "clocks")}

@@ -125,3 +125,29 @@ def test_batch_mixing_grid_output_and_trajectories(gpu_ready):
     assert alone[2].ntraj == mixed[2].ntraj == len(t_b)
     order = lambda t: t[np.argsort(t[:, 0].view(np.uint32), kind="stable")].view(np.uint32)  # noqa: E731
     assert np.array_equal(order(t_a), order(t_b))
+
+
+def test_simulate_many_equals_solo_runs(gpu_ready, small_inclusion):
+    """Size-aware scheduling (batching.simulate_many): the large simulations run
+    on their own, chained on one stream, the small ones batched on another;
+    every result equals the simulation run alone."""
+    import dataclasses
+    from mmc_gb300.batching import simulate_many
+    m = small_inclusion
+    mesh = Mesh(m.node, m.elem, m.label)
+    rng = np.random.default_rng(21)
+    cfgs = []
+    for i, n in enumerate([3000, 120000, 8000, 90000, 500, 20000]):
+        media = m.media.copy()
+        media[1:, 0] *= rng.uniform(0.5, 2.0, len(media) - 1)
+        cfgs.append(SimConfig(media=media, nphoton=n, seed=300 + i, srcpos=(30.0, 30.0, 0.0),
+                              srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=1e-9, basisorder=0, isnormalized=1,
+                              issavedet=1, issaveseed=1, detpos=meshgen.c1_detectors(), maxdetphoton=50000))
+    for group in (None, 25000):
+        got = simulate_many([mesh] * len(cfgs), cfgs, solo_photons=50000, group_photons=group)
+        for c, r in zip(cfgs, got):
+            ref = simulate(mesh, c)
+            assert r.raytet == ref.raytet and r.detected == ref.detected
+            np.testing.assert_allclose(r.field, ref.field, rtol=1e-10, atol=1e-14)
+            rows = lambda x: sorted(map(bytes, np.concatenate([x.detp.view(np.uint8).reshape(len(x.detp), -1), x.seeds], 1)))  # noqa: E731
+            assert rows(r) == rows(ref)
