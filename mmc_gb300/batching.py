@@ -1,15 +1,21 @@
 """Size-aware scheduling of many simulations on one GPU.
 
 One persistent batched launch over every simulation (simulate_batch) removes
-the start-up and drain of each small simulation's own launch, but it also
-traces the large simulations unphased, with every simulation's fluence
-buffer live at once.  A simulation of a few million photons fills the GPU by
-itself and gains from gate-phased tracing (only a window of its gate planes
-live in L2), so simulate_many runs those on their own, one after another on
-one stream, and the small ones together in batched launches on a second
-stream; the two streams overlap, so one side's launch drain is filled by the
-other side's blocks.  Each result equals the simulation run alone: photon
-streams depend only on (seed, photon index).
+the start-up and drain of each small simulation's own launch, but it keeps
+every simulation's fluence buffer live and stages every media table in each
+block's shared memory for the whole run.  simulate_many sorts the simulations
+by photon count and runs them as a sequence of batched launches of about
+`group_photons` photons each, so a launch holds simulations of similar size
+and only their buffers.  On the 256-simulation shell workload (photons
+log-uniform 1e5-1e7) groups of 6e7 photons ran the whole set in 14.0 s
+against 17.1 s for one launch and 20.5 s for one plain launch per simulation;
+groups of 3e7, 1e8 and 2e8 photons took 14.5, 14.0 and 14.6 s.  Two options
+measured no better and are off by default: running the largest simulations
+on their own, gate-phased, on a stream of their own (solo_photons; 14.5-15.6 s
+with 4e6-8e6 photon thresholds) and spreading the groups over several
+overlapping streams (streams; 14.9-15.0 s with 2 or 3), which makes
+concurrent launches compete for the L2.  Each result equals the simulation
+run alone: photon streams depend only on (seed, photon index).
 """
 from __future__ import annotations
 
@@ -18,13 +24,16 @@ from typing import Optional, Sequence
 from .core import Mesh, Session, SimConfig, SimResult, launch_batch
 
 
-def simulate_many(meshes: Sequence[Mesh], cfgs: Sequence[SimConfig], solo_photons: int = 4_000_000,
-                  group_photons: Optional[int] = None) -> list:
+def simulate_many(meshes: Sequence[Mesh], cfgs: Sequence[SimConfig], group_photons: Optional[int] = 60_000_000,
+                  solo_photons: Optional[int] = None, streams: int = 1) -> list:
     """Runs every (mesh, cfg) pair and returns their SimResults in order.
-    Simulations of at least `solo_photons` photons run as their own session
-    launches (gate-phased where the automatic mode engages), chained on one
-    stream; the others run as batched launches of at most `group_photons`
-    photons each (None: one launch) on another stream."""
+    The simulations, in increasing photon count, run as batched launches of
+    at most `group_photons` photons each (a larger simulation alone; None:
+    one launch for all) on a stream of their own; with `streams` > 1 the
+    launches alternate over that many streams.  With `solo_photons`, the
+    simulations of at least that many photons run instead as their own
+    session launches (gate-phased where the automatic mode engages), chained
+    on another stream that overlaps the batched launches."""
     import torch
     n = len(cfgs)
     if len(meshes) != n or n == 0:
@@ -36,10 +45,11 @@ def simulate_many(meshes: Sequence[Mesh], cfgs: Sequence[SimConfig], solo_photon
     try:
         for m, c in zip(meshes, cfgs):
             sessions.append(Session(m, c))
-        solo = [i for i, c in enumerate(cfgs) if int(c.nphoton) >= solo_photons]
-        small = [i for i, c in enumerate(cfgs) if int(c.nphoton) < solo_photons and int(c.nphoton) > 0]
-        # the small simulations: batched launches on their own stream
-        side = torch.cuda.Stream(device=dev)
+        big = solo_photons if solo_photons is not None else float("inf")
+        solo = [i for i, c in enumerate(cfgs) if int(c.nphoton) >= big]
+        small = [i for i, c in enumerate(cfgs) if 0 < int(c.nphoton) < big]
+        # batched launches of simulations of similar size, on their own stream(s)
+        sides = [torch.cuda.Stream(device=dev) for _ in range(max(1, int(streams)))]
         groups, cur, tot = [], [], 0
         for i in sorted(small, key=lambda k: int(cfgs[k].nphoton)):
             if cur and group_photons is not None and tot + int(cfgs[i].nphoton) > group_photons:
@@ -49,9 +59,9 @@ def simulate_many(meshes: Sequence[Mesh], cfgs: Sequence[SimConfig], solo_photon
             tot += int(cfgs[i].nphoton)
         if cur:
             groups.append(cur)
-        for g in groups:
+        for k, g in enumerate(groups):  # consecutive groups alternate over the side streams
             launch_batch([sessions[i] for i in g], [0] * len(g), [int(cfgs[i].nphoton) for i in g],
-                         stream=side.cuda_stream)
+                         stream=sides[k % len(sides)].cuda_stream)
         # the large ones: each on its session's stream, each waiting for the one before
         prev = None
         for i in solo:
@@ -65,7 +75,8 @@ def simulate_many(meshes: Sequence[Mesh], cfgs: Sequence[SimConfig], solo_photon
         results = []
         for s in sessions:
             results.append(s.end())
-        side.synchronize()
+        for st in sides:
+            st.synchronize()
         return results
     finally:
         for s in sessions:

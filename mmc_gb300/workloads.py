@@ -85,13 +85,12 @@ def run_batched(args):
     batched_ms = results[0].kernel_ms
     absorbed = float(np.mean([r.absorbed_fraction for r in results]))
     del results
-    # size-aware scheduling: simulations of >= 4e6 photons on their own (gate-phased), chained on
-    # one stream; the others batched on a second stream (batching.simulate_many)
+    # size-aware scheduling (batching.simulate_many): the simulations grouped by photon count into
+    # batched launches of about 6e7 photons
     from mmc_gb300.batching import simulate_many
     t0 = time.perf_counter()
     results = simulate_many([mesh] * len(cfgs), cfgs)
     scheduled_wall = time.perf_counter() - t0
-    n_solo = sum(1 for c in cfgs if c.nphoton >= 4_000_000)
     del results
     clk = clocks.stop()
     # the drop-in path as the reference runs it: every simulation prepares and uploads its mesh
@@ -105,7 +104,7 @@ def run_batched(args):
             "speedup_vs_serial_dropin_with_mesh_setup": dropin_wall / batched_wall,
             "scheduled_photons_per_ms": total / (scheduled_wall * 1e3),
             "scheduled_speedup_vs_serial_plain": serial_wall / scheduled_wall,
-            "scheduled_wall_s": scheduled_wall, "scheduled_solo_simulations": n_solo,
+            "scheduled_wall_s": scheduled_wall,
             "batched_wall_s": batched_wall, "batched_kernel_ms": batched_ms,
             "serial_wall_s": serial_wall, "serial_kernel_ms": serial_ms, "mesh_setup_s": mesh_s,
             "photons": total, "mean_absorbed_fraction": absorbed,

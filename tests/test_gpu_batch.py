@@ -128,9 +128,10 @@ def test_batch_mixing_grid_output_and_trajectories(gpu_ready):
 
 
 def test_simulate_many_equals_solo_runs(gpu_ready, small_inclusion):
-    """Size-aware scheduling (batching.simulate_many): the large simulations run
-    on their own, chained on one stream, the small ones batched on another;
-    every result equals the simulation run alone."""
+    """Size-aware scheduling (batching.simulate_many): simulations grouped by
+    photon count into batched launches, optionally the largest run on their own
+    on a second stream, optionally the groups over two streams; every result
+    equals the simulation run alone."""
     import dataclasses
     from mmc_gb300.batching import simulate_many
     m = small_inclusion
@@ -143,8 +144,8 @@ def test_simulate_many_equals_solo_runs(gpu_ready, small_inclusion):
         cfgs.append(SimConfig(media=media, nphoton=n, seed=300 + i, srcpos=(30.0, 30.0, 0.0),
                               srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=1e-9, basisorder=0, isnormalized=1,
                               issavedet=1, issaveseed=1, detpos=meshgen.c1_detectors(), maxdetphoton=50000))
-    for group in (None, 25000):
-        got = simulate_many([mesh] * len(cfgs), cfgs, solo_photons=50000, group_photons=group)
+    for solo, group, streams in ((50000, None, 1), (50000, 25000, 2), (None, 100000, 1)):
+        got = simulate_many([mesh] * len(cfgs), cfgs, group_photons=group, solo_photons=solo, streams=streams)
         for c, r in zip(cfgs, got):
             ref = simulate(mesh, c)
             assert r.raytet == ref.raytet and r.detected == ref.detected
