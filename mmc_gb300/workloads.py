@@ -114,8 +114,10 @@ def run_batched(args):
     return line
 
 
-def run_serving(args):
-    from mmc_gb300.serving import Request, Server
+def serving_requests(nreq: int):
+    """The serving workload's three resident meshes and its `nreq` requests
+    (arrival times relative to 0)."""
+    from mmc_gb300.serving import Request
     rng = np.random.default_rng(7)
     meshes = {}
     recipes = {"cube162k": meshgen.homogeneous_cube(n=30),
@@ -126,7 +128,7 @@ def run_serving(args):
     keys = list(meshes)
     reqs = []
     t = 0.0
-    for i in range(args.requests):
+    for i in range(nreq):
         key = keys[rng.integers(len(keys))]
         mm = meshes[key][1]
         t += rng.exponential(1.0 / 200.0)
@@ -149,6 +151,12 @@ def run_serving(args):
                         tend=5e-9, tstep=0.5e-9, issavedet=1, detpos=np.array(det, np.float32),
                         maxdetphoton=200_000, basisorder=0, isnormalized=1, accum_f64=0)
         reqs.append(Request(mesh=key, cfg=cfg, arrival=t))
+    return meshes, reqs
+
+
+def run_serving(args):
+    from mmc_gb300.serving import Server
+    meshes, reqs = serving_requests(args.requests)
     # continuous batching
     srv = Server({k: v[0] for k, v in meshes.items()}, wave_photons=8_000_000, min_share=100_000)
     clocks = ClockSampler(0)
