@@ -288,3 +288,53 @@ def test_replay_loss_autograd_function(gpu_ready):
         fd = (vals[0] - vals[1]) / (2 * d)
         g = float(mua.grad[k])
         assert g == pytest.approx(fd, rel=5e-3, abs=1e-4 * abs(float(L.detach())) + 1e-6), (k, g, fd)
+
+
+def test_mua_gradient_on_50_element_groups_of_the_differentiation_workload(gpu_ready):
+    """The differentiation workload as specified: the 4-layer shell mesh (1 mm
+    grid, 1.296M tets), pencil (30,30,5.5) +z, 8 detectors R=1.5 mm at polar
+    angles 10..80 degrees, 1e7 photons with saved seeds, L = sum_d c_d log W_d
+    with c_d ~ N(0,1).  50 element groups (2 mm spheres at random places between
+    the source and the detectors, each relabelled as its own copy of its
+    layer's medium): dL/dmua of each group from one replay pair equals the
+    central difference (+-1%, common random numbers) of two forward runs."""
+    m = meshgen.shell_mesh(n=60, jitter=0.25, seed=4321)
+    cen = meshgen.centroids(m.node, m.elem)
+    rng = np.random.default_rng(50)
+    label = m.label.copy()
+    media = [row for row in m.media]
+    groups = []
+    while len(groups) < 50:
+        a = np.deg2rad(rng.uniform(2.0, 80.0))
+        p = CENTER + rng.uniform(18.5, 24.5) * np.array([np.sin(a), rng.uniform(-0.1, 0.1), -np.cos(a)])
+        near = np.nonzero((np.linalg.norm(cen - p, axis=1) < 2.0) & np.isin(label, [1, 2, 3, 4]))[0]
+        if near.size < 4:
+            continue
+        lay = np.bincount(label[near]).argmax()
+        label[near[label[near] == lay]] = len(media)
+        groups.append(len(media))
+        media.append(m.media[lay].copy())
+    media = np.array(media, np.float32)
+    mesh = Mesh(m.node, m.elem, label)
+    det = np.array([[*(CENTER + 25.0 * np.array([np.sin(a), 0.0, -np.cos(a)])), 1.5]
+                    for a in np.deg2rad(np.arange(10, 90, 10))], np.float32)
+    cfg = _cfg(media, 10_000_000, seed=31, detpos=det, maxdetphoton=5_000_000)
+    c = np.random.default_rng(3).normal(size=len(det))
+    fwd = simulate(mesh, cfg)
+    L, W, gmua, gmus = rp.loss_and_grads(mesh, cfg, fwd.detp, fwd.seeds, c)
+    assert np.all(W > 0)
+    an, fd = [], []
+    for g in groups:
+        dm = 0.01 * media[g, 0]
+        mp, mm = media.copy(), media.copy()
+        mp[g, 0] += dm
+        mm[g, 0] -= dm
+        lp = _loss(simulate(mesh, dataclasses.replace(cfg, media=mp, issaveseed=0)), mp, c)
+        lm = _loss(simulate(mesh, dataclasses.replace(cfg, media=mm, issaveseed=0)), mm, c)
+        fd.append((lp - lm) / (2 * dm))
+        an.append(float(gmua[label == g].sum()))
+    an, fd = np.array(an), np.array(fd)
+    scale = np.abs(fd).max()
+    print(f"dL/dmua on 50 groups: max |grad| {scale:.3e}, max |analytic - central| {np.abs(an - fd).max():.3e}")
+    assert scale > 0 and np.count_nonzero(np.abs(fd) > 1e-3 * scale) >= 10  # the groups see light
+    np.testing.assert_allclose(an, fd, rtol=2e-3, atol=1e-4 * scale)
