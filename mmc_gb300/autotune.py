@@ -93,7 +93,9 @@ def autotune_batch(meshes, cfgs, photons_per_lane: int = 32, threads: Iterable[i
     """As autotune, for one batched launch over all of `cfgs` (each on its
     mesh): every candidate shape runs trial batched launches of the whole
     batch, the trial photons of a launch split over the simulations in
-    proportion to their photon counts (at least one each)."""
+    proportion to their photon counts (at least one each).  Each candidate
+    holds a session -- a fluence buffer -- per simulation while it runs, as
+    the batched run itself does."""
     key = ("batch", tuple(_signature(m, c) for m, c in zip(meshes, cfgs)), photons_per_lane, tuple(threads),
            tuple(blocks_per_sm), tuple(accum))
     if use_cache and key in _cache:

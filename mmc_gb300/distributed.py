@@ -144,7 +144,9 @@ def simulate_sharded(mesh: Mesh, cfg: SimConfig, group=None,
                      runner: Optional[Callable[[SimConfig], SimResult]] = None) -> SimResult:
     """One simulation split over the ranks of `group`.  Default: the rank's GPU
     traces its shard and, with NCCL, the ranks combine their device buffers
-    before the output stage (`mesh` a resident Mesh).  `runner` replaces the
+    before the output stage (`mesh` a resident Mesh; the shards accumulate in
+    float64 there whatever cfg.accum_f64 says, since the float32 scheme's
+    two buffers are not summed across ranks).  `runner` replaces the
     rank's simulation (it returns raw element deposits, e.g. the CPU oracle);
     its result is combined on the host (`mesh` needs node/elem/label)."""
     dist = _dist()
