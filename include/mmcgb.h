@@ -232,6 +232,18 @@ int32_t mmcgb_session_launch_batch(int32_t n, mmcgb_session* const* sessions, co
  * reference. */
 int32_t mmcgb_session_launch_batch_on(int32_t n, mmcgb_session* const* sessions, const uint64_t* offsets,
                                       const uint64_t* counts, void* stream);
+/* A sequence of batched launches, captured as one CUDA graph and enqueued on
+ * `stream` (a cudaStream_t): group g runs one persistent launch over the next
+ * group_sizes[g] sessions of `sessions` (session i simulating photons
+ * [offsets[i], offsets[i]+counts[i]) of its run), the groups one after
+ * another.  The graph is instantiated once per device and updated in place by
+ * later calls of the same shape (the same number of launches of the same
+ * kernels).  The groups wait for every session's setup, and every session's
+ * later work waits for the groups.  No counterpart in the reference (one
+ * simulation per device, src/mmc_core.cl:464-467); batching.simulate_many
+ * runs its size-sorted groups through it. */
+int32_t mmcgb_session_launch_batches(int32_t ngroups, const int32_t* group_sizes, mmcgb_session* const* sessions,
+                                     const uint64_t* offsets, const uint64_t* counts, void* stream);
 /* The reference's respin loop (src/mmc_cu_host.cu:656-906: `repeats` launches
  * accumulating into one set of buffers) as one CUDA graph: launch k traces
  * photons [photon_offset + k*nphoton, photon_offset + (k+1)*nphoton).  The

@@ -85,6 +85,7 @@ EXPORTS = [
     "mmcgb_session_launch_batch", "mmcgb_session_stream", "mmcgb_session_launch_batch_on",
     "mmcgb_session_launch_repeat", "mmcgb_grid_info", "mmcgb_check_config",
     "mmcgb_session_device_buffers", "mmcgb_l2_read_bandwidth", "mmcgb_session_phase_window",
+    "mmcgb_session_launch_batches",
 ]
 
 
@@ -128,6 +129,8 @@ def load():
         lib.mmcgb_session_launch_batch_on.argtypes = [C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
                                                       C.POINTER(C.c_uint64), C.c_void_p]
         lib.mmcgb_session_launch_repeat.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32]
+        lib.mmcgb_session_launch_batches.argtypes = [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_void_p),
+                                                     C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_void_p]
         lib.mmcgb_session_phase_window.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(C.c_int32),
                                                     C.POINTER(C.c_uint64)]
         lib.mmcgb_l2_read_bandwidth.argtypes = [C.c_int32, C.c_uint64, C.c_int32, C.POINTER(C.c_double)]
@@ -136,7 +139,7 @@ def load():
         lib.mmcgb_grid_info.argtypes = [C.c_void_p, C.c_float, C.POINTER(C.c_int32), C.POINTER(C.c_float)]
         for name in ("mmcgb_session_launch_batch", "mmcgb_session_launch_batch_on", "mmcgb_session_launch_repeat",
                      "mmcgb_grid_info", "mmcgb_check_config", "mmcgb_session_device_buffers", "mmcgb_l2_read_bandwidth", "mmcgb_session_phase_window",
-                     "mmcgb_prepare_host", "mmcgb_normalize_host", "mmcgb_session_begin", "mmcgb_session_launch", "mmcgb_session_sync", "mmcgb_session_end",
+                     "mmcgb_session_launch_batches", "mmcgb_prepare_host", "mmcgb_normalize_host", "mmcgb_session_begin", "mmcgb_session_launch", "mmcgb_session_sync", "mmcgb_session_end",
                      "mmcgb_mesh_create", "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export",
                      "mmcgb_mesh_locate", "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run"):
             getattr(lib, name).restype = C.c_int32

@@ -6,7 +6,9 @@ every simulation's fluence buffer live and stages every media table in each
 block's shared memory for the whole run.  simulate_many sorts the simulations
 by photon count and runs them as a sequence of batched launches of about
 `group_photons` photons each, so a launch holds simulations of similar size
-and only their buffers.  On the 256-simulation shell workload (photons
+and only their buffers; the sequence is captured as one CUDA graph
+(mmcgb_session_launch_batches), instantiated once and updated in place by
+later calls of the same shape.  On the 256-simulation shell workload (photons
 log-uniform 1e5-1e7) groups of 6e7 photons ran the whole set in 14.0 s
 against 17.1 s for one launch and 20.5 s for one plain launch per simulation;
 groups of 3e7, 1e8 and 2e8 photons took 14.5, 14.0 and 14.6 s.  Two options
@@ -21,7 +23,7 @@ from __future__ import annotations
 
 from typing import Optional, Sequence
 
-from .core import Mesh, Session, SimConfig, SimResult, launch_batch
+from .core import Mesh, Session, SimConfig, SimResult, launch_batch, launch_batches
 
 
 def simulate_many(meshes: Sequence[Mesh], cfgs: Sequence[SimConfig], group_photons: Optional[int] = 60_000_000,
@@ -59,9 +61,13 @@ def simulate_many(meshes: Sequence[Mesh], cfgs: Sequence[SimConfig], group_photo
             tot += int(cfgs[i].nphoton)
         if cur:
             groups.append(cur)
-        for k, g in enumerate(groups):  # consecutive groups alternate over the side streams
-            launch_batch([sessions[i] for i in g], [0] * len(g), [int(cfgs[i].nphoton) for i in g],
-                         stream=sides[k % len(sides)].cuda_stream)
+        if len(sides) == 1 and groups:  # the groups in sequence, as one CUDA graph
+            launch_batches([[sessions[i] for i in g] for g in groups], [[0] * len(g) for g in groups],
+                           [[int(cfgs[i].nphoton) for i in g] for g in groups], sides[0].cuda_stream)
+        else:
+            for k, g in enumerate(groups):  # consecutive groups alternate over the side streams
+                launch_batch([sessions[i] for i in g], [0] * len(g), [int(cfgs[i].nphoton) for i in g],
+                             stream=sides[k % len(sides)].cuda_stream)
         # the large ones: each on its session's stream, each waiting for the one before
         prev = None
         for i in solo:

@@ -523,6 +523,22 @@ def launch_batch(sessions, offsets, counts, stream: Optional[int] = None):
         N.check(N.load().mmcgb_session_launch_batch_on(n, h, o, k, C.c_void_p(int(stream))))
 
 
+def launch_batches(groups, offsets, counts, stream: int):
+    """A sequence of batched launches captured as one CUDA graph
+    (mmcgb_session_launch_batches): groups[g] is a list of sessions run in one
+    persistent launch, the groups one after another on `stream` (a
+    cudaStream_t handle); offsets/counts hold each group's photon ranges as
+    lists parallel to the groups."""
+    sizes = [len(g) for g in groups]
+    flat = [s._h for g in groups for s in g]
+    off = [int(x) for o in offsets for x in o]
+    cnt = [int(x) for c in counts for x in c]
+    n = len(flat)
+    N.check(N.load().mmcgb_session_launch_batches(len(groups), (C.c_int32 * len(sizes))(*sizes), (C.c_void_p * n)(*flat),
+                                                   (C.c_uint64 * n)(*off), (C.c_uint64 * n)(*cnt),
+                                                   C.c_void_p(int(stream))))
+
+
 def pinned_empty(shape, dtype=np.float64) -> np.ndarray:
     """A page-locked host array (through torch's pinned allocator): device to
     host copies into it run at the interconnect's full rate."""

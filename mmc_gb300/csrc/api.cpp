@@ -7,7 +7,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -825,6 +827,74 @@ int32_t mmcgb_session_launch(mmcgb_session* s, uint64_t photon_offset, uint64_t 
 
 namespace {
 
+// The parameter blocks and photon-count prefix sums of one batched launch over
+// sessions ss[0..n) (session i simulating photons [offsets[i], offsets[i]+counts[i])
+// of its run), with what the kernel needs to know about them.
+struct BatchPlan {
+    std::vector<SimDev> sims;
+    std::vector<unsigned long long> cum;
+    unsigned long long total = 0;
+    int nmed_stride = 0, reclen_max = 0, want_seed = 0, want_io = 0, want_replay = 0, fast = 0;
+};
+
+int plan_batch(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets, const uint64_t* counts, BatchPlan& B) {
+    if (n <= 0 || !ss || !offsets || !counts || !ss[0]) return fail(MMCGB_E_ARG, "null or empty batch");
+    const int device = ss[0]->mesh->device;
+    B.fast = ss[0]->cfg.fast_math ? 1 : 0;
+    B.sims.resize(n);
+    B.cum.resize(n);
+    for (int i = 0; i < n; i++) {
+        mmcgb_session* s = ss[i];
+        if (!s || s->mesh->device != device) return fail(MMCGB_E_ARG, "batched sessions must live on one device");
+        if ((s->cfg.fast_math ? 1 : 0) != B.fast) return fail(MMCGB_E_ARG, "batched sessions must share fast_math");
+        if (s->cfg.replayseed && (offsets[i] != 0 || counts[i] != s->cfg.nphoton))
+            return fail(MMCGB_E_ARG, "replay sessions run all replayed photons in one launch");
+        if ((s->P.buf.pw || s->P.buf.ps || s->P.buf.pd) && counts[i] > s->cfg.nphoton)
+            return fail(MMCGB_E_ARG, "per-photon trace buffers hold cfg.nphoton photons");
+        B.sims[i] = s->P.sim;
+        B.sims[i].nphoton = counts[i];
+        B.sims[i].photon_offset = s->cfg.photon_offset + offsets[i];
+        B.nmed_stride = std::max(B.nmed_stride, s->cfg.nmedia);
+        if (s->cfg.issavedet) B.reclen_max = std::max(B.reclen_max, s->P.sim.reclen);
+        if (s->cfg.issavedet && s->P.sim.seeds) B.want_seed = 1;
+        if (general_source(s->P.sim) || s->P.sim.roulette_on) B.want_io = 1;  // batched kernels: lean or general
+        if (s->P.sim.replay) B.want_replay = 1;
+        B.total += counts[i];
+        B.cum[i] = B.total;
+    }
+    if ((size_t)n * B.nmed_stride * sizeof(float4) > 40 * 1024)
+        return fail(MMCGB_E_ARG, "batch media tables exceed shared memory; split the batch");
+    return MMCGB_OK;
+}
+
+// Instantiated graphs of mmcgb_session_launch_batches, one per device: a new
+// capture of the same shape (the same number of launches of the same kernels)
+// updates the instantiated graph in place instead of instantiating again.
+// The executable graphs live until the process exits.
+std::mutex g_graph_mu;
+std::map<int, cudaGraphExec_t> g_graph_exec;
+
+cudaError_t launch_cached_graph(int device, cudaGraph_t graph, cudaStream_t st) {
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    cudaGraphExec_t& ex = g_graph_exec[device];
+    if (ex) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(ex, graph, &info) != cudaSuccess) {
+            (void)cudaGetLastError();
+            cudaGraphExecDestroy(ex);
+            ex = nullptr;
+        }
+    }
+    if (!ex) {
+        const cudaError_t e = cudaGraphInstantiate(&ex, graph, 0);
+        if (e != cudaSuccess) {
+            ex = nullptr;
+            return e;
+        }
+    }
+    return cudaGraphLaunch(ex, st);
+}
+
 // One persistent launch over several sessions.  `ordered`: on the first
 // session's stream, after every session's earlier work and before its later
 // work, timed with the first session's events.  Otherwise on `st` with its own
@@ -835,32 +905,14 @@ int batch_launch(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets, c
     mmcgb_session* s0 = ss[0];
     if (!s0) return fail(MMCGB_E_ARG, "null session");
     const int device = s0->mesh->device;
-    const int fast = s0->cfg.fast_math ? 1 : 0;
-    std::vector<SimDev> sims(n);
-    std::vector<unsigned long long> cum(n);
-    unsigned long long total = 0;
-    int nmed_stride = 0, reclen_max = 0, want_seed = 0, want_io = 0, want_replay = 0;
-    for (int i = 0; i < n; i++) {
-        mmcgb_session* s = ss[i];
-        if (!s || s->mesh->device != device) return fail(MMCGB_E_ARG, "batched sessions must live on one device");
-        if ((s->cfg.fast_math ? 1 : 0) != fast) return fail(MMCGB_E_ARG, "batched sessions must share fast_math");
-        if (s->cfg.replayseed && (offsets[i] != 0 || counts[i] != s->cfg.nphoton))
-            return fail(MMCGB_E_ARG, "replay sessions run all replayed photons in one launch");
-        if ((s->P.buf.pw || s->P.buf.ps || s->P.buf.pd) && counts[i] > s->cfg.nphoton)
-            return fail(MMCGB_E_ARG, "per-photon trace buffers hold cfg.nphoton photons");
-        sims[i] = s->P.sim;
-        sims[i].nphoton = counts[i];
-        sims[i].photon_offset = s->cfg.photon_offset + offsets[i];
-        nmed_stride = std::max(nmed_stride, s->cfg.nmedia);
-        if (s->cfg.issavedet) reclen_max = std::max(reclen_max, s->P.sim.reclen);
-        if (s->cfg.issavedet && s->P.sim.seeds) want_seed = 1;
-        if (general_source(s->P.sim) || s->P.sim.roulette_on) want_io = 1;  // batched kernels: lean or general
-        if (s->P.sim.replay) want_replay = 1;
-        total += counts[i];
-        cum[i] = total;
-    }
-    if ((size_t)n * nmed_stride * sizeof(float4) > 40 * 1024)
-        return fail(MMCGB_E_ARG, "batch media tables exceed shared memory; split the batch");
+    BatchPlan B;
+    int rc = plan_batch(n, ss, offsets, counts, B);
+    if (rc) return rc;
+    std::vector<SimDev>& sims = B.sims;
+    std::vector<unsigned long long>& cum = B.cum;
+    const unsigned long long total = B.total;
+    const int nmed_stride = B.nmed_stride, reclen_max = B.reclen_max, want_seed = B.want_seed,
+              want_io = B.want_io, want_replay = B.want_replay, fast = B.fast;
     CK(cudaSetDevice(device));
     if (ordered) st = s0->stream;
     // order the batch after every session's earlier work, and every session's later work after it
@@ -925,6 +977,88 @@ int32_t mmcgb_session_launch_batch_on(int32_t n, mmcgb_session* const* ss, const
                                       const uint64_t* counts, void* stream) {
     if (!stream) return fail(MMCGB_E_ARG, "null stream");
     return batch_launch(n, ss, offsets, counts, (cudaStream_t)stream, false);
+}
+
+int32_t mmcgb_session_launch_batches(int32_t ngroups, const int32_t* group_sizes, mmcgb_session* const* ss,
+                                     const uint64_t* offsets, const uint64_t* counts, void* stream_handle) {
+    if (ngroups <= 0 || !group_sizes || !ss || !offsets || !counts || !stream_handle)
+        return fail(MMCGB_E_ARG, "null or empty group list");
+    cudaStream_t st = static_cast<cudaStream_t>(stream_handle);
+    // plan every group before anything is enqueued
+    std::vector<BatchPlan> plans(ngroups);
+    std::vector<int> first(ngroups);
+    int nsess = 0;
+    for (int g = 0; g < ngroups; g++) {
+        if (group_sizes[g] <= 0) return fail(MMCGB_E_ARG, "every group needs a session");
+        first[g] = nsess;
+        const int rc = plan_batch(group_sizes[g], ss + nsess, offsets + nsess, counts + nsess, plans[g]);
+        if (rc) return rc;
+        nsess += group_sizes[g];
+    }
+    const int device = ss[0]->mesh->device;
+    for (int i = 0; i < nsess; i++)
+        if (ss[i]->mesh->device != device) return fail(MMCGB_E_ARG, "batched sessions must live on one device");
+    CK(cudaSetDevice(device));
+    // one device buffer holds every group's parameter blocks, prefix sums and work counter
+    size_t bytes = 0;
+    std::vector<size_t> off_sims(ngroups), off_cum(ngroups), off_work(ngroups);
+    for (int g = 0; g < ngroups; g++) {
+        off_sims[g] = bytes;
+        bytes += (sizeof(SimDev) * group_sizes[g] + 255) & ~(size_t)255;
+        off_cum[g] = bytes;
+        bytes += (sizeof(unsigned long long) * group_sizes[g] + 255) & ~(size_t)255;
+        off_work[g] = bytes;
+        bytes += 256;
+    }
+    std::vector<unsigned char> host(bytes, 0);
+    for (int g = 0; g < ngroups; g++) {
+        std::memcpy(host.data() + off_sims[g], plans[g].sims.data(), sizeof(SimDev) * group_sizes[g]);
+        std::memcpy(host.data() + off_cum[g], plans[g].cum.data(), sizeof(unsigned long long) * group_sizes[g]);
+    }
+    const LaunchShape bshape = default_shape(device, true);
+    // the groups run after every session's setup
+    for (int i = 0; i < nsess; i++) CK(cudaStreamWaitEvent(st, ss[i]->ready, 0));
+    unsigned char* dev = nullptr;
+    CK(cudaMallocAsync((void**)&dev, bytes, st));
+    CK(cudaMemcpyAsync(dev, host.data(), bytes, cudaMemcpyHostToDevice, st));
+    // the launches, captured as one graph (each zeroes its own work counter first)
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (int g = 0; g < ngroups && e == cudaSuccess; g++) {
+        const BatchPlan& B = plans[g];
+        mmcgb_session* s0 = ss[first[g]];
+        auto* work = reinterpret_cast<unsigned long long*>(dev + off_work[g]);
+        if (group_sizes[g] == 1) {
+            e = launch_plain(B.sims[0], work, s0->shape, st);
+        } else {
+            LaunchShape shape = bshape;
+            if (s0->cfg.threads > 0) shape.threads = std::max(32, std::min(s0->cfg.threads, 128) / 32 * 32);
+            if (s0->cfg.blocks > 0) shape.blocks = s0->cfg.blocks;
+            e = launch_batched(reinterpret_cast<const SimDev*>(dev + off_sims[g]),
+                               reinterpret_cast<const unsigned long long*>(dev + off_cum[g]), group_sizes[g], B.total,
+                               B.nmed_stride, B.reclen_max, B.want_seed, work, shape, st, B.fast, B.want_io,
+                               B.want_replay);
+        }
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+    if (e == cudaSuccess) e = ec;
+    if (e == cudaSuccess) e = launch_cached_graph(device, graph, st);
+    if (graph) cudaGraphDestroy(graph);
+    cudaFreeAsync(dev, st);
+    if (e != cudaSuccess) return cuda_fail(e, "batched graph");
+    // every session's later work (sync, output stage, freeing its buffers) waits for the groups
+    cudaEvent_t done = nullptr;
+    CK(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+    CK(cudaEventRecord(done, st));
+    for (int i = 0; i < nsess; i++) {
+        ss[i]->launched += counts[i];
+        ss[i]->launches++;
+        ss[i]->timed = false;
+        if (ss[i]->stream != st) CK(cudaStreamWaitEvent(ss[i]->stream, done, 0));
+    }
+    cudaEventDestroy(done);
+    return MMCGB_OK;
 }
 
 int32_t mmcgb_session_launch_repeat(mmcgb_session* s, uint64_t photon_offset, uint64_t nphoton, int32_t repeats) {

@@ -152,3 +152,36 @@ def test_simulate_many_equals_solo_runs(gpu_ready, small_inclusion):
             np.testing.assert_allclose(r.field, ref.field, rtol=1e-10, atol=1e-14)
             rows = lambda x: sorted(map(bytes, np.concatenate([x.detp.view(np.uint8).reshape(len(x.detp), -1), x.seeds], 1)))  # noqa: E731
             assert rows(r) == rows(ref)
+
+
+def test_batched_launches_as_one_graph(gpu_ready, small_inclusion):
+    """mmcgb_session_launch_batches: a sequence of batched launches captured as
+    one CUDA graph.  Two calls of the same shape (the second updates the
+    instantiated graph in place) over consecutive photon ranges, then a call
+    of another shape: every simulation equals its solo run of all its photons."""
+    import torch
+    from mmc_gb300.core import launch_batches
+    m = small_inclusion
+    mesh = Mesh(m.node, m.elem, m.label)
+    cfgs = [SimConfig(media=m.media, nphoton=n, seed=700 + i, srcpos=(30.0, 30.0, 0.0), srcdir=(0.0, 0.0, 1.0),
+                      tend=5e-9, tstep=1e-9, basisorder=0, isnormalized=1, issavedet=1, issaveseed=1,
+                      detpos=meshgen.c1_detectors(), maxdetphoton=50000)
+            for i, n in enumerate([6000, 9000, 30000, 12000, 4000])]
+    st = torch.cuda.Stream()
+    sess = [Session(mesh, c) for c in cfgs]
+    groups = [[sess[0], sess[1]], [sess[2]], [sess[3], sess[4]]]
+    idx = [[0, 1], [2], [3, 4]]
+    half = [[cfgs[i].nphoton // 2 for i in g] for g in idx]
+    rest = [[cfgs[i].nphoton - cfgs[i].nphoton // 2 for i in g] for g in idx]
+    launch_batches(groups, [[0] * len(g) for g in idx], half, st.cuda_stream)
+    launch_batches(groups, half, rest, st.cuda_stream)  # same shape: the graph is updated in place
+    got = [s.end() for s in sess]
+    sess2 = [Session(mesh, c) for c in cfgs]
+    launch_batches([sess2], [[0] * 5], [[c.nphoton for c in cfgs]], st.cuda_stream)  # another shape
+    got2 = [s.end() for s in sess2]
+    st.synchronize()
+    for c, a, b in zip(cfgs, got, got2):
+        ref = simulate(mesh, c)
+        for r in (a, b):
+            assert r.raytet == ref.raytet and r.detected == ref.detected
+            np.testing.assert_allclose(r.field, ref.field, rtol=1e-10, atol=1e-14)
