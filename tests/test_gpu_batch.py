@@ -142,13 +142,16 @@ def test_simulate_many_equals_solo_runs(gpu_ready, small_inclusion):
         media = m.media.copy()
         media[1:, 0] *= rng.uniform(0.5, 2.0, len(media) - 1)
         cfgs.append(SimConfig(media=media, nphoton=n, seed=300 + i, srcpos=(30.0, 30.0, 0.0),
-                              srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=1e-9, basisorder=0, isnormalized=1,
+                              srcdir=(0.0, 0.0, 1.0), tend=5e-9, tstep=1e-9, basisorder=0, isnormalized=0,
                               issavedet=1, issaveseed=1, detpos=meshgen.c1_detectors(), maxdetphoton=50000))
     for solo, group, streams in ((50000, None, 1), (50000, 25000, 2), (None, 100000, 1)):
         got = simulate_many([mesh] * len(cfgs), cfgs, group_photons=group, solo_photons=solo, streams=streams)
         for c, r in zip(cfgs, got):
             ref = simulate(mesh, c)
             assert r.raytet == ref.raytet and r.detected == ref.detected
+            # raw deposits (float64 atomics): equal up to summation order; the escaped weight is
+            # summed per lane in float32 first, so it agrees to float32 rounding across launch shapes
+            assert r.energyesc == pytest.approx(ref.energyesc, rel=1e-6)
             np.testing.assert_allclose(r.field, ref.field, rtol=1e-10, atol=1e-14)
             rows = lambda x: sorted(map(bytes, np.concatenate([x.detp.view(np.uint8).reshape(len(x.detp), -1), x.seeds], 1)))  # noqa: E731
             assert rows(r) == rows(ref)
@@ -164,7 +167,7 @@ def test_batched_launches_as_one_graph(gpu_ready, small_inclusion):
     m = small_inclusion
     mesh = Mesh(m.node, m.elem, m.label)
     cfgs = [SimConfig(media=m.media, nphoton=n, seed=700 + i, srcpos=(30.0, 30.0, 0.0), srcdir=(0.0, 0.0, 1.0),
-                      tend=5e-9, tstep=1e-9, basisorder=0, isnormalized=1, issavedet=1, issaveseed=1,
+                      tend=5e-9, tstep=1e-9, basisorder=0, isnormalized=0, issavedet=1, issaveseed=1,
                       detpos=meshgen.c1_detectors(), maxdetphoton=50000)
             for i, n in enumerate([6000, 9000, 30000, 12000, 4000])]
     st = torch.cuda.Stream()
