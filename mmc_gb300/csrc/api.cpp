@@ -1020,10 +1020,13 @@ int32_t mmcgb_session_launch_batches(int32_t ngroups, const int32_t* group_sizes
     for (int i = 0; i < nsess; i++) CK(cudaStreamWaitEvent(st, ss[i]->ready, 0));
     unsigned char* dev = nullptr;
     CK(cudaMallocAsync((void**)&dev, bytes, st));
-    CK(cudaMemcpyAsync(dev, host.data(), bytes, cudaMemcpyHostToDevice, st));
+    cudaError_t e = cudaMemcpyAsync(dev, host.data(), bytes, cudaMemcpyHostToDevice, st);
     // the launches, captured as one graph (each zeroes its own work counter first)
-    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(dev, st);
+        return cuda_fail(e, "batched graph capture");
+    }
     for (int g = 0; g < ngroups && e == cudaSuccess; g++) {
         const BatchPlan& B = plans[g];
         mmcgb_session* s0 = ss[first[g]];
