@@ -182,7 +182,10 @@ const char* mmcgb_last_error(void);
  * Replaces mesh_getvolume/mesh_getfacenb/tracer_build/tracer_prep
  * (src/mmc_mesh.c:910-974, src/mmc_highorder.cpp:128-159,
  * src/mmc_mesh.c:1496-1602, :1241-1483) and the uploads of
- * src/mmc_cu_host.cu:447-487. */
+ * src/mmc_cu_host.cu:447-487.  Labels must lie in -1..63 (-1 = void); a mesh
+ * whose largest label needs b bits may hold up to 2^(31-b) - 1 elements
+ * (1,073,741,823 with labels 0-1, 33,554,431 with labels up to 63), else
+ * MMCGB_E_MESH. */
 int32_t mmcgb_mesh_create(const mmcgb_mesh_desc* desc, int32_t device, mmcgb_mesh** out);
 int32_t mmcgb_mesh_destroy(mmcgb_mesh* mesh);
 /* Sizes of a resident mesh: nodes, elements, exterior faces. */

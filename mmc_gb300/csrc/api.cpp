@@ -290,6 +290,8 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     S.node = mesh->node;
     S.label = mesh->label;
     S.ne = m.ne;
+    S.lbits = m.lbits;
+    S.lmask = (1 << m.lbits) - 1;
     S.e0 = e0;
     S.nmedia = c.nmedia;
     S.detnum = c.detnum;

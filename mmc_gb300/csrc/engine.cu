@@ -116,7 +116,8 @@ struct FastMath {
     static constexpr bool kFast = true;
 };
 
-__device__ __forceinline__ int decode_nb(int w) { return (w << (32 - kNbBits)) >> (32 - kNbBits); }
+// A packed face word: neighbour id (signed) << lb | its label.
+__device__ __forceinline__ int decode_nb(int w, int lb) { return w >> lb; }
 
 // Morton index of the bounding-box grid cell holding p (cells clamped to the grid).
 __device__ __forceinline__ unsigned spatial_key(float px, float py, float pz, const PhaseArgs& pa) {
@@ -169,7 +170,7 @@ __global__ void k_bucket_order(const PState* rec, const unsigned long long* coun
         if (slot < n) order[slot] = (unsigned)i;
     }
 }
-__device__ __forceinline__ int decode_label(int w) { return (int)((unsigned)w >> kNbBits); }
+__device__ __forceinline__ int decode_label(int w, int lmask) { return w & lmask; }
 
 __device__ __forceinline__ void deposit(const SimDev& S, unsigned idx, float val) {
     if (S.accum_f64) {
@@ -1170,8 +1171,8 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
             if (cross) {
                 // face crossing, src/mmc_core.cl:1950-1993
                 const int oldeid = L.eid, oldlabel = L.label;
-                int eid = decode_nb(L.nbword);
-                int nlabel = decode_label(L.nbword);
+                int eid = decode_nb(L.nbword, S.lbits);
+                int nlabel = decode_label(L.nbword, S.lmask);
                 // a crossing into the same medium cannot refract: its index loads are skipped (1.5% faster)
                 if (S.isreflect && (eid <= 0 || nlabel != oldlabel)) {
                     const float nold = med[oldlabel].w;

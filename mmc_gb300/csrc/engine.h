@@ -17,9 +17,17 @@ enum Boundary { BC_NOREFLECT = 0, BC_REFLECT = 1, BC_ABSORBEXT = 2, BC_MIRROR = 
 
 constexpr int kMaxMedia = 64;        // media rows (incl. background) staged in shared memory
 constexpr int kMaxSimsShared = 256;  // simulations whose media tables fit in one block's shared memory
-constexpr int kNbBits = 26;          // neighbour id bits in a packed face word (the label takes 6)
-constexpr int kMaxLabel = 63;        // medium labels a packed face word holds (kMaxMedia - 1)
-constexpr int kMaxElem = (1 << (kNbBits - 1)) - 1;
+constexpr int kMaxLabel = 63;        // medium labels a mesh may use (kMaxMedia - 1)
+// A packed face word holds the neighbour's medium label in its low lbits bits and the
+// neighbour id, signed, in the 32 - lbits bits above, lbits being the fewest bits (1..6) that
+// hold the mesh's largest label: a mesh of two media keeps 30 bits for element ids
+// (1,073,741,823 elements), one of 64 media 25 (33,554,431).
+inline int label_bits(int maxlabel) {
+    int b = 1;
+    while (b < 6 && (1 << b) <= maxlabel) b++;
+    return b;
+}
+inline int max_elem(int lbits) { return (int)((1u << (31 - lbits)) - 1u); }
 // Fluence cells (gates x elements or voxels) one simulation may hold: deposit indices are
 // 32-bit and 0x7FFFFFFF marks "no pending deposit", so every index stays below it.
 constexpr unsigned kMaxFluenceCells = 0x7FFFFFFFu;
@@ -28,9 +36,9 @@ constexpr unsigned kMaxFluenceCells = 0x7FFFFFFFu;
 //   nx/ny/nz/nd : outward unit normals and plane offsets of the 4 faces
 //                 (face k of the reference normal table, src/mmc_mesh.c:1572-1601)
 //   nb          : for each face in neighbour order (src/mmc_highorder.cpp:50),
-//                 bits 0..25 = neighbour element (1-based, signed: <=0 is an
-//                 exterior face numbered -1,-2,...), bits 26..31 = the
-//                 neighbour's medium label (0 for exterior faces).
+//                 word = neighbour element << lbits | its medium label (element
+//                 1-based, signed: <=0 is an exterior face numbered -1,-2,...,
+//                 whose label is 0).
 struct __align__(16) TetRec {
     float4 nx, ny, nz, nd;
     int4 nb;
@@ -47,6 +55,8 @@ struct SimDev {
     const float4* node;    // xyz + pad
     const int* label;      // medium label per element
     int ne;
+    int lbits;             // label bits of the packed face words (label_bits of the mesh)
+    int lmask;             // (1 << lbits) - 1
     int e0;                // initial element (1-based)
     int nmedia;
     int detnum;

@@ -104,31 +104,37 @@ int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
         err = "mesh needs nn > 0, ne > 0 and node/elem/label arrays";
         return MMCGB_E_ARG;
     }
-    if (d.ne > kMaxElem) {
-        err = "mesh has more elements than the packed record format holds (" + std::to_string(kMaxElem) + ")";
-        return MMCGB_E_MESH;
-    }
-    m.nn = d.nn;
-    m.ne = d.ne;
-    m.node.assign(d.node, d.node + 3 * (size_t)d.nn);
-    m.elem.assign(d.elem, d.elem + 4 * (size_t)d.ne);
-    m.label.assign(d.label, d.label + (size_t)d.ne);
-    m.evol.assign(d.ne, 0.f);
-    m.nvol.assign(d.nn, 0.f);
     int maxlabel = 0;
     for (int i = 0; i < d.ne; i++) {
         // -1 marks the reference's source-element candidates, which it then treats as
         // void (mesh_srcdetelem, src/mmc_mesh.c:390-425); sources are located here by a
         // search over all elements, so such a tet is simply void
-        if (m.label[i] == -1) m.label[i] = 0;
-        if (m.label[i] < 0 || m.label[i] > kMaxLabel) {
+        const int lab = (d.label[i] == -1) ? 0 : d.label[i];
+        if (lab < 0 || lab > kMaxLabel) {
             err = "medium labels must be in -1.." + std::to_string(kMaxLabel) +
                   " (-2, wide-field detector elements, is not supported)";
             return MMCGB_E_MESH;
         }
-        maxlabel = std::max(maxlabel, m.label[i]);
+        maxlabel = std::max(maxlabel, lab);
     }
+    // the packed face words share 32 bits between the neighbour id and its label
+    const int lbits = label_bits(maxlabel);
+    if (d.ne > max_elem(lbits)) {
+        err = "mesh has more elements than the packed record format holds with labels up to " +
+              std::to_string(maxlabel) + " (" + std::to_string(max_elem(lbits)) + ")";
+        return MMCGB_E_MESH;
+    }
+    m.nn = d.nn;
+    m.ne = d.ne;
     m.maxlabel = maxlabel;
+    m.lbits = lbits;
+    m.node.assign(d.node, d.node + 3 * (size_t)d.nn);
+    m.elem.assign(d.elem, d.elem + 4 * (size_t)d.ne);
+    m.label.assign(d.label, d.label + (size_t)d.ne);
+    for (int& lab : m.label)
+        if (lab == -1) lab = 0;
+    m.evol.assign(d.ne, 0.f);
+    m.nvol.assign(d.nn, 0.f);
     // volumes and orientation (src/mmc_mesh.c:910-974): swap nodes 3,4 of a
     // negatively oriented tet so that the face tables give outward normals
     for (int i = 0; i < d.ne; i++) {
@@ -194,7 +200,7 @@ int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
     int nf = 0;
     for (size_t i = 0; i < m.facenb.size(); i++)
         if (m.facenb[i] == 0) m.facenb[i] = -(++nf);
-    if (nf > kMaxElem + 1) {
+    if (nf > max_elem(m.lbits) + 1) {
         err = "too many exterior faces for the packed record format";
         return MMCGB_E_MESH;
     }
@@ -205,6 +211,7 @@ int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
 
 void pack_records(const HostMesh& m, std::vector<TetRec>& rec) {
     rec.resize(m.ne);
+    const int lb = m.lbits;
     parallel_ranges((size_t)m.ne, [&](size_t b, size_t end) {
     for (size_t i = b; i < end; i++) {
         const float* vn = &m.normals[16 * i];
@@ -217,7 +224,7 @@ void pack_records(const HostMesh& m, std::vector<TetRec>& rec) {
         for (int j = 0; j < 4; j++) {
             const int nbid = m.facenb[4 * i + j];
             const int lab = (nbid > 0) ? m.label[nbid - 1] : 0;
-            w[j] = (int)(((uint32_t)nbid & ((1u << kNbBits) - 1u)) | ((uint32_t)lab << kNbBits));
+            w[j] = (int)(((uint32_t)nbid << lb) | (uint32_t)lab);
         }
         r.nb = make_int4(w[0], w[1], w[2], w[3]);
     }

@@ -24,6 +24,7 @@ struct LocGrid {
 
 struct HostMesh {
     int nn = 0, ne = 0, nf = 0, maxlabel = 0;
+    int lbits = 1;               // label bits of the packed face words (label_bits(maxlabel))
     std::vector<float> node;     // nn*3
     std::vector<int> elem;       // ne*4, 1-based, orientation-fixed
     std::vector<int> label;      // ne

@@ -139,6 +139,8 @@ extern "C" int32_t mmcgb_simulate_noalloc(mmcgb_mesh* mesh, const mmcgb_config* 
     S.node = mesh->node;
     S.label = mesh->label;
     S.ne = m.ne;
+    S.lbits = m.lbits;
+    S.lmask = (1 << m.lbits) - 1;
     S.e0 = e0;
     S.nmedia = c->nmedia;
     S.detnum = c->detnum;

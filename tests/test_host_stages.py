@@ -52,14 +52,23 @@ def test_normalize_host_matches_oracle_exactly(oracle_mod):
 
 
 def test_oversized_mesh_rejected_before_any_gpu_work():
+    """A packed face word keeps 32 - b bits for the neighbour id, b being the bits of
+    the mesh's largest label: with labels up to 63 (b = 6) a mesh holds at most
+    2^25 - 1 elements.  The check reads only the labels, before any other array."""
     from mmc_gb300 import _native
+    lib = _native.load()
     node = np.zeros((4, 3), np.float32)
     elem = np.ones((4, 4), np.int32)
-    lab = np.ones(4, np.int32)
+    lab = np.ones(2**25, np.int32)
+    lab[7] = 63
     d, keep = core._desc(node, elem, lab)
-    d.ne = 34_000_000  # beyond the 26-bit neighbour field of the packed records (33,554,431)
-    rc = _native.load().mmcgb_prepare_host(d, None, None, None, None, None, None)
+    d.ne = 2**25  # one element more than 25 neighbour bits hold
+    rc = lib.mmcgb_prepare_host(d, None, None, None, None, None, None)
     assert rc == 3
+    assert "33554431" in lib.mmcgb_last_error().decode()
+    lab[7] = 64  # labels are limited to 0..63 whatever the mesh size
+    d.ne = 16
+    assert lib.mmcgb_prepare_host(d, None, None, None, None, None, None) == 3
 
 
 def test_fluence_beyond_the_32bit_cell_index_rejected_before_any_gpu_work():
