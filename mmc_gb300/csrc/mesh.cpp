@@ -197,15 +197,21 @@ int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
     }
     });
     // exterior faces numbered -1,-2,... (src/mmc_mesh.c:1466-1474)
-    int nf = 0;
+    const long long nf_max = (long long)max_elem(m.lbits) + 1;
+    long long nf = 0;
     for (size_t i = 0; i < m.facenb.size(); i++)
-        if (m.facenb[i] == 0) m.facenb[i] = -(++nf);
-    if (nf > max_elem(m.lbits) + 1) {
-        err = "too many exterior faces for the packed record format";
+        if (m.facenb[i] == 0) {
+            if (++nf > nf_max) {
+                err = "too many exterior faces for the packed record format";
+                return MMCGB_E_MESH;
+            }
+            m.facenb[i] = -(int)nf;
+        }
+    m.nf = (int)nf;
+    if (!build_locator(m)) {
+        err = "mesh too large for the source locator (more than 2^32 element-bin pairs)";
         return MMCGB_E_MESH;
     }
-    m.nf = nf;
-    build_locator(m);
     return MMCGB_OK;
 }
 
@@ -237,7 +243,7 @@ void pack_records(const HostMesh& m, std::vector<TetRec>& rec) {
 // :1170-1205).  A uniform grid of bounding boxes gives the same answer (the
 // smallest qualifying index) without the O(ne) scan per request.
 // ---------------------------------------------------------------------------
-void build_locator(HostMesh& m) {
+bool build_locator(HostMesh& m) {
     float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
     for (int i = 0; i < m.nn; i++)
         for (int d = 0; d < 3; d++) {
@@ -296,6 +302,11 @@ void build_locator(HostMesh& m) {
         std::vector<uint32_t>& k = cnt[c];
         for (size_t e = ne * c / nchunk; e < ne * (c + 1) / nchunk; e++) for_bins(e, [&](size_t bin) { k[bin]++; });
     });
+    // the CSR offsets are 32-bit (the device walks them as such)
+    uint64_t pairs = 0;
+    for (size_t c = 0; c < nchunk; c++)
+        for (size_t bin = 0; bin < nbin; bin++) pairs += cnt[c][bin];
+    if (pairs > 0xFFFFFFFFull) return false;
     g.start.assign(nbin + 1, 0);
     uint32_t run = 0;
     for (size_t bin = 0; bin < nbin; bin++) {
@@ -313,6 +324,7 @@ void build_locator(HostMesh& m) {
         for (size_t e = ne * c / nchunk; e < ne * (c + 1) / nchunk; e++)
             for_bins(e, [&](size_t bin) { g.items[k[bin]++] = (uint32_t)e; });
     });
+    return true;
 }
 
 static bool encloses(const HostMesh& m, int e, const float* p) {

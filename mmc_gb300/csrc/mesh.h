@@ -37,7 +37,7 @@ struct HostMesh {
 
 int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err);
 void pack_records(const HostMesh& m, std::vector<TetRec>& rec);
-void build_locator(HostMesh& m);
+bool build_locator(HostMesh& m);  // false when its 32-bit offsets would overflow
 int locate(const HostMesh& m, const float p[3]);
 
 // The configuration checks every simulation entry makes before it allocates
