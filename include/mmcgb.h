@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define MMCGB_ABI_VERSION 4
+#define MMCGB_ABI_VERSION 5
 
 typedef enum mmcgb_status {
     MMCGB_OK = 0,
@@ -123,7 +123,8 @@ typedef struct mmcgb_config {
     float focus;             /* focal length (the reference's srcdir.w): 0 none, > 0 converging,
                                 < 0 diverging; NaN random direction, -inf Lambertian */
     const float* srcpattern; /* pattern source weights: srcparam1.w x srcparam2.w values (type 5)
-                                or srcparam1.x x .y x .z (type 15), row-major, else NULL */
+                                or srcparam1.x x .y x .z (type 15), row-major, else NULL; with
+                                srcnum > 1 patterns, srcnum values per pixel, adjacent */
     int32_t issaveref;       /* 1: accumulate the weight of photons leaving through each exterior
                                 face per gate (diffuse reflectance/transmittance, -X) into
                                 mmcgb_result.dref */
@@ -145,11 +146,19 @@ typedef struct mmcgb_config {
                                 then normalized in place with this run's energies -- what
                                 mmc_run_cu does to cfg->exportfield / mesh->dref
                                 (src/mmc_cu_host.cu:916-976, normalization :984-1061) */
+    int32_t srcnum;          /* pattern sources (type 5): number of patterns sharing each photon
+                                (the reference's cfg->srcnum, photon sharing: a photon starts with
+                                weight 1 and every deposit is scaled by each pattern's value at its
+                                launch pixel, src/mmc_core.cl:929-942, :1907-1911); the field then
+                                holds srcnum values per (gate, element|node|voxel), adjacent, each
+                                pattern normalized with its own energies; the last column of a
+                                detected record holds the launch pixel (uint32 bits) instead of
+                                the initial weight.  0 or 1: one pattern */
 } mmcgb_config;
 
 /* Outputs.  Pointers may be NULL to skip an output; counts are always set. */
 typedef struct mmcgb_result {
-    double* field;           /* maxgate*datalen, datalen = ne (basisorder 0) or nn */
+    double* field;           /* maxgate*datalen(*srcnum), datalen = ne (basisorder 0) or nn */
     float* detp;             /* maxdetphoton*reclen detected-photon records */
     uint8_t* seeds;          /* maxdetphoton*16 */
     float* photon_weight;    /* nphoton final weights (parity tracing), or NULL; any of the three
@@ -173,6 +182,9 @@ typedef struct mmcgb_result {
                                 numbered as mmcgb_mesh_info's nf), divided by the launched weight
                                 when isnormalized, else NULL */
     float kernel_ms;         /* device time of the photon kernel */
+    double* energy_src;      /* srcnum > 1: 2*srcnum values, the launched weight of each pattern,
+                                then the escaped weight of each (energytot/energyesc are their
+                                sums, as the reference reports them), or NULL */
 } mmcgb_result;
 
 int32_t mmcgb_abi_version(void);
@@ -326,12 +338,15 @@ int32_t mmcgb_run(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, int32_t 
 #define MMCGB_NOALLOC_MAX_MEDIA 64
 #define MMCGB_NOALLOC_MAX_DET 256
 struct mmcgb_device_out {
-    double* field_raw;       /* device, maxgate*ne */
+    double* field_raw;       /* device, maxgate*ne(*srcnum) */
     float* detp;             /* device, maxdetphoton*reclen (issavedet) */
     uint8_t* seeds;          /* device, maxdetphoton*16 (issaveseed) */
     uint32_t* detcount;      /* device, 1 (issavedet) */
     double* energy;          /* device, 2 */
     uint64_t* counters;      /* device, 2 */
+    double* energy_src;      /* device, 64*2*srcnum (srcnum > 1, else NULL): launched and escaped
+                                weight per pattern in 64 slots [slot][launched|escaped][pattern],
+                                summed over the slots at the end (mmcgb_simulate_noalloc: unused) */
 };
 int32_t mmcgb_simulate_noalloc(mmcgb_mesh* mesh, const mmcgb_config* cfg, const mmcgb_device_out* out,
                                void* stream);

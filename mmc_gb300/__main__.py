@@ -145,7 +145,7 @@ def main(argv=None):
         io.write_mch(base + ".mch", res.detp, res.seeds if cfg.issaveseed else None,
                      maxmedia=np.asarray(cfg.media).shape[0] - 1,
                      detnum=0 if cfg.detpos is None else len(cfg.detpos), totalphoton=nphoton,
-                     detected=res.detected, unitinmm=cfg.unitinmm, normalizer=res.normalizer)
+                     detected=res.detected, unitinmm=cfg.unitinmm, normalizer=res.normalizer, srcnum=cfg.srcnum)
     if res.traj is not None:
         if res.ntraj > len(res.traj):
             print(f"WARNING: the saved trajectory positions ({res.ntraj}) are more than what you have specified "

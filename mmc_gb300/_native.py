@@ -56,7 +56,7 @@ class Config(C.Structure):
         ("threads", C.c_int32), ("blocks", C.c_int32), ("fast_math", C.c_int32), ("phased", C.c_int32),
         ("srcparam1", C.c_float * 4), ("srcparam2", C.c_float * 4), ("focus", C.c_float), ("srcpattern", C.c_void_p),
         ("issaveref", C.c_int32), ("method", C.c_int32), ("gridstep", C.c_float), ("maxjumpdebug", C.c_uint32),
-        ("phase_chunk", C.c_uint64), ("accumulate", C.c_int32),
+        ("phase_chunk", C.c_uint64), ("accumulate", C.c_int32), ("srcnum", C.c_int32),
     ]
 
 
@@ -68,13 +68,14 @@ class Result(C.Structure):
         ("energytot", C.c_double), ("energyesc", C.c_double), ("normalizer", C.c_double),
         ("raytet", C.c_uint64), ("aborted", C.c_uint64), ("outside", C.c_uint64), ("traj", C.c_void_p),
         ("ntraj", C.c_uint32), ("dref", C.c_void_p),
-        ("kernel_ms", C.c_float),
+        ("kernel_ms", C.c_float), ("energy_src", C.c_void_p),
     ]
 
 
 class DeviceOut(C.Structure):
     _fields_ = [("field_raw", C.c_void_p), ("detp", C.c_void_p), ("seeds", C.c_void_p),
-                ("detcount", C.c_void_p), ("energy", C.c_void_p), ("counters", C.c_void_p)]
+                ("detcount", C.c_void_p), ("energy", C.c_void_p), ("counters", C.c_void_p),
+                ("energy_src", C.c_void_p)]
 
 
 EXPORTS = [
@@ -143,7 +144,7 @@ def load():
                      "mmcgb_mesh_create", "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export",
                      "mmcgb_mesh_locate", "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run"):
             getattr(lib, name).restype = C.c_int32
-        if lib.mmcgb_abi_version() != 4:
+        if lib.mmcgb_abi_version() != 5:
             raise NativeLibraryError("libmmcgb ABI version mismatch")
         _lib = lib
         return lib

@@ -189,6 +189,8 @@ class SimConfig:
     gridstep: float = 1.0                       # voxel edge of the grid output (mm)
     phase_chunk: int = 0                        # max photons per gate-phased launch (0: what memory holds)
     accumulate: int = 0                         # 1: add into the caller's field/dref (mmc_run_cu's +=)
+    srcnum: int = 1                             # patterns sharing each photon (pattern source; the field
+                                                # gains a last axis of srcnum, srcpattern is pixel-major)
     save_field: bool = True
 
     @property
@@ -216,6 +218,7 @@ class SimConfig:
         c.maxjumpdebug = int(self.maxjumpdebug)
         c.phase_chunk = int(self.phase_chunk)
         c.accumulate = int(self.accumulate)
+        c.srcnum = int(self.srcnum)
         m = self.method
         c.method = {"elem": 0, "grid": 1}[m] if isinstance(m, str) else int(m)
         c.gridstep = float(self.gridstep)
@@ -273,6 +276,7 @@ class SimResult:
     dref: Optional[np.ndarray] = None   # (maxgate, nf) exiting weight per exterior face (issaveref)
     traj: Optional[np.ndarray] = None   # (records, 6) trajectory: id bits, x, y, z, weight, eid bits
     ntraj: int = 0                      # trajectory records produced (more than kept when truncated)
+    energy_src: Optional[np.ndarray] = None  # srcnum > 1: (2, srcnum) launched / escaped weight per pattern
 
     @property
     def absorbed_fraction(self) -> float:
@@ -287,13 +291,16 @@ def _alloc_result(mesh: Mesh, cfg: SimConfig, trace: bool, out: Optional[np.ndar
         datalen = mesh.nn if cfg.basisorder else mesh.ne
     nmed = np.asarray(cfg.media).reshape(-1, 4).shape[0]
     reclen = 1 + (2 + (1 if cfg.ismomentum else 0)) * (nmed - 1) + (6 if cfg.issaveexit else 0) + 1
+    K = max(1, int(cfg.srcnum))
+    shape = (G, datalen) if K == 1 else (G, datalen, K)
     arrs = {}
     if out is not None:
-        if out.dtype != np.float64 or out.shape != (G, datalen) or not out.flags.c_contiguous:
-            raise ValueError(f"out must be a C-contiguous float64 array of shape {(G, datalen)}")
+        if out.dtype != np.float64 or out.shape != shape or not out.flags.c_contiguous:
+            raise ValueError(f"out must be a C-contiguous float64 array of shape {shape}")
         arrs["field"] = out
     else:
-        arrs["field"] = np.empty((G, datalen), np.float64) if cfg.save_field else None
+        arrs["field"] = np.empty(shape, np.float64) if cfg.save_field else None
+    arrs["energy_src"] = np.zeros((2, K), np.float64) if K > 1 else None
     if cfg.issavedet:
         arrs["detp"] = np.zeros((int(cfg.maxdetphoton), reclen), np.float32)
         arrs["seeds"] = np.zeros((int(cfg.maxdetphoton), 16), np.uint8) if cfg.issaveseed else None
@@ -309,7 +316,7 @@ def _alloc_result(mesh: Mesh, cfg: SimConfig, trace: bool, out: Optional[np.ndar
     arrs["dref"] = np.zeros((G, mesh.nf), np.float64) if cfg.issaveref else None
     arrs["traj"] = np.zeros((int(cfg.maxjumpdebug), 6), np.float32) if cfg.maxjumpdebug else None
     r = N.Result()
-    for k in ("field", "detp", "seeds", "photon_weight", "photon_steps", "photon_det", "dref", "traj"):
+    for k in ("field", "detp", "seeds", "photon_weight", "photon_steps", "photon_det", "dref", "traj", "energy_src"):
         setattr(r, k, _ptr(arrs[k]))
     return r, arrs
 
@@ -324,7 +331,7 @@ def _make_result(r: N.Result, arrs) -> SimResult:
                      maxgate=int(r.maxgate), reclen=int(r.reclen), photon_weight=arrs["photon_weight"],
                      photon_steps=arrs["photon_steps"], photon_det=arrs["photon_det"], dref=arrs["dref"],
                      traj=None if arrs["traj"] is None else arrs["traj"][:min(int(r.ntraj), len(arrs["traj"]))].copy(),
-                     ntraj=int(r.ntraj))
+                     ntraj=int(r.ntraj), energy_src=arrs.get("energy_src"))
 
 
 def simulate(mesh: Mesh, cfg: SimConfig, trace: bool = False, out: Optional[np.ndarray] = None) -> SimResult:
@@ -453,8 +460,10 @@ class Session:
         """Torch tensors aliasing the session's raw device buffers
         (mmcgb_session_device_buffers): ``field`` (maxgate*datalen float64, None
         with float32 accumulation), ``energy`` (2 float64), ``counters`` (3 int64),
-        ``detcount`` (1 int32), ``detp`` (maxdetphoton*reclen float32) and
-        ``seeds`` (maxdetphoton*16 uint8) where the run saves them.  What they
+        ``detcount`` (1 int32), ``detp`` (maxdetphoton*reclen float32),
+        ``seeds`` (maxdetphoton*16 uint8) where the run saves them, and with
+        srcnum > 1 patterns ``energy_src`` (64 slots x 2 x srcnum float64) and a
+        field of maxgate*datalen*srcnum.  What they
         hold when the session ends is what end() reads back and normalizes.
         Synchronize the session before using them."""
         import torch
@@ -477,7 +486,9 @@ class Session:
                      "strides": None}
             return torch.as_tensor(type("DevArray", (), {"__cuda_array_interface__": iface})(), device=dev)
 
-        return dict(field=wrap(o.field_raw, G * datalen, "<f8"), energy=wrap(o.energy, 2, "<f8"),
+        K = max(1, int(cfg.srcnum))
+        return dict(field=wrap(o.field_raw, G * datalen * K, "<f8"), energy=wrap(o.energy, 2, "<f8"),
+                    energy_src=wrap(o.energy_src, 64 * 2 * K, "<f8") if K > 1 else None,
                     counters=wrap(o.counters, 3, "<i8"), detcount=wrap(o.detcount, 1, "<i4"),
                     detp=wrap(o.detp, maxdet * reclen, "<f4"),
                     seeds=wrap(o.seeds, maxdet * 16, "|u1") if cfg.issaveseed else None, reclen=reclen)

@@ -48,6 +48,9 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 int gates_of(const mmcgb_config& c) { return (int)((c.tend - c.tstart) / c.tstep + 0.5f); }
 
+// Patterns sharing each photon (mmcgb_config.srcnum; 0 means 1).
+int src_count(const mmcgb_config& c) { return c.srcnum > 1 ? c.srcnum : 1; }
+
 // Free device memory for new stream-ordered allocations: what the driver
 // reports plus what the default pool holds without using.
 size_t free_device_memory(int device) {
@@ -100,7 +103,9 @@ size_t frame_len(const HostMesh& m, const mmcgb_config& c) {
 bool point_source(int t) { return t == 0 || t == 1 || t == 2 || t == 7; }
 
 size_t pattern_len(const mmcgb_config& c) {
-    if (c.srctype == 5) return (size_t)std::max(0, (int)c.srcparam1[3]) * (size_t)std::max(0, (int)c.srcparam2[3]);
+    if (c.srctype == 5)
+        return (size_t)std::max(0, (int)c.srcparam1[3]) * (size_t)std::max(0, (int)c.srcparam2[3]) *
+               (size_t)src_count(c);
     if (c.srctype == 15)
         return (size_t)std::max(0, (int)c.srcparam1[0]) * (size_t)std::max(0, (int)c.srcparam1[1]) *
                (size_t)std::max(0, (int)c.srcparam1[2]);
@@ -126,13 +131,18 @@ int mmcgb::validate_config(const HostMesh& m, const mmcgb_config& c, std::string
     }
     for (int k = 0; k < 4; k++)
         if (!std::isfinite(c.srcparam1[k]) || !std::isfinite(c.srcparam2[k])) { err = "source parameters must be finite"; return MMCGB_E_ARG; }
+    if (c.srcnum < 0) { err = "srcnum must be >= 0"; return MMCGB_E_ARG; }
+    if (c.srcnum > 1 && c.srctype != 5) { err = "srcnum > 1 needs a pattern source (srctype 5)"; return MMCGB_E_ARG; }
+    // the reference refuses the same (src/mmc_utils.c:3534-3536)
+    if (c.srcnum > 1 && c.replayseed) { err = "photon sharing (srcnum > 1) does not replay"; return MMCGB_E_ARG; }
     if (!(c.tstep > 0.f) || !(c.tend > c.tstart)) { err = "time gates need tstep > 0 and tend > tstart"; return MMCGB_E_ARG; }
     if (gates_of(c) < 1) { err = "time window holds no gate"; return MMCGB_E_ARG; }
     // The engine addresses a fluence cell (gate, element or voxel) with a 32-bit index and keeps
     // 0x7FFFFFFF as its "no pending deposit" mark, so every cell index must stay below it.
-    if (frame_len(m, c) * (size_t)gates_of(c) >= (size_t)kMaxFluenceCells) {
+    if (frame_len(m, c) * (size_t)gates_of(c) * (size_t)src_count(c) >= (size_t)kMaxFluenceCells) {
         err = "fluence of " + std::to_string(frame_len(m, c)) + " cells x " + std::to_string(gates_of(c)) +
-              " gates exceeds the engine's 2^31-1 cells: use fewer gates" + (c.method == 1 ? " or a larger gridstep" : "");
+              " gates" + (src_count(c) > 1 ? " x " + std::to_string(src_count(c)) + " patterns" : std::string()) +
+              " exceeds the engine's 2^31-1 cells: use fewer gates" + (c.method == 1 ? " or a larger gridstep" : "");
         return MMCGB_E_ARG;
     }
     if (c.nmedia < 2 || c.nmedia > kMaxMedia || !c.media) { err = "media table needs 2..64 rows (row 0 = background)"; return MMCGB_E_ARG; }
@@ -186,6 +196,7 @@ struct SimBuffers {
     unsigned long long* seeds = nullptr;
     unsigned int* detcount = nullptr;
     double* energy = nullptr;
+    double* energy_src = nullptr;  // photon sharing: 64 slots x 2 x srcnum
     unsigned long long* counters = nullptr;
     float* pattern = nullptr;
     double* dref = nullptr;
@@ -234,7 +245,7 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     const int M = c.nmedia - 1;
     const int reclen_dev = (2 + (c.ismomentum > 0)) * M + (c.issaveexit > 0) * 6 + 1;
     P.reclen = reclen_dev + 1;
-    P.flen = frame_len(m, c) * P.maxgate;
+    P.flen = frame_len(m, c) * P.maxgate * (size_t)src_count(c);
     SimBuffers& B = P.buf;
     B.stream = stream;
     const bool f64 = c.accum_f64 != 0;
@@ -249,6 +260,10 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     if (c.issaveseed) CK(B.alloc(&B.seeds, maxdet * 2));
     CK(B.alloc(&B.detcount, 1));
     CK(B.alloc(&B.energy, 2));
+    if (src_count(c) > 1) {
+        CK(B.alloc(&B.energy_src, (size_t)kEnergySlots * 2 * src_count(c)));
+        CK(cudaMemsetAsync(B.energy_src, 0, sizeof(double) * kEnergySlots * 2 * src_count(c), stream));
+    }
     CK(B.alloc(&B.counters, 3));
     if (c.maxjumpdebug) {
         CK(B.alloc(&B.traj, (size_t)c.maxjumpdebug * 6));
@@ -310,6 +325,8 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     S.srcp2 = make_float4(c.srcparam2[0], c.srcparam2[1], c.srcparam2[2], c.srcparam2[3]);
     S.focus = c.focus;
     S.srcpattern = B.pattern;
+    S.srcnum = src_count(c);
+    S.energy_src = B.energy_src;
     S.loc_start = mesh->loc_start;
     S.loc_items = mesh->loc_items;
     S.loc_res = m.grid.res;
@@ -380,8 +397,55 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
     CK(cudaMemcpyAsync(energy, B.energy, sizeof(energy), cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(counters, B.counters, sizeof(counters), cudaMemcpyDeviceToHost, stream));
     const size_t saved = std::min<size_t>(detected, c.issavedet ? c.maxdetphoton : 0);
+    const int K = src_count(c);
+    std::vector<double> esrc;  // photon sharing: launched weight per pattern, then escaped weight
+    if (K > 1) {
+        std::vector<double> slots((size_t)kEnergySlots * 2 * K);
+        CK(cudaMemcpyAsync(slots.data(), B.energy_src, sizeof(double) * slots.size(), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        esrc.assign(2 * (size_t)K, 0.0);
+        for (int sl = 0; sl < kEnergySlots; sl++)
+            for (size_t i = 0; i < 2 * (size_t)K; i++) esrc[i] += slots[(size_t)sl * 2 * K + i];
+    }
     double normalizer = 1.0;
-    if (res->field && c.accumulate) {
+    if (res->field && K > 1) {
+        // Photon sharing: each pattern's deposits (cells of one gate and element adjacent,
+        // src/mmc_cu_host.cu:961-971) scattered, accumulated and normalized with that pattern's
+        // energies (src/mmc_cu_host.cu:984-995); the normalizer reported is their mean.
+        // Host output stage.
+        const int G = P.maxgate;
+        std::vector<double> raw(P.flen);
+        if (B.f64) {
+            CK(cudaMemcpyAsync(raw.data(), B.f64, sizeof(double) * P.flen, cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+        } else {
+            std::vector<float> ab(2 * P.flen);
+            CK(cudaMemcpyAsync(ab.data(), B.f32, sizeof(float) * 2 * P.flen, cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+            for (size_t i = 0; i < P.flen; i++) raw[i] = (double)ab[i] + (double)ab[P.flen + i];
+        }
+        const size_t frame = P.flen / ((size_t)G * K);
+        const size_t datalen = (c.method == 1) ? frame : (c.basisorder ? (size_t)mesh->host.nn : (size_t)mesh->host.ne);
+        const size_t nout = datalen * G;
+        std::vector<double> raw_p(frame * G), add(nout), field_p(nout);
+        double sum_norm = 0.0;
+        for (int p = 0; p < K; p++) {
+            for (size_t i = 0; i < frame * G; i++) raw_p[i] = raw[i * K + p];
+            for (size_t i = 0; i < nout; i++) field_p[i] = c.accumulate ? res->field[i * K + p] : 0.0;
+            double norm;
+            if (c.method == 1) {
+                norm = grid_normalizer(c, esrc[p]);
+                for (size_t i = 0; i < nout; i++) field_p[i] = (field_p[i] + raw_p[i]) * norm;
+            } else {
+                scatter_output(mesh->host, c, G, raw_p.data(), add.data());
+                for (size_t i = 0; i < nout; i++) field_p[i] += add[i];
+                norm = normalize_in_place(mesh->host, c, G, esrc[p], esrc[K + p], field_p.data());
+            }
+            sum_norm += norm;
+            for (size_t i = 0; i < nout; i++) res->field[i * K + p] = field_p[i];
+        }
+        normalizer = sum_norm / K;
+    } else if (res->field && c.accumulate) {
         // mmc_run_cu's semantics (src/mmc_cu_host.cu:916-976, :984-1061): this run's deposits
         // (scattered to the nodes) are added to what the caller's field holds, then the sum is
         // normalized in place with this run's energies.  Host output stage.
@@ -475,6 +539,15 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
     (void)launched;
     res->energytot = energy[0];  // launched weight, summed on the device (source weights may be < 1)
     res->energyesc = energy[1];
+    const double launched_w = energy[0];
+    if (K > 1) {  // the patterns' sums, as the reference reports them (src/mmc_cu_host.cu:776-781)
+        res->energytot = res->energyesc = 0.0;
+        for (int p = 0; p < K; p++) {
+            res->energytot += esrc[p];
+            res->energyesc += esrc[K + p];
+        }
+        if (res->energy_src) std::memcpy(res->energy_src, esrc.data(), sizeof(double) * 2 * K);
+    }
     res->raytet = counters[0];
     res->aborted = counters[1];
     res->outside = counters[2];
@@ -482,8 +555,10 @@ int finish_sim(mmcgb_mesh* mesh, const mmcgb_config& c, Prepared& P, mmcgb_resul
     if (!dref_run.empty())  // mesh->dref += dref (src/mmc_cu_host.cu:978-982)
         for (size_t i = 0; i < nref; i++) res->dref[i] += dref_run[i];
     if (res->dref && B.dref == nullptr && nref && !c.accumulate) std::memset(res->dref, 0, sizeof(double) * nref);
-    if (res->dref && c.isnormalized && energy[0] > 0) {  // src/mmc_mesh.c:2160-2167
-        const float normalizor = 1.f / (float)energy[0];
+    if (res->dref && c.isnormalized && launched_w > 0) {  // src/mmc_mesh.c:2160-2167
+        // (a shared photon's exit weight is not scaled by the patterns: the launched photon
+        // weight normalizes it)
+        const float normalizor = 1.f / (float)launched_w;
         for (size_t i = 0; i < nref; i++) res->dref[i] *= normalizor;
     }
     if (res->outside)
@@ -562,6 +637,7 @@ void mmcgb_config_defaults(mmcgb_config* c) {
     c->maxdetphoton = 1000000;
     c->accum_f64 = 1;
     c->fast_math = 1;
+    c->srcnum = 1;
 }
 
 int32_t mmcgb_mesh_create(const mmcgb_mesh_desc* desc, int32_t device, mmcgb_mesh** out) {
@@ -1140,6 +1216,7 @@ int32_t mmcgb_session_device_buffers(mmcgb_session* s, mmcgb_device_out* out) {
     out->detcount = B.detcount;
     out->energy = B.energy;
     out->counters = reinterpret_cast<uint64_t*>(B.counters);
+    out->energy_src = B.energy_src;
     return MMCGB_OK;
 }
 

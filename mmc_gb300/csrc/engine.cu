@@ -67,6 +67,7 @@ struct Lane {
     unsigned long long t0, t1;
     unsigned long long pid;  // photon index inside its simulation
     int sim;
+    int posidx;  // launch pixel of a photon shared by several patterns (general kernels only)
 };
 
 // Arithmetic policies.  Exact: IEEE division and square root, the project's
@@ -190,6 +191,21 @@ __device__ __forceinline__ void deposit(const SimDev& S, unsigned idx, float val
     }
 }
 
+// Photon sharing (a pattern source with srcnum > 1 patterns, src/mmc_core.cl:929-942,
+// :989-1002): one photon, launched with weight 1, stands for every pattern; a deposit of
+// weight w adds w x (the pattern's value at the photon's launch pixel) to each pattern's
+// cell, cells of one (element, gate) adjacent.
+template <bool GEN>
+__device__ __forceinline__ void deposit_at(const SimDev& S, const Lane& L, unsigned idx, float val) {
+    if (GEN && S.srcnum > 1) {
+        const float* pat = S.srcpattern + (size_t)L.posidx * S.srcnum;
+        const unsigned base = idx * (unsigned)S.srcnum;
+        for (int p = 0; p < S.srcnum; p++) deposit(S, base + p, val * __ldg(pat + p));
+        return;
+    }
+    deposit(S, idx, val);
+}
+
 // One branchless Badouel step with fused deposit.  Requires 1 <= L.eid <= ne.
 // REPLAY: the kernel may run replay simulations (output types wl, wp, wn and
 // the Jacobian); kernels for forward runs are compiled without those branches.
@@ -307,14 +323,14 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
                 const float dw = w0 * frac;
                 if (L.oldidx == (unsigned)kIdUndef) L.oldidx = newidx;
                 if (newidx != L.oldidx) {
-                    if (L.oldw > 0.f) deposit(S, L.oldidx, L.oldw);
+                    if (L.oldw > 0.f) deposit_at<GEN>(S, L, L.oldidx, L.oldw);
                     L.oldidx = newidx;
                     L.oldw = dw;
                 } else {
                     L.oldw += dw;
                 }
                 if (flush) {
-                    deposit(S, newidx, L.oldw);
+                    deposit_at<GEN>(S, L, newidx, L.oldw);
                     L.oldw = 0.f;
                 }
                 w0 *= segloss;
@@ -331,14 +347,14 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
         const unsigned newidx = (unsigned)(L.eid - 1) + (unsigned)(gate * S.ne);
         if (L.oldidx == (unsigned)kIdUndef) L.oldidx = newidx;
         if (newidx != L.oldidx) {
-            if (L.oldw > 0.f) deposit(S, L.oldidx, L.oldw);
+            if (L.oldw > 0.f) deposit_at<GEN>(S, L, L.oldidx, L.oldw);
             L.oldidx = newidx;
             L.oldw = ww;
         } else {
             L.oldw += ww;
         }
         if (L.faceid == -2 || !L.isend) {
-            deposit(S, newidx, L.oldw);
+            deposit_at<GEN>(S, L, newidx, L.oldw);
             L.oldw = 0.f;
         }
         L.px = MP::mad(Lmove, L.vx, L.px);
@@ -602,7 +618,10 @@ __device__ __forceinline__ bool launch_photon(Lane& L, const SimDev& S) {
             if (st == ST_PATTERN) {
                 const int nx = (int)p1.w, ny = (int)p2.w;
                 const int idx = min((int)(ry * ny), ny - 1) * nx + min((int)(rx * nx), nx - 1);
-                L.weight = __ldg(S.srcpattern + idx);
+                // several patterns share the photon: it starts with weight 1 and its deposits
+                // are scaled per pattern (src/mmc_core.cl:1545-1549)
+                L.posidx = idx;
+                L.weight = (S.srcnum > 1) ? 1.f : __ldg(S.srcpattern + idx);
             } else if (st == ST_FOURIER) {
                 float sv, cv;
                 MP::sincos2pi(floorf(p1.w) * rx + floorf(p2.w) * ry + p1.w - floorf(p1.w), sv, cv);
@@ -836,6 +855,15 @@ __device__ __forceinline__ void flush_tally(Tally& t, const SimDev& S) {
     t.outside = 0;
 }
 
+// Launched (which = 0) or escaped (1) weight of a photon shared by srcnum > 1 patterns, per
+// pattern: w x the pattern's value at the launch pixel (src/mmc_core.cl:1907-1911, :2154-2159).
+// Blocks add into 64 slots of [srcnum launched | srcnum escaped] doubles to spread the atomics.
+__device__ __forceinline__ void tally_sources(const SimDev& S, int posidx, float w, int which) {
+    double* e = S.energy_src + ((size_t)(blockIdx.x % kEnergySlots) * 2 + which) * S.srcnum;
+    const float* pat = S.srcpattern + (size_t)posidx * S.srcnum;
+    for (int p = 0; p < S.srcnum; p++) atomicAdd(e + p, (double)(w * __ldg(pat + p)));
+}
+
 struct SingleSim {
     const SimDev& s;
     __device__ __forceinline__ const SimDev& operator()(int) const { return s; }
@@ -937,6 +965,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                         L.weight = r.dir.w;
                         L.slen = r.len.x;
                         L.slen0 = r.len.y;
+                        if (SRC && !REPLAY) L.posidx = __float_as_int(r.len.y);
                         L.oldw = r.len.z;
                         L.oldidx = __float_as_uint(r.len.w);
                         L.eid = r.elem.x;
@@ -996,9 +1025,13 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                         placed = launch_photon<MP>(L, S);
                     }
                     tally.etot += L.weight;
+                    const bool shared = SRC && S.srcnum > 1;
+                    if (shared) tally_sources(S, L.posidx, L.weight, 0);
                     if (S.issavedet) {
                         for (int i = 0; i < S.reclen; i++) PP(i) = 0.f;
-                        PP(S.reclen - 1) = L.weight;
+                        // the last column: initial weight, or the launch pixel of a shared photon
+                        // (src/mmc_core.cl:1894-1898)
+                        PP(S.reclen - 1) = shared ? __int_as_float(L.posidx) : L.weight;
                     }
                     if (placed) {
                         L.mode = M_OUTER;
@@ -1006,6 +1039,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                     } else {  // launch position in no element: counted, reported as an error
                         if (BATCHED) tally.outside++; else atomicAdd(&s_cnt[2], 1ull);
                         tally.eesc += L.weight;
+                        if (shared) tally_sources(S, L.posidx, L.weight, 1);
                         if (SRC && S.photon_det) S.photon_det[L.pid] = 0;
                         if (SRC && S.photon_weight) S.photon_weight[L.pid] = L.weight;
                         if (SRC && S.photon_steps) S.photon_steps[L.pid] = 0;
@@ -1040,7 +1074,9 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                     __stcs(&q->pos, make_float4(L.px, L.py, L.pz, L.ptime));
                     __stcs(&q->dir, make_float4(L.vx, L.vy, L.vz, L.weight));
                     // slen0 is read only by replay kernels; the others leave it out so it holds no register
-                    __stcs(&q->len, make_float4(L.slen, REPLAY ? L.slen0 : 0.f, L.oldw, __uint_as_float(L.oldidx)));
+                    // (forward kernels carry a shared photon's launch pixel there instead)
+                    __stcs(&q->len, make_float4(L.slen, REPLAY ? L.slen0 : (SRC ? __int_as_float(L.posidx) : 0.f),
+                                               L.oldw, __uint_as_float(L.oldidx)));
                     __stcs(&q->elem, make_int4(L.eid, L.label, L.mode, L.fixcount));
                     __stcs(&q->meta, make_uint4(L.steps, (unsigned)L.pid, (unsigned)(L.pid >> 32), key));
                     __stcs(&q->rng, make_uint4((unsigned)L.t0, (unsigned)(L.t0 >> 32), (unsigned)L.t1,
@@ -1075,6 +1111,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
                     if (SRC && S.traj) save_traj(S, L);
                     if (SRC && S.photon_det) S.photon_det[L.pid] = 0;
                     tally.eesc += L.weight;
+                    if (SRC && S.srcnum > 1) tally_sources(S, L.posidx, L.weight, 1);
                     if (BATCHED) tally.raytet += L.steps; else atomicAdd(&s_cnt[0], (unsigned long long)L.steps);
                     if (SRC && S.photon_weight) S.photon_weight[L.pid] = L.weight;
                     if (SRC && S.photon_steps) S.photon_steps[L.pid] = L.steps;
@@ -1255,6 +1292,7 @@ __device__ __forceinline__ void engine_body(const Sims& sims, const unsigned lon
         if (ended) {
             if (SRC && S.traj) save_traj(S, L);
             tally.eesc += L.weight;
+            if (SRC && S.srcnum > 1) tally_sources(S, L.posidx, L.weight, 1);
             if (BATCHED) tally.raytet += L.steps; else atomicAdd(&s_cnt[0], (unsigned long long)L.steps);
             if (SRC && S.photon_weight) S.photon_weight[L.pid] = L.weight;
             if (SRC && S.photon_steps) S.photon_steps[L.pid] = L.steps;

@@ -31,6 +31,8 @@ inline int max_elem(int lbits) { return (int)((1u << (31 - lbits)) - 1u); }
 // Fluence cells (gates x elements or voxels) one simulation may hold: deposit indices are
 // 32-bit and 0x7FFFFFFF marks "no pending deposit", so every index stays below it.
 constexpr unsigned kMaxFluenceCells = 0x7FFFFFFFu;
+// Slots of per-pattern energy tallies (photon sharing): a block adds into slot blockIdx % 64.
+constexpr int kEnergySlots = 64;
 
 // One tetrahedron as the step kernel reads it: 80 bytes, 16-byte aligned.
 //   nx/ny/nz/nd : outward unit normals and plane offsets of the 4 faces
@@ -73,7 +75,9 @@ struct SimDev {
     int srctype;
     float4 srcp1, srcp2;   // srcparam1, srcparam2
     float focus;
-    const float* srcpattern;
+    const float* srcpattern;  // pixel-major: the srcnum patterns' values of a pixel adjacent
+    int srcnum;               // patterns sharing each photon (pattern sources), 1 otherwise
+    double* energy_src;       // srcnum > 1: 64 slots of [launched, escaped] weight per pattern
     // bounding-box grid of the mesh (per-photon source element search):
     // cell (x,y,z) lists the elements whose bounding boxes overlap it
     const unsigned* loc_start;  // res^3 + 1 offsets

@@ -123,7 +123,7 @@ def _simulate_sharded_on_device(mesh: Mesh, cfg: SimConfig, off: int, n: int, gr
         saved = 0
         if b["detcount"] is not None:
             saved = min(int(b["detcount"].item()), int(cfg.maxdetphoton))
-        for key in ("field", "energy", "counters", "detcount"):
+        for key in ("field", "energy", "energy_src", "counters", "detcount"):
             if b[key] is not None:
                 dist.all_reduce(b[key], op=dist.ReduceOp.SUM, group=group)
         detp = seeds = None
@@ -154,6 +154,8 @@ def simulate_sharded(mesh: Mesh, cfg: SimConfig, group=None,
     off, n = shard(cfg.nphoton, rank, world)
     if runner is None and dist.get_backend(group) == "nccl":
         return _simulate_sharded_on_device(mesh, cfg, off, n, group)
+    if int(cfg.srcnum) > 1:
+        raise ValueError("a simulation whose patterns share photons (srcnum > 1) is combined on the GPUs (NCCL) only")
     local_cfg = dataclasses.replace(cfg, photon_offset=cfg.photon_offset + off, nphoton=n, isnormalized=0,
                                     basisorder=0, save_field=True)
     run = runner or (lambda c: simulate(mesh, c))

@@ -54,6 +54,26 @@ def read_dat_mesh(mesh_id: str, root: str):
     return out
 
 
+_JDATA_TYPES = {"single": np.float32, "double": np.float64, "int32": np.int32, "uint32": np.uint32,
+                "int8": np.int8, "uint8": np.uint8, "int16": np.int16, "uint16": np.uint16}
+
+
+def _jdata_array(obj) -> np.ndarray:
+    """A JData array object: _ArrayData_ (a list) or _ArrayZipData_ (base64 of zlib or
+    gzip bytes), row-major, of _ArrayType_ and _ArraySize_."""
+    import base64
+    import zlib
+    dt = _JDATA_TYPES[str(obj.get("_ArrayType_", "double"))]
+    shape = [int(x) for x in np.ravel(obj["_ArraySize_"])]
+    if "_ArrayZipData_" in obj:
+        ztype = str(obj.get("_ArrayZipType_", "zlib")).lower()
+        if ztype not in ("zlib", "gzip"):
+            raise ValueError(f"JData compression '{ztype}' is not supported (zlib, gzip)")
+        raw = zlib.decompress(base64.b64decode(obj["_ArrayZipData_"]), 31 if ztype == "gzip" else 15)
+        return np.frombuffer(raw, dt).reshape(shape)
+    return np.asarray(obj["_ArrayData_"], dt).reshape(shape)
+
+
 def _media_from_json(media):
     rows = []
     for m in media:
@@ -140,7 +160,16 @@ def load_input(path):
     if stype not in SOURCE_TYPES:
         raise ValueError(f"unknown source type '{stype}'")
     pattern = src.get("Pattern")
-    if isinstance(pattern, dict):
+    srcnum = 1
+    if isinstance(pattern, dict) and ("_ArrayZipData_" in pattern or "_ArrayData_" in pattern):
+        # a JData array, row-major as stored, turned column-major as the reference does
+        # (mcx_convertrow2col); [srcnum, Nx, Ny] holds patterns sharing each photon
+        # (src/mmc_utils.c:2086-2104)
+        arr = _jdata_array(pattern)
+        if arr.ndim == 3 and arr.shape[0] > 1 and arr.shape[2] > 1 and stype == "pattern":
+            srcnum = int(arr.shape[0])
+        pattern = arr.ravel(order="F")
+    elif isinstance(pattern, dict):
         pattern = pattern.get("Data")
     pattern = None if pattern is None else np.asarray(pattern, np.float32).ravel()
     t0 = float(fwd.get("T0", 0.0))
@@ -153,7 +182,7 @@ def load_input(path):
         srcpos=tuple(float(x) for x in src.get("Pos", [0, 0, 0])[:3]), srcdir=tuple(float(x) for x in srcdir),
         srctype=stype, srcparam1=tuple(float(x) for x in (list(src.get("Param1", [])) + [0.0] * 4)[:4]),
         srcparam2=tuple(float(x) for x in (list(src.get("Param2", [])) + [0.0] * 4)[:4]), focus=focus,
-        srcpattern=pattern,
+        srcpattern=pattern, srcnum=srcnum,
         e0=int(msh.get("InitElem", 0)), tstart=t0, tend=t1, tstep=dt,
         isreflect=int(ses.get("DoMismatch", 1)), issaveref=int(ses.get("DoSaveRef", 0)),
         gridstep=float(np.ravel(dom.get("Step", [1.0]))[0]), isspecular=int(ses.get("DoSpecular", 0)),
@@ -182,12 +211,12 @@ def _debug_letters(level: int) -> str:
 # ---------------------------------------------------------------------------
 def write_mch(path: str, detp: np.ndarray, seeds: Optional[np.ndarray], maxmedia: int, detnum: int,
               totalphoton: int, detected: int, unitinmm: float = 1.0, normalizer: float = 1.0,
-              savedetflag: int = 0):
+              savedetflag: int = 0, srcnum: int = 1):
     detp = np.ascontiguousarray(detp, np.float32)
     n, cols = detp.shape if detp.ndim == 2 else (0, 0)
     seedbyte = 16 if seeds is not None else 0
     hdr = MCH_HEADER.pack(b"MCXH", 1, maxmedia, detnum, cols, int(totalphoton) & 0xFFFFFFFF, int(detected), n,
-                          float(unitinmm), seedbyte, float(normalizer), 1, 1, savedetflag, 0, 0)
+                          float(unitinmm), seedbyte, float(normalizer), max(1, int(srcnum)), 1, savedetflag, 0, 0)
     with open(path, "wb") as f:
         f.write(hdr)
         f.write(detp.tobytes())

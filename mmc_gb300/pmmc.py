@@ -71,8 +71,14 @@ def _parse(cfg: dict):
             v = list(np.asarray(cfg[k], np.float64).ravel()) + [0.0] * 4
             kw[k] = tuple(float(x) for x in v[:4])
     if "srcpattern" in cfg:
-        # pmmc passes patterns as [Nx, Ny(, Nz)] arrays in Fortran order: x runs fastest
-        kw["srcpattern"] = np.asarray(cfg["srcpattern"], np.float32).ravel(order="F")
+        # pmmc passes patterns as [Nx, Ny(, Nz)] arrays in Fortran order: x runs fastest.  A pattern
+        # source given [srcnum, Nx, Ny] (srcnum > 1, Ny > 1) holds patterns that share each photon,
+        # as the reference reads a 3-D JSON pattern (src/mmc_utils.c:2100-2102)
+        pat = np.asarray(cfg["srcpattern"], np.float32)
+        if (pat.ndim == 3 and pat.shape[0] > 1 and pat.shape[2] > 1
+                and srctype == "pattern"):
+            kw["srcnum"] = int(pat.shape[0])
+        kw["srcpattern"] = pat.ravel(order="F")
     for k in _SCALARS_INT:
         if k in cfg:
             kw[k] = int(cfg[k])
@@ -132,10 +138,14 @@ def run(cfg: dict) -> dict:
         if e.code == 1:
             raise ValueError(str(e)) from e
         raise RuntimeError(str(e)) from e
+    # [datalen, maxgate]; with patterns sharing photons [srcnum, datalen, maxgate] (src/pmmc.cpp:1196-1207)
     field = res.field.T
-    if sc.method == "grid":  # [dim.x, dim.y, dim.z, maxgate], x fastest as the reference
+    if sc.method == "grid":  # [dim.x, dim.y, dim.z, maxgate] (+ a leading srcnum), x fastest as the reference
         dx, dy, dz = mesh_dims
-        field = res.field.reshape(-1, dz, dy, dx).transpose(3, 2, 1, 0)
+        if res.field.ndim == 3:
+            field = res.field.reshape(-1, dz, dy, dx, res.field.shape[-1]).transpose(4, 3, 2, 1, 0)
+        else:
+            field = res.field.reshape(-1, dz, dy, dx).transpose(3, 2, 1, 0)
     out = {"flux": field, "stat": dict(runtime=(time.perf_counter() - t0) * 1e3, nphoton=nph,
                                              energytot=res.energytot, energyabs=res.energytot - res.energyesc,
                                              normalizer=res.normalizer, raytet=res.raytet,

@@ -324,6 +324,7 @@ typedef struct {
     float* f32b;
     double* f64;     /* double fluence (accum_f64 == 1) */
     int reclen;      /* detreclen (without the det id column) */
+    int K;           /* patterns sharing each photon */
 } engine;
 
 typedef struct {
@@ -332,6 +333,7 @@ typedef struct {
     float weight, photontimer, slen, Lmove, slen0, oldweight;
     uint32_t oldidx;
     uint32_t photonid;
+    int posidx;      /* launch pixel of a pattern source */
 } ray;
 
 static void deposit(engine* g, uint32_t idx, float val) {
@@ -354,6 +356,17 @@ static void deposit(engine* g, uint32_t idx, float val) {
             g->f32b[idx] += moved;
         }
     }
+}
+
+/* photon sharing (src/mmc_core.cl:929-942, :989-1002): a deposit of w adds w times each
+ * pattern's value at the photon's launch pixel to that pattern's cell */
+static void deposit_src(engine* g, const ray* r, uint32_t idx, float val) {
+    if (g->K > 1) {
+        const float* pat = g->cfg->srcpattern + (size_t)r->posidx * g->K;
+        for (int p = 0; p < g->K; p++) deposit(g, idx * (uint32_t)g->K + (uint32_t)p, val * pat[p]);
+        return;
+    }
+    deposit(g, idx, val);
 }
 
 static float medium(const engine* g, int t, int k) { return g->cfg->media[4 * t + k]; }
@@ -454,14 +467,14 @@ static float raytet_step(engine* g, ray* r) {
                 float dw = w0 * frac;
                 if (r->oldidx == (uint32_t)O_ID_UNDEF) r->oldidx = nidx;
                 if (nidx != r->oldidx) {
-                    if (r->oldweight > 0.f) deposit(g, r->oldidx, r->oldweight);
+                    if (r->oldweight > 0.f) deposit_src(g, r, r->oldidx, r->oldweight);
                     r->oldidx = nidx;
                     r->oldweight = dw;
                 } else {
                     r->oldweight += dw;
                 }
                 if (flush) {
-                    deposit(g, nidx, r->oldweight);
+                    deposit_src(g, r, nidx, r->oldweight);
                     r->oldweight = 0.f;
                 }
                 w0 *= segloss;
@@ -475,14 +488,14 @@ static float raytet_step(engine* g, ray* r) {
         uint32_t newidx = (uint32_t)(r->eid - 1) + tshift;
         if (r->oldidx == (uint32_t)O_ID_UNDEF) r->oldidx = newidx;
         if (newidx != r->oldidx) {
-            if (r->oldweight > 0.f) deposit(g, r->oldidx, r->oldweight);
+            if (r->oldweight > 0.f) deposit_src(g, r, r->oldidx, r->oldweight);
             r->oldidx = newidx;
             r->oldweight = ww;
         } else {
             r->oldweight += ww;
         }
         if (r->faceid == -2 || !r->isend) {
-            deposit(g, newidx, r->oldweight);
+            deposit_src(g, r, newidx, r->oldweight);
             r->oldweight = 0.f;
         }
         r->px = r->px + r->Lmove * r->vx;
@@ -768,7 +781,9 @@ static int launch_photon(const engine* g, ray* r, uint64_t* ran) {
                 int iy = (int)(ry * ny), ix = (int)(rx * nx);
                 if (iy > ny - 1) iy = ny - 1;
                 if (ix > nx - 1) ix = nx - 1;
-                r->weight = cfg->srcpattern[iy * nx + ix];
+                /* with several patterns the photon starts with weight 1 (src/mmc_raytrace.c:2394) */
+                r->posidx = iy * nx + ix;
+                r->weight = (g->K > 1) ? 1.f : cfg->srcpattern[iy * nx + ix];
             } else if (st == 6) {
                 float sv, cv;
                 oracle_sincos2pi(floorf(p1[3]) * rx + floorf(p2[3]) * ry + p1[3] - floorf(p1[3]), &sv, &cv);
@@ -935,7 +950,15 @@ typedef struct {
     uint64_t raytet;
     uint64_t aborted;
     uint64_t outside;
+    double* esrc;    /* srcnum > 1: launched weight per pattern, then escaped (2*srcnum) */
 } tallies;
+
+/* a shared photon's launched (which 0) or escaped (1) weight per pattern (src/mmc_core.cl:
+ * 1907-1911, :2154-2159) */
+static void tally_src(const engine* g, const ray* r, tallies* tl, int which) {
+    const float* pat = g->cfg->srcpattern + (size_t)r->posidx * g->K;
+    for (int p = 0; p < g->K; p++) tl->esrc[which * g->K + p] += (double)(r->weight * pat[p]);
+}
 
 /* the photon life: src/mmc_core.cl:1851-2161 */
 /* One trajectory record, savedebugdata in src/mmc_raytrace.c:1739-1756:
@@ -984,11 +1007,14 @@ static void onephoton(engine* g, uint64_t pidx, float* ppath, oracle_out* out, t
     int aborted = 0;
     /* launch: src/mmc_raytrace.c:2346-2671 */
     const int placed = launch_photon(g, r, ran);
-    if (cfg->issavedet) ppath[reclen - 1] = r->weight;
+    /* the last record column: the initial weight, or a shared photon's launch pixel */
+    if (cfg->issavedet) ppath[reclen - 1] = (g->K > 1) ? bits2f((uint32_t)r->posidx) : r->weight;
     tl->etot += r->weight;
+    if (g->K > 1) tally_src(g, r, tl, 0);
     if (!placed) {
         tl->outside++;
         tl->eesc += r->weight;
+        if (g->K > 1) tally_src(g, r, tl, 1);
         if (out->photon_weight) out->photon_weight[pidx] = r->weight;
         if (out->photon_steps) out->photon_steps[pidx] = 0;
         if (out->photon_det) out->photon_det[pidx] = 0;
@@ -1117,6 +1143,7 @@ done:
 #undef PPATH
     if (out->traj) save_traj(g, r, pidx, out);   /* src/mmc_raytrace.c:2109-2111 */
     tl->eesc += r->weight;
+    if (g->K > 1) tally_src(g, r, tl, 1);
     tl->raytet += steps;
     tl->aborted += aborted;
     if (out->photon_weight) out->photon_weight[pidx] = r->weight;
@@ -1149,6 +1176,7 @@ int oracle_run(int nn, const float* node, int ne, const int* elem, const int* la
     g.Rtstep = 1.f / cfg->tstep;
     g.maxgate = cfg->maxgate;
     g.reclen = (2 + (cfg->ismomentum > 0)) * g.M + (cfg->issaveexit > 0) * 6 + 1;
+    g.K = (cfg->srcnum > 1 && cfg->srctype == 5) ? cfg->srcnum : 1;
     out->reclen = g.reclen + 1;
     out->nf = nf;
     if (out->dref) memset(out->dref, 0, sizeof(double) * (size_t)nf * cfg->maxgate);
@@ -1162,7 +1190,8 @@ int oracle_run(int nn, const float* node, int ne, const int* elem, const int* la
         for (int k = 0; k < 3; k++) g.gdim[k] = (uint32_t)d[k];
         g.framelen = (uint32_t)d[0] * (uint32_t)d[1] * (uint32_t)d[2];
     }
-    size_t flen = (size_t)g.framelen * cfg->maxgate;
+    size_t flen = (size_t)g.framelen * cfg->maxgate * g.K;
+    if (out->energy_src && g.K > 1) memset(out->energy_src, 0, sizeof(double) * 2 * g.K);
     if (cfg->accum_f64) {
         g.f64 = out->field_raw;
         memset(g.f64, 0, sizeof(double) * flen);
@@ -1184,16 +1213,30 @@ int oracle_run(int nn, const float* node, int ne, const int* elem, const int* la
 #pragma omp parallel reduction(+:etot, eesc, raytet, aborted, outside)
     {
         float* ppath = (float*)calloc((size_t)g.reclen + 1, sizeof(float));
-        tallies tl = {0, 0, 0, 0, 0};
+        tallies tl = {0, 0, 0, 0, 0, NULL};
+        if (g.K > 1) tl.esrc = (double*)calloc(2 * (size_t)g.K, sizeof(double));
 #pragma omp for schedule(dynamic, 64)
         for (long long i = 0; i < (long long)cfg->nphoton; i++) onephoton(&g, (uint64_t)i, ppath, out, &tl);
         etot += tl.etot; eesc += tl.eesc; raytet += tl.raytet; aborted += tl.aborted; outside += tl.outside;
+        if (tl.esrc) {
+#pragma omp critical
+            for (int k = 0; k < 2 * g.K; k++)
+                if (out->energy_src) out->energy_src[k] += tl.esrc[k];
+            free(tl.esrc);
+        }
         free(ppath);
     }
     clock_gettime(CLOCK_MONOTONIC, &t_end);
     out->sim_seconds = (double)(t_end.tv_sec - t_start.tv_sec) + 1e-9 * (double)(t_end.tv_nsec - t_start.tv_nsec);
     out->energytot = etot;
     out->energyesc = eesc;
+    if (g.K > 1 && out->energy_src) {  /* the patterns' sums, as the reference reports them */
+        out->energytot = out->energyesc = 0.0;
+        for (int k = 0; k < g.K; k++) {
+            out->energytot += out->energy_src[k];
+            out->energyesc += out->energy_src[g.K + k];
+        }
+    }
     out->raytet = raytet;
     out->aborted = aborted;
     out->outside = outside;

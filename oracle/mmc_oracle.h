@@ -59,10 +59,12 @@ typedef struct oracle_cfg {
     int issaveref;          /* exiting weight per exterior face and gate into oracle_out.dref */
     int method;             /* 0 element output, 1 dual-grid (DMMC) output */
     float gridstep;         /* voxel edge of the grid output (mm), 0 = 1 */
+    int srcnum;             /* patterns sharing each photon (pattern source, src/mmc_core.cl:1907-1911);
+                               field_raw then holds srcnum values per cell, adjacent; 0 or 1 = one */
 } oracle_cfg;
 
 typedef struct oracle_out {
-    double* field_raw;      /* maxgate*ne raw element deposits (required) */
+    double* field_raw;      /* maxgate*ne(*srcnum) raw element deposits (required) */
     float* detp;            /* maxdetphoton*reclen, may be NULL */
     uint8_t* seeds;         /* maxdetphoton*16, may be NULL */
     float* photon_weight;   /* per photon final weight, may be NULL */
@@ -80,6 +82,8 @@ typedef struct oracle_out {
     uint32_t maxtraj;
     uint32_t ntraj;         /* records written or attempted (may exceed maxtraj) */
     double sim_seconds;     /* wall time of the photon loop (mesh preparation excluded) */
+    double* energy_src;     /* srcnum > 1: launched weight per pattern, then escaped weight per
+                               pattern (2*srcnum); energytot/energyesc are then their sums */
 } oracle_out;
 
 /* Mesh preparation (volumes with orientation fix, face neighbours, normals,

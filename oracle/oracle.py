@@ -37,6 +37,7 @@ class OCfg(C.Structure):
         ("accum_f64", C.c_int), ("step_budget", C.c_uint64),
         ("srctype", C.c_int), ("srcparam1", C.c_float * 4), ("srcparam2", C.c_float * 4), ("focus", C.c_float),
         ("srcpattern", C.c_void_p), ("issaveref", C.c_int), ("method", C.c_int), ("gridstep", C.c_float),
+        ("srcnum", C.c_int),
     ]
 
 
@@ -48,7 +49,7 @@ class OOut(C.Structure):
         ("energyesc", C.c_double), ("raytet", C.c_uint64), ("aborted", C.c_uint64), ("outside", C.c_uint64),
         ("dref", C.c_void_p), ("nf", C.c_int),
         ("traj", C.c_void_p), ("maxtraj", C.c_uint32), ("ntraj", C.c_uint32),
-        ("sim_seconds", C.c_double),
+        ("sim_seconds", C.c_double), ("energy_src", C.c_void_p),
     ]
 
 
@@ -179,6 +180,7 @@ def _ocfg(cfg, maxgate, e0, keep):
     m = getattr(cfg, "method", 0)
     c.method = {"elem": 0, "grid": 1}[m] if isinstance(m, str) else int(m)
     c.gridstep = float(getattr(cfg, "gridstep", 1.0))
+    c.srcnum = int(getattr(cfg, "srcnum", 1))
     pat = getattr(cfg, "srcpattern", None)
     if pat is not None:
         pat = np.ascontiguousarray(pat, np.float32).ravel()
@@ -204,7 +206,9 @@ def run(node, elem, label, cfg, nthreads=1, trace=False, normalize=True):
     framelen = ne
     if c.method == 1:
         framelen = int(np.prod(grid_dims(node, cfg.gridstep if cfg.gridstep > 0 else 1.0)))
-    raw = np.zeros((maxgate, framelen), np.float64)
+    K = max(1, c.srcnum) if c.srctype == 5 else 1
+    raw = np.zeros((maxgate, framelen) if K == 1 else (maxgate, framelen, K), np.float64)
+    esrc = np.zeros((2, K), np.float64) if K > 1 else None
     nmed = c.nmedia
     reclen = 1 + (2 + (1 if cfg.ismomentum else 0)) * (nmed - 1) + (6 if cfg.issaveexit else 0) + 1
     out = OOut()
@@ -220,6 +224,7 @@ def run(node, elem, label, cfg, nthreads=1, trace=False, normalize=True):
     maxtraj = int(getattr(cfg, "maxjumpdebug", 0))
     traj = np.zeros((maxtraj, 6), np.float32) if maxtraj else None
     out.traj, out.maxtraj = _p(traj), maxtraj
+    out.energy_src = _p(esrc)
     rc = lib.oracle_run(nn, _p(node), ne, _p(elem), _p(label), C.byref(c), C.byref(out), int(nthreads))
     if rc:
         raise ValueError("oracle run failed")
@@ -234,23 +239,36 @@ def run(node, elem, label, cfg, nthreads=1, trace=False, normalize=True):
     res["ntraj"] = int(out.ntraj)
     res["sim_seconds"] = float(out.sim_seconds)
     res["traj"] = traj[:min(int(out.ntraj), maxtraj)] if traj is not None else None
-    if normalize and c.method == 1:  # dual grid: one scale factor (src/mmc_mesh.c:2204-2206)
-        norm = 1.0
-        if cfg.isnormalized:
-            et = float(np.float32(out.energytot))
-            if c.outputtype == OUTPUT_TYPES["energy"]:
-                norm = float(np.float32(1.0) / np.float32(et))
-            else:
-                norm = 1.0 / (et * cfg.unitinmm ** 3)
-                if c.outputtype == OUTPUT_TYPES["flux"]:
-                    norm /= float(np.float32(cfg.tstep))
-        res["normalizer"], res["field"] = norm, raw * norm
-    elif normalize:
-        datalen = nn if cfg.basisorder else ne
-        field = np.zeros((maxgate, datalen), np.float64)
-        res["normalizer"] = lib.oracle_normalize(nn, _p(node), ne, _p(elem), _p(label), C.byref(c), _p(raw),
-                                                 out.energytot, out.energyesc, _p(field))
-        res["field"] = field
+    res["energy_src"] = esrc
+    if not normalize:
+        return res
+    # each pattern is normalized with its own energies (src/mmc_cu_host.cu:984-995); the
+    # normalizer reported is their mean
+    tot = esrc[0] if K > 1 else [out.energytot]
+    esc = esrc[1] if K > 1 else [out.energyesc]
+    fields, norms = [], []
+    for p in range(K):
+        raw_p = np.ascontiguousarray(raw[..., p] if K > 1 else raw)
+        if c.method == 1:  # dual grid: one scale factor (src/mmc_mesh.c:2204-2206)
+            norm = 1.0
+            if cfg.isnormalized:
+                et = float(np.float32(tot[p]))
+                if c.outputtype == OUTPUT_TYPES["energy"]:
+                    norm = float(np.float32(1.0) / np.float32(et))
+                else:
+                    norm = 1.0 / (et * cfg.unitinmm ** 3)
+                    if c.outputtype == OUTPUT_TYPES["flux"]:
+                        norm /= float(np.float32(cfg.tstep))
+            fields.append(raw_p * norm)
+        else:
+            datalen = nn if cfg.basisorder else ne
+            field = np.zeros((maxgate, datalen), np.float64)
+            norm = lib.oracle_normalize(nn, _p(node), ne, _p(elem), _p(label), C.byref(c), _p(raw_p),
+                                        float(tot[p]), float(esc[p]), _p(field))
+            fields.append(field)
+        norms.append(norm)
+    res["field"] = fields[0] if K == 1 else np.stack(fields, axis=-1)
+    res["normalizer"] = norms[0] if K == 1 else sum(norms) / K
     return res
 
 

@@ -25,6 +25,12 @@ Badouel tracer and element-based output (-M s -C 0), unnormalized (-U 0):
   bench_dmmc-cube60, bench_dmmc-cube60b
            the reference's built-in benchmarks (-Q), dual-grid output on
            1 mm voxels, 1e5 photons
+  src_pattern3
+           three patterns sharing each photon (srcnum 3, photon sharing): a
+           4 x 3 pixel pattern source over 20 x 20 mm of the void-layer cube6k
+           face, the patterns given as a JData array [3, 4, 3]; statistics per
+           (element, pattern), and the seed-SEED0 run's raw and normalized
+           output with the per-pattern energies the reference prints
 
 Six more runs with fresh seeds calibrate the null: their coverage of the
 10-run statistics (fraction of cells within 3 sigma, mean z) is stored, and a
@@ -268,6 +274,79 @@ def make_dref_case(wd):
     print(name, "nf", nf, "escaped per photon", per_gate.sum(1).mean() / c["photons"])
 
 
+PATTERN3 = np.random.default_rng(77).uniform(0.1, 1.0, (3, 4, 3)).astype(np.float32)  # [pattern, x, y]
+
+
+def jdata_array(a):
+    """A float32 array as a zlib-compressed JData object, row-major as JData stores it."""
+    import base64
+    b = np.ascontiguousarray(a, np.float32).tobytes()
+    return {"_ArrayType_": "single", "_ArraySize_": list(a.shape), "_ArrayZipType_": "zlib",
+            "_ArrayZipSize_": [1, int(a.size)], "_ArrayZipData_": base64.b64encode(zlib.compress(b)).decode()}
+
+
+def run_ref_patterns(workdir, name, seed, photons, ne, K, normalized=False):
+    """Raw (or normalized) element output of one multi-pattern run, (ne, K), and the
+    per-pattern launched energy / absorbed percentage / normalizer lines of its log."""
+    sess = f"{name}_{seed}_{int(normalized)}"
+    cmd = [REF, "-f", os.path.join(workdir, name + ".json"), "-c", "sse", "-M", "s", "-C", "0", "-b", "1",
+           "-U", "1" if normalized else "0", "-F", "bin", "-s", sess, "-E", str(seed), "-n", str(photons), "-D", "T"]
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    p = subprocess.run(cmd, cwd=workdir, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(p.stdout[-2000:])
+    raw = np.fromfile(os.path.join(workdir, sess + ".bin"), np.float64).reshape(ne, K)
+    energies = []
+    for line in p.stdout.splitlines():
+        if "total simulated energy:" in line:
+            import re
+            clean = re.sub(r"\x1b\[[0-9;]*m", "", line)
+            etot = float(clean.split("total simulated energy:")[1].split()[0])
+            absp = float(clean.split("absorbed:")[1].split("%")[0])
+            norm = float(clean.split("normalizor=")[1].split()[0])
+            energies.append((etot, absp, norm))
+    return raw, np.array(energies)
+
+
+def make_pattern_case(wd):
+    """src_pattern3: three patterns sharing each photon; 10 runs + 6 null runs."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    name = "src_pattern3"
+    cube = meshgen.homogeneous_cube(n=10)
+    lab = void_layer_labels(cube)
+    m = meshgen.Mesh(cube.node, cube.elem, lab, cube.media, "cube6k-void")
+    K, nx, ny = PATTERN3.shape
+    src = dict(Type="pattern", Pos=[20.0, 20.0, 0.0], Dir=[0.0, 0.0, 1.0], Param1=[20.0, 0, 0, nx],
+               Param2=[0, 20.0, 0, ny])
+    c = dict(mesh=m, photons=100000, t1=5e-9, dt=5e-9, det=None, src=src, reflabel=np.where(lab == 0, -1, lab))
+    c["e0"] = oracle.initelem(m.node, m.elem, m.label, (20.0, 20.0, 0.0))
+    path = os.path.join(wd, name + ".json")
+    write_json(path, name, c)
+    cfgj = json.load(open(path))
+    cfgj["Optode"]["Source"]["Pattern"] = jdata_array(PATTERN3)
+    json.dump(cfgj, open(path, "w"))
+    ne = m.ne
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        runs = list(ex.map(lambda s: run_ref_patterns(wd, name, s, c["photons"], ne, K)[0],
+                           [SEED0 + k for k in range(NRUNS)]))
+        nulls = list(ex.map(lambda s: run_ref_patterns(wd, name, s, c["photons"], ne, K)[0],
+                            [SEED0 + 1000 + k for k in range(NNULL)]))
+        normed, energies = ex.submit(run_ref_patterns, wd, name, SEED0, c["photons"], ne, K, True).result()
+    runs = np.stack(runs)  # (runs, ne, K)
+    flat = runs.reshape(NRUNS, -1)
+    tot = runs.sum(1)      # (runs, K)
+    sys.path.insert(0, os.path.dirname(HERE))
+    import golden_checks as gc
+    fx = dict(ne=ne, srcnum=K, photons=c["photons"], pattern=PATTERN3,
+              cell_mean=flat.mean(0), cell_std=flat.std(0, ddof=1), total_mean=tot.mean(0), total_std=tot.std(0, ddof=1),
+              raw_seed0=runs[0], norm_seed0=normed, energies_seed0=energies)
+    st = [gc.zstats(x.reshape(-1), fx["cell_mean"], fx["cell_std"]) for x in nulls]
+    fx.update(null_cell_frac=np.array([t[0] for t in st]), null_cell_meanz=np.array([t[1] for t in st]))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **fx)
+    print(name, "per-pattern totals", tot.mean(0), "energies", energies)
+
+
 def run_ref_grid(workdir, name, seed, photons, nvox):
     """Dual-grid (DMMC, -M G) fluence of one reference run, unnormalized."""
     sess = f"{name}_{seed}_grid"
@@ -412,6 +491,8 @@ def main(only=()):
             make_traj_case(wd)
         if not only or "bench" in only:
             make_bench_cases(wd)
+        if not only or "src_pattern3" in only:
+            make_pattern_case(wd)
         for name, c in case_defs().items():
             if only and name not in only:
                 continue

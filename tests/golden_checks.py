@@ -72,6 +72,19 @@ def case_mesh_and_config(name, nphoton=None, seed=4242):
         m = meshgen.Mesh(d["node"], d["elem"], d["label"], cfg.media, name)
         cfg = dataclasses.replace(cfg, nphoton=nphoton or int(fx["photons"]), seed=seed, isnormalized=0,
                                   method="grid", gridstep=1.0, basisorder=0, issavedet=0)
+    elif name == "src_pattern3":
+        # three patterns sharing each photon over the void-layer cube6k face; the fixture holds them
+        # as [pattern, x, y], the engine takes them pixel-major (pixel y*nx+x, patterns adjacent)
+        m = meshgen.homogeneous_cube(n=10)
+        label = m.label.copy()
+        label[meshgen.centroids(m.node, m.elem)[:, 2] < 6.0] = 0
+        m = meshgen.Mesh(m.node, m.elem, label, m.media, "cube6k-void")
+        pat = fx["pattern"]
+        K, nx, ny = pat.shape
+        cfg = SimConfig(media=m.media, nphoton=nphoton or int(fx["photons"]), seed=seed, tend=5e-9, tstep=5e-9,
+                        basisorder=0, isnormalized=0, srctype="pattern", srcpos=(20.0, 20.0, 0.0),
+                        srcdir=(0.0, 0.0, 1.0), srcparam1=(20.0, 0, 0, nx), srcparam2=(0, 20.0, 0, ny),
+                        srcpattern=np.ascontiguousarray(pat.transpose(2, 1, 0)).ravel(), srcnum=K)
     elif name.startswith("src_"):
         # source types (tests/golden/make_golden.py SOURCE_CASES): the cube6k mesh, with the
         # voxel layer z < 6 mm void for the sources on the z=0 face
@@ -137,6 +150,17 @@ def check_field(raw, fx, media, label, photons):
     a = fx["absorbed"]
     if abs(absorbed - a.mean()) > 3 * a.std(ddof=1) * INFLATE:
         msgs.append(f"absorbed fraction {absorbed:.5f} vs reference {a.mean():.5f} +- {a.std(ddof=1):.5f}")
+    return msgs
+
+
+def check_patterns(raw, fx):
+    """raw: (ne, srcnum) element deposits of one single-gate run whose patterns
+    share photons: every (element, pattern) cell and each pattern's total."""
+    msgs = _zcheck("(element,pattern) cells", raw.reshape(-1), fx["cell_mean"], fx["cell_std"], 100,
+                   fx["null_cell_frac"], fx["null_cell_meanz"])
+    tz = np.abs(raw.sum(0) - fx["total_mean"]) / (fx["total_std"] * INFLATE)
+    if np.any(tz > 4.0):
+        msgs.append(f"per-pattern totals z = {np.round(tz, 2)}")
     return msgs
 
 

@@ -122,3 +122,33 @@ def test_host_check_reports_the_initial_element():
     assert e.value == located
     c.srcpos = (C.c_float * 3)(100.0, 30.0, 0.0)  # outside the mesh: a pencil cannot start
     assert lib.mmcgb_check_config(d, C.byref(c), C.byref(e)) == 4
+
+
+def test_shared_pattern_options_checked_before_any_gpu_work():
+    """srcnum > 1 needs a pattern source, does not replay, and multiplies the
+    fluence cells that the 32-bit index must hold."""
+    import ctypes as C
+    from mmc_gb300 import _native
+    from mmc_gb300.core import SimConfig
+    lib = _native.load()
+    m = meshgen.homogeneous_cube(n=4)  # 384 tets
+    d, keep = core._desc(m.node, m.elem, m.label)
+    pat = np.ones(4 * 3 * 2, np.float32)
+    base = dict(media=m.media, srcpos=(10.0, 10.0, 0.0), tend=5e-9, tstep=1e-9, srctype="pattern",
+                srcparam1=(20.0, 0, 0, 4), srcparam2=(0, 20.0, 0, 3), srcpattern=pat, srcnum=2)
+    e0 = C.c_int32(-1)
+
+    def rc(**kw):
+        c, k = SimConfig(**{**base, **kw}).to_c()
+        return lib.mmcgb_check_config(d, C.byref(c), C.byref(e0))
+
+    assert rc() == 0, lib.mmcgb_last_error()
+    assert rc(srctype="planar") == 1
+    assert rc(srcnum=-1) == 1
+    seeds = np.zeros((5, 2), np.uint64)
+    assert rc(nphoton=5, replayseed=seeds, replayweight=np.ones(5, np.float32),
+              replaytime=np.ones(5, np.float32)) == 1
+    gates = (2**31 - 1) // m.ne // 8 + 1  # fits alone, not with 8 patterns
+    assert rc(srcnum=1, srcpattern=pat[:12], tend=gates * 1e-9) == 0
+    assert rc(srcnum=8, srcpattern=np.ones(12 * 8, np.float32), tend=gates * 1e-9) == 1
+    assert "patterns" in lib.mmcgb_last_error().decode()

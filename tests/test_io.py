@@ -131,3 +131,38 @@ def test_pmmc_debuglevel_parsing():
     for bad in ("", "Q"):
         with pytest.raises(ValueError):
             pmmc._parse(dict(base, debuglevel=bad))
+
+
+def test_shared_patterns_from_json_and_pmmc(tmp_path):
+    """A 3-D pattern [srcnum, Nx, Ny] (srcnum, Ny > 1) of a pattern source holds
+    patterns sharing each photon: from a JData array in JSON (zlib-compressed,
+    as the reference reads it, or plain) and from a pmmc array; both give the
+    engine's pixel-major layout (pixel y*Nx + x, patterns adjacent)."""
+    import base64
+    import zlib
+    K, nx, ny = 3, 4, 2
+    A = np.arange(K * nx * ny, dtype=np.float32).reshape(K, nx, ny)  # [pattern, x, y]
+    want = np.ascontiguousarray(A.transpose(2, 1, 0)).ravel()
+    path, m = _write_case(tmp_path)
+    cfg = json.loads(open(path).read())
+    src = dict(Type="pattern", Pos=[10, 10, 0], Dir=[0, 0, 1], Param1=[20, 0, 0, nx], Param2=[0, 20, 0, ny])
+    for enc in ("zlib", "gzip", "plain"):
+        if enc == "plain":
+            src["Pattern"] = {"_ArrayType_": "single", "_ArraySize_": [K, nx, ny], "_ArrayData_": A.ravel().tolist()}
+        else:
+            co = zlib.compressobj(wbits=31 if enc == "gzip" else 15)
+            z = co.compress(A.tobytes()) + co.flush()
+            src["Pattern"] = {"_ArrayType_": "single", "_ArraySize_": [K, nx, ny], "_ArrayZipType_": enc,
+                              "_ArrayZipSize_": [1, A.size], "_ArrayZipData_": base64.b64encode(z).decode()}
+        cfg["Optode"]["Source"] = src
+        p = tmp_path / f"pat_{enc}.json"
+        p.write_text(json.dumps(cfg))
+        _, sc, _ = io.load_input(str(p))
+        assert sc.srcnum == K and np.array_equal(sc.srcpattern, want), enc
+    *_, sc, _ = pmmc._parse(dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[10, 10, 0], srctype="pattern",
+                                srcparam1=[20, 0, 0, nx], srcparam2=[0, 20, 0, ny], srcpattern=np.asfortranarray(A)))
+    assert sc.srcnum == K and np.array_equal(sc.srcpattern, want)
+    # a 2-D pattern stays one pattern; so does a 3-D array for the 3-D pattern source
+    *_, sc, _ = pmmc._parse(dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[10, 10, 0], srctype="pattern3d",
+                                srcparam1=[K, nx, ny, 0], srcpattern=A))
+    assert sc.srcnum == 1

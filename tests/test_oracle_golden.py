@@ -114,3 +114,36 @@ def test_oracle_matches_reference_runs_on_the_benchmark_workloads(oracle_mod, na
         msgs += gc.check_nodes(node[0], fx)
     assert r["aborted"] == 0
     assert not msgs, "\n".join(msgs)
+
+
+def test_oracle_shared_patterns_match_reference_runs(oracle_mod):
+    """Three patterns sharing each photon (srcnum 3): every (element, pattern)
+    cell and each pattern's total against the reference runs; each pattern's
+    launched weight is the sum of its values at the photons' launch pixels."""
+    m, cfg, fx = gc.case_mesh_and_config("src_pattern3")
+    r = oracle_mod.run(m.node, m.elem, m.label, cfg, nthreads=NTHREADS, normalize=False)
+    assert r["raw"].shape == (1, m.ne, 3)
+    msgs = gc.check_patterns(r["raw"][0], fx)
+    assert not msgs, "\n".join(msgs)
+    # the reference's seed-SEED0 run printed each pattern's launched weight: the same mean per photon
+    # within sampling noise of the pixel draws (12 pixels, values 0.1-1)
+    et = fx["energies_seed0"][:, 0]
+    assert r["energy_src"][0] == pytest.approx(et, rel=0.03)
+    assert r["energytot"] == pytest.approx(r["energy_src"][0].sum(), rel=1e-12)
+
+
+def test_per_pattern_normalization_matches_reference(oracle_mod):
+    """The reference's normalized output of a multi-pattern run equals each
+    pattern's raw deposits put through the single-pattern output stage with that
+    pattern's own energies (the values its log printed)."""
+    import numpy as np
+    from mmc_gb300 import core
+    m, cfg, fx = gc.case_mesh_and_config("src_pattern3")
+    raw, normed, en = fx["raw_seed0"], fx["norm_seed0"], fx["energies_seed0"]
+    one = dataclasses.replace(cfg, srcnum=1, isnormalized=1, srcpattern=None, srctype="pencil")
+    for p in range(raw.shape[1]):
+        etot = float(en[p, 0])
+        eesc = etot * (1.0 - float(en[p, 1]) / 100.0)
+        field, norm = core.normalize_host(m.node, m.elem, m.label, one, raw[:, p][None, :], etot, eesc)
+        np.testing.assert_allclose(field[0], normed[:, p], rtol=2e-5)
+        assert norm == pytest.approx(float(en[p, 2]), rel=1e-5)
