@@ -61,7 +61,6 @@ def main(argv=None):
 
     from . import io
     from .core import Mesh, simulate
-    from .io import OUTPUT_LETTERS
 
     if args.bench == "":
         print("Built-in benchmarks:\n" + "".join(f"\t{n}\n" for n in io.BENCHMARKS), end="")
@@ -87,7 +86,7 @@ def main(argv=None):
     if args.normalize is not None:
         upd["isnormalized"] = args.normalize
     if args.outputtype:
-        upd["outputtype"] = OUTPUT_LETTERS[args.outputtype.lower()]
+        upd["outputtype"] = io.output_type(args.outputtype)
     for k, a in (("issavedet", args.savedet), ("issaveexit", args.saveexit), ("issaveseed", args.saveseed),
                  ("ismomentum", args.momentum), ("isreflect", args.reflect), ("minenergy", args.minenergy),
                  ("maxdetphoton", args.maxdetphoton), ("issaveref", args.saveref)):

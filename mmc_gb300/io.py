@@ -25,6 +25,22 @@ MCH_HEADER = struct.Struct("<4sIIIIIIIfIfIiI2i")  # 64 bytes
 OUTPUT_LETTERS = {"x": "flux", "f": "fluence", "e": "energy", "j": "jacobian", "l": "wl", "p": "wp", "n": "wn"}
 OUTPUT_NAMES = {"flux": "flux", "fluence": "fluence", "energy": "energy", "jacobian": "jacobian", "wl": "wl",
                 "wp": "wp", "wn": "wn"}
+# the reference's frequency-domain (RF) and adjoint outputs, which this library does not provide
+UNSUPPORTED_OUTPUTS = {"r": "RF (frequency-domain) fluence", "a": "adjoint mua Jacobian",
+                       "d": "adjoint D Jacobian", "u": "adjoint mus Jacobian", "v": "adjoint musp Jacobian",
+                       "w": "dual adjoint Jacobian"}
+
+
+def output_type(code) -> str:
+    """The output type named by a -O letter or a name; unsupported ones are an error."""
+    k = str(code).lower()
+    if k in OUTPUT_LETTERS:
+        return OUTPUT_LETTERS[k]
+    if k in OUTPUT_NAMES:
+        return OUTPUT_NAMES[k]
+    if k in UNSUPPORTED_OUTPUTS:
+        raise ValueError(f"output type '{code}' ({UNSUPPORTED_OUTPUTS[k]}) is not supported")
+    raise ValueError(f"unknown output type '{code}'")
 
 
 # ---------------------------------------------------------------------------
@@ -175,8 +191,9 @@ def load_input(path):
     t0 = float(fwd.get("T0", 0.0))
     t1 = float(fwd.get("T1", 5e-9))
     dt = float(fwd.get("Dt", t1 - t0))
-    otype = ses.get("OutputType", "x")
-    otype = OUTPUT_LETTERS.get(str(otype).lower(), OUTPUT_NAMES.get(str(otype).lower(), "flux"))
+    otype = output_type(ses.get("OutputType", "x"))
+    if float(fwd.get("Omega", 0.0)) > 0.0:
+        raise ValueError("Forward.Omega > 0 asks for RF (frequency-domain) output, which is not supported")
     cfg = SimConfig(
         media=media, nphoton=int(float(ses.get("Photons", 1e6))), seed=int(ses.get("RNGSeed", 0x623F9A9E)),
         srcpos=tuple(float(x) for x in src.get("Pos", [0, 0, 0])[:3]), srcdir=tuple(float(x) for x in srcdir),

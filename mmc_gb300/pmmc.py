@@ -85,6 +85,8 @@ def _parse(cfg: dict):
     for k in _SCALARS_FLOAT:
         if k in cfg:
             kw[k] = float(cfg[k])
+    if float(cfg.get("omega", 0.0) or 0.0) > 0.0:
+        raise ValueError("omega > 0 asks for RF (frequency-domain) output, which is not supported")
     if "outputtype" in cfg:
         ot = str(cfg["outputtype"]).lower()
         if ot not in _OUTPUTS:

@@ -49,7 +49,7 @@ class Request:
 
 def device_bytes(mesh: Mesh, cfg: SimConfig) -> int:
     """Device memory a request holds while admitted (fluence + detector buffers)."""
-    flen = mesh.ne * cfg.maxgate
+    flen = mesh.ne * cfg.maxgate * max(1, int(cfg.srcnum))
     per = 8 if cfg.accum_f64 else 8  # float64, or two float32 halves
     nmed = np.asarray(cfg.media).reshape(-1, 4).shape[0]
     reclen = 2 + (2 + (1 if cfg.ismomentum else 0)) * (nmed - 1) + (6 if cfg.issaveexit else 0)

@@ -50,3 +50,20 @@ def test_sharded_default_runner_equals_one_simulation(nccl_group, small_inclusio
     assert got.energytot == ref.energytot
     rows = lambda d, s: sorted(map(bytes, np.concatenate([d.view(np.uint8).reshape(len(d), -1), s], 1)))  # noqa: E731
     assert rows(got.detp, got.seeds) == rows(ref.detp, ref.seeds)
+
+
+def test_sharded_shared_patterns_equal_one_simulation(nccl_group, small_inclusion):
+    """Patterns sharing each photon: the per-pattern energy slots are summed with
+    the deposits, so every pattern is normalized as in one simulation."""
+    m = small_inclusion
+    mesh = Mesh(m.node, m.elem, m.label)
+    pat = np.random.default_rng(3).uniform(0.1, 1.0, 4 * 3 * 2).astype(np.float32)
+    cfg = SimConfig(media=m.media, nphoton=40000, seed=77, srctype="pattern", srcpos=(20.0, 20.0, 0.5),
+                    srcdir=(0.0, 0.0, 1.0), srcparam1=(20.0, 0, 0, 4), srcparam2=(0, 20.0, 0, 3), srcpattern=pat,
+                    srcnum=2, tend=5e-9, tstep=1e-9, basisorder=1, isnormalized=1)
+    got = D.simulate_sharded(mesh, cfg)
+    ref = simulate(mesh, cfg)
+    assert got.field.shape == ref.field.shape == (5, m.nn, 2)
+    np.testing.assert_allclose(got.field, ref.field, rtol=1e-10, atol=1e-14)
+    assert got.normalizer == pytest.approx(ref.normalizer, rel=1e-10)
+    np.testing.assert_allclose(got.energy_src, ref.energy_src, rtol=1e-12)

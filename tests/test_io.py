@@ -166,3 +166,26 @@ def test_shared_patterns_from_json_and_pmmc(tmp_path):
     *_, sc, _ = pmmc._parse(dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[10, 10, 0], srctype="pattern3d",
                                 srcparam1=[K, nx, ny, 0], srcpattern=A))
     assert sc.srcnum == 1
+
+
+def test_unsupported_outputs_are_errors(tmp_path):
+    """The reference's RF (frequency-domain) and adjoint outputs are refused by
+    name rather than replaced by another output."""
+    path, m = _write_case(tmp_path)
+    cfg = json.loads(open(path).read())
+    for key, val in (("OutputType", "R"), ("OutputType", "A"), ("OutputType", "q")):
+        c = json.loads(json.dumps(cfg))
+        c["Session"][key] = val
+        p = tmp_path / f"o_{val}.json"
+        p.write_text(json.dumps(c))
+        with pytest.raises(ValueError):
+            io.load_input(str(p))
+    c = json.loads(json.dumps(cfg))
+    c["Forward"]["Omega"] = 6.28e8
+    p = tmp_path / "omega.json"
+    p.write_text(json.dumps(c))
+    with pytest.raises(ValueError, match="RF"):
+        io.load_input(str(p))
+    with pytest.raises(ValueError, match="RF"):
+        pmmc._parse(dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[30, 30, 0], omega=1e8))
+    assert io.output_type("F") == "fluence" and io.output_type("wl") == "wl"
