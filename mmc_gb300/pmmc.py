@@ -22,6 +22,11 @@ _SCALARS_INT = ["nphoton", "isreflect", "isspecular", "ismomentum", "issaveexit"
 _SCALARS_FLOAT = ["tstart", "tstep", "tend", "roulettesize", "minenergy", "unitinmm", "nout"]
 _METHODS = {"plucker": None, "havel": None, "badouel": None, "elem": "elem", "grid": "grid"}
 _OUTPUTS = {"flux", "fluence", "energy", "jacobian", "wl", "wp", "wn"}
+# keys of the reference's binding for options this library does not provide: refused when set,
+# rather than ignored
+_UNSUPPORTED = {"mcmethod": "MCML-style albedo weighting (an option of the reference's CPU engine)",
+                "isextdet": "wide-field detector elements", "isnodalmua": "per-node absorption",
+                "isnodalmusp": "per-node scattering", "adjointmode": "adjoint outputs"}
 
 
 def version() -> str:
@@ -38,6 +43,9 @@ def _parse(cfg: dict):
     for req in ("node", "elem", "prop", "srcpos"):
         if req not in cfg:
             raise ValueError(f"cfg.{req} is required")
+    for k, what in _UNSUPPORTED.items():
+        if k in cfg and np.any(np.asarray(cfg[k]) != 0):
+            raise ValueError(f"cfg.{k} ({what}) is not supported")
     node = np.asarray(cfg["node"], np.float32)
     elem = np.asarray(cfg["elem"])
     if elem.ndim != 2 or elem.shape[1] not in (4, 5):

@@ -189,3 +189,7 @@ def test_unsupported_outputs_are_errors(tmp_path):
     with pytest.raises(ValueError, match="RF"):
         pmmc._parse(dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[30, 30, 0], omega=1e8))
     assert io.output_type("F") == "fluence" and io.output_type("wl") == "wl"
+    for k in ("mcmethod", "isextdet", "isnodalmua", "isnodalmusp", "adjointmode"):
+        with pytest.raises(ValueError, match=k):
+            pmmc._parse(dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[30, 30, 0], **{k: 1}))
+    pmmc._parse(dict(node=m.node, elem=m.elem, prop=m.media, srcpos=[30, 30, 0], mcmethod=0, isextdet=0))
