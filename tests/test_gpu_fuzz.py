@@ -139,3 +139,30 @@ def test_random_configuration_matches_oracle(oracle_mod, fuzz_meshes, k):
     assert f.raytet == o["raytet"]
     if cfg.issavedet:
         assert _rows(f.detp, f.seeds) == _rows(o["detp"], o["seeds"])
+
+
+def test_random_configurations_batched_equal_solo_runs(fuzz_meshes):
+    """Sixteen of the random configurations (four meshes, mixed options) in one
+    batched launch: each result equals its solo run."""
+    from mmc_gb300.core import simulate_batch
+    meshes, cfgs, solo = [], [], []
+    for k in range(16):
+        name, kw, rng = _case(k)
+        m, mesh = fuzz_meshes[name]
+        cfg = SimConfig(media=_media(m, rng), **kw)
+        try:
+            solo.append(simulate(mesh, cfg))
+        except _native.MmcgbError:  # a source outside the mesh: not batched
+            continue
+        cfgs.append(cfg)
+        meshes.append(mesh)
+    assert len(cfgs) >= 12
+    batch = simulate_batch(meshes, cfgs)
+    for k, (cfg, b, s) in enumerate(zip(cfgs, batch, solo)):
+        tol = dict(rtol=1e-7, atol=1e-9) if cfg.accum_f64 else dict(rtol=3e-5, atol=1e-6)
+        np.testing.assert_allclose(b.field, s.field, **tol, err_msg=f"case {k}")
+        assert b.raytet == s.raytet and b.detected == s.detected, k
+        if cfg.issavedet:
+            assert _rows(b.detp, b.seeds) == _rows(s.detp, s.seeds), k
+        if cfg.issaveref:
+            np.testing.assert_allclose(b.dref, s.dref, rtol=1e-7, atol=1e-9)
