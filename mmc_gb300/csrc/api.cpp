@@ -1352,7 +1352,7 @@ int32_t mmcgb_prepare_host(const mmcgb_mesh_desc* desc, int32_t* elem, int32_t* 
     if (rc) return fail(rc, err);
     if (elem) std::memcpy(elem, h.elem.data(), sizeof(int) * h.elem.size());
     if (facenb) std::memcpy(facenb, h.facenb.data(), sizeof(int) * h.facenb.size());
-    if (normals) std::memcpy(normals, h.normals.data(), sizeof(float) * h.normals.size());
+    if (normals) element_normals_all(h, normals);
     if (evol) std::memcpy(evol, h.evol.data(), sizeof(float) * h.evol.size());
     if (nvol) std::memcpy(nvol, h.nvol.data(), sizeof(float) * h.nvol.size());
     if (nf) *nf = h.nf;

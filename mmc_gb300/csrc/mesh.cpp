@@ -65,13 +65,20 @@ void compute_facenb(int nn, int ne, const std::vector<int>& elem, std::vector<in
                 std::sort(v, v + 3);
             }
     });
+    // bucket the faces by smallest node (counts and fill with relaxed atomics: the order inside a
+    // bucket does not matter, the sort below breaks ties by face slot)
     std::vector<uint32_t> start((size_t)nn + 2, 0);
-    for (size_t f = 0; f < nface; f++) start[(size_t)tri[3 * f] + 1]++;
+    parallel_ranges(nface, [&](size_t b, size_t e) {
+        for (size_t f = b; f < e; f++) __atomic_fetch_add(&start[(size_t)tri[3 * f] + 1], 1u, __ATOMIC_RELAXED);
+    });
     for (size_t i = 1; i < start.size(); i++) start[i] += start[i - 1];
     std::vector<uint32_t> order(nface);
     {
         std::vector<uint32_t> fill(start.begin(), start.end() - 1);
-        for (size_t f = 0; f < nface; f++) order[fill[(size_t)tri[3 * f]]++] = (uint32_t)f;  // ascending slots
+        parallel_ranges(nface, [&](size_t b, size_t e) {
+            for (size_t f = b; f < e; f++)
+                order[__atomic_fetch_add(&fill[(size_t)tri[3 * f]], 1u, __ATOMIC_RELAXED)] = (uint32_t)f;
+        });
     }
     parallel_ranges((size_t)nn + 1, [&](size_t b, size_t e) {
         for (size_t v0 = b; v0 < e; v0++) {
@@ -135,15 +142,16 @@ int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
         if (lab == -1) lab = 0;
     m.evol.assign(d.ne, 0.f);
     m.nvol.assign(d.nn, 0.f);
+    for (size_t i = 0; i < 4 * (size_t)d.ne; i++)
+        if (m.elem[i] < 1 || m.elem[i] > d.nn) {
+            err = "element " + std::to_string(i / 4 + 1) + " references a node outside 1..nn";
+            return MMCGB_E_MESH;
+        }
     // volumes and orientation (src/mmc_mesh.c:910-974): swap nodes 3,4 of a
     // negatively oriented tet so that the face tables give outward normals
-    for (int i = 0; i < d.ne; i++) {
-        int* e = &m.elem[4 * (size_t)i];
-        for (int j = 0; j < 4; j++)
-            if (e[j] < 1 || e[j] > d.nn) {
-                err = "element " + std::to_string(i + 1) + " references a node outside 1..nn";
-                return MMCGB_E_MESH;
-            }
+    parallel_ranges((size_t)d.ne, [&](size_t b, size_t end) {
+    for (size_t i = b; i < end; i++) {
+        int* e = &m.elem[4 * i];
         F3 n0 = node_at(m.node, e[0] - 1), n1 = node_at(m.node, e[1] - 1), n2 = node_at(m.node, e[2] - 1),
            n3 = node_at(m.node, e[3] - 1);
         float dx = n2.x - n3.x, dy = n2.y - n3.y, dz = n2.z - n3.z;
@@ -159,8 +167,14 @@ int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
         }
         v *= (1.f / 6.f);
         m.evol[i] = v;
+    }
+    });
+    // nodal volumes: float sums in element order, as the reference adds them
+    for (size_t i = 0; i < (size_t)d.ne; i++) {
         if (m.label[i] == 0) continue;
-        for (int j = 0; j < 4; j++) m.nvol[e[j] - 1] += v * 0.25f;
+        const int* e = &m.elem[4 * i];
+        const float q = m.evol[i] * 0.25f;
+        for (int j = 0; j < 4; j++) m.nvol[e[j] - 1] += q;
     }
     if (d.facenb) {
         m.facenb.assign(d.facenb, d.facenb + 4 * (size_t)d.ne);
@@ -172,30 +186,6 @@ int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
     } else {
         compute_facenb(d.nn, d.ne, m.elem, m.facenb);
     }
-    // outward unit normals and plane offsets (src/mmc_mesh.c:1572-1601)
-    m.normals.assign(16 * (size_t)d.ne, 0.f);
-    parallel_ranges((size_t)d.ne, [&](size_t b, size_t end) {
-    for (size_t i = b; i < end; i++) {
-        float* vn = &m.normals[16 * i];
-        const int* e = &m.elem[4 * i];
-        for (int j = 0; j < 4; j++) {
-            F3 a = node_at(m.node, e[kOut[j][0]] - 1);
-            F3 b = node_at(m.node, e[kOut[j][1]] - 1);
-            F3 c = node_at(m.node, e[kOut[j][2]] - 1);
-            F3 ab{b.x - a.x, b.y - a.y, b.z - a.z};
-            F3 ac{c.x - a.x, c.y - a.y, c.z - a.z};
-            F3 n{ab.y * ac.z - ab.z * ac.y, ab.z * ac.x - ab.x * ac.z, ab.x * ac.y - ab.y * ac.x};
-            float rn = (float)(1.f / std::sqrt((double)(n.x * n.x + n.y * n.y + n.z * n.z)));
-            n.x *= rn;
-            n.y *= rn;
-            n.z *= rn;
-            vn[j] = n.x;
-            vn[j + 4] = n.y;
-            vn[j + 8] = n.z;
-            vn[j + 12] = n.x * a.x + n.y * a.y + n.z * a.z;
-        }
-    }
-    });
     // exterior faces numbered -1,-2,... (src/mmc_mesh.c:1466-1474)
     const long long nf_max = (long long)max_elem(m.lbits) + 1;
     long long nf = 0;
@@ -215,12 +205,42 @@ int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
     return MMCGB_OK;
 }
 
+// Outward unit normals and plane offsets of element i (src/mmc_mesh.c:1572-1601):
+// vn = nx[4] ny[4] nz[4] d[4].  Computed where they are used (the packed records,
+// the host-stage export) rather than kept as a mesh array.
+void element_normals(const HostMesh& m, size_t i, float vn[16]) {
+    const int* e = &m.elem[4 * i];
+    for (int j = 0; j < 4; j++) {
+        F3 a = node_at(m.node, e[kOut[j][0]] - 1);
+        F3 b = node_at(m.node, e[kOut[j][1]] - 1);
+        F3 c = node_at(m.node, e[kOut[j][2]] - 1);
+        F3 ab{b.x - a.x, b.y - a.y, b.z - a.z};
+        F3 ac{c.x - a.x, c.y - a.y, c.z - a.z};
+        F3 n{ab.y * ac.z - ab.z * ac.y, ab.z * ac.x - ab.x * ac.z, ab.x * ac.y - ab.y * ac.x};
+        float rn = (float)(1.f / std::sqrt((double)(n.x * n.x + n.y * n.y + n.z * n.z)));
+        n.x *= rn;
+        n.y *= rn;
+        n.z *= rn;
+        vn[j] = n.x;
+        vn[j + 4] = n.y;
+        vn[j + 8] = n.z;
+        vn[j + 12] = n.x * a.x + n.y * a.y + n.z * a.z;
+    }
+}
+
+void element_normals_all(const HostMesh& m, float* out) {
+    parallel_ranges((size_t)m.ne, [&](size_t b, size_t end) {
+        for (size_t i = b; i < end; i++) element_normals(m, i, out + 16 * i);
+    });
+}
+
 void pack_records(const HostMesh& m, std::vector<TetRec>& rec) {
     rec.resize(m.ne);
     const int lb = m.lbits;
     parallel_ranges((size_t)m.ne, [&](size_t b, size_t end) {
     for (size_t i = b; i < end; i++) {
-        const float* vn = &m.normals[16 * i];
+        float vn[16];
+        element_normals(m, i, vn);
         TetRec& r = rec[i];
         r.nx = make_float4(vn[0], vn[1], vn[2], vn[3]);
         r.ny = make_float4(vn[4], vn[5], vn[6], vn[7]);

@@ -29,7 +29,6 @@ struct HostMesh {
     std::vector<int> elem;       // ne*4, 1-based, orientation-fixed
     std::vector<int> label;      // ne
     std::vector<int> facenb;     // ne*4, exterior faces numbered -1,-2,...
-    std::vector<float> normals;  // ne*16: nx[4] ny[4] nz[4] d[4]
     std::vector<float> evol;     // ne
     std::vector<float> nvol;     // nn (before the surface fix)
     LocGrid grid;
@@ -37,6 +36,8 @@ struct HostMesh {
 
 int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err);
 void pack_records(const HostMesh& m, std::vector<TetRec>& rec);
+// Face normals and plane offsets of every element, ne*16 floats: nx[4] ny[4] nz[4] d[4].
+void element_normals_all(const HostMesh& m, float* out);
 bool build_locator(HostMesh& m);  // false when its 32-bit offsets would overflow
 int locate(const HostMesh& m, const float p[3]);
 
