@@ -44,7 +44,17 @@ def main(argv=None):
     ap.add_argument("-d", "--savedet", type=int)
     ap.add_argument("-x", "--saveexit", type=int)
     ap.add_argument("-q", "--saveseed", type=int)
-    ap.add_argument("-m", "--momentum", type=int)
+    ap.add_argument("-m", "--mc", type=int)        # 0 MCX-style photon weights; 1 (MCML) is a CPU-engine option
+    ap.add_argument("--momentum", type=int)        # save momentum transfer (implies -d 1, src/mmc_utils.c:4185-4190)
+    ap.add_argument("-u", "--unitinmm", type=float)
+    ap.add_argument("-V", "--specular", type=int)
+    ap.add_argument("-k", "--voidtime", type=int)
+    # launch and back-end choices of the reference with no counterpart here: accepted, ignored
+    ap.add_argument("-A", "--autopilot")
+    ap.add_argument("-c", "--compute")
+    ap.add_argument("-W", "--workload")
+    ap.add_argument("--atomic")
+    ap.add_argument("-v", "--version", action="store_true")
     ap.add_argument("-b", "--reflect", type=int)
     ap.add_argument("-e", "--minenergy", type=float)
     ap.add_argument("-P", "--replaydet", type=int, default=0)
@@ -58,6 +68,12 @@ def main(argv=None):
     ap.add_argument("-X", "--saveref", type=int)
     ap.add_argument("-r", "--root", default="")
     args = ap.parse_args(argv)
+    if args.version:
+        from . import __version__
+        print(f"mmc_gb300 {__version__}")
+        return 0
+    if args.mc:
+        ap.error("-m 1 (MCML-style albedo weighting) is an option of the reference's CPU engine, not provided here")
 
     from . import io
     from .core import Mesh, simulate
@@ -89,9 +105,12 @@ def main(argv=None):
         upd["outputtype"] = io.output_type(args.outputtype)
     for k, a in (("issavedet", args.savedet), ("issaveexit", args.saveexit), ("issaveseed", args.saveseed),
                  ("ismomentum", args.momentum), ("isreflect", args.reflect), ("minenergy", args.minenergy),
-                 ("maxdetphoton", args.maxdetphoton), ("issaveref", args.saveref)):
+                 ("maxdetphoton", args.maxdetphoton), ("issaveref", args.saveref), ("unitinmm", args.unitinmm),
+                 ("isspecular", args.specular), ("voidtime", args.voidtime)):
         if a is not None:
             upd[k] = a
+    if args.momentum:
+        upd["issavedet"] = 1
     replay_file = None
     if args.seed is not None:
         if args.seed.endswith(".mch"):

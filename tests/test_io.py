@@ -118,6 +118,13 @@ def test_cli_lists_builtin_benchmarks():
     r = subprocess.run([sys.executable, "-m", "mmc_gb300", "-Q"], env=dict(os.environ, PYTHONPATH=root),
                        capture_output=True, text=True)
     assert r.returncode == 0 and r.stdout.split() == ["Built-in", "benchmarks:", "dmmc-cube60", "dmmc-cube60b"]
+    # the reference's flags: -v prints the version; -m is its MC method (1, MCML, is refused), not momentum
+    r = subprocess.run([sys.executable, "-m", "mmc_gb300", "-v"], env=dict(os.environ, PYTHONPATH=root),
+                       capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.startswith("mmc_gb300")
+    r = subprocess.run([sys.executable, "-m", "mmc_gb300", "-Q", "dmmc-cube60", "-m", "1"],
+                       env=dict(os.environ, PYTHONPATH=root), capture_output=True, text=True)
+    assert r.returncode != 0 and "MCML" in r.stderr
 
 
 def test_pmmc_debuglevel_parsing():
