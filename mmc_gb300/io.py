@@ -205,6 +205,7 @@ def load_input(path):
         gridstep=float(np.ravel(dom.get("Step", [1.0]))[0]), isspecular=int(ses.get("DoSpecular", 0)),
         issavedet=int(ses.get("DoPartialPath", 1 if dets else 0)), issaveseed=int(ses.get("DoSaveSeed", 0)),
         issaveexit=int(ses.get("DoSaveExit", 0)), isnormalized=int(ses.get("DoNormalize", 1)),
+        ismomentum=int(ses.get("DoDCS", 0)),
         basisorder=int(ses.get("BasisOrder", 1)), outputtype=otype, nout=float(fwd.get("N0", 1.0)),
         detpos=detpos, unitinmm=unit)
     meta = dict(session=str(ses.get("ID", "default")), outputformat=str(ses.get("OutputFormat", "bin")),

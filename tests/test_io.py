@@ -54,7 +54,11 @@ def test_json_input(tmp_path, inline):
     assert np.array_equal(mesh["elem"], m.elem) and np.array_equal(mesh["label"], m.label)
     assert cfg.nphoton == 1234 and cfg.seed == 77 and cfg.maxgate == 5 and cfg.basisorder == 0
     assert cfg.issavedet == 1 and cfg.detpos.shape == (1, 4) and meta["session"] == "t"
-    assert cfg.media.shape == (3, 4)
+    assert cfg.media.shape == (3, 4) and cfg.ismomentum == 0
+    c = json.loads(open(path).read())
+    c["Session"]["DoDCS"] = 1  # the reference's key for momentum transfer (src/mmc_utils.c:2269)
+    open(path, "w").write(json.dumps(c))
+    assert io.load_input(path)[1].ismomentum == 1
 
 
 def test_pmmc_dict_parsing():
