@@ -121,6 +121,8 @@ def _parse(cfg: dict):
                 raise ValueError("the row number of cfg.seed does not match RNG seed byte-length")
     if "tend" in kw and "tstep" not in kw:
         kw["tstep"] = kw["tend"] - kw.get("tstart", 0.0)
+    if "issave2pt" in cfg and not int(cfg["issave2pt"]):  # no fluence output (src/pmmc.cpp:1154)
+        kw["save_field"] = False
     return node, elem, label, cfg.get("facenb"), SimConfig(**kw), seeds
 
 
@@ -149,17 +151,19 @@ def run(cfg: dict) -> dict:
             raise ValueError(str(e)) from e
         raise RuntimeError(str(e)) from e
     # [datalen, maxgate]; with patterns sharing photons [srcnum, datalen, maxgate] (src/pmmc.cpp:1196-1207)
-    field = res.field.T
-    if sc.method == "grid":  # [dim.x, dim.y, dim.z, maxgate] (+ a leading srcnum), x fastest as the reference
+    field = None if res.field is None else res.field.T
+    if field is not None and sc.method == "grid":  # [dim.x, dim.y, dim.z, maxgate] (+ a leading srcnum), x fastest
         dx, dy, dz = mesh_dims
         if res.field.ndim == 3:
             field = res.field.reshape(-1, dz, dy, dx, res.field.shape[-1]).transpose(4, 3, 2, 1, 0)
         else:
             field = res.field.reshape(-1, dz, dy, dx).transpose(3, 2, 1, 0)
-    out = {"flux": field, "stat": dict(runtime=(time.perf_counter() - t0) * 1e3, nphoton=nph,
+    out = {"stat": dict(runtime=(time.perf_counter() - t0) * 1e3, nphoton=nph,
                                              energytot=res.energytot, energyabs=res.energytot - res.energyesc,
                                              normalizer=res.normalizer, raytet=res.raytet,
                                              kernel_ms=res.kernel_ms)}
+    if field is not None:
+        out["flux"] = field
     if sc.issaveref and res.dref is not None:
         out["dref"] = res.dref.T  # [nf, maxgate], as pmmc (src/pmmc.cpp:1226-1234)
     if res.traj is not None:

@@ -65,6 +65,14 @@ def test_pmmc_run_matches_api(gpu_ready):
     assert rep["flux"].sum() > 0
     with pytest.raises(ValueError):
         pmmc.run(dict(cfg, prop=m.media[:1]))
+    # issave2pt=0: records only, no fluence output (src/pmmc.cpp:1154)
+    rec = pmmc.run(dict(cfg, issave2pt=0))
+    assert "flux" not in rec and rec["detp"].shape == out["detp"].shape
+    # patterns sharing each photon: a leading srcnum axis, [srcnum, datalen, maxgate]
+    pat = np.random.default_rng(1).uniform(0.1, 1, (2, 4, 3)).astype(np.float32)
+    sh = pmmc.run(dict(cfg, srctype="pattern", srcpos=[20, 20, 0.5], srcparam1=[20, 0, 0, 4], srcparam2=[0, 20, 0, 3],
+                       srcpattern=pat, issavedet=0, basisorder=0))
+    assert sh["flux"].shape == (2, m.ne, 5)
 
 
 def test_cli_sources_grid_and_exiting_weight(gpu_ready, tmp_path):
