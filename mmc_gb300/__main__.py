@@ -159,6 +159,8 @@ def main(argv=None):
             io.write_bin(base + ".bin", res.field)
     if res.dref is not None:  # exiting weight per exterior face: <session>_dref.dat (src/mmc_mesh.c:1726-1800)
         io.write_dat(base + "_dref.dat", res.dref)
+    if res.detp is not None and cfg.issavedet and cfg.issaveexit == 2:  # <session>.img (src/mmc_host.c:424-430)
+        io.detector_image(res.detp, cfg, meta.get("detparam1", (0, 0, 0, 0)), meta.get("detparam2", (0, 0, 0, 0))).tofile(base + ".img")
     if res.detp is not None and cfg.issavedet:
         io.write_mch(base + ".mch", res.detp, res.seeds if cfg.issaveseed else None,
                      maxmedia=np.asarray(cfg.media).shape[0] - 1,

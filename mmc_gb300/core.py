@@ -189,6 +189,8 @@ class SimConfig:
     gridstep: float = 1.0                       # voxel edge of the grid output (mm)
     phase_chunk: int = 0                        # max photons per gate-phased launch (0: what memory holds)
     accumulate: int = 0                         # 1: add into the caller's field/dref (mmc_run_cu's +=)
+    detparam1: Sequence[float] = (0.0, 0.0, 0.0, 0.0)  # area detector of the exit image (issaveexit = 2,
+    detparam2: Sequence[float] = (0.0, 0.0, 0.0, 0.0)  # io.detector_image): edge vectors, pixels in w
     srcnum: int = 1                             # patterns sharing each photon (pattern source; the field
                                                 # gains a last axis of srcnum, srcpattern is pixel-major)
     save_field: bool = True

@@ -208,7 +208,14 @@ def load_input(path):
         ismomentum=int(ses.get("DoDCS", 0)),
         basisorder=int(ses.get("BasisOrder", 1)), outputtype=otype, nout=float(fwd.get("N0", 1.0)),
         detpos=detpos, unitinmm=unit)
+    # the area detector of the exit image (issaveexit = 2): the reference's JSON reader takes its
+    # Param1/Param2 from the Source object (src/mmc_utils.c:1811, :2194-2226)
+    def vec4(v):
+        v = list(np.ravel(v)) if v is not None else []
+        return tuple(float(x) for x in v) if len(v) == 4 else (0.0, 0.0, 0.0, 0.0)
+    meta_det = dict(detparam1=vec4(src.get("Param1")), detparam2=vec4(src.get("Param2")))
     meta = dict(session=str(ses.get("ID", "default")), outputformat=str(ses.get("OutputFormat", "bin")),
+                **meta_det,
                 saveweight=int(ses.get("DoSaveVolume", 1)), root=root,
                 raytracer=str(ses.get("RayTracer", "")).lower()[:1],
                 debugflag=str(ses.get("DebugFlag", "")) if not isinstance(ses.get("DebugFlag"), int) else
@@ -279,3 +286,46 @@ def write_dat(path: str, field: np.ndarray):
         for g in range(field.shape[0]):
             for j, v in enumerate(field[g]):
                 f.write(f"{j + 1}\t{v:e}\n")
+
+
+# ---------------------------------------------------------------------------
+# detector image (issaveexit = 2)
+# ---------------------------------------------------------------------------
+R_C0 = np.float32(3.335640951981520e-12)  # 1 / speed of light, s/mm
+
+
+def detector_image(detp: np.ndarray, cfg: SimConfig, detparam1, detparam2) -> np.ndarray:
+    """Time-resolved image of the detected photons' exit positions over an area
+    detector (mesh_getdetimage, src/mmc_mesh.c:2028-2074): records with exit
+    columns (issaveexit) are binned by exit (x, y) into detparam1.w x
+    detparam2.w pixels spanning detparam1.x + detparam2.x by detparam1.y +
+    detparam2.y from the first detector's (x, y), and by time of flight into the
+    gates, each adding its detected weight w0 * exp(-sum mua * L).  Returns
+    (maxgate, ny, nx) float32, the layout of the reference's <session>.img.
+    As in the reference, the time bin takes the optical path truncated to whole
+    millimetres and a photon whose exit lies outside the image is left out."""
+    media = np.asarray(cfg.media, np.float32).reshape(-1, 4)
+    M = media.shape[0] - 1
+    nx, ny = int(detparam1[3]), int(detparam2[3])
+    G = cfg.maxgate
+    img = np.zeros((G, ny, nx), np.float32)
+    detp = np.asarray(detp, np.float32)
+    if len(detp) == 0 or nx <= 0 or ny <= 0 or cfg.detpos is None or len(cfg.detpos) == 0:
+        return img
+    unit = np.float32(cfg.unitinmm)
+    path = np.zeros(len(detp), np.float32)
+    weight = detp[:, -1].copy()
+    for j in range(1, M + 1):
+        pp = detp[:, M + j]
+        path = (path + pp * media[j, 3]).astype(np.float32)
+        weight = (weight * np.exp(-(pp * media[j, 0] * unit)).astype(np.float32)).astype(np.float32)
+    ntg = (path.astype(np.int32).astype(np.float32) * R_C0 / np.float32(cfg.tstep)).astype(np.int32)
+    ntg = np.minimum(ntg, G - 1)
+    x0, y0 = np.float32(cfg.detpos[0][0]), np.float32(cfg.detpos[0][1])
+    xr = np.float32(detparam1[0]) + np.float32(detparam2[0])
+    yr = np.float32(detparam1[1]) + np.float32(detparam2[1])
+    xi = ((detp[:, -7] - x0) / xr * np.float32(nx)).astype(np.int32)  # truncation toward zero, as C
+    yi = ((detp[:, -6] - y0) / yr * np.float32(ny)).astype(np.int32)
+    ok = (xi >= 0) & (xi <= nx - 1) & (yi >= 0) & (yi <= ny - 1)
+    np.add.at(img, (ntg[ok], yi[ok], xi[ok]), weight[ok])
+    return img

@@ -102,6 +102,10 @@ def _parse(cfg: dict):
         kw["outputtype"] = ot
     if "detpos" in cfg:
         kw["detpos"] = np.asarray(cfg["detpos"], np.float32).reshape(-1, 4)
+    for k in ("detparam1", "detparam2"):  # the area detector of the exit image (issaveexit = 2)
+        if k in cfg:
+            v = list(np.asarray(cfg[k], np.float64).ravel()) + [0.0] * 4
+            kw[k] = tuple(float(x) for x in v[:4])
     if "debuglevel" in cfg:  # letters R, M, P (src/pmmc.cpp:692-710); M saves photon trajectories
         dl = str(cfg["debuglevel"]).upper()
         if not dl:
@@ -168,7 +172,11 @@ def run(cfg: dict) -> dict:
         out["dref"] = res.dref.T  # [nf, maxgate], as pmmc (src/pmmc.cpp:1226-1234)
     if res.traj is not None:
         out["traj"] = res.traj.T  # [6, records]: id, x, y, z, weight, element (src/pmmc.cpp:1092-1108)
-    if sc.issavedet and res.detp is not None and len(res.detp):
+    if sc.issavedet and res.detp is not None and sc.issaveexit == 2:
+        # the exit image [nx, ny, maxgate] instead of the records (src/pmmc.cpp:1135-1146)
+        from .io import detector_image
+        out["detp"] = detector_image(res.detp, sc, sc.detparam1, sc.detparam2).transpose(2, 1, 0)
+    elif sc.issavedet and res.detp is not None and len(res.detp):
         out["detp"] = res.detp.T
         if sc.issaveseed and res.seeds is not None:
             out["seeds"] = res.seeds.T

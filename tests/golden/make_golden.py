@@ -25,6 +25,13 @@ Badouel tracer and element-based output (-M s -C 0), unnormalized (-U 0):
   bench_dmmc-cube60, bench_dmmc-cube60b
            the reference's built-in benchmarks (-Q), dual-grid output on
            1 mm voxels, 1e5 photons
+  detimage_cube6k
+           the exit image of an area detector (-x 2): the cube6k pencil run
+           with one 30 mm detector at (10,10,0), 5 gates of 1 ns, 2e4 photons;
+           the reference's detected records (with exit columns) and the
+           <session>.img it bins from them, 8 x 8 pixels over 40 x 40 mm given
+           as the Source's Param1/Param2, where the reference's JSON reader
+           takes them
   src_pattern3
            three patterns sharing each photon (srcnum 3, photon sharing): a
            4 x 3 pixel pattern source over 20 x 20 mm of the void-layer cube6k
@@ -347,6 +354,35 @@ def make_pattern_case(wd):
     print(name, "per-pattern totals", tot.mean(0), "energies", energies)
 
 
+def make_detimage_case(wd):
+    """detimage_cube6k: the reference's records and its exit image of one run."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    name = "detimage_cube6k"
+    m = meshgen.homogeneous_cube(n=10)
+    det = np.array([[10.0, 10.0, 0.0, 30.0]])
+    src = dict(Pos=[30.0, 30.0, 0.0], Dir=[0.0, 0.0, 1.0], Param1=[40.0, 0, 0, 8], Param2=[0, 40.0, 0, 8])
+    c = dict(mesh=m, photons=20000, t1=5e-9, dt=1e-9, det=det, src=src)
+    c["e0"] = oracle.initelem(m.node, m.elem, m.label, (30.0, 30.0, 0.0))
+    write_json(os.path.join(wd, name + ".json"), name, c)
+    sess = f"{name}_{SEED0}"
+    out = os.path.join(wd, sess + ".detp")
+    cmd = [REF + "_detp", "-f", os.path.join(wd, name + ".json"), "-c", "sse", "-M", "s", "-C", "0", "-b", "1",
+           "-U", "0", "-F", "bin", "-s", sess, "-E", str(SEED0), "-n", str(c["photons"]), "-d", "1", "-x", "2"]
+    env = dict(os.environ, OMP_NUM_THREADS="1", MMCGB_DETP_OUT=out)
+    p = subprocess.run(cmd, cwd=wd, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(p.stdout[-2000:])
+    buf = open(out, "rb").read()
+    count, cols = struct.unpack("<ii", buf[:8])
+    detp = np.frombuffer(buf, np.float32, count=count * cols, offset=8).reshape(count, cols)
+    img = np.fromfile(os.path.join(wd, sess + ".img"), np.float32).reshape(5, 8, 8)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), detp=detp, img=img, detpos=det.astype(np.float32),
+                        detparam1=np.array(src["Param1"], np.float32), detparam2=np.array(src["Param2"], np.float32),
+                        tstep=np.float32(c["dt"]), gates=5)
+    print(name, "records", detp.shape, "image sum", img.sum())
+
+
 def run_ref_grid(workdir, name, seed, photons, nvox):
     """Dual-grid (DMMC, -M G) fluence of one reference run, unnormalized."""
     sess = f"{name}_{seed}_grid"
@@ -493,6 +529,8 @@ def main(only=()):
             make_bench_cases(wd)
         if not only or "src_pattern3" in only:
             make_pattern_case(wd)
+        if not only or "detimage_cube6k" in only:
+            make_detimage_case(wd)
         for name, c in case_defs().items():
             if only and name not in only:
                 continue

@@ -107,3 +107,37 @@ def test_pmmc_sources_grid_and_exiting_weight(gpu_ready):
                         issaveref=1, isnormalized=1))
     assert out["flux"].shape == (21, 21, 21, 5)   # [dim.x, dim.y, dim.z, maxgate]
     assert out["dref"].shape[1] == 5 and out["dref"].sum() > 0
+
+
+def test_exit_image_through_pmmc_and_cli(gpu_ready, tmp_path):
+    """issaveexit=2: pmmc returns the exit image [nx, ny, maxgate] as 'detp'
+    and the command line writes <session>.img; the image per launched photon
+    agrees with the reference's run of the same configuration
+    (tests/golden/detimage_cube6k.npz) within sampling noise."""
+    import golden_checks as gc
+    fx = gc.load("detimage_cube6k")
+    m = meshgen.homogeneous_cube(n=10)
+    n = 200000
+    out = pmmc.run(dict(node=m.node, elem=m.elem, elemprop=m.label, prop=m.media, srcpos=[30, 30, 0], srcdir=[0, 0, 1],
+                        nphoton=n, seed=5, tstart=0.0, tend=5e-9, tstep=1e-9, issavedet=1, issaveexit=2,
+                        detpos=fx["detpos"], detparam1=fx["detparam1"], detparam2=fx["detparam2"], basisorder=0))
+    img = out["detp"]
+    assert img.shape == (8, 8, 5)
+    ref = fx["img"].transpose(2, 1, 0) / 20000.0
+    assert img.sum() / n == pytest.approx(ref.sum(), rel=0.05)
+    hot = ref.sum(2) > 0.02 * ref.sum(2).max()  # well-populated pixels: within 20%
+    np.testing.assert_allclose(img.sum(2)[hot] / n, ref.sum(2)[hot], rtol=0.2)
+    # the command line writes the same image from its own run
+    cfgj = {"Session": {"ID": "img", "Photons": 50000, "RNGSeed": 5, "DoSaveExit": 2, "DoPartialPath": 1,
+                        "BasisOrder": 0},
+            "Domain": {"Media": [dict(mua=float(r[0]), mus=float(r[1]), g=float(r[2]), n=float(r[3])) for r in m.media]},
+            "Mesh": {"MeshNode": m.node.tolist(), "MeshElem": np.c_[m.elem, m.label].tolist()},
+            "Forward": {"T0": 0.0, "T1": 5e-9, "Dt": 1e-9},
+            "Optode": {"Source": {"Pos": [30, 30, 0], "Dir": [0, 0, 1], "Param1": [40, 0, 0, 8], "Param2": [0, 40, 0, 8]},
+                       "Detector": [{"Pos": [10, 10, 0], "R": 30}]}}
+    (tmp_path / "in.json").write_text(json.dumps(cfgj))
+    r = subprocess.run([sys.executable, "-m", "mmc_gb300", "-f", "in.json"], cwd=tmp_path,
+                       env=dict(os.environ, PYTHONPATH=ROOT), capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    cli = np.fromfile(tmp_path / "img.img", np.float32).reshape(5, 8, 8)
+    assert cli.sum() / 50000 == pytest.approx(ref.sum(), rel=0.08)

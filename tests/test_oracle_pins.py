@@ -36,3 +36,18 @@ def test_normalization_matches_reference(oracle_mod, name, basisorder):
     # the reference stages the raw field through float32 (src/mmc_cu_host.cu:430)
     np.testing.assert_allclose(field[:, idx], pin[f"norm{basisorder}_field"], rtol=2e-6)
     assert norm == pytest.approx(float(pin[f"norm{basisorder}_normalizer"]), rel=2e-6)
+
+
+def test_exit_image_matches_reference():
+    """The exit image of an area detector (-x 2): the reference's own records
+    binned by io.detector_image equal the <session>.img the reference wrote
+    from them (tests/golden/detimage_cube6k.npz)."""
+    from mmc_gb300 import io, meshgen
+    from mmc_gb300.core import SimConfig
+    fx = gc.load("detimage_cube6k")
+    m = meshgen.homogeneous_cube(n=10)
+    cfg = SimConfig(media=m.media, tend=5e-9, tstep=float(fx["tstep"]), detpos=fx["detpos"], issavedet=1,
+                    issaveexit=2)
+    img = io.detector_image(fx["detp"], cfg, fx["detparam1"], fx["detparam2"])
+    assert img.shape == fx["img"].shape == (5, 8, 8) and fx["img"].sum() > 0
+    np.testing.assert_allclose(img, fx["img"], rtol=2e-6, atol=1e-6)
