@@ -143,8 +143,12 @@ def load_input(path):
     fwd = cfgj.get("Forward", {})
     opt = cfgj.get("Optode", {})
     if "MeshNode" in msh:
-        node = np.asarray(msh["MeshNode"], np.float32).reshape(-1, 3)
-        el = np.asarray(msh["MeshElem"], np.int64)
+        # plain nested lists, or JData arrays (N x 3 'single', N x 5 'int32', row-major as stored;
+        # src/mmc_utils.c:1594-1675)
+        def arr(v, dt):
+            return _jdata_array(v).astype(dt) if isinstance(v, dict) else np.asarray(v, dt)
+        node = arr(msh["MeshNode"], np.float32).reshape(-1, 3)
+        el = arr(msh["MeshElem"], np.int64)
         elem = el[:, :4].astype(np.int32)
         label = el[:, 4].astype(np.int32) if el.shape[1] > 4 else np.ones(len(el), np.int32)
         mesh = dict(node=node, elem=elem, label=label)

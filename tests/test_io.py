@@ -46,6 +46,26 @@ def _write_case(tmp_path, inline=True):
     return str(p), m
 
 
+def test_json_input_with_jdata_mesh(tmp_path):
+    """MeshNode / MeshElem as zlib-compressed JData arrays, as the reference's
+    tools write large meshes, read like the inline lists."""
+    import base64
+    import zlib
+    path, m = _write_case(tmp_path)
+    cfg = json.loads(open(path).read())
+
+    def jd(a, t):
+        return {"_ArrayType_": t, "_ArraySize_": list(a.shape), "_ArrayZipType_": "zlib",
+                "_ArrayZipSize_": [1, int(a.size)], "_ArrayZipData_": base64.b64encode(zlib.compress(a.tobytes())).decode()}
+    cfg["Mesh"]["MeshNode"] = jd(np.ascontiguousarray(m.node, np.float32), "single")
+    cfg["Mesh"]["MeshElem"] = jd(np.ascontiguousarray(np.c_[m.elem, m.label], np.int32), "int32")
+    p = tmp_path / "jd.json"
+    p.write_text(json.dumps(cfg))
+    mesh, _, _ = io.load_input(str(p))
+    assert np.array_equal(mesh["node"], m.node) and np.array_equal(mesh["elem"], m.elem)
+    assert np.array_equal(mesh["label"], m.label)
+
+
 @pytest.mark.parametrize("inline", [True, False])
 def test_json_input(tmp_path, inline):
     path, m = _write_case(tmp_path, inline)
