@@ -1,7 +1,8 @@
 // Output stage of a simulation: element -> node scatter of the raw element
 // deposits (src/mmc_cu_host.cu:916-976), the surface nodal-volume correction
 // (src/mmc_mesh.c:1344-1386) and the fluence normalization
-// (src/mmc_mesh.c:2154-2279), for a single source.
+// (src/mmc_mesh.c:2154-2279), for one pattern's deposits (patterns sharing
+// photons run it once per pattern with that pattern's energies, api.cpp).
 #include <cmath>
 #include <cstring>
 #include <vector>
