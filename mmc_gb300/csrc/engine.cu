@@ -73,8 +73,9 @@ struct Lane {
 // Arithmetic policies.  Exact: IEEE division and square root, the project's
 // polynomial exp/log/sincos, no contraction -- bit-identical to the CPU
 // oracle.  Fast: hardware approximations (__fdividef, __expf, __logf,
-// __sincosf, rsqrtf) and fused multiply-adds, as the reference's CUDA build
-// gets from -use_fast_math; validated statistically.
+// __sincosf, rsqrtf), fused multiply-adds and float denormals flushed to zero
+// (its translation unit is built with -ftz=true), as the reference's CUDA
+// build gets from -use_fast_math; validated statistically.
 struct ExactMath {
     static __device__ __forceinline__ float div(float a, float b) { return a / b; }
     static __device__ __forceinline__ float exp(float x) { return mmc_expf(x); }
