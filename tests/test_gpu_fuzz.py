@@ -11,6 +11,8 @@ deposits, records and tallies must agree, through the general kernels (per-photo
 tracing on) and through the kernels the configuration selects otherwise.
 """
 
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -166,3 +168,32 @@ def test_random_configurations_batched_equal_solo_runs(fuzz_meshes):
             assert _rows(b.detp, b.seeds) == _rows(s.detp, s.seeds), k
         if cfg.issaveref:
             np.testing.assert_allclose(b.dref, s.dref, rtol=1e-7, atol=1e-9)
+
+
+@pytest.mark.parametrize("k", range(0, NCASES, 4))
+def test_fast_policy_launch_forms_agree(fuzz_meshes, k):
+    """With the fast arithmetic policy the plain, gate-phased and batched kernels,
+    and a simulation split into two launches, compute the same photons: equal
+    ray-tet counts and records, deposits equal up to summation order."""
+    from mmc_gb300.core import Session, simulate_batch
+    name, kw, rng = _case(k)
+    m, mesh = fuzz_meshes[name]
+    cfg = SimConfig(media=_media(m, rng), **dict(kw, fast_math=1, nphoton=4000))
+    tol = dict(rtol=1e-7, atol=1e-9) if cfg.accum_f64 else dict(rtol=3e-5, atol=1e-6)
+    try:
+        ref = simulate(mesh, dataclasses.replace(cfg, phased=-1))
+    except _native.MmcgbError:
+        return  # a source outside the mesh
+    runs = [simulate_batch([mesh], [cfg])[0]]
+    if cfg.maxgate > 2:
+        runs.append(simulate(mesh, dataclasses.replace(cfg, phased=1)))
+    s = Session(mesh, cfg)
+    s.launch(0, 1500)
+    s.launch(1500, 2500)
+    s.sync()
+    runs.append(s.end())
+    for r in runs:
+        assert r.raytet == ref.raytet and r.detected == ref.detected
+        np.testing.assert_allclose(r.field, ref.field, **tol)
+        if cfg.issavedet:
+            assert _rows(r.detp, r.seeds) == _rows(ref.detp, ref.seeds)
