@@ -304,8 +304,8 @@ def _alloc_result(mesh: Mesh, cfg: SimConfig, trace: bool, out: Optional[np.ndar
         arrs["field"] = np.empty(shape, np.float64) if cfg.save_field else None
     arrs["energy_src"] = np.zeros((2, K), np.float64) if K > 1 else None
     if cfg.issavedet:
-        arrs["detp"] = np.zeros((int(cfg.maxdetphoton), reclen), np.float32)
-        arrs["seeds"] = np.zeros((int(cfg.maxdetphoton), 16), np.uint8) if cfg.issaveseed else None
+        arrs["detp"] = np.empty((int(cfg.maxdetphoton), reclen), np.float32)
+        arrs["seeds"] = np.empty((int(cfg.maxdetphoton), 16), np.uint8) if cfg.issaveseed else None
     else:
         arrs["detp"] = arrs["seeds"] = None
     if trace:
@@ -325,8 +325,12 @@ def _alloc_result(mesh: Mesh, cfg: SimConfig, trace: bool, out: Optional[np.ndar
 
 def _make_result(r: N.Result, arrs) -> SimResult:
     saved = int(r.saved)
-    detp = arrs["detp"][:saved].copy() if arrs["detp"] is not None else None
-    seeds = arrs["seeds"][:saved].copy() if arrs["seeds"] is not None else None
+
+    def rows(a):  # the saved rows; a copy only when it frees most of the buffer
+        if a is None:
+            return None
+        return a[:saved].copy() if 4 * saved < len(a) else a[:saved]
+    detp, seeds = rows(arrs["detp"]), rows(arrs["seeds"])
     return SimResult(field=arrs["field"], detp=detp, seeds=seeds, detected=int(r.detected),
                      energytot=r.energytot, energyesc=r.energyesc, normalizer=r.normalizer,
                      raytet=int(r.raytet), aborted=int(r.aborted), kernel_ms=float(r.kernel_ms),
