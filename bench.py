@@ -208,7 +208,14 @@ def main():
     # rank r simulates photons [r*K*nps, (r+1)*K*nps) of the job: no data-path collective
     sess = Session(mesh, dataclasses.replace(cfg, photon_offset=rank * (args.steps + args.warmup) * nps))
     window = sess.phase_window(nps)
+    # every step saves its own detected photons, as a fresh job would: the record count is reset
+    # before each launch (outside the timed region), so no step finds the record buffer full
+    detcount = sess.device_buffers()["detcount"]
+    if detcount is None:
+        detcount = torch.zeros(1, device=f"cuda:{local_rank}")  # no records saved: nothing to reset
     for w in range(args.warmup):
+        detcount.zero_()
+        torch.cuda.synchronize()
         sess.launch(w * nps, nps)
         sess.sync()
     from mmc_gb300.clocks import ClockSampler
@@ -221,6 +228,7 @@ def main():
     t_wall = time.perf_counter()
     for k in range(args.steps):
         flush.zero_()
+        detcount.zero_()
         torch.cuda.synchronize()
         sess.launch((args.warmup + k) * nps, nps)
         kernel_ms.append(sess.sync())
@@ -338,7 +346,7 @@ def main():
                        "tracing": f"gate-phased, automatic window of {window} gates (the live gate planes "
                                   "fill ~70% of L2; parked photons resumed in spatial order)" if window else
                                   "one launch per step",
-                       "steps_per_photon": steps_per_photon, "detected": res.detected,
+                       "steps_per_photon": steps_per_photon, "detected_per_step": res.detected,
                        "absorbed_fraction": res.absorbed_fraction, "wall_s": wall},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
