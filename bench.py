@@ -264,12 +264,14 @@ def main():
         from mmc_gb300.core import pinned_empty
         ecfg = dataclasses.replace(cfg, photon_offset=10 ** 12)
         out = pinned_empty((ecfg.maxgate, mesh.ne))  # the application's host buffer, reused every step
-        simulate(mesh, dataclasses.replace(ecfg, nphoton=100000), out=out)  # warm the allocator
+        # one untimed full-size call: the device pool grows to the run's buffers (the gate-phasing
+        # queues of 1e8 photons) once per process, as in any application that calls repeatedly
+        simulate(mesh, dataclasses.replace(ecfg, photon_offset=ecfg.photon_offset - nps), out=out)
         esteps = max(1, min(args.steps, 3))
         if dist is not None:
             from mmc_gb300.distributed import simulate_sharded
             job = dataclasses.replace(ecfg, nphoton=nps * world)  # per-rank work fixed: weak scaling
-            simulate_sharded(mesh, dataclasses.replace(job, nphoton=100000 * world))
+            simulate_sharded(mesh, dataclasses.replace(job, photon_offset=job.photon_offset - nps * world))
         barrier()
         t0 = time.perf_counter()
         d2h = 0
@@ -296,7 +298,8 @@ def main():
             # prepares and uploads the mesh, simulates, normalizes and frees, every call
             from mmc_gb300 import core
             dsteps = 2
-            core.run(m.node, m.elem, m.label, dataclasses.replace(ecfg, nphoton=100000), out=out)
+            core.run(m.node, m.elem, m.label, dataclasses.replace(ecfg, photon_offset=ecfg.photon_offset - nps),
+                     out=out)
             t0 = time.perf_counter()
             for k in range(dsteps):
                 core.run(m.node, m.elem, m.label,
