@@ -1,5 +1,5 @@
-"""The drop-in shim of INTEGRATION.md -- mmc_run_cu implemented over
-libmmcgb -- compiles against the reference's own headers
+"""The drop-in shim of the repository's integration guide -- mmc_run_cu
+implemented over libmmcgb, the guide's C block -- compiles against the reference's own headers
 (src/mmc_cu_host.h, mmc_utils.h, mmc_mesh.h), so every mcconfig/tetmesh
 field it maps exists with a compatible type.  Needs the reference sources:
 their location comes from MMC_REFERENCE or from the reference build in
