@@ -232,6 +232,29 @@ struct Prepared {
     size_t flen = 0;
 };
 
+// The source locator on the device, for simulations whose launch positions are located per
+// photon (every source but the pencil beam): built and uploaded once per mesh.
+int ensure_device_locator(mmcgb_mesh* m) {
+    std::lock_guard<std::mutex> lock(m->loc_mu);
+    if (m->loc_start) return MMCGB_OK;
+    if (!ensure_locator(m->host))
+        return fail(MMCGB_E_MESH, "mesh too large for the source locator (more than 2^32 element-bin pairs)");
+    const LocGrid& g = m->host.grid;
+    unsigned *start = nullptr, *items = nullptr;
+    cudaError_t e;
+    if ((e = cudaMalloc((void**)&start, sizeof(unsigned) * g.start.size())) != cudaSuccess ||
+        (e = cudaMalloc((void**)&items, sizeof(unsigned) * std::max<size_t>(1, g.items.size()))) != cudaSuccess ||
+        (e = cudaMemcpy(start, g.start.data(), sizeof(unsigned) * g.start.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(items, g.items.data(), sizeof(unsigned) * g.items.size(), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        if (start) cudaFree(start);
+        if (items) cudaFree(items);
+        return cuda_fail(e, "source locator upload");
+    }
+    m->loc_start = start;
+    m->loc_items = items;
+    return MMCGB_OK;
+}
+
 int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res, cudaStream_t stream, Prepared& P) {
     const HostMesh& m = mesh->host;
     std::string err;
@@ -241,6 +264,10 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     // point sources start in e0; the others are located per photon and may lie outside the mesh
     if (e0 <= 0 && point_source(c.srctype)) return fail(MMCGB_E_SOURCE, "initial element does not enclose the source");
 
+    if (c.srctype != 0) {  // launch positions located on the device
+        rc = ensure_device_locator(mesh);
+        if (rc) return rc;
+    }
     P.maxgate = gates_of(c);
     const int M = c.nmedia - 1;
     const int reclen_dev = (2 + (c.ismomentum > 0)) * M + (c.issaveexit > 0) * 6 + 1;
@@ -685,13 +712,7 @@ int32_t mmcgb_mesh_create(const mmcgb_mesh_desc* desc, int32_t device, mmcgb_mes
         (e = cudaMemcpy(m->rec, rec.data(), sizeof(TetRec) * rec.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(m->elem, m->host.elem.data(), sizeof(int4) * m->host.ne, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(m->node, node.data(), sizeof(float4) * m->host.nn, cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMemcpy(m->label, m->host.label.data(), sizeof(int) * m->host.ne, cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMalloc((void**)&m->loc_start, sizeof(unsigned) * m->host.grid.start.size())) != cudaSuccess ||
-        (e = cudaMalloc((void**)&m->loc_items, sizeof(unsigned) * std::max<size_t>(1, m->host.grid.items.size()))) != cudaSuccess ||
-        (e = cudaMemcpy(m->loc_start, m->host.grid.start.data(), sizeof(unsigned) * m->host.grid.start.size(),
-                        cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMemcpy(m->loc_items, m->host.grid.items.data(), sizeof(unsigned) * m->host.grid.items.size(),
-                        cudaMemcpyHostToDevice)) != cudaSuccess) {
+        (e = cudaMemcpy(m->label, m->host.label.data(), sizeof(int) * m->host.ne, cudaMemcpyHostToDevice)) != cudaSuccess) {
         free_mesh_device(m.get());
         return cuda_fail(e, "mesh upload");
     }

@@ -198,10 +198,6 @@ int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err) {
             m.facenb[i] = -(int)nf;
         }
     m.nf = (int)nf;
-    if (!build_locator(m)) {
-        err = "mesh too large for the source locator (more than 2^32 element-bin pairs)";
-        return MMCGB_E_MESH;
-    }
     return MMCGB_OK;
 }
 
@@ -263,6 +259,7 @@ void pack_records(const HostMesh& m, std::vector<TetRec>& rec) {
 // :1170-1205).  A uniform grid of bounding boxes gives the same answer (the
 // smallest qualifying index) without the O(ne) scan per request.
 // ---------------------------------------------------------------------------
+namespace {
 bool build_locator(HostMesh& m) {
     float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
     for (int i = 0; i < m.nn; i++)
@@ -346,6 +343,16 @@ bool build_locator(HostMesh& m) {
     });
     return true;
 }
+}  // namespace
+
+bool ensure_locator(HostMesh& m) {
+    if (m.grid_built.load(std::memory_order_acquire)) return true;
+    std::lock_guard<std::mutex> lock(m.grid_mu);
+    if (m.grid_built.load(std::memory_order_relaxed)) return true;
+    if (!build_locator(m)) return false;
+    m.grid_built.store(true, std::memory_order_release);
+    return true;
+}
 
 static bool encloses(const HostMesh& m, int e, const float* p) {
     const int* el = &m.elem[4 * (size_t)e];
@@ -375,6 +382,21 @@ static bool encloses(const HostMesh& m, int e, const float* p) {
 }
 
 int locate(const HostMesh& m, const float p[3]) {
+    if (!m.grid_built.load(std::memory_order_acquire)) {
+        // no grid yet: every element, in parallel ranges, each range's lowest enclosing index
+        std::vector<int> best_of(16, -1);
+        std::atomic<int> slot{0};
+        parallel_ranges((size_t)m.ne, [&](size_t b, size_t e) {
+            int best = -1;
+            for (size_t i = b; i < e && best < 0; i++)
+                if (encloses(m, (int)i, p)) best = (int)i;
+            best_of[slot.fetch_add(1)] = best;
+        });
+        int best = -1;
+        for (int v : best_of)
+            if (v >= 0 && (best < 0 || v < best)) best = v;
+        return best >= 0 ? best + 1 : 0;
+    }
     const LocGrid& g = m.grid;
     int b[3];
     for (int d = 0; d < 3; d++) {

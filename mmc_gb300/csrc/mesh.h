@@ -1,6 +1,8 @@
 // Host mesh representation and preparation routines (see mesh.cpp).
 #pragma once
+#include <atomic>
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -31,14 +33,20 @@ struct HostMesh {
     std::vector<int> facenb;     // ne*4, exterior faces numbered -1,-2,...
     std::vector<float> evol;     // ne
     std::vector<float> nvol;     // nn (before the surface fix)
+    // the bounding-box grid of the source locator, built on first need (ensure_locator)
     LocGrid grid;
+    std::atomic<bool> grid_built{false};
+    std::mutex grid_mu;
 };
 
 int prepare_mesh(const mmcgb_mesh_desc& d, HostMesh& m, std::string& err);
 void pack_records(const HostMesh& m, std::vector<TetRec>& rec);
 // Face normals and plane offsets of every element, ne*16 floats: nx[4] ny[4] nz[4] d[4].
 void element_normals_all(const HostMesh& m, float* out);
-bool build_locator(HostMesh& m);  // false when its 32-bit offsets would overflow
+// Builds the locator grid once (thread-safe); false when its 32-bit offsets would overflow.
+bool ensure_locator(HostMesh& m);
+// First element (1-based, by index) enclosing p, 0 if none: through the grid when it is built,
+// else by a scan of every element on all host threads (what one query costs less than the grid).
 int locate(const HostMesh& m, const float p[3]);
 
 // The configuration checks every simulation entry makes before it allocates

@@ -120,3 +120,20 @@ def test_exiting_weight_per_face(oracle_mod, gpu_ready):
     assert not msgs, "\n".join(msgs)
     n = simulate(mesh, dataclasses.replace(small, isnormalized=1))
     np.testing.assert_allclose(n.dref, g.dref / np.float32(g.energytot), rtol=1e-6)
+
+
+def test_host_locate_before_and_after_the_locator_grid(oracle_mod, void_layer_cube):
+    """The initial-element search scans every element until a simulation needs
+    the locator grid (any source but the pencil beam); with the grid built it
+    gives the same elements (the lowest-index enclosing one, 0 outside)."""
+    m, _ = void_layer_cube
+    mesh = Mesh(m.node, m.elem, m.label)
+    rng = np.random.default_rng(9)
+    pts = np.concatenate([rng.uniform(-5, 65, (200, 3)), m.node[rng.integers(0, m.nn, 50)],  # nodes: shared corners
+                          rng.uniform(0, 60, (50, 3)).round(0)]).astype(np.float32)      # faces and edges
+    before = [mesh.locate(p) for p in pts]
+    simulate(mesh, SimConfig(media=m.media, nphoton=100, seed=1, tend=5e-9, tstep=5e-9, basisorder=0,
+                             **CASES["disk"]))
+    after = [mesh.locate(p) for p in pts]
+    assert before == after
+    assert before == [oracle_mod.initelem(m.node, m.elem, m.label, p) for p in pts]
