@@ -197,3 +197,32 @@ def test_fast_policy_launch_forms_agree(fuzz_meshes, k):
         np.testing.assert_allclose(r.field, ref.field, **tol)
         if cfg.issavedet:
             assert _rows(r.detp, r.seeds) == _rows(ref.detp, ref.seeds)
+
+
+@pytest.mark.parametrize("k", range(0, NCASES, 3))
+@pytest.mark.parametrize("outputtype", ["wl", "wp", "jacobian", "wn"])
+def test_random_replays_match_oracle(oracle_mod, fuzz_meshes, k, outputtype):
+    """The replay of a random configuration's detected photons (their seeds,
+    weights and times) deposits what the oracle's replay does (IEEE arithmetic)."""
+    from mmc_gb300 import replay as rp
+    name, kw, rng = _case(k)
+    m, mesh = fuzz_meshes[name]
+    det = np.array([[30.0, 30.0, 0.0, 25.0], [30.0, 30.0, 60.0, 25.0]], np.float32)
+    kw = dict(kw, issavedet=1, issaveseed=1, detpos=det, maxdetphoton=20000, issaveexit=0, ismomentum=0,
+              method="elem", issaveref=0, phased=-1, accum_f64=1, nphoton=4000, srcnum=1)
+    if kw.get("srctype") == "pattern":
+        kw.update(srcpattern=np.asarray(kw["srcpattern"])[:6])
+    cfg = SimConfig(media=_media(m, rng), **kw)
+    try:
+        fwd = simulate(mesh, cfg)
+    except _native.MmcgbError:
+        return  # a source outside the mesh
+    if fwd.detected < 5:
+        return
+    s, w, t, idx = rp.replay_inputs(fwd.detp, fwd.seeds, np.asarray(cfg.media), 0, cfg.tstart, cfg.tend)
+    rcfg = dataclasses.replace(cfg, nphoton=len(idx), replayseed=s, replayweight=w, replaytime=t,
+                               outputtype=outputtype, photon_offset=0)
+    g = simulate(mesh, rcfg)
+    o = oracle_mod.run(m.node, m.elem, m.label, rcfg, nthreads=4, normalize=False)
+    assert g.raytet == o["raytet"]
+    np.testing.assert_allclose(g.field, o["raw"], rtol=1e-7, atol=1e-12 * max(1.0, np.abs(o["raw"]).max()))
