@@ -126,6 +126,10 @@ def main(argv=None):
     cfg = dataclasses.replace(cfg, **upd)
     session = args.session or meta["session"]
     fmt = (args.outputformat or meta["outputformat"]).lower()
+    # the reference's formats (src/mmc_utils.c:171): text (its default) or raw float64; the NIfTI,
+    # JNIfTI, mc2 and tx3 containers are not written here
+    if fmt not in ("ascii", "dat", "bin"):
+        ap.error(f"output format '{fmt}' is not supported (ascii, bin)")
     outdir = args.root or os.getcwd()
     device = max(0, args.gpu - 1)
     mesh = Mesh(mesh_d["node"], mesh_d["elem"], mesh_d["label"], mesh_d.get("facenb"), device=device)
@@ -153,7 +157,7 @@ def main(argv=None):
     base = os.path.join(outdir, session)
     save2pt = args.save2pt if args.save2pt is not None else meta.get("saveweight", 1)
     if res.field is not None and save2pt:
-        if fmt == "dat":
+        if fmt in ("ascii", "dat"):
             io.write_dat(base + ".dat", res.field)
         else:
             io.write_bin(base + ".bin", res.field)

@@ -218,7 +218,7 @@ def load_input(path):
         v = list(np.ravel(v)) if v is not None else []
         return tuple(float(x) for x in v) if len(v) == 4 else (0.0, 0.0, 0.0, 0.0)
     meta_det = dict(detparam1=vec4(src.get("Param1")), detparam2=vec4(src.get("Param2")))
-    meta = dict(session=str(ses.get("ID", "default")), outputformat=str(ses.get("OutputFormat", "bin")),
+    meta = dict(session=str(ses.get("ID", "default")), outputformat=str(ses.get("OutputFormat", "ascii")),
                 **meta_det,
                 saveweight=int(ses.get("DoSaveVolume", 1)), root=root,
                 raytracer=str(ses.get("RayTracer", "")).lower()[:1],
@@ -285,11 +285,19 @@ def read_bin(path: str, gates: int):
 
 
 def write_dat(path: str, field: np.ndarray):
+    """Text output (mesh_saveweight, src/mmc_mesh.c:1759-1797): per gate and element (or
+    node), `index value`; with patterns sharing photons (a trailing srcnum axis)
+    `index pattern value` for each pattern."""
     field = np.asarray(field, np.float64)
     with open(path, "w") as f:
         for g in range(field.shape[0]):
-            for j, v in enumerate(field[g]):
-                f.write(f"{j + 1}\t{v:e}\n")
+            if field.ndim == 3:
+                for j in range(field.shape[1]):
+                    for k in range(field.shape[2]):
+                        f.write(f"{j + 1}\t{k + 1}\t{field[g, j, k]:e}\n")
+            else:
+                for j, v in enumerate(field[g]):
+                    f.write(f"{j + 1}\t{v:e}\n")
 
 
 # ---------------------------------------------------------------------------

@@ -25,8 +25,8 @@ def test_cli_run_and_replay(gpu_ready, tmp_path):
                       "Detector": [{"Pos": [40, 30, 0], "R": 3}, {"Pos": [45, 30, 0], "R": 3}]}}
     (tmp_path / "in.json").write_text(json.dumps(cfg))
     env = dict(os.environ, PYTHONPATH=ROOT)
-    r = subprocess.run([sys.executable, "-m", "mmc_gb300", "-f", "in.json", "-s", "base", "-d", "1", "-q", "1"],
-                       cwd=tmp_path, env=env, capture_output=True, text=True)
+    r = subprocess.run([sys.executable, "-m", "mmc_gb300", "-f", "in.json", "-s", "base", "-d", "1", "-q", "1",
+                        "-F", "bin"], cwd=tmp_path, env=env, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     field = io.read_bin(str(tmp_path / "base.bin"), 5)
     detp, hdr, seeds = io.read_mch(str(tmp_path / "base.mch"))
@@ -39,12 +39,23 @@ def test_cli_run_and_replay(gpu_ready, tmp_path):
     np.testing.assert_allclose(field, ref.field, rtol=1e-9)
     # replay of detector 1 from the .mch file (-E file.mch -P 1 -O l)
     r = subprocess.run([sys.executable, "-m", "mmc_gb300", "-f", "in.json", "-s", "rep", "-E", "base.mch", "-P", "1",
-                        "-O", "l", "-d", "1", "-U", "0"], cwd=tmp_path, env=env, capture_output=True, text=True)
+                        "-O", "l", "-d", "1", "-U", "0", "-F", "bin"], cwd=tmp_path, env=env, capture_output=True,
+                       text=True)
     assert r.returncode == 0, r.stderr
     rep = io.read_bin(str(tmp_path / "rep.bin"), 5)
     assert rep.sum() > 0
     d2, h2, _ = io.read_mch(str(tmp_path / "rep.mch"))
     assert h2["savedphoton"] == int((detp[:, 0] == 1).sum())
+    # the reference's default output format is text: <session>.dat, `index value` per gate
+    r = subprocess.run([sys.executable, "-m", "mmc_gb300", "-f", "in.json", "-s", "txt"], cwd=tmp_path, env=env,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    txt = np.loadtxt(tmp_path / "txt.dat")
+    assert txt.shape == (5 * m.ne, 2) and np.array_equal(txt[:m.ne, 0], np.arange(1, m.ne + 1))
+    np.testing.assert_allclose(txt[:, 1].reshape(5, m.ne), field, rtol=1e-5, atol=1e-30)
+    r = subprocess.run([sys.executable, "-m", "mmc_gb300", "-f", "in.json", "-F", "jnii"], cwd=tmp_path, env=env,
+                       capture_output=True, text=True)
+    assert r.returncode != 0 and "not supported" in r.stderr
 
 
 def test_pmmc_run_matches_api(gpu_ready):
@@ -88,8 +99,8 @@ def test_cli_sources_grid_and_exiting_weight(gpu_ready, tmp_path):
            "Optode": {"Source": {"Type": "disk", "Pos": [30, 30, 0], "Dir": [0, 0, 1], "Param1": [10, 0, 0, 0]}}}
     (tmp_path / "in.json").write_text(json.dumps(cfg))
     env = dict(os.environ, PYTHONPATH=ROOT)
-    r = subprocess.run([sys.executable, "-m", "mmc_gb300", "-f", "in.json", "-M", "G", "-U", "0"], cwd=tmp_path,
-                       env=env, capture_output=True, text=True)
+    r = subprocess.run([sys.executable, "-m", "mmc_gb300", "-f", "in.json", "-M", "G", "-U", "0", "-F", "bin"],
+                       cwd=tmp_path, env=env, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     grid = io.read_bin(str(tmp_path / "g.bin"), 1)
     assert grid.shape == (1, 31 * 31 * 31) and grid.sum() > 0
