@@ -20,8 +20,8 @@ constexpr int kMaxSimsShared = 256;  // simulations whose media tables fit in on
 constexpr int kMaxLabel = 63;        // medium labels a mesh may use (kMaxMedia - 1)
 // A packed face word holds the neighbour's medium label in its low lbits bits and the
 // neighbour id, signed, in the 32 - lbits bits above, lbits being the fewest bits (1..6) that
-// hold the mesh's largest label: a mesh of two media keeps 30 bits for element ids
-// (1,073,741,823 elements), one of 64 media 25 (33,554,431).
+// hold the mesh's largest label: labels 0-1 leave 31 bits for signed element ids
+// (1,073,741,823 elements), labels up to 63 leave 26 (33,554,431).
 inline int label_bits(int maxlabel) {
     int b = 1;
     while (b < 6 && (1 << b) <= maxlabel) b++;
