@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define MMCGB_ABI_VERSION 5
+#define MMCGB_ABI_VERSION 6
 
 typedef enum mmcgb_status {
     MMCGB_OK = 0,
@@ -154,6 +154,16 @@ typedef struct mmcgb_config {
                                 pattern normalized with its own energies; the last column of a
                                 detected record holds the launch pixel (uint32 bits) instead of
                                 the initial weight.  0 or 1: one pattern */
+    const float* nodemua;    /* nn per-node absorption coefficients (1/mm), or NULL: each step then
+                                takes its element's mua as the mean of the element's four nodal
+                                values instead of the media row of its label -- the reference's
+                                DOT-reconstruction mode (cfg->nodemua with isnodalmua,
+                                src/mmc_core.cl:785-793, src/mmc_utils.h:314-322); the deposit
+                                divides by that mua, the output stage still normalizes with the
+                                media table */
+    const float* nodemusp;   /* nn per-node scattering coefficients (1/mm) taking the element's mus
+                                the same way (isnodalmusp); read only with nodemua, as the
+                                reference reads it; g and n stay those of the label's media row */
 } mmcgb_config;
 
 /* Outputs.  Pointers may be NULL to skip an output; counts are always set. */
@@ -207,12 +217,12 @@ int32_t mmcgb_mesh_info(const mmcgb_mesh* mesh, int32_t* nn, int32_t* ne, int32_
  * (ne*4), element volumes (ne), nodal volumes before the surface fix (nn). */
 int32_t mmcgb_mesh_export(const mmcgb_mesh* mesh, int32_t* elem, int32_t* facenb,
                           float* evol, float* nvol);
-/* First element (1-based, by index) enclosing p, 0 if none
- * (src/mmc_mesh.c:1060-1090). */
 /* Dimensions and origin of the dual-grid output of `m` for voxel edge `step`
  * (mesh_createdualmesh, src/mmc_mesh.c:349-381): origin = node minimum - 1e-6,
  * dim = (int)((max - min + 2e-6) / step) + 1 per axis. */
 int32_t mmcgb_grid_info(const mmcgb_mesh* m, float step, int32_t dim[3], float origin[3]);
+/* First element (1-based, by index) enclosing p, 0 if none
+ * (src/mmc_mesh.c:1060-1090). */
 int32_t mmcgb_mesh_locate(const mmcgb_mesh* mesh, const float p[3]);
 
 /* One simulation on a resident mesh (src/mmc_cu_host.cu:204-1528). */
@@ -328,7 +338,7 @@ int32_t mmcgb_run(const mmcgb_mesh_desc* desc, const mmcgb_config* cfg, int32_t 
  *     is used only if it encloses srcpos, otherwise the source is located);
  *     then limits: point sources, element output, nmedia <=
  *     MMCGB_NOALLOC_MAX_MEDIA, detnum <= MMCGB_NOALLOC_MAX_DET, accum_f64 = 1,
- *     no replay, exiting weight or trajectories; anything else returns
+ *     no replay, exiting weight, trajectories or per-node properties; anything else returns
  *     MMCGB_E_ARG
  *   - the first call on a device looks up the array's device address; make it
  *     before any stream capture

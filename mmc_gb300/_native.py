@@ -57,6 +57,7 @@ class Config(C.Structure):
         ("srcparam1", C.c_float * 4), ("srcparam2", C.c_float * 4), ("focus", C.c_float), ("srcpattern", C.c_void_p),
         ("issaveref", C.c_int32), ("method", C.c_int32), ("gridstep", C.c_float), ("maxjumpdebug", C.c_uint32),
         ("phase_chunk", C.c_uint64), ("accumulate", C.c_int32), ("srcnum", C.c_int32),
+        ("nodemua", C.c_void_p), ("nodemusp", C.c_void_p),
     ]
 
 
@@ -144,7 +145,7 @@ def load():
                      "mmcgb_mesh_create", "mmcgb_mesh_destroy", "mmcgb_mesh_info", "mmcgb_mesh_export",
                      "mmcgb_mesh_locate", "mmcgb_simulate", "mmcgb_simulate_batch", "mmcgb_run"):
             getattr(lib, name).restype = C.c_int32
-        if lib.mmcgb_abi_version() != 5:
+        if lib.mmcgb_abi_version() != 6:
             raise NativeLibraryError("libmmcgb ABI version mismatch")
         _lib = lib
         return lib

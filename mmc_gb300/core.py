@@ -56,7 +56,7 @@ def prepare_host(node, elem, label, facenb=None):
 def normalize_host(node, elem, label, cfg: "SimConfig", raw, energytot: float, energyesc: float):
     """Output stage on the host (mmcgb_normalize_host): returns (field, normalizer)."""
     d, keep = _desc(node, elem, label)
-    c, ckeep = cfg.to_c()
+    c, ckeep = cfg.to_c(d.nn)
     raw = np.ascontiguousarray(raw, np.float64)
     datalen = d.nn if cfg.basisorder else d.ne
     field = np.zeros((cfg.maxgate, datalen), np.float64)
@@ -193,13 +193,17 @@ class SimConfig:
     detparam2: Sequence[float] = (0.0, 0.0, 0.0, 0.0)  # io.detector_image): edge vectors, pixels in w
     srcnum: int = 1                             # patterns sharing each photon (pattern source; the field
                                                 # gains a last axis of srcnum, srcpattern is pixel-major)
+    nodemua: Optional[np.ndarray] = None        # per-node mua (nn): element mua = mean of its nodes'
+    nodemusp: Optional[np.ndarray] = None       # per-node mus (nn), used only with nodemua
     save_field: bool = True
 
     @property
     def maxgate(self) -> int:
         return int((np.float32(self.tend) - np.float32(self.tstart)) / np.float32(self.tstep) + np.float32(0.5))
 
-    def to_c(self):
+    def to_c(self, nn: Optional[int] = None):
+        """The C configuration and the arrays it points into.  `nn`: the mesh's
+        node count, against which per-node arrays are checked."""
         keep = {}
         c = N.Config()
         c.nphoton = int(self.nphoton)
@@ -221,6 +225,14 @@ class SimConfig:
         c.phase_chunk = int(self.phase_chunk)
         c.accumulate = int(self.accumulate)
         c.srcnum = int(self.srcnum)
+        for k in ("nodemua", "nodemusp"):
+            v = getattr(self, k)
+            if v is not None:
+                v = np.ascontiguousarray(v, dtype=np.float32).reshape(-1)
+                if nn is not None and v.shape[0] != nn:
+                    raise ValueError(f"{k} needs one value per node ({nn}), got {v.shape[0]}")
+                keep[k] = v
+                setattr(c, k, _ptr(v))
         m = self.method
         c.method = {"elem": 0, "grid": 1}[m] if isinstance(m, str) else int(m)
         c.gridstep = float(self.gridstep)
@@ -347,7 +359,7 @@ def simulate(mesh: Mesh, cfg: SimConfig, trace: bool = False, out: Optional[np.n
     each photon's final weight, ray-tet test count and detector; such runs
     take the general kernels (the same results, a few percent slower)."""
     lib = N.load()
-    c, keep = cfg.to_c()
+    c, keep = cfg.to_c(mesh.nn)
     r, arrs = _alloc_result(mesh, cfg, trace, out)
     N.check(lib.mmcgb_simulate(mesh.handle, C.byref(c), C.byref(r)))
     del keep
@@ -385,7 +397,7 @@ def run(node, elem, label, cfg: SimConfig, device: int = 0, out: Optional[np.nda
         nfo = C.c_int32()
         N.check(lib.mmcgb_prepare_host(C.byref(d), None, None, None, None, None, C.byref(nfo)))
         nf = nfo.value
-    c, keep = cfg.to_c()
+    c, keep = cfg.to_c(d.nn)
     r, arrs = _alloc_result(_HostMesh(node, elem, nf), cfg, False, out)
     if dref is not None:
         if dref.dtype != np.float64 or dref.shape != (cfg.maxgate, nf) or not dref.flags.c_contiguous:
@@ -408,7 +420,7 @@ def simulate_batch(meshes: Sequence[Mesh], cfgs: Sequence[SimConfig]) -> list:
     harr = (C.c_void_p * n)()
     keeps, allarrs = [], []
     for i in range(n):
-        c, keep = cfgs[i].to_c()
+        c, keep = cfgs[i].to_c(meshes[i].nn)
         carr[i] = c
         keeps.append(keep)
         r, arrs = _alloc_result(meshes[i], cfgs[i], False)
@@ -427,7 +439,7 @@ class Session:
     def __init__(self, mesh: Mesh, cfg: SimConfig):
         lib = N.load()
         self.mesh, self.cfg = mesh, cfg
-        self._c, self._keep = cfg.to_c()
+        self._c, self._keep = cfg.to_c(mesh.nn)
         h = C.c_void_p()
         N.check(lib.mmcgb_session_begin(mesh.handle, C.byref(self._c), None, C.byref(h)))
         self._h = h

@@ -156,6 +156,10 @@ int mmcgb::validate_config(const HostMesh& m, const mmcgb_config& c, std::string
             if (!std::isfinite(c.media[4 * i + k])) { err = "media values must be finite"; return MMCGB_E_ARG; }
     const float vn = c.srcdir[0] * c.srcdir[0] + c.srcdir[1] * c.srcdir[1] + c.srcdir[2] * c.srcdir[2];
     if (!(std::fabs(vn - 1.f) < 1e-3f)) { err = "srcdir must be a unit vector"; return MMCGB_E_ARG; }
+    for (const float* v : {c.nodemua, c.nodemua ? c.nodemusp : nullptr})
+        if (v)
+            for (int i = 0; i < m.nn; i++)
+                if (!std::isfinite(v[i])) { err = "per-node mua/musp values must be finite"; return MMCGB_E_ARG; }
     return MMCGB_OK;
 }
 
@@ -199,6 +203,8 @@ struct SimBuffers {
     double* energy_src = nullptr;  // photon sharing: 64 slots x 2 x srcnum
     unsigned long long* counters = nullptr;
     float* pattern = nullptr;
+    float* nodemua = nullptr;   // per-node mua / mus (nn each), when given
+    float* nodemusp = nullptr;
     double* dref = nullptr;
     float* traj = nullptr;
     unsigned* trajcount = nullptr;
@@ -306,6 +312,14 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
         CK(B.alloc(&B.pattern, plen));
         CK(cudaMemcpyAsync(B.pattern, c.srcpattern, sizeof(float) * plen, cudaMemcpyHostToDevice, stream));
     }
+    if (c.nodemua) {
+        CK(B.alloc(&B.nodemua, (size_t)m.nn));
+        CK(cudaMemcpyAsync(B.nodemua, c.nodemua, sizeof(float) * m.nn, cudaMemcpyHostToDevice, stream));
+        if (c.nodemusp) {
+            CK(B.alloc(&B.nodemusp, (size_t)m.nn));
+            CK(cudaMemcpyAsync(B.nodemusp, c.nodemusp, sizeof(float) * m.nn, cudaMemcpyHostToDevice, stream));
+        }
+    }
     if (c.replayseed) {
         CK(B.alloc(&B.rseed, 2 * c.nphoton));
         CK(B.alloc(&B.rweight, c.nphoton));
@@ -338,6 +352,8 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
     S.nmedia = c.nmedia;
     S.detnum = c.detnum;
     S.media = B.media;
+    S.nodemua = B.nodemua;
+    S.nodemusp = B.nodemusp;
     S.det = B.det;
     S.nphoton = c.nphoton;
     S.photon_offset = c.photon_offset;

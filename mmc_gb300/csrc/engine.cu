@@ -248,7 +248,18 @@ __device__ __forceinline__ void raytet_step(Lane& L, const SimDev& S, const floa
         // only the exit face's word is loaded, once the face is known: holding all four through
         // the plane tests measured 1.9% slower than the extra dependent load
         L.nbword = __ldg(reinterpret_cast<const int*>(&R->nb) + faceid);
-        const float4 prop = med[L.label];  // mua mus g n
+        float4 prop = med[L.label];  // mua mus g n
+        if (GEN && S.nodemua) {
+            // per-node properties (the reference's DOT-reconstruction mode, src/mmc_core.cl:785-793):
+            // the mean of the element's four nodal values, summed in node order
+            const int4 e = __ldg(S.elem + (L.eid - 1));
+            const float* nm = S.nodemua;
+            prop.x = 0.25f * (((__ldg(nm + e.x - 1) + __ldg(nm + e.y - 1)) + __ldg(nm + e.z - 1)) + __ldg(nm + e.w - 1));
+            if (S.nodemusp) {
+                const float* ns = S.nodemusp;
+                prop.y = 0.25f * (((__ldg(ns + e.x - 1) + __ldg(ns + e.y - 1)) + __ldg(ns + e.z - 1)) + __ldg(ns + e.w - 1));
+            }
+        }
         float currweight = L.weight;
         float Lmove = (prop.y <= kEps) ? kRMinMus : MP::div(L.slen, prop.y);
         L.isend = (Lmin > Lmove);
@@ -1360,7 +1371,7 @@ size_t smem_bytes(int nmed_rows, int reclen_max, int threads, int want_seed) {
 // Kernels compiled with the general launch and deposit (SRC) serve
 // simulations whose source is not a pencil beam starting in a known element,
 // that deposit into a voxel grid, record trajectories, write the per-photon
-// trace outputs or save momentum transfer; the others carry only the pencil
+// trace outputs, save momentum transfer or read per-node properties; the others carry only the pencil
 // launch and the element deposit, which keeps the step loop lean (the trace
 // outputs' eleven null tests alone cost the pencil kernels 4.9%, the roulette
 // and momentum tests 2%).  Forward single-simulation runs with Russian
@@ -1368,7 +1379,7 @@ size_t smem_bytes(int nmed_rows, int reclen_max, int threads, int want_seed) {
 #if MMCGB_ENGINE_FAST
 bool general_source(const SimDev& s) {
     return s.srctype != ST_PENCIL || s.e0 <= 0 || s.grid || s.traj || s.photon_weight || s.photon_steps ||
-           s.photon_det || s.ismomentum;
+           s.photon_det || s.ismomentum || s.nodemua;
 }
 #endif
 

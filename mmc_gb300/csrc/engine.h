@@ -63,6 +63,8 @@ struct SimDev {
     int nmedia;
     int detnum;
     const float4* media;   // nmedia rows: mua mus g n
+    const float* nodemua;  // per-node mua (nn), or null: an element's mua is the mean of its nodes'
+    const float* nodemusp; // per-node mus (nn), read only with nodemua
     const float4* det;     // detnum rows: x y z r
     // photons
     unsigned long long nphoton;

@@ -101,6 +101,7 @@ extern "C" int32_t mmcgb_simulate_noalloc(mmcgb_mesh* mesh, const mmcgb_config* 
     if (c->replayseed) return fail(MMCGB_E_ARG, "no-alloc entry does not replay");
     if (c->method != 0) return fail(MMCGB_E_ARG, "no-alloc entry deposits on the elements (method 0)");
     if (c->issaveref || c->maxjumpdebug) return fail(MMCGB_E_ARG, "no-alloc entry has no exiting-weight or trajectory output");
+    if (c->nodemua) return fail(MMCGB_E_ARG, "no-alloc entry reads no per-node properties");
     if (c->issavedet && (!out->detp || !out->detcount))
         return fail(MMCGB_E_ARG, "issavedet needs detp and detcount");
     if (c->issavedet && c->issaveseed && !out->seeds) return fail(MMCGB_E_ARG, "issaveseed needs seeds");

@@ -25,8 +25,7 @@ _OUTPUTS = {"flux", "fluence", "energy", "jacobian", "wl", "wp", "wn"}
 # keys of the reference's binding for options this library does not provide: refused when set,
 # rather than ignored
 _UNSUPPORTED = {"mcmethod": "MCML-style albedo weighting (an option of the reference's CPU engine)",
-                "isextdet": "wide-field detector elements", "isnodalmua": "per-node absorption",
-                "isnodalmusp": "per-node scattering", "adjointmode": "adjoint outputs"}
+                "isextdet": "wide-field detector elements", "adjointmode": "adjoint outputs"}
 
 
 def version() -> str:
@@ -102,6 +101,13 @@ def _parse(cfg: dict):
         kw["outputtype"] = ot
     if "detpos" in cfg:
         kw["detpos"] = np.asarray(cfg["detpos"], np.float32).reshape(-1, 4)
+    # per-node mua/musp (src/pmmc.cpp:630-672): giving the array switches the mode on; the flags
+    # alone would have the reference's kernel read an array it never uploaded, so they are refused
+    for arr, flag in (("nodemua", "isnodalmua"), ("nodemusp", "isnodalmusp")):
+        if arr in cfg:
+            kw[arr] = np.asarray(cfg[arr], np.float32).ravel(order="F")
+        elif int(cfg.get(flag, 0) or 0):
+            raise ValueError(f"cfg.{flag} needs cfg.{arr}, one value per node")
     for k in ("detparam1", "detparam2"):  # the area detector of the exit image (issaveexit = 2)
         if k in cfg:
             v = list(np.asarray(cfg[k], np.float64).ravel()) + [0.0] * 4

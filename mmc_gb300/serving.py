@@ -54,7 +54,8 @@ def device_bytes(mesh: Mesh, cfg: SimConfig) -> int:
     nmed = np.asarray(cfg.media).reshape(-1, 4).shape[0]
     reclen = 2 + (2 + (1 if cfg.ismomentum else 0)) * (nmed - 1) + (6 if cfg.issaveexit else 0)
     det = cfg.maxdetphoton * (reclen * 4 + (16 if cfg.issaveseed else 0)) if cfg.issavedet else 0
-    return flen * per + det + (1 << 16)
+    nodal = 4 * mesh.nn * ((cfg.nodemua is not None) + (cfg.nodemua is not None and cfg.nodemusp is not None))
+    return flen * per + det + nodal + (1 << 16)
 
 
 class Server:

@@ -392,6 +392,17 @@ static float raytet_step(engine* g, ray* r) {
     if (r->faceid >= 0 && Lmin >= 0.f) {
         int type = g->type[r->eid - 1];
         float mua = medium(g, type, 0), mus = medium(g, type, 1), nmed = medium(g, type, 3);
+        if (g->cfg->nodemua) {
+            /* src/mmc_core.cl:785-793: the mean of the element's four nodal values, summed in
+               node order */
+            const int* e = g->elem + 4 * (size_t)(r->eid - 1);
+            const float* nm = g->cfg->nodemua;
+            mua = 0.25f * (((nm[e[0] - 1] + nm[e[1] - 1]) + nm[e[2] - 1]) + nm[e[3] - 1]);
+            if (g->cfg->nodemusp) {
+                const float* ns = g->cfg->nodemusp;
+                mus = 0.25f * (((ns[e[0] - 1] + ns[e[1] - 1]) + ns[e[2] - 1]) + ns[e[3] - 1]);
+            }
+        }
         float currweight = r->weight;
         r->Lmove = (mus <= O_EPS) ? O_R_MIN_MUS : r->slen / mus;
         r->isend = (Lmin > r->Lmove);

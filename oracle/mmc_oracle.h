@@ -61,6 +61,9 @@ typedef struct oracle_cfg {
     float gridstep;         /* voxel edge of the grid output (mm), 0 = 1 */
     int srcnum;             /* patterns sharing each photon (pattern source, src/mmc_core.cl:1907-1911);
                                field_raw then holds srcnum values per cell, adjacent; 0 or 1 = one */
+    const float* nodemua;   /* nn per-node absorption, or NULL: an element's mua is then the mean of
+                               its four nodes' values (src/mmc_core.cl:785-793) */
+    const float* nodemusp;  /* nn per-node scattering coefficients, read only with nodemua */
 } oracle_cfg;
 
 typedef struct oracle_out {

@@ -37,7 +37,7 @@ class OCfg(C.Structure):
         ("accum_f64", C.c_int), ("step_budget", C.c_uint64),
         ("srctype", C.c_int), ("srcparam1", C.c_float * 4), ("srcparam2", C.c_float * 4), ("focus", C.c_float),
         ("srcpattern", C.c_void_p), ("issaveref", C.c_int), ("method", C.c_int), ("gridstep", C.c_float),
-        ("srcnum", C.c_int),
+        ("srcnum", C.c_int), ("nodemua", C.c_void_p), ("nodemusp", C.c_void_p),
     ]
 
 
@@ -186,6 +186,12 @@ def _ocfg(cfg, maxgate, e0, keep):
         pat = np.ascontiguousarray(pat, np.float32).ravel()
         keep.append(pat)
         c.srcpattern = _p(pat)
+    for k in ("nodemua", "nodemusp"):
+        v = getattr(cfg, k, None)
+        if v is not None:
+            v = np.ascontiguousarray(v, np.float32).ravel()
+            keep.append(v)
+            setattr(c, k, _p(v))
     return c
 
 
@@ -203,6 +209,10 @@ def run(node, elem, label, cfg, nthreads=1, trace=False, normalize=True):
     e0 = max(int(e0), 0)
     keep = []
     c = _ocfg(cfg, maxgate, e0, keep)
+    for k in ("nodemua", "nodemusp"):
+        v = getattr(cfg, k, None)
+        if v is not None and np.size(v) != nn:
+            raise ValueError(f"oracle: {k} needs one value per node ({nn})")
     framelen = ne
     if c.method == 1:
         framelen = int(np.prod(grid_dims(node, cfg.gridstep if cfg.gridstep > 0 else 1.0)))

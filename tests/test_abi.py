@@ -26,6 +26,6 @@ def test_library_exports_every_declared_symbol():
 def test_python_binding_loads_without_gpu():
     from mmc_gb300 import _native
     lib = _native.load()
-    assert lib.mmcgb_abi_version() == 5
+    assert lib.mmcgb_abi_version() == 6
     for n in _native.EXPORTS:
         getattr(lib, n)

@@ -166,5 +166,11 @@ def test_noalloc_rejects_sizes_beyond_its_maximum(gpu_ready, small_cube):
     assert fn(mesh.handle, C.byref(c2), C.byref(out), None) == 1
     msg = lib.mmcgb_last_error().decode()
     assert "maximum" in msg and "256" in msg, msg
+    # per-node properties would need device copies of the nodal arrays
+    cfg = SimConfig(media=m.media, nphoton=1000, srcpos=(30.0, 30.0, 0.0), basisorder=0, isnormalized=0,
+                    nodemua=np.full(mesh.nn, 0.01, np.float32))
+    c3, keep3 = cfg.to_c(mesh.nn)
+    assert fn(mesh.handle, C.byref(c3), C.byref(out), None) == 1
+    assert "per-node" in lib.mmcgb_last_error().decode()
     torch.cuda.synchronize(dev)
-    del keep, keep2
+    del keep, keep2, keep3
