@@ -5,7 +5,7 @@ at a time: meshes with void layers and inclusions, media (zero absorption,
 index mismatches), boundary conditions, gate counts (one gate: roulette on),
 sources, patterns sharing photons, detectors with exit/momentum columns and
 seeds, float32 or float64 accumulation, element or dual-grid output, the
-exiting weight per face and gate-phased tracing.  With IEEE arithmetic every
+exiting weight per face, per-node mua/mus and gate-phased tracing.  With IEEE arithmetic every
 photon must end as the oracle's (weight bits, ray-tet tests, detector), and the
 deposits, records and tallies must agree, through the general kernels (per-photon
 tracing on) and through the kernels the configuration selects otherwise.
@@ -89,6 +89,19 @@ def _case(k):
     return name, kw, rng
 
 
+def _nodal(k, m):
+    """Per-node mua (and mus) for a fifth of the cases, from a stream of their own
+    so that the other draws of a case stay as they are."""
+    rng = np.random.default_rng(5000 + k)
+    if rng.random() >= 0.2:
+        return {}
+    nn = len(m.node)
+    out = dict(nodemua=rng.uniform(0.0, 0.05, nn).astype(np.float32))
+    if rng.random() < 0.5:
+        out["nodemusp"] = rng.uniform(0.2, 5.0, nn).astype(np.float32)
+    return out
+
+
 def _media(m, rng):
     media = np.array(m.media, np.float32).copy()
     for r in range(1, media.shape[0]):
@@ -110,7 +123,7 @@ def _rows(detp, seeds):
 def test_random_configuration_matches_oracle(oracle_mod, fuzz_meshes, k):
     name, kw, rng = _case(k)
     m, mesh = fuzz_meshes[name]
-    cfg = SimConfig(media=_media(m, rng), **kw)
+    cfg = SimConfig(media=_media(m, rng), **kw, **_nodal(k, m))
     # float32 sums depend on the order of the additions; float64 ones hardly
     tol = dict(rtol=1e-7, atol=1e-9) if cfg.accum_f64 else dict(rtol=3e-5, atol=1e-6)
     try:
