@@ -250,6 +250,9 @@ def main():
     # engine launches per step: one per window of gates (the library's automatic window)
     span = window
     launches_per_step = -(-cfg.maxgate // span) if span > 0 else 1
+    # all of the library's kernels in a step: the engine launches, the two kernels that order the
+    # parked photons between windows, and the fold of the replicated near-source cells
+    kernels_per_step = launches_per_step + 2 * (launches_per_step - 1) + 1
     achieved = raytet_per_launch * BYTES_PER_STEP / (avg_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
     tpp = profiled_traffic()
@@ -361,7 +364,7 @@ def main():
             "cpu_baseline": cpu,
             "e2e": e2e,
             "e2e_dropin": e2e_dropin,
-            "gpu_launches": args.steps * launches_per_step,
+            "gpu_launches": args.steps * kernels_per_step,
             "clocks": clocks,
             "forms": forms,
         }

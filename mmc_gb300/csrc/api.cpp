@@ -203,6 +203,7 @@ struct SimBuffers {
     double* energy_src = nullptr;  // photon sharing: 64 slots x 2 x srcnum
     unsigned long long* counters = nullptr;
     float* pattern = nullptr;
+    double* hot = nullptr;        // replicated near-source cells (SimDev::hot), allocated at first launch
     float* nodemua = nullptr;   // per-node mua / mus (nn each), when given
     float* nodemusp = nullptr;
     double* dref = nullptr;
@@ -236,6 +237,7 @@ struct Prepared {
     int maxgate = 0;
     int reclen = 0;   // columns per record incl. detector id
     size_t flen = 0;
+    bool hot_ok = false;  // the simulation may use replicated near-source cells (SimDev::hot)
 };
 
 // The source locator on the device, for simulations whose launch positions are located per
@@ -312,6 +314,9 @@ int prepare_sim(mmcgb_mesh* mesh, const mmcgb_config& c, const mmcgb_result* res
         CK(B.alloc(&B.pattern, plen));
         CK(cudaMemcpyAsync(B.pattern, c.srcpattern, sizeof(float) * plen, cudaMemcpyHostToDevice, stream));
     }
+    // replicated near-source cells (allocated by the first unbatched launch, ensure_hot):
+    // forward element-output runs of a point source with float64 sums
+    P.hot_ok = f64 && c.method == 0 && !c.replayseed && point_source(c.srctype) && src_count(c) == 1;
     if (c.nodemua) {
         CK(B.alloc(&B.nodemua, (size_t)m.nn));
         CK(cudaMemcpyAsync(B.nodemua, c.nodemua, sizeof(float) * m.nn, cudaMemcpyHostToDevice, stream));
@@ -904,6 +909,32 @@ int phased_setup(mmcgb_session* s, const PhasePlan& plan) {
 
 extern "C" {
 
+namespace {
+
+// The replicated near-source cells of an unbatched session, allocated at its first launch:
+// kHotReps copies of the gate-0 plane, when they take at most 2 GiB and fit in free memory.
+// A session without them deposits into the cells themselves (same sums, other order).
+int ensure_hot(mmcgb_session* s) {
+    Prepared& P = s->P;
+    if (!P.hot_ok || P.buf.hot) return MMCGB_OK;
+    P.hot_ok = false;  // one attempt
+    const size_t n = (size_t)kHotReps * (size_t)P.sim.ne;
+    if (n * sizeof(double) > (2ull << 30) ||
+        n * sizeof(double) + (256ull << 20) > free_device_memory(s->mesh->device))
+        return MMCGB_OK;
+    if (P.buf.alloc(&P.buf.hot, n) != cudaSuccess) {
+        (void)cudaGetLastError();
+        P.buf.hot = nullptr;
+        return MMCGB_OK;
+    }
+    CK(cudaMemsetAsync(P.buf.hot, 0, sizeof(double) * n, s->stream));
+    P.sim.hot = P.buf.hot;
+    P.sim.hot_steps = kHotSteps;
+    return MMCGB_OK;
+}
+
+}  // namespace
+
 int32_t mmcgb_session_launch(mmcgb_session* s, uint64_t photon_offset, uint64_t nphoton) {
     if (!s) return fail(MMCGB_E_ARG, "null session");
     if (s->cfg.replayseed && (photon_offset != 0 || nphoton != s->cfg.nphoton))
@@ -911,6 +942,7 @@ int32_t mmcgb_session_launch(mmcgb_session* s, uint64_t photon_offset, uint64_t 
     if ((s->P.buf.pw || s->P.buf.ps || s->P.buf.pd) && nphoton > s->cfg.nphoton)
         return fail(MMCGB_E_ARG, "per-photon trace buffers hold cfg.nphoton photons");
     CK(cudaSetDevice(s->mesh->device));
+    if (const int rc = ensure_hot(s)) return rc;
     SimDev sim = s->P.sim;
     sim.nphoton = nphoton;
     sim.photon_offset = s->cfg.photon_offset + photon_offset;
@@ -931,6 +963,7 @@ int32_t mmcgb_session_launch(mmcgb_session* s, uint64_t photon_offset, uint64_t 
     } else {
         CK(launch_plain(sim, s->work, s->shape, s->stream));
     }
+    CK(fold_hot(sim, s->stream));
     CK(cudaEventRecord(s->ev1, s->stream));
     s->launched += nphoton;
     s->launches++;
@@ -967,6 +1000,7 @@ int plan_batch(int32_t n, mmcgb_session* const* ss, const uint64_t* offsets, con
         if ((s->P.buf.pw || s->P.buf.ps || s->P.buf.pd) && counts[i] > s->cfg.nphoton)
             return fail(MMCGB_E_ARG, "per-photon trace buffers hold cfg.nphoton photons");
         B.sims[i] = s->P.sim;
+        B.sims[i].hot_steps = 0;  // batched launches deposit into the cells themselves
         B.sims[i].nphoton = counts[i];
         B.sims[i].photon_offset = s->cfg.photon_offset + offsets[i];
         B.nmed_stride = std::max(B.nmed_stride, s->cfg.nmedia);
@@ -1186,6 +1220,7 @@ int32_t mmcgb_session_launch_repeat(mmcgb_session* s, uint64_t photon_offset, ui
     if ((s->P.buf.pw || s->P.buf.ps || s->P.buf.pd) && nphoton * (uint64_t)repeats > s->cfg.nphoton)
         return fail(MMCGB_E_ARG, "per-photon trace buffers hold cfg.nphoton photons");
     CK(cudaSetDevice(s->mesh->device));
+    if (const int rc = ensure_hot(s)) return rc;  // allocates outside the capture
     CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < repeats && e == cudaSuccess; k++) {
@@ -1194,6 +1229,7 @@ int32_t mmcgb_session_launch_repeat(mmcgb_session* s, uint64_t photon_offset, ui
         sim.photon_offset = s->cfg.photon_offset + photon_offset + (uint64_t)k * nphoton;
         e = launch_plain(sim, s->work, s->shape, s->stream);
     }
+    if (e == cudaSuccess) e = fold_hot(s->P.sim, s->stream);
     cudaGraph_t g = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(s->stream, &g);
     if (e == cudaSuccess) e = ec;
@@ -1342,7 +1378,10 @@ int32_t mmcgb_simulate_batch(int32_t n, mmcgb_mesh* const* meshes, const mmcgb_c
     cudaEventCreate(&ev1);
     if (rc == MMCGB_OK) {
         std::vector<SimDev> sims(n);
-        for (int i = 0; i < n; i++) sims[i] = P[i].sim;
+        for (int i = 0; i < n; i++) {
+            sims[i] = P[i].sim;
+            sims[i].hot_steps = 0;  // batched launches deposit into the cells themselves
+        }
         cudaError_t e = cudaMallocAsync((void**)&dsims, sizeof(SimDev) * n, stream);
         if (e == cudaSuccess) e = cudaMallocAsync((void**)&dcum, sizeof(unsigned long long) * n, stream);
         if (e == cudaSuccess) e = cudaMallocAsync((void**)&work, sizeof(unsigned long long), stream);

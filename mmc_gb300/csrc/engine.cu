@@ -204,6 +204,11 @@ __device__ __forceinline__ void deposit_at(const SimDev& S, const Lane& L, unsig
         for (int p = 0; p < S.srcnum; p++) deposit(S, base + p, val * __ldg(pat + p));
         return;
     }
+    // gate-0 deposits (idx < ne) of the photon's first tests: this block's copy of the cell
+    if (L.steps < S.hot_steps && idx < (unsigned)S.ne) {
+        atomicAdd(S.hot + (size_t)(blockIdx.x & (kHotReps - 1)) * (unsigned)S.ne + idx, (double)val);
+        return;
+    }
     deposit(S, idx, val);
 }
 
@@ -1367,6 +1372,35 @@ size_t smem_bytes(int nmed_rows, int reclen_max, int threads, int want_seed) {
 }
 
 }  // namespace
+
+#if MMCGB_ENGINE_FAST
+namespace {
+// Per gate-0 cell: the sum of its copies, in copy order, is added to the cell and the copies
+// are cleared for the next launch (only the ones that took deposits are written).
+__global__ void fold_hot_kernel(double* __restrict__ hot, double* __restrict__ f64, unsigned ne) {
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < ne; i += gridDim.x * blockDim.x) {
+        double sum = 0.0;
+        for (int r = 0; r < kHotReps; r++) {
+            double* p = hot + (size_t)r * ne + i;
+            const double v = *p;
+            if (v != 0.0) {
+                sum += v;
+                *p = 0.0;
+            }
+        }
+        if (sum != 0.0) f64[i] += sum;
+    }
+}
+}  // namespace
+
+cudaError_t fold_hot(const SimDev& s, cudaStream_t stream) {
+    if (!s.hot_steps) return cudaSuccess;
+    const unsigned blocks = std::min<unsigned>(((unsigned)s.ne + 255) / 256, 152u * 8u);
+    fold_hot_kernel<<<blocks, 256, 0, stream>>>(s.hot, s.f64, (unsigned)s.ne);
+    return cudaGetLastError();
+}
+
+#endif
 
 // Kernels compiled with the general launch and deposit (SRC) serve
 // simulations whose source is not a pencil beam starting in a known element,

@@ -33,6 +33,13 @@ inline int max_elem(int lbits) { return (int)((1u << (31 - lbits)) - 1u); }
 constexpr unsigned kMaxFluenceCells = 0x7FFFFFFFu;
 // Slots of per-pattern energy tallies (photon sharing): a block adds into slot blockIdx % 64.
 constexpr int kEnergySlots = 64;
+// Replicated accumulators of the cells next to a point source.  Every photon deposits into the
+// few elements around its launch point first, so their reductions queue on the L2 slices that
+// hold those cells.  The gate-0 deposits of a photon's first kHotSteps ray-tet tests go instead
+// to one of kHotReps copies of the gate-0 plane, chosen by block; the copies are added into the
+// fluence after each launch.
+constexpr int kHotReps = 4;
+constexpr unsigned kHotSteps = 16;
 
 // One tetrahedron as the step kernel reads it: 80 bytes, 16-byte aligned.
 //   nx/ny/nz/nd : outward unit normals and plane offsets of the 4 faces
@@ -130,6 +137,9 @@ struct SimDev {
     float* photon_weight;
     unsigned int* photon_steps;
     int* photon_det;
+    // replicated near-source accumulators (kHot*), or hot_steps = 0 when off
+    double* hot;              // kHotReps copies of the gate-0 plane, copy r at hot + r * ne
+    unsigned hot_steps;
 };
 
 struct LaunchShape {
@@ -211,6 +221,9 @@ LaunchShape default_shape(int device, bool batched);
 // runs in a pencil kernel of its own for forward single-simulation launches and
 // in the general kernels otherwise.
 bool general_source(const SimDev& s);
+// Adds the replicated near-source cells of `s` into its fluence and clears them
+// (nothing when s.hot_steps == 0).
+cudaError_t fold_hot(const SimDev& s, cudaStream_t stream);
 
 // The launchers of each arithmetic policy: engine.cu is compiled once per
 // policy, and the entry points above dispatch on SimDev::fast_math.
